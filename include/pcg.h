@@ -1,0 +1,203 @@
+/*
+ * pcg.h -- C ABI of the GB300 SWE patch-update library (libpcg.so).
+ *
+ * The library is a drop-in for PeanoClaw's SWE numerics plugin: the host-side
+ * spacetree traversal keeps calling the peanoclaw::Numerics interface
+ * (src/peanoclaw/Numerics.h:30-204 in the reference); each virtual of that
+ * interface maps onto one entry point below, and every patch's data vector
+ * (h, hu, hv + ghost layers, the bathymetry parameter b and the face fluxes,
+ * in the reference's LinearizationZYXQ layout) stays resident in HBM.
+ *
+ * Conventions
+ *  - Every function returns PCG_OK (0) or a negative PCG_E_* code; the text of
+ *    the last error of the calling thread is returned by pcg_last_error().
+ *    No C++ exception crosses this boundary.
+ *  - Patches are named by the int32 id that pcg_patch_alloc returns.
+ *  - All floating point data is IEEE double (FP64).
+ *  - Work is issued on the context's CUDA stream; calls that return values to
+ *    the host synchronise that stream.
+ */
+#ifndef PCG_H
+#define PCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCG_OK 0
+#define PCG_E_INVALID (-1)   /* bad argument, unknown id, unsupported shape */
+#define PCG_E_NOMEM (-2)     /* device memory (slab) exhausted: admission refused */
+#define PCG_E_CUDA (-3)      /* a CUDA runtime call failed */
+#define PCG_E_TIMEOUT (-4)   /* a bounded device-side wait ran out */
+#define PCG_E_STATE (-5)     /* call not allowed in the current state */
+#define PCG_E_NUMERIC (-6)   /* NaN or negative water height detected */
+
+typedef struct pcg_context pcg_context;
+
+/* SWE solver parameters.  The reference block's constants
+ * (tools/SWE_WaveAccumulationBlock.cpp:225-239,270-284) are cfl = 0.4,
+ * dry_tol_update = 0.1, s_min = 1e-5, dt_inf = FLT_MAX. */
+typedef struct pcg_swe_params {
+  double g;
+  double cfl;
+  double dry_tol;        /* Riemann solver: a cell is wet iff h > dry_tol */
+  double dry_tol_update; /* updateUnknowns: h < this zeroes hu and hv */
+  double s_min;          /* max wave speed <= s_min gives dt = dt_inf */
+  double dt_inf;
+} pcg_swe_params;
+
+typedef struct pcg_config {
+  int32_t device;          /* CUDA device ordinal */
+  int32_t max_patches;     /* capacity of the patch table */
+  int32_t max_groups;      /* independent simulations advanced together */
+  int32_t reserved_;
+  int64_t slab_doubles;    /* HBM slab for all patch vectors, in doubles */
+  pcg_swe_params params;
+} pcg_config;
+
+/* Geometry and layout of one patch (peanoclaw::Patch / CellDescription,
+ * src/peanoclaw/Patch.cpp:201-280). */
+typedef struct pcg_patch_desc {
+  int32_t nx, ny;      /* subdivision factor */
+  int32_t ghost;       /* ghost layer width */
+  int32_t nq;          /* unknowns per subcell */
+  int32_t np_wo;       /* parameter fields without ghost layer */
+  int32_t np_w;        /* parameter fields with ghost layer */
+  int32_t level;
+  int32_t flags;       /* PCG_PATCH_LEAF | PCG_PATCH_VIRTUAL */
+  double pos[2];
+  double size[2];
+} pcg_patch_desc;
+
+#define PCG_PATCH_LEAF 1
+#define PCG_PATCH_VIRTUAL 2
+
+/* TimeIntervals state of one patch (src/peanoclaw/grid/TimeIntervals.cpp). */
+typedef struct pcg_patch_time {
+  double time;               /* current time (uOld time of a leaf) */
+  double dt;                 /* size of the last step (uNew = time + dt) */
+  double est_next;           /* estimated next timestep size (CFL) */
+  double min_neighbor_time;  /* uOld time of a virtual patch */
+  double max_neighbor_dt;    /* uNew - uOld of a virtual patch */
+  double restr_lower[2];     /* neighbouring ghost-layer bounds used by */
+  double restr_upper[2];     /* restrictSolution(onlyOverlapped)        */
+} pcg_patch_time;
+
+/* One ghost-layer transfer of a precomputed face-pair list: the arguments of
+ * Numerics::transferGhostlayer (kind COPY) or of the SWE interpolateSolution
+ * the compositor issues from a coarse leaf (kind INTERP: toUOld, not current
+ * time, time of uNew/uOld), see GhostlayerCompositorFunctors.cpp:23-221. */
+typedef struct pcg_ghost_item {
+  int32_t kind;
+  int32_t src, dst;
+  int32_t size[2];
+  int32_t src_offset[2];
+  int32_t dst_offset[2];
+} pcg_ghost_item;
+
+#define PCG_GHOST_COPY 0
+#define PCG_GHOST_INTERP 1
+
+/* Execution forms of a synchronous grid step. */
+#define PCG_MODE_PLAIN 0    /* one launch per patch for fill, sweep and update */
+#define PCG_MODE_BATCHED 1  /* batched fill + persistent sweep + update, one set per step */
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on cfg->device; reserves the patch slab.
+ * Replaces the construction through NumericsFactory::createSWENumerics
+ * (src/peanoclaw/NumericsFactory.cpp:28-51). */
+int pcg_create(const pcg_config *cfg, pcg_context **out);
+int pcg_destroy(pcg_context *ctx);
+const char *pcg_last_error(void);
+/* Free and total bytes of the slab (for admission by free HBM). */
+int pcg_slab_info(pcg_context *ctx, int64_t *free_doubles, int64_t *total_doubles);
+int pcg_set_params(pcg_context *ctx, const pcg_swe_params *params);
+
+/* ---------------------------------------------------------------- patches */
+
+/* Allocate a patch vector in the slab, zero-filled like Patch::switchToVirtual
+ * (src/peanoclaw/Patch.cpp:732-776).  Returns PCG_E_NOMEM when it does not fit. */
+int pcg_patch_alloc(pcg_context *ctx, const pcg_patch_desc *desc, int32_t *id);
+int pcg_patch_free(pcg_context *ctx, int32_t id);
+/* Number of doubles of a patch vector in the reference layout. */
+int64_t pcg_patch_vector_size(const pcg_patch_desc *desc);
+/* Host <-> device copy of the whole patch vector (reference layout). */
+int pcg_patch_upload(pcg_context *ctx, int32_t id, const double *vec, int64_t n);
+int pcg_patch_download(pcg_context *ctx, int32_t id, double *vec, int64_t n);
+/* Contiguous multi-patch copies: vecs holds the vectors of ids[0..n) back to back. */
+int pcg_patches_upload(pcg_context *ctx, int32_t n, const int32_t *ids, const double *vecs);
+int pcg_patches_download(pcg_context *ctx, int32_t n, const int32_t *ids, double *vecs);
+int pcg_patch_set_desc_flags(pcg_context *ctx, int32_t id, int32_t flags);
+int pcg_patch_set_time(pcg_context *ctx, int32_t id, const pcg_patch_time *t);
+int pcg_patch_get_time(pcg_context *ctx, int32_t id, pcg_patch_time *t);
+/* Domain-boundary faces of a patch: bit (2*dim + upper); filled as reflecting
+ * walls in the order of SolveTimestep::fillBoundaryLayers
+ * (src/peanoclaw/mappings/SolveTimestep.cpp:87-142). */
+int pcg_patch_set_boundary(pcg_context *ctx, int32_t id, uint32_t wall_mask);
+/* Group (independent simulation) the patch belongs to; default 0. */
+int pcg_patch_set_group(pcg_context *ctx, int32_t id, int32_t group);
+
+/* ------------------------------------------- Numerics virtuals, one launch each */
+
+/* DefaultTransfer::copyUNewToUOld (DefaultTransfer.cpph:103-113). */
+int pcg_copy_unew_to_uold(pcg_context *ctx, int32_t id);
+/* SWEKernel::fillBoundaryLayer (src/peanoclaw/native/SWEKernel.cpp:176-237). */
+int pcg_fill_boundary_layer(pcg_context *ctx, int32_t id, int32_t dimension, int32_t set_upper);
+/* SWEKernel::solveTimestep (src/peanoclaw/native/SWEKernel.cpp:125-167):
+ * f-wave sweep on uOld(+ghost), dt = min(block dt, max_dt), update, swap,
+ * time-interval update.  Synchronous: returns the dt used and the estimate. */
+int pcg_solve_timestep(pcg_context *ctx, int32_t id, double max_dt, double *dt_used,
+                       double *est_next);
+/* Numerics::transferGhostlayer -> DefaultTransfer (DefaultTransfer.cpph:15-101). */
+int pcg_transfer_ghostlayer(pcg_context *ctx, const int32_t size[2], const int32_t src_offset[2],
+                            const int32_t dst_offset[2], int32_t src, int32_t dst);
+/* SWEKernel::interpolateSolution (SWEKernel.cpp:239-286) over
+ * DefaultInterpolation (DefaultInterpolation.cpph:29-270); swe = 0 gives the
+ * plain Numerics::interpolateSolution. */
+int pcg_interpolate_solution(pcg_context *ctx, const int32_t size[2], const int32_t dst_offset[2],
+                             int32_t src, int32_t dst, int32_t to_uold, int32_t to_current_time,
+                             int32_t use_time_unew_or_uold, int32_t swe);
+/* SWEKernel::restrictSolution (SWEKernel.cpp:288-307) over DefaultRestriction
+ * (DefaultRestriction.cpph:17-150); swe = 0 gives Numerics::restrictSolution. */
+int pcg_restrict_solution(pcg_context *ctx, int32_t src, int32_t dst, int32_t only_overlapped,
+                          int32_t swe);
+/* SWEKernel::postProcessRestriction (SWEKernel.cpp:309-316). */
+int pcg_post_process_restriction(pcg_context *ctx, int32_t dst);
+/* Numerics::computeFluxes -> DefaultFluxCorrection::computeFluxes
+ * (DefaultFluxCorrection.cpph:43-85); g_flux is the constant of
+ * Numerics::computeFlux (1.0 in the reference, Numerics.h:198). */
+int pcg_compute_fluxes(pcg_context *ctx, int32_t id, double g_flux);
+/* Numerics::applyFluxCorrection -> DefaultFluxCorrection::applyCorrection
+ * (DefaultFluxCorrection.cpph:87-164). */
+int pcg_apply_flux_correction(pcg_context *ctx, int32_t src, int32_t dst, int32_t dimension,
+                              int32_t direction);
+
+/* ------------------------------------------------------ batched grid step */
+
+/* Install the precomputed face-pair list used by every following grid step
+ * (replaces the per-vertex GhostLayerCompositor traversal,
+ * GhostLayerCompositor.cpp:280-320).  Items must write disjoint ghost cells. */
+int pcg_set_ghost_items(pcg_context *ctx, const pcg_ghost_item *items, int32_t n);
+/* Upper bound for the dt of a group (maximumTimestepSize). */
+int pcg_set_group_max_dt(pcg_context *ctx, int32_t group, double max_dt);
+/* One synchronous step of every leaf patch: fill ghost layers (items, then
+ * walls), f-wave sweep with per-patch CFL, dt_g = min(max_dt_g, min over the
+ * group's patches), update with dt_g, swap, time update.  dt_out (may be NULL)
+ * receives max_groups values. */
+int pcg_step(pcg_context *ctx, int32_t mode, double *dt_out);
+/* `steps` synchronous steps; BATCHED mode replays a captured CUDA graph.  The
+ * dt of every step and group is written to dt_hist[steps * max_groups] (may be NULL). */
+int pcg_run(pcg_context *ctx, int32_t steps, int32_t mode, double *dt_hist);
+/* Cumulative interior cell updates and device time of pcg_step / pcg_run. */
+int pcg_stats(pcg_context *ctx, int64_t *cell_updates, double *device_ms);
+/* Block until all work issued on the context has finished. */
+int pcg_synchronize(pcg_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,864 @@
+// pcg_api.cu -- C ABI (include/pcg.h) of the GB300 SWE patch-update library.
+//
+// The context owns one HBM slab holding every patch vector (reference
+// layout), the patch table, the precomputed face-pair list and the sweep
+// work list; host calls only enqueue work on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pcg.h"
+#include "pcg_device.cuh"
+#include "pcg_kernels.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define PCG_CUDA(call)                                                                     \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(PCG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+__global__ void k_scatter(double *slab, const double *staging, const long long *dst_off,
+                          const long long *src_off, const long long *len, int n, int to_slab) {
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    long long d = dst_off[i], s = src_off[i], l = len[i];
+    for (long long k = threadIdx.x; k < l; k += blockDim.x) {
+      if (to_slab) slab[d + k] = staging[s + k];
+      else ((double *)staging)[s + k] = slab[d + k];
+    }
+  }
+}
+
+__global__ void k_record_hist(int n_groups, const unsigned long long *group_dt, double *hist,
+                              int *counter, int capacity) {
+  __shared__ int idx;
+  if (threadIdx.x == 0) idx = *counter;
+  __syncthreads();
+  if (idx < capacity)
+    for (int g = threadIdx.x; g < n_groups; g += blockDim.x)
+      hist[(long long)idx * n_groups + g] = __longlong_as_double((long long)group_dt[g]);
+  __syncthreads();
+  if (threadIdx.x == 0) *counter = idx + 1;
+}
+
+constexpr int64_t kAlign = 32;  // doubles (256 B)
+
+int64_t vector_size(const pcg_patch_desc &d) {
+  int64_t vn = (int64_t)d.nx * d.ny, vo = (int64_t)(d.nx + 2 * d.ghost) * (d.ny + 2 * d.ghost);
+  return d.nq * vn + d.nq * vo + d.np_wo * vn + d.np_w * vo + 2LL * d.nq * (d.nx + d.ny);
+}
+
+}  // namespace
+
+struct pcg_context {
+  int device = 0;
+  int num_sms = 152;
+  cudaStream_t stream = nullptr;
+  pcg::SweParamsDev prm{};
+  std::mutex mu;
+
+  double *slab = nullptr;
+  int64_t slab_doubles = 0;
+  std::map<int64_t, int64_t> free_list;  // offset -> length
+
+  int max_patches = 0, max_groups = 1;
+  std::vector<pcg::PatchDev> h_patches;
+  std::vector<int64_t> h_len;
+  std::vector<char> used;
+  pcg::PatchDev *d_patches = nullptr;
+  pcg::PatchTimeDev *d_times = nullptr;
+  bool patches_dirty = true;
+  bool topo_dirty = true;
+
+  unsigned long long *d_patch_smax = nullptr, *d_group_dt = nullptr;
+  double *d_group_max_dt = nullptr;
+  double *d_dt_out = nullptr;
+  double *h_pinned = nullptr;  // pinned scratch for small D2H/H2D
+  std::vector<double> h_group_max_dt;
+
+  // face-pair list, sorted by destination for the plain form
+  std::vector<pcg_ghost_item> items_user;
+  std::vector<pcg::GhostItemDev> h_items;
+  std::vector<int> item_first, item_count;  // per patch (plain form)
+  pcg::GhostItemDev *d_items = nullptr;
+  size_t d_items_cap = 0;
+
+  std::vector<pcg::TileItem> h_tiles;
+  pcg::TileItem *d_tiles = nullptr;
+  size_t d_tiles_cap = 0;
+  std::vector<int> h_wall;
+  int *d_wall = nullptr;
+  size_t d_wall_cap = 0;
+  std::vector<int> leaf_ids;
+  int64_t cells_per_step = 0;
+  int sweep_grid = 0;
+
+  double *d_solve_out = nullptr;
+  size_t solve_smem_set = 0;
+
+  // graph of one batched step
+  cudaGraphExec_t graph = nullptr;
+  bool graph_valid = false;
+  double *d_hist = nullptr;
+  int hist_cap = 0;
+  int *d_counter = nullptr;
+
+  // staging for multi-patch copies
+  double *d_staging = nullptr;
+  size_t staging_cap = 0;
+  long long *d_copy_meta = nullptr;
+  size_t copy_meta_cap = 0;
+
+  int64_t cell_updates = 0;
+  double device_ms = 0.0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+bool valid_id(pcg_context *c, int32_t id) {
+  return c && id >= 0 && id < c->max_patches && c->used[id];
+}
+
+int slab_alloc(pcg_context *c, int64_t len, int64_t *off) {
+  int64_t need = (len + kAlign - 1) / kAlign * kAlign;
+  for (auto it = c->free_list.begin(); it != c->free_list.end(); ++it) {
+    if (it->second >= need) {
+      *off = it->first;
+      int64_t rest = it->second - need;
+      int64_t noff = it->first + need;
+      c->free_list.erase(it);
+      if (rest > 0) c->free_list[noff] = rest;
+      return PCG_OK;
+    }
+  }
+  return fail(PCG_E_NOMEM, "slab exhausted: patch vector of " + std::to_string(len) + " doubles does not fit");
+}
+
+void slab_free(pcg_context *c, int64_t off, int64_t len) {
+  int64_t need = (len + kAlign - 1) / kAlign * kAlign;
+  auto it = c->free_list.emplace(off, need).first;
+  auto nx = std::next(it);
+  if (nx != c->free_list.end() && it->first + it->second == nx->first) {
+    it->second += nx->second;
+    c->free_list.erase(nx);
+  }
+  if (it != c->free_list.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first + pv->second == it->first) {
+      pv->second += it->second;
+      c->free_list.erase(it);
+    }
+  }
+}
+
+template <class T>
+int ensure_device(pcg_context *c, T **ptr, size_t *cap, size_t n) {
+  if (n <= *cap && *ptr) return PCG_OK;
+  if (*ptr) PCG_CUDA(cudaFree(*ptr));
+  *ptr = nullptr;
+  size_t nc = std::max<size_t>(n, 16);
+  PCG_CUDA(cudaMalloc((void **)ptr, nc * sizeof(T)));
+  *cap = nc;
+  return PCG_OK;
+}
+
+int upload_patches(pcg_context *c) {
+  if (!c->patches_dirty) return PCG_OK;
+  PCG_CUDA(cudaMemcpyAsync(c->d_patches, c->h_patches.data(),
+                           sizeof(pcg::PatchDev) * c->max_patches, cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  c->patches_dirty = false;
+  return PCG_OK;
+}
+
+// Rebuild the sweep work list, the wall list and the per-patch item ranges.
+int rebuild_topology(pcg_context *c) {
+  if (!c->topo_dirty) return upload_patches(c);
+  c->h_tiles.clear();
+  c->h_wall.clear();
+  c->leaf_ids.clear();
+  c->cells_per_step = 0;
+  for (int p = 0; p < c->max_patches; p++) {
+    pcg::PatchDev &P = c->h_patches[p];
+    P.tile_begin = 0;
+    P.tile_count = 0;
+    if (!c->used[p] || !(P.flags & pcg::kFlagLeaf)) continue;
+    c->leaf_ids.push_back(p);
+    c->cells_per_step += (int64_t)P.nx * P.ny;
+    P.tile_begin = (int)c->h_tiles.size();
+    for (int x0 = 0; x0 < P.nx; x0 += pcg::kTile)
+      for (int y0 = 0; y0 < P.ny; y0 += pcg::kTile) {
+        pcg::TileItem t;
+        t.pid = p;
+        t.x0 = (short)x0;
+        t.y0 = (short)y0;
+        t.tw = (short)std::min(pcg::kTile, P.nx - x0);
+        t.th = (short)std::min(pcg::kTile, P.ny - y0);
+        t.pad_ = 0;
+        c->h_tiles.push_back(t);
+      }
+    P.tile_count = (int)c->h_tiles.size() - P.tile_begin;
+    if (P.wall) c->h_wall.push_back(p);
+  }
+  // items: keep the user's order within each destination (plain form needs
+  // per-destination ranges; the batched kernel relies on disjoint writes)
+  c->h_items.clear();
+  c->item_first.assign(c->max_patches, 0);
+  c->item_count.assign(c->max_patches, 0);
+  std::vector<std::vector<int>> by_dst(c->max_patches);
+  for (size_t k = 0; k < c->items_user.size(); k++) {
+    const pcg_ghost_item &u = c->items_user[k];
+    if (!valid_id(c, u.src) || !valid_id(c, u.dst)) continue;
+    by_dst[u.dst].push_back((int)k);
+  }
+  for (int p = 0; p < c->max_patches; p++) {
+    c->item_first[p] = (int)c->h_items.size();
+    for (int k : by_dst[p]) {
+      const pcg_ghost_item &u = c->items_user[k];
+      pcg::GhostItemDev d;
+      d.kind = u.kind; d.src = u.src; d.dst = u.dst;
+      d.size[0] = u.size[0]; d.size[1] = u.size[1];
+      d.src_off[0] = u.src_offset[0]; d.src_off[1] = u.src_offset[1];
+      d.dst_off[0] = u.dst_offset[0]; d.dst_off[1] = u.dst_offset[1];
+      c->h_items.push_back(d);
+    }
+    c->item_count[p] = (int)c->h_items.size() - c->item_first[p];
+  }
+  int rc;
+  if ((rc = ensure_device(c, &c->d_tiles, &c->d_tiles_cap, c->h_tiles.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_wall, &c->d_wall_cap, c->h_wall.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_items, &c->d_items_cap, c->h_items.size())) != PCG_OK) return rc;
+  if (!c->h_tiles.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_tiles, c->h_tiles.data(), sizeof(pcg::TileItem) * c->h_tiles.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+  if (!c->h_wall.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_wall, c->h_wall.data(), sizeof(int) * c->h_wall.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+  if (!c->h_items.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_items, c->h_items.data(), sizeof(pcg::GhostItemDev) * c->h_items.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+  int per_sm = 0;
+  PCG_CUDA(pcg::sweep_occupancy(&per_sm));
+  if (per_sm < 1) per_sm = 1;
+  c->sweep_grid = (int)std::min<int64_t>((int64_t)c->num_sms * per_sm, std::max<int64_t>(1, (int64_t)c->h_tiles.size()));
+  c->patches_dirty = true;
+  c->topo_dirty = false;
+  c->graph_valid = false;
+  return upload_patches(c);
+}
+
+int upload_group_max_dt(pcg_context *c) {
+  PCG_CUDA(cudaMemcpyAsync(c->d_group_max_dt, c->h_group_max_dt.data(), sizeof(double) * c->max_groups,
+                           cudaMemcpyHostToDevice, c->stream));
+  return PCG_OK;
+}
+
+// Enqueue one synchronous step (no synchronisation, capturable in BATCHED mode).
+int enqueue_step(pcg_context *c, int mode) {
+  using namespace pcg;
+  PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
+                        c->d_patch_smax));
+  if (mode == PCG_MODE_BATCHED) {
+    PCG_CUDA(launch_ghost_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, 0,
+                                (int)c->h_items.size(), nullptr));
+    PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
+    PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
+                          (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+    PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
+                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+  } else {
+    for (int p : c->leaf_ids)
+      PCG_CUDA(launch_fill_patch(c->stream, c->slab, c->d_patches, c->d_times, c->d_items,
+                                 c->item_first[p], c->item_count[p], p));
+    for (int p : c->leaf_ids) {
+      const PatchDev &P = c->h_patches[p];
+      PCG_CUDA(launch_sweep(c->stream, P.tile_count, c->slab, c->d_patches, c->d_tiles, P.tile_begin,
+                            P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+    }
+    for (int p : c->leaf_ids) {
+      const PatchDev &P = c->h_patches[p];
+      PCG_CUDA(launch_update(c->stream, P.tile_count, c->slab, c->d_patches, c->d_times, c->d_tiles,
+                             P.tile_begin, P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+    }
+  }
+  return PCG_OK;
+}
+
+int ensure_staging(pcg_context *c, size_t doubles, size_t metas) {
+  int rc;
+  if ((rc = ensure_device(c, &c->d_staging, &c->staging_cap, doubles)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_copy_meta, &c->copy_meta_cap, 3 * metas)) != PCG_OK) return rc;
+  return PCG_OK;
+}
+
+int multi_copy(pcg_context *c, int32_t n, const int32_t *ids, double *vecs, bool upload) {
+  if (n <= 0) return PCG_OK;
+  std::vector<long long> meta(3 * (size_t)n);
+  long long total = 0;
+  for (int i = 0; i < n; i++) {
+    if (!valid_id(c, ids[i])) return fail(PCG_E_INVALID, "unknown patch id " + std::to_string(ids[i]));
+    meta[i] = c->h_patches[ids[i]].off;
+    meta[n + i] = total;
+    meta[2 * n + i] = c->h_len[ids[i]];
+    total += c->h_len[ids[i]];
+  }
+  int rc = ensure_staging(c, (size_t)total, (size_t)n);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(c->d_copy_meta, meta.data(), sizeof(long long) * meta.size(),
+                           cudaMemcpyHostToDevice, c->stream));
+  int grid = std::min(n, 152 * 8);
+  if (upload) {
+    PCG_CUDA(cudaMemcpyAsync(c->d_staging, vecs, sizeof(double) * total, cudaMemcpyHostToDevice, c->stream));
+    k_scatter<<<grid, 256, 0, c->stream>>>(c->slab, c->d_staging, c->d_copy_meta, c->d_copy_meta + n,
+                                           c->d_copy_meta + 2 * n, n, 1);
+    PCG_CUDA(cudaGetLastError());
+  } else {
+    k_scatter<<<grid, 256, 0, c->stream>>>(c->slab, c->d_staging, c->d_copy_meta, c->d_copy_meta + n,
+                                           c->d_copy_meta + 2 * n, n, 0);
+    PCG_CUDA(cudaGetLastError());
+    PCG_CUDA(cudaMemcpyAsync(vecs, c->d_staging, sizeof(double) * total, cudaMemcpyDeviceToHost, c->stream));
+  }
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+pcg::GhostItemDev make_item(int kind, const int32_t size[2], const int32_t so[2], const int32_t dof[2],
+                            int src, int dst) {
+  pcg::GhostItemDev it;
+  it.kind = kind; it.src = src; it.dst = dst;
+  it.size[0] = size[0]; it.size[1] = size[1];
+  it.src_off[0] = so ? so[0] : 0; it.src_off[1] = so ? so[1] : 0;
+  it.dst_off[0] = dof[0]; it.dst_off[1] = dof[1];
+  return it;
+}
+
+bool region_inside(const pcg::PatchDev &P, const int32_t off[2], const int32_t size[2], bool with_ghost) {
+  int n[2] = {P.nx, P.ny};
+  int g = with_ghost ? P.g : 0;
+  for (int d = 0; d < 2; d++) {
+    if (size[d] < 0 || off[d] < -g || off[d] + size[d] > n[d] + g) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *pcg_last_error(void) { return g_last_error.c_str(); }
+
+int64_t pcg_patch_vector_size(const pcg_patch_desc *desc) {
+  if (!desc) return -1;
+  return vector_size(*desc);
+}
+
+int pcg_create(const pcg_config *cfg, pcg_context **out) {
+  if (!cfg || !out) return fail(PCG_E_INVALID, "null argument");
+  if (cfg->max_patches <= 0 || cfg->max_groups <= 0 || cfg->slab_doubles <= 0)
+    return fail(PCG_E_INVALID, "max_patches, max_groups and slab_doubles must be positive");
+  int ndev = 0;
+  PCG_CUDA(cudaGetDeviceCount(&ndev));
+  if (cfg->device < 0 || cfg->device >= ndev) return fail(PCG_E_INVALID, "no such CUDA device");
+  PCG_CUDA(cudaSetDevice(cfg->device));
+  pcg_context *c = new pcg_context();
+  c->device = cfg->device;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, cfg->device);
+  if (e != cudaSuccess) { delete c; return fail(PCG_E_CUDA, cudaGetErrorString(e)); }
+  c->num_sms = prop.multiProcessorCount;
+  c->prm = {cfg->params.g, cfg->params.cfl, cfg->params.dry_tol, cfg->params.dry_tol_update,
+            cfg->params.s_min, cfg->params.dt_inf};
+  c->max_patches = cfg->max_patches;
+  c->max_groups = cfg->max_groups;
+  c->slab_doubles = cfg->slab_doubles;
+  c->h_patches.assign(c->max_patches, pcg::PatchDev{});
+  c->h_len.assign(c->max_patches, 0);
+  c->used.assign(c->max_patches, 0);
+  c->h_group_max_dt.assign(c->max_groups, cfg->params.dt_inf);
+  auto cleanup = [&](cudaError_t err) {
+    pcg_destroy(c);
+    return fail(PCG_E_CUDA, std::string("pcg_create: ") + cudaGetErrorString(err));
+  };
+#define CREATE_CK(x) do { cudaError_t err_ = (x); if (err_ != cudaSuccess) return cleanup(err_); } while (0)
+  CREATE_CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CREATE_CK(cudaEventCreate(&c->ev0));
+  CREATE_CK(cudaEventCreate(&c->ev1));
+  CREATE_CK(cudaMalloc(&c->slab, sizeof(double) * c->slab_doubles));
+  c->free_list[0] = c->slab_doubles / kAlign * kAlign;
+  CREATE_CK(cudaMalloc(&c->d_patches, sizeof(pcg::PatchDev) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_times, sizeof(pcg::PatchTimeDev) * c->max_patches));
+  CREATE_CK(cudaMemset(c->d_times, 0, sizeof(pcg::PatchTimeDev) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_patch_smax, sizeof(unsigned long long) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_group_dt, sizeof(unsigned long long) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_group_max_dt, sizeof(double) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_dt_out, sizeof(double) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_solve_out, sizeof(double) * 2));
+  CREATE_CK(cudaMalloc(&c->d_counter, sizeof(int)));
+  CREATE_CK(cudaMallocHost(&c->h_pinned, sizeof(double) * std::max(64, c->max_groups)));
+#undef CREATE_CK
+  *out = c;
+  return PCG_OK;
+}
+
+int pcg_destroy(pcg_context *c) {
+  if (!c) return PCG_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  cudaFree(c->slab);
+  cudaFree(c->d_patches);
+  cudaFree(c->d_times);
+  cudaFree(c->d_patch_smax);
+  cudaFree(c->d_group_dt);
+  cudaFree(c->d_group_max_dt);
+  cudaFree(c->d_dt_out);
+  cudaFree(c->d_items);
+  cudaFree(c->d_tiles);
+  cudaFree(c->d_wall);
+  cudaFree(c->d_solve_out);
+  cudaFree(c->d_hist);
+  cudaFree(c->d_counter);
+  cudaFree(c->d_staging);
+  cudaFree(c->d_copy_meta);
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return PCG_OK;
+}
+
+int pcg_slab_info(pcg_context *c, int64_t *free_doubles, int64_t *total_doubles) {
+  if (!c) return fail(PCG_E_INVALID, "null context");
+  int64_t f = 0;
+  for (auto &kv : c->free_list) f += kv.second;
+  if (free_doubles) *free_doubles = f;
+  if (total_doubles) *total_doubles = c->slab_doubles;
+  return PCG_OK;
+}
+
+int pcg_set_params(pcg_context *c, const pcg_swe_params *p) {
+  if (!c || !p) return fail(PCG_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->prm = {p->g, p->cfl, p->dry_tol, p->dry_tol_update, p->s_min, p->dt_inf};
+  c->graph_valid = false;
+  return PCG_OK;
+}
+
+int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
+  if (!c || !d || !id) return fail(PCG_E_INVALID, "null argument");
+  if (d->nx <= 0 || d->ny <= 0 || d->ghost < 0 || d->nq <= 0 || d->np_wo < 0 || d->np_w < 0)
+    return fail(PCG_E_INVALID, "invalid patch shape");
+  if (!(d->size[0] > 0.0) || !(d->size[1] > 0.0)) return fail(PCG_E_INVALID, "patch size must be positive");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int slot = -1;
+  for (int p = 0; p < c->max_patches; p++)
+    if (!c->used[p]) { slot = p; break; }
+  if (slot < 0) return fail(PCG_E_NOMEM, "patch table full");
+  int64_t len = vector_size(*d), off = 0;
+  int rc = slab_alloc(c, len, &off);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(cudaSetDevice(c->device));
+  PCG_CUDA(cudaMemsetAsync(c->slab + off, 0, sizeof(double) * len, c->stream));
+  pcg::PatchDev &P = c->h_patches[slot];
+  P = pcg::PatchDev{};
+  P.off = off;
+  P.nx = d->nx; P.ny = d->ny; P.g = d->ghost; P.nq = d->nq;
+  P.np_wo = d->np_wo; P.np_w = d->np_w; P.level = d->level; P.flags = d->flags;
+  P.group = 0; P.wall = 0;
+  P.pos[0] = d->pos[0]; P.pos[1] = d->pos[1];
+  P.size[0] = d->size[0]; P.size[1] = d->size[1];
+  c->h_len[slot] = len;
+  c->used[slot] = 1;
+  pcg::PatchTimeDev t{};
+  const double big = 1.7976931348623157e308;
+  t.rl[0] = t.rl[1] = big;
+  t.ru[0] = t.ru[1] = -big;
+  PCG_CUDA(cudaMemcpyAsync(c->d_times + slot, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  c->patches_dirty = c->topo_dirty = true;
+  *id = slot;
+  return PCG_OK;
+}
+
+int pcg_patch_free(pcg_context *c, int32_t id) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  slab_free(c, c->h_patches[id].off, c->h_len[id]);
+  c->used[id] = 0;
+  c->h_patches[id] = pcg::PatchDev{};
+  c->patches_dirty = c->topo_dirty = true;
+  return PCG_OK;
+}
+
+int pcg_patch_upload(pcg_context *c, int32_t id, const double *vec, int64_t n) {
+  if (!valid_id(c, id) || !vec) return fail(PCG_E_INVALID, "unknown patch id or null vector");
+  if (n != c->h_len[id]) return fail(PCG_E_INVALID, "vector length does not match the patch layout");
+  PCG_CUDA(cudaMemcpyAsync(c->slab + c->h_patches[id].off, vec, sizeof(double) * n,
+                           cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+int pcg_patch_download(pcg_context *c, int32_t id, double *vec, int64_t n) {
+  if (!valid_id(c, id) || !vec) return fail(PCG_E_INVALID, "unknown patch id or null vector");
+  if (n != c->h_len[id]) return fail(PCG_E_INVALID, "vector length does not match the patch layout");
+  PCG_CUDA(cudaMemcpyAsync(vec, c->slab + c->h_patches[id].off, sizeof(double) * n,
+                           cudaMemcpyDeviceToHost, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+int pcg_patches_upload(pcg_context *c, int32_t n, const int32_t *ids, const double *vecs) {
+  if (!c || (n > 0 && (!ids || !vecs))) return fail(PCG_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  return multi_copy(c, n, ids, const_cast<double *>(vecs), true);
+}
+
+int pcg_patches_download(pcg_context *c, int32_t n, const int32_t *ids, double *vecs) {
+  if (!c || (n > 0 && (!ids || !vecs))) return fail(PCG_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  return multi_copy(c, n, ids, vecs, false);
+}
+
+int pcg_patch_set_desc_flags(pcg_context *c, int32_t id, int32_t flags) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->h_patches[id].flags = flags;
+  c->patches_dirty = c->topo_dirty = true;
+  return PCG_OK;
+}
+
+int pcg_patch_set_time(pcg_context *c, int32_t id, const pcg_patch_time *t) {
+  if (!valid_id(c, id) || !t) return fail(PCG_E_INVALID, "unknown patch id or null time");
+  pcg::PatchTimeDev d{};
+  d.time = t->time; d.dt = t->dt; d.est_next = t->est_next;
+  d.min_nb_time = t->min_neighbor_time; d.max_nb_dt = t->max_neighbor_dt;
+  d.rl[0] = t->restr_lower[0]; d.rl[1] = t->restr_lower[1];
+  d.ru[0] = t->restr_upper[0]; d.ru[1] = t->restr_upper[1];
+  PCG_CUDA(cudaMemcpyAsync(c->d_times + id, &d, sizeof(d), cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+int pcg_patch_get_time(pcg_context *c, int32_t id, pcg_patch_time *t) {
+  if (!valid_id(c, id) || !t) return fail(PCG_E_INVALID, "unknown patch id or null time");
+  pcg::PatchTimeDev d;
+  PCG_CUDA(cudaMemcpyAsync(&d, c->d_times + id, sizeof(d), cudaMemcpyDeviceToHost, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  t->time = d.time; t->dt = d.dt; t->est_next = d.est_next;
+  t->min_neighbor_time = d.min_nb_time; t->max_neighbor_dt = d.max_nb_dt;
+  t->restr_lower[0] = d.rl[0]; t->restr_lower[1] = d.rl[1];
+  t->restr_upper[0] = d.ru[0]; t->restr_upper[1] = d.ru[1];
+  return PCG_OK;
+}
+
+int pcg_patch_set_boundary(pcg_context *c, int32_t id, uint32_t wall_mask) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  if (wall_mask > 15u) return fail(PCG_E_INVALID, "wall mask has 4 bits in 2D");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->h_patches[id].wall = (int)wall_mask;
+  c->patches_dirty = c->topo_dirty = true;
+  return PCG_OK;
+}
+
+int pcg_patch_set_group(pcg_context *c, int32_t id, int32_t group) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  if (group < 0 || group >= c->max_groups) return fail(PCG_E_INVALID, "group out of range");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->h_patches[id].group = group;
+  c->patches_dirty = true;
+  c->graph_valid = false;
+  return PCG_OK;
+}
+
+// ---------------------------------------------------------------- single ops
+
+int pcg_copy_unew_to_uold(pcg_context *c, int32_t id) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  const pcg::PatchDev &P = c->h_patches[id];
+  PCG_CUDA(pcg::launch_copy_unew_to_uold(c->stream, c->slab, c->d_patches, id, P.nq * P.nx * P.ny));
+  return PCG_OK;
+}
+
+int pcg_fill_boundary_layer(pcg_context *c, int32_t id, int32_t dimension, int32_t set_upper) {
+  if (!valid_id(c, id) || dimension < 0 || dimension > 1) return fail(PCG_E_INVALID, "bad patch or dimension");
+  if (c->h_patches[id].g != 1 || c->h_patches[id].nq < 3)
+    return fail(PCG_E_INVALID, "SWE wall boundary needs ghost width 1 and 3 unknowns");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_fill_boundary_layer(c->stream, c->slab, c->d_patches, id, dimension, set_upper ? 1 : 0));
+  return PCG_OK;
+}
+
+int pcg_solve_timestep(pcg_context *c, int32_t id, double max_dt, double *dt_used, double *est_next) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  const pcg::PatchDev &P = c->h_patches[id];
+  if (P.g != 1 || P.nq != 3 || P.np_w < 1)
+    return fail(PCG_E_INVALID, "SWE solve needs ghost width 1, 3 unknowns and the bathymetry parameter");
+  size_t smem = pcg::solve_patch_smem(P.nx, P.ny);
+  if (smem > 190 * 1024) return fail(PCG_E_INVALID, "patch too large for the fused per-patch solve");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  if (smem > c->solve_smem_set) {
+    PCG_CUDA(pcg::prepare_solve_patch(190 * 1024));
+    c->solve_smem_set = 190 * 1024;
+  }
+  PCG_CUDA(pcg::launch_solve_patch(c->stream, c->slab, c->d_patches, c->d_times, id, P.nx, P.ny, c->prm,
+                                   max_dt, c->d_solve_out));
+  PCG_CUDA(cudaMemcpyAsync(c->h_pinned, c->d_solve_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  if (dt_used) *dt_used = c->h_pinned[0];
+  if (est_next) *est_next = c->h_pinned[1];
+  return PCG_OK;
+}
+
+int pcg_transfer_ghostlayer(pcg_context *c, const int32_t size[2], const int32_t so[2],
+                            const int32_t dof[2], int32_t src, int32_t dst) {
+  if (!valid_id(c, src) || !valid_id(c, dst) || !size || !so || !dof) return fail(PCG_E_INVALID, "bad argument");
+  const pcg::PatchDev &S = c->h_patches[src], &D = c->h_patches[dst];
+  if (S.nq != D.nq) return fail(PCG_E_INVALID, "unknowns per subcell differ");
+  if (!region_inside(S, so, size, false) || !region_inside(D, dof, size, true))
+    return fail(PCG_E_INVALID, "transfer region outside the patches");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_transfer(c->stream, c->slab, c->d_patches, c->d_times,
+                                make_item(0, size, so, dof, src, dst)));
+  return PCG_OK;
+}
+
+int pcg_interpolate_solution(pcg_context *c, const int32_t size[2], const int32_t dof[2], int32_t src,
+                             int32_t dst, int32_t to_uold, int32_t to_current_time,
+                             int32_t use_time_unew_or_uold, int32_t swe) {
+  if (!valid_id(c, src) || !valid_id(c, dst) || !size || !dof) return fail(PCG_E_INVALID, "bad argument");
+  const pcg::PatchDev &S = c->h_patches[src], &D = c->h_patches[dst];
+  if (S.nq != D.nq) return fail(PCG_E_INVALID, "unknowns per subcell differ");
+  if (S.nx < 2 || S.ny < 2) return fail(PCG_E_INVALID, "source needs at least 2x2 cells");
+  if (!region_inside(D, dof, size, to_uold != 0)) return fail(PCG_E_INVALID, "region outside the destination");
+  if (swe && (S.np_w < 1 || D.np_w < 1)) return fail(PCG_E_INVALID, "SWE interpolation needs the bathymetry parameter");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_interpolate(c->stream, c->slab, c->d_patches, c->d_times,
+                                   make_item(1, size, nullptr, dof, src, dst), to_uold, to_current_time,
+                                   use_time_unew_or_uold, swe));
+  return PCG_OK;
+}
+
+int pcg_restrict_solution(pcg_context *c, int32_t src, int32_t dst, int32_t only_overlapped, int32_t swe) {
+  if (!valid_id(c, src) || !valid_id(c, dst)) return fail(PCG_E_INVALID, "unknown patch id");
+  const pcg::PatchDev &S = c->h_patches[src], &D = c->h_patches[dst];
+  if (S.nq != D.nq) return fail(PCG_E_INVALID, "unknowns per subcell differ");
+  if (swe && S.np_w < 1) return fail(PCG_E_INVALID, "SWE restriction needs the bathymetry parameter");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_restrict(c->stream, c->slab, c->d_patches, c->d_times, src, dst, only_overlapped, swe));
+  return PCG_OK;
+}
+
+int pcg_post_process_restriction(pcg_context *c, int32_t dst) {
+  if (!valid_id(c, dst)) return fail(PCG_E_INVALID, "unknown patch id");
+  if (c->h_patches[dst].np_w < 1) return fail(PCG_E_INVALID, "needs the bathymetry parameter");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  int *ids = nullptr;
+  size_t cap = 0;
+  // one-element id list in the pinned-free path: reuse d_counter-sized scratch
+  rc = ensure_device(c, &ids, &cap, 1);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(ids, &dst, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(pcg::launch_post_process_restriction(c->stream, c->slab, c->d_patches, ids, 1));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  PCG_CUDA(cudaFree(ids));
+  return PCG_OK;
+}
+
+int pcg_compute_fluxes(pcg_context *c, int32_t id, double g_flux) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  if (c->h_patches[id].nq != 3 || c->h_patches[id].g < 1)
+    return fail(PCG_E_INVALID, "flux computation needs 3 unknowns and a ghost layer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  int *ids = nullptr;
+  size_t cap = 0;
+  rc = ensure_device(c, &ids, &cap, 1);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(ids, &id, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(pcg::launch_compute_fluxes(c->stream, c->slab, c->d_patches, ids, 1, g_flux));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  PCG_CUDA(cudaFree(ids));
+  return PCG_OK;
+}
+
+int pcg_apply_flux_correction(pcg_context *c, int32_t src, int32_t dst, int32_t dimension, int32_t direction) {
+  if (!valid_id(c, src) || !valid_id(c, dst)) return fail(PCG_E_INVALID, "unknown patch id");
+  if (dimension < 0 || dimension > 1 || (direction != 1 && direction != -1))
+    return fail(PCG_E_INVALID, "bad dimension/direction");
+  if (c->h_patches[src].nq != 3 || c->h_patches[dst].nq != 3) return fail(PCG_E_INVALID, "needs 3 unknowns");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_flux_correction(c->stream, c->slab, c->d_patches, c->d_times, src, dst, dimension, direction));
+  return PCG_OK;
+}
+
+// ---------------------------------------------------------------- batched
+
+int pcg_set_ghost_items(pcg_context *c, const pcg_ghost_item *items, int32_t n) {
+  if (!c || n < 0 || (n > 0 && !items)) return fail(PCG_E_INVALID, "bad item list");
+  std::lock_guard<std::mutex> lk(c->mu);
+  for (int k = 0; k < n; k++) {
+    const pcg_ghost_item &it = items[k];
+    if (!valid_id(c, it.src) || !valid_id(c, it.dst) || (it.kind != 0 && it.kind != 1))
+      return fail(PCG_E_INVALID, "ghost item " + std::to_string(k) + ": bad ids or kind");
+    const pcg::PatchDev &S = c->h_patches[it.src], &D = c->h_patches[it.dst];
+    if (S.nq != D.nq) return fail(PCG_E_INVALID, "ghost item " + std::to_string(k) + ": unknowns differ");
+    if (!region_inside(D, it.dst_offset, it.size, true) ||
+        (it.kind == 0 && !region_inside(S, it.src_offset, it.size, false)))
+      return fail(PCG_E_INVALID, "ghost item " + std::to_string(k) + ": region outside the patches");
+    if (it.kind == 1 && (S.nx < 2 || S.ny < 2 || S.np_w < 1 || D.np_w < 1))
+      return fail(PCG_E_INVALID, "ghost item " + std::to_string(k) + ": interpolation source unsupported");
+  }
+  c->items_user.assign(items, items + n);
+  c->topo_dirty = true;
+  return PCG_OK;
+}
+
+int pcg_set_group_max_dt(pcg_context *c, int32_t group, double max_dt) {
+  if (!c || group < 0 || group >= c->max_groups) return fail(PCG_E_INVALID, "group out of range");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->h_group_max_dt[group] = max_dt;
+  return PCG_OK;
+}
+
+static int check_solvable(pcg_context *c) {
+  for (int p : c->leaf_ids) {
+    const pcg::PatchDev &P = c->h_patches[p];
+    if (P.g != 1 || P.nq != 3 || P.np_w < 1)
+      return fail(PCG_E_INVALID, "leaf patch " + std::to_string(p) + " is not an SWE patch (ghost 1, 3 unknowns, b)");
+  }
+  return PCG_OK;
+}
+
+int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
+  if (!c || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED)) return fail(PCG_E_INVALID, "bad mode");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  if ((rc = check_solvable(c)) != PCG_OK) return rc;
+  if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+  if ((rc = enqueue_step(c, mode)) != PCG_OK) return rc;
+  PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+  PCG_CUDA(pcg::launch_record_dt(c->stream, c->max_groups, c->d_group_dt, c->d_dt_out));
+  PCG_CUDA(cudaMemcpyAsync(c->h_pinned, c->d_dt_out, sizeof(double) * c->max_groups, cudaMemcpyDeviceToHost,
+                           c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->device_ms += ms;
+  c->cell_updates += c->cells_per_step;
+  if (dt_out) std::memcpy(dt_out, c->h_pinned, sizeof(double) * c->max_groups);
+  return PCG_OK;
+}
+
+int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
+  if (!c || steps < 0 || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED))
+    return fail(PCG_E_INVALID, "bad arguments");
+  if (steps == 0) return PCG_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  if ((rc = check_solvable(c)) != PCG_OK) return rc;
+  if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  if (steps > c->hist_cap) {
+    if (c->d_hist) PCG_CUDA(cudaFree(c->d_hist));
+    PCG_CUDA(cudaMalloc(&c->d_hist, sizeof(double) * (size_t)steps * c->max_groups));
+    c->hist_cap = steps;
+    c->graph_valid = false;
+  }
+  PCG_CUDA(cudaMemsetAsync(c->d_counter, 0, sizeof(int), c->stream));
+  int threads = std::min(1024, std::max(32, (c->max_groups + 31) / 32 * 32));
+  if (mode == PCG_MODE_BATCHED) {
+    if (!c->graph_valid) {
+      if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+      cudaGraph_t g;
+      PCG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      int erc = enqueue_step(c, PCG_MODE_BATCHED);
+      k_record_hist<<<1, threads, 0, c->stream>>>(c->max_groups, c->d_group_dt, c->d_hist, c->d_counter,
+                                                 c->hist_cap);
+      cudaError_t le = cudaGetLastError();
+      cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+      if (erc != PCG_OK) return erc;
+      if (le != cudaSuccess) return fail(PCG_E_CUDA, cudaGetErrorString(le));
+      if (ce != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+      c->graph_valid = true;
+    }
+    PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+    for (int s = 0; s < steps; s++) PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+  } else {
+    PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+    for (int s = 0; s < steps; s++) {
+      if ((rc = enqueue_step(c, PCG_MODE_PLAIN)) != PCG_OK) return rc;
+      k_record_hist<<<1, threads, 0, c->stream>>>(c->max_groups, c->d_group_dt, c->d_hist, c->d_counter,
+                                                 c->hist_cap);
+      PCG_CUDA(cudaGetLastError());
+    }
+    PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+  }
+  if (dt_hist)
+    PCG_CUDA(cudaMemcpyAsync(dt_hist, c->d_hist, sizeof(double) * (size_t)steps * c->max_groups,
+                             cudaMemcpyDeviceToHost, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->device_ms += ms;
+  c->cell_updates += c->cells_per_step * steps;
+  return PCG_OK;
+}
+
+int pcg_stats(pcg_context *c, int64_t *cell_updates, double *device_ms) {
+  if (!c) return fail(PCG_E_INVALID, "null context");
+  if (cell_updates) *cell_updates = c->cell_updates;
+  if (device_ms) *device_ms = c->device_ms;
+  return PCG_OK;
+}
+
+int pcg_synchronize(pcg_context *c) {
+  if (!c) return fail(PCG_E_INVALID, "null context");
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+}  // extern "C"

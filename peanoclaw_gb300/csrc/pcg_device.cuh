@@ -1,0 +1,197 @@
+// pcg_device.cuh -- device-side data structures and arithmetic of the GB300
+// SWE patch-update path.
+//
+// All FP64 arithmetic below is spelled with explicit round-to-nearest
+// intrinsics (__dadd_rn, __dmul_rn, __fma_rn, ...) and the library is built
+// with -fmad=false, so the compiler neither contracts nor reorders anything:
+// every result is the IEEE result of the written operation sequence.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pcg {
+
+// Patch table entry.  `off` is the offset (in doubles) of the patch's data
+// vector inside the slab; the vector uses the reference's LinearizationZYXQ
+// layout (src/peanoclaw/grid/LinearizationZYXQ.h:20-88).
+struct __align__(16) PatchDev {
+  long long off;
+  int nx, ny, g, nq;
+  int np_wo, np_w, level, flags;
+  int group, wall, tile_begin, tile_count;
+  double pos[2];
+  double size[2];
+};
+
+struct __align__(16) PatchTimeDev {
+  double time, dt, est_next, min_nb_time, max_nb_dt;
+  double rl[2], ru[2];
+  double pad_;
+};
+
+// One sweep/update work item: a tile of at most kTile x kTile cells of a patch.
+struct __align__(16) TileItem {
+  int pid;
+  short x0, y0, tw, th;
+  int pad_;
+};
+
+struct SweParamsDev {
+  double g, cfl, dry_tol, dry_tol_update, s_min, dt_inf;
+};
+
+struct GhostItemDev {
+  int kind, src, dst;
+  int size[2];
+  int src_off[2];
+  int dst_off[2];
+};
+
+constexpr int kTile = 16;           // tile edge of the sweep
+constexpr int kSweepThreads = 256;  // kTile * kTile
+constexpr int kFlagLeaf = 1;
+constexpr int kFlagVirtual = 2;
+// tarch::la comparison tolerance (same constant as the oracle).
+constexpr double kTarchEps = 1.0e-8;
+
+__device__ __forceinline__ long long vol_new(const PatchDev &p) { return (long long)p.nx * p.ny; }
+__device__ __forceinline__ long long vol_old(const PatchDev &p) {
+  return (long long)(p.nx + 2 * p.g) * (p.ny + 2 * p.g);
+}
+__device__ __forceinline__ long long idx_unew(const PatchDev &p, int q, int x, int y) {
+  return p.off + q * vol_new(p) + (long long)x * p.ny + y;
+}
+__device__ __forceinline__ long long idx_uold(const PatchDev &p, int q, int x, int y) {
+  return p.off + p.nq * vol_new(p) + q * vol_old(p) + (long long)(x + p.g) * (p.ny + 2 * p.g) +
+         (y + p.g);
+}
+__device__ __forceinline__ long long idx_pw(const PatchDev &p, int k, int x, int y) {
+  return p.off + p.nq * vol_new(p) + p.nq * vol_old(p) + p.np_wo * vol_new(p) + k * vol_old(p) +
+         (long long)(x + p.g) * (p.ny + 2 * p.g) + (y + p.g);
+}
+__device__ __forceinline__ long long idx_flux(const PatchDev &p, int q, int c, int dim, int dir) {
+  long long base = p.off + p.nq * vol_new(p) + p.nq * vol_old(p) + p.np_wo * vol_new(p) +
+                   p.np_w * vol_old(p);
+  long long qs0 = p.ny, qs1 = p.nx;
+  long long f1 = qs0 * p.nq, f2 = f1 + qs0 * p.nq, f3 = f2 + qs1 * p.nq;
+  int k = 2 * dim + (1 + dir) / 2;
+  long long fo = (k == 0) ? 0 : (k == 1) ? f1 : (k == 2) ? f2 : f3;
+  return base + fo + c + q * (dim == 0 ? qs0 : qs1);
+}
+
+__device__ __forceinline__ bool is_leaf(const PatchDev &p) { return (p.flags & kFlagLeaf) != 0; }
+__device__ __forceinline__ bool is_virtual(const PatchDev &p) { return (p.flags & kFlagVirtual) != 0; }
+
+// TimeIntervals::getTimeUOld / getTimeUNew (src/peanoclaw/grid/TimeIntervals.cpp:102-123)
+__device__ __forceinline__ double time_uold(const PatchDev &p, const PatchTimeDev &t) {
+  return is_leaf(p) ? t.time : t.min_nb_time;
+}
+__device__ __forceinline__ double time_unew(const PatchDev &p, const PatchTimeDev &t) {
+  return is_leaf(p) ? __dadd_rn(t.time, t.dt) : __dadd_rn(t.min_nb_time, t.max_nb_dt);
+}
+__device__ __forceinline__ bool tl_greater(double a, double b) { return __dsub_rn(a, b) > kTarchEps; }
+__device__ __forceinline__ bool tl_equals(double a, double b) {
+  return fabs(__dsub_rn(a, b)) <= kTarchEps;
+}
+
+__device__ __forceinline__ double subcell(const PatchDev &p, int d) {
+  return __ddiv_rn(p.size[d], (double)(d == 0 ? p.nx : p.ny));
+}
+// Patch::getSubcellCenter: (pos + h*i) + h*0.5
+__device__ __forceinline__ double subcell_center(const PatchDev &p, int d, int i) {
+  double h = subcell(p, d);
+  return __dadd_rn(__dadd_rn(p.pos[d], __dmul_rn(h, (double)i)), __dmul_rn(h, 0.5));
+}
+// SubgridIterator::getCellPosition: pos + i * (size * (1/n))
+__device__ __forceinline__ double iter_sub(const PatchDev &p, int d) {
+  return __dmul_rn(p.size[d], __ddiv_rn(1.0, (double)(d == 0 ? p.nx : p.ny)));
+}
+__device__ __forceinline__ double iter_pos(const PatchDev &p, int d, int i) {
+  return __dadd_rn(p.pos[d], __dmul_rn((double)i, iter_sub(p, d)));
+}
+
+// Positive doubles order like their bit patterns; used for exact max/min
+// reductions with integer atomics.
+__device__ __forceinline__ unsigned long long dbits(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+__device__ __forceinline__ double bitsd(unsigned long long b) {
+  return __longlong_as_double((long long)b);
+}
+
+// ---------------------------------------------------------------------------
+// f-wave edge solve (same operation sequence as the oracle's fwave_derived).
+// Cell quantities: h, hu (normal momentum, zero for dry cells), b, s = sqrt(h),
+// p = hu / s, F = p*p; wet = h > dry_tol.
+// ---------------------------------------------------------------------------
+struct CellQ {
+  double h, hu, b, s, p, F;
+  bool wet;
+};
+
+__device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu, double hv,
+                                             double b, CellQ &cx, CellQ &cy) {
+  bool wet = h > dry_tol;
+  cx.h = h; cx.b = b; cx.wet = wet;
+  cy.h = h; cy.b = b; cy.wet = wet;
+  if (wet) {
+    double s = __dsqrt_rn(h);
+    double rs = __ddiv_rn(1.0, s);
+    double p = __dmul_rn(hu, rs);
+    double q = __dmul_rn(hv, rs);
+    cx.s = s; cx.p = p; cx.F = __dmul_rn(p, p); cx.hu = hu;
+    cy.s = s; cy.p = q; cy.F = __dmul_rn(q, q); cy.hu = hv;
+  } else {
+    cx.s = 0.0; cx.p = 0.0; cx.F = 0.0; cx.hu = 0.0;
+    cy.s = 0.0; cy.p = 0.0; cy.F = 0.0; cy.hu = 0.0;
+  }
+}
+
+// out: Lh, Lhu, Rh, Rhu (net updates of the left/right cell) and the edge's
+// max wave speed.
+__device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, double &Lh,
+                                           double &Lhu, double &Rh, double &Rhu, double &speed) {
+  if (!L.wet && !R.wet) {
+    Lh = Lhu = Rh = Rhu = speed = 0.0;
+    return;
+  }
+  bool wallR = L.wet && !R.wet && (__dadd_rn(L.h, L.b) <= R.b);
+  bool wallL = R.wet && !L.wet && (__dadd_rn(R.h, R.b) <= L.b);
+  if (wallR) { R.h = L.h; R.hu = -L.hu; R.b = L.b; R.s = L.s; R.p = -L.p; R.F = L.F; }
+  if (wallL) { L.h = R.h; L.hu = -R.hu; L.b = R.b; L.s = R.s; L.p = -R.p; L.F = R.F; }
+  double a = __dmul_rn(halfg, __dadd_rn(L.h, R.h));
+  double cb = __dsqrt_rn(a);
+  double ub = __ddiv_rn(__dadd_rn(L.p, R.p), __dadd_rn(L.s, R.s));
+  double l1 = __dsub_rn(ub, cb);
+  double l2 = __dadd_rn(ub, cb);
+  double df1 = __dsub_rn(R.hu, L.hu);
+  double deta = __dadd_rn(__dsub_rn(R.h, L.h), __dsub_rn(R.b, L.b));
+  double df2 = __fma_rn(a, deta, __dsub_rn(R.F, L.F));
+  double inv = __ddiv_rn(1.0, __dsub_rn(l2, l1));
+  double b1 = __dmul_rn(__fma_rn(l2, df1, -df2), inv);
+  double b2 = __dmul_rn(__fma_rn(-l1, df1, df2), inv);
+  double z1 = __dmul_rn(b1, l1);
+  double z2 = __dmul_rn(b2, l2);
+  if (l1 < 0.0) {
+    if (l2 < 0.0) {
+      Lh = __dadd_rn(b1, b2); Lhu = __dadd_rn(z1, z2); Rh = 0.0; Rhu = 0.0;
+    } else {
+      Lh = b1; Lhu = z1; Rh = b2; Rhu = z2;
+    }
+  } else {
+    Lh = 0.0; Lhu = 0.0; Rh = __dadd_rn(b1, b2); Rhu = __dadd_rn(z1, z2);
+  }
+  if (wallR) { Rh = 0.0; Rhu = 0.0; }
+  if (wallL) { Lh = 0.0; Lhu = 0.0; }
+  speed = fmax(fabs(l1), fabs(l2));
+}
+
+// CFL timestep of a block whose maximum wave speed is s
+// (tools/SWE_WaveAccumulationBlock.cpp:225-239).
+__device__ __forceinline__ double cfl_dt(const SweParamsDev &prm, double s, double dx, double dy) {
+  if (s > prm.s_min) return __dmul_rn(prm.cfl, fmin(__ddiv_rn(dx, s), __ddiv_rn(dy, s)));
+  return prm.dt_inf;
+}
+
+}  // namespace pcg

@@ -1,0 +1,935 @@
+// pcg_kernels.cu -- CUDA kernels (sm_103a) of the SWE patch-update path.
+//
+// Kernels and the reference code each one replaces:
+//   k_sweep_tiles / k_update_tiles  SWE_WaveAccumulationBlock::computeNumericalFluxes
+//                                    + updateUnknowns (tools/SWE_WaveAccumulationBlock.cpp:84-296)
+//                                    + SWEKernel::advanceBlockInTime swap/time update
+//                                    (src/peanoclaw/native/SWEKernel.cpp:50-88)
+//   k_solve_patch                    SWEKernel::solveTimestep, fused, one CTA per patch
+//   k_ghost_items / k_walls          GhostLayerCompositor face/corner functors ->
+//                                    DefaultTransfer / SWE interpolation, SWEKernel::fillBoundaryLayer
+//   k_restrict                       DefaultRestriction (+ SWE h+b wrapping)
+//   k_compute_fluxes / k_flux_corr   DefaultFluxCorrection
+#include "pcg_device.cuh"
+#include "pcg_kernels.h"
+
+namespace pcg {
+
+// ===========================================================================
+// Sweep: one 16x16 (or smaller) tile per CTA iteration.
+// ===========================================================================
+struct SweepSmem {
+  double h[kTile + 2][kTile + 2];
+  double b[kTile + 2][kTile + 2];
+  double hu[kTile + 2][kTile + 2];
+  double hv[kTile + 2][kTile + 2];
+  double s[kTile + 2][kTile + 2];
+  double p[kTile + 2][kTile + 2];
+  double q[kTile + 2][kTile + 2];
+  double F[kTile + 2][kTile + 2];
+  double G[kTile + 2][kTile + 2];
+  unsigned char wet[kTile + 2][kTile + 2];
+  double xl_h[kTile][kTile], xl_hu[kTile][kTile];  // left-going parts of x-edges
+  double yl_h[kTile][kTile], yl_hv[kTile][kTile];  // down-going parts of y-edges
+  double red[kSweepThreads / 32];
+};
+
+__device__ __forceinline__ CellQ load_x(const SweepSmem &S, int i, int j) {
+  CellQ c;
+  c.h = S.h[i][j]; c.b = S.b[i][j]; c.hu = S.hu[i][j]; c.s = S.s[i][j]; c.p = S.p[i][j];
+  c.F = S.F[i][j]; c.wet = S.wet[i][j] != 0;
+  return c;
+}
+__device__ __forceinline__ CellQ load_y(const SweepSmem &S, int i, int j) {
+  CellQ c;
+  c.h = S.h[i][j]; c.b = S.b[i][j]; c.hu = S.hv[i][j]; c.s = S.s[i][j]; c.p = S.q[i][j];
+  c.F = S.G[i][j]; c.wet = S.wet[i][j] != 0;
+  return c;
+}
+
+// Computes the net updates of one tile.  The state is read from `interior`
+// (uNew in the batched form, uOld in the fused solveTimestep form) for cells
+// inside the patch and from uOld for the ghost ring.  Returns, in the calling
+// thread, the accumulated net updates of its cell (valid iff t < tw*th) and
+// the tile's max wave speed (valid in every thread).
+__device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restrict__ slab,
+                                             const PatchDev &P, const SweParamsDev &prm,
+                                             int x0, int y0, int tw, int th, bool interior_is_unew,
+                                             double &nh, double &nhu, double &nhv) {
+  const int t = threadIdx.x;
+  const double dry = prm.dry_tol;
+  // ---- stage tile + halo (corners skipped: the 5-point sweep never reads them)
+  const int sw = tw + 2, sh = th + 2;
+  for (int k = t; k < sw * sh; k += blockDim.x) {
+    int sx = k / sh, sy = k - sx * sh;
+    bool cx = (sx == 0 || sx == sw - 1), cy = (sy == 0 || sy == sh - 1);
+    if (cx && cy) continue;
+    int x = x0 - 1 + sx, y = y0 - 1 + sy;
+    bool inside = (x >= 0 && x < P.nx && y >= 0 && y < P.ny);
+    double h, hu, hv;
+    if (inside && interior_is_unew) {
+      h = slab[idx_unew(P, 0, x, y)];
+      hu = slab[idx_unew(P, 1, x, y)];
+      hv = slab[idx_unew(P, 2, x, y)];
+    } else {
+      h = slab[idx_uold(P, 0, x, y)];
+      hu = slab[idx_uold(P, 1, x, y)];
+      hv = slab[idx_uold(P, 2, x, y)];
+    }
+    double b = slab[idx_pw(P, 0, x, y)];
+    CellQ qx, qy;
+    cell_derived(dry, h, hu, hv, b, qx, qy);
+    S.h[sx][sy] = h; S.b[sx][sy] = b; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
+    S.s[sx][sy] = qx.s; S.p[sx][sy] = qx.p; S.q[sx][sy] = qy.p;
+    S.F[sx][sy] = qx.F; S.G[sx][sy] = qy.F; S.wet[sx][sy] = qx.wet ? 1 : 0;
+  }
+  __syncthreads();
+  const double halfg = __dmul_rn(0.5, prm.g);
+  double smax = 0.0;
+  double xr_h = 0.0, xr_hu = 0.0, yr_h = 0.0, yr_hv = 0.0;
+  const bool active = t < tw * th;
+  const int lx = active ? t / th : 0, ly = active ? t - (t / th) * th : 0;
+  if (active) {
+    double Lh, Lhu, Rh, Rhu, sp;
+    // x-edge between (lx-1, ly) and (lx, ly)
+    fwave_edge(halfg, load_x(S, lx, ly + 1), load_x(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
+    smax = fmax(smax, sp);
+    xr_h = Rh; xr_hu = Rhu;
+    if (lx >= 1) { S.xl_h[lx - 1][ly] = Lh; S.xl_hu[lx - 1][ly] = Lhu; }
+    // y-edge between (lx, ly-1) and (lx, ly)
+    fwave_edge(halfg, load_y(S, lx + 1, ly), load_y(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
+    smax = fmax(smax, sp);
+    yr_h = Rh; yr_hv = Rhu;
+    if (ly >= 1) { S.yl_h[lx][ly - 1] = Lh; S.yl_hv[lx][ly - 1] = Lhu; }
+  }
+  // closing edges on the upper x and y side of the tile
+  if (t < th + tw) {
+    double Lh, Lhu, Rh, Rhu, sp;
+    if (t < th) {
+      int j = t;
+      fwave_edge(halfg, load_x(S, tw, j + 1), load_x(S, tw + 1, j + 1), Lh, Lhu, Rh, Rhu, sp);
+      S.xl_h[tw - 1][j] = Lh; S.xl_hu[tw - 1][j] = Lhu;
+    } else {
+      int i = t - th;
+      fwave_edge(halfg, load_y(S, i + 1, th), load_y(S, i + 1, th + 1), Lh, Lhu, Rh, Rhu, sp);
+      S.yl_h[i][th - 1] = Lh; S.yl_hv[i][th - 1] = Lhu;
+    }
+    smax = fmax(smax, sp);
+  }
+  __syncthreads();
+  if (active) {
+    double dx = subcell(P, 0), dy = subcell(P, 1);
+    double dxi = __ddiv_rn(1.0, dx), dyi = __ddiv_rn(1.0, dy);
+    // accumulation order of computeNumericalFluxes: x-edges (own left edge,
+    // then right edge), then y-edges (own lower edge, then upper edge)
+    double a = __fma_rn(dxi, xr_h, 0.0);
+    a = __fma_rn(dxi, S.xl_h[lx][ly], a);
+    a = __fma_rn(dyi, yr_h, a);
+    nh = __fma_rn(dyi, S.yl_h[lx][ly], a);
+    double u = __fma_rn(dxi, xr_hu, 0.0);
+    nhu = __fma_rn(dxi, S.xl_hu[lx][ly], u);
+    double v = __fma_rn(dyi, yr_hv, 0.0);
+    nhv = __fma_rn(dyi, S.yl_hv[lx][ly], v);
+  }
+  // ---- tile max wave speed (speeds are >= 0: bit patterns order like values)
+  unsigned long long m = dbits(smax);
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long other = __shfl_xor_sync(0xffffffffu, m, o);
+    m = other > m ? other : m;
+  }
+  if ((t & 31) == 0) S.red[t >> 5] = bitsd(m);
+  __syncthreads();
+  unsigned long long r = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+    unsigned long long v = dbits(S.red[w]);
+    r = v > r ? v : r;
+  }
+  __syncthreads();  // S is reused by the next tile
+  return bitsd(r);
+}
+
+// Batched sweep: tiles [first, first + count) of the work list, grid-strided.
+// Net updates go to the uOld interior (free between the ghost fill and the
+// update), the tile's max speed to the patch and its CFL dt to the group.
+__global__ void __launch_bounds__(kSweepThreads)
+    k_sweep_tiles(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                  const TileItem *__restrict__ tiles, int first, int count, SweParamsDev prm,
+                  unsigned long long *__restrict__ patch_smax,
+                  unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active) {
+  __shared__ SweepSmem S;
+  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    TileItem ti = tiles[first + it];
+    PatchDev P = patches[ti.pid];
+    if (group_active && !group_active[P.group]) continue;
+    double nh = 0, nhu = 0, nhv = 0;
+    double smax = sweep_tile(S, slab, P, prm, ti.x0, ti.y0, ti.tw, ti.th, true, nh, nhu, nhv);
+    int t = threadIdx.x;
+    if (t < ti.tw * ti.th) {
+      int x = ti.x0 + t / ti.th, y = ti.y0 + t % ti.th;
+      slab[idx_uold(P, 0, x, y)] = nh;
+      slab[idx_uold(P, 1, x, y)] = nhu;
+      slab[idx_uold(P, 2, x, y)] = nhv;
+    }
+    if (t == 0) {
+      atomicMax(&patch_smax[ti.pid], dbits(smax));
+      double dtc = cfl_dt(prm, smax, subcell(P, 0), subcell(P, 1));
+      atomicMin(&group_dt[P.group], dbits(dtc));
+    }
+  }
+}
+
+// Batched update: q_new = q - dt * net (tools/SWE_WaveAccumulationBlock.cpp:247-296)
+// with the dry clamps, then the swap (uOld interior <- old state, uNew <- new)
+// and, once per patch, the time-interval update of advanceBlockInTime.
+__global__ void __launch_bounds__(kSweepThreads)
+    k_update_tiles(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                   PatchTimeDev *__restrict__ times, const TileItem *__restrict__ tiles, int first,
+                   int count, SweParamsDev prm, const unsigned long long *__restrict__ patch_smax,
+                   const unsigned long long *__restrict__ group_dt,
+                   const int *__restrict__ group_active) {
+  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    TileItem ti = tiles[first + it];
+    PatchDev P = patches[ti.pid];
+    if (group_active && !group_active[P.group]) continue;
+    double dt = bitsd(group_dt[P.group]);
+    int t = threadIdx.x;
+    if (t < ti.tw * ti.th) {
+      int x = ti.x0 + t / ti.th, y = ti.y0 + t % ti.th;
+      long long io0 = idx_uold(P, 0, x, y), io1 = idx_uold(P, 1, x, y), io2 = idx_uold(P, 2, x, y);
+      long long in0 = idx_unew(P, 0, x, y), in1 = idx_unew(P, 1, x, y), in2 = idx_unew(P, 2, x, y);
+      double h = slab[in0], hu = slab[in1], hv = slab[in2];
+      double nh = __fma_rn(-dt, slab[io0], h);
+      double nhu = __fma_rn(-dt, slab[io1], hu);
+      double nhv = __fma_rn(-dt, slab[io2], hv);
+      if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
+      if (nh < 0.0) nh = 0.0;
+      slab[io0] = h; slab[io1] = hu; slab[io2] = hv;
+      slab[in0] = nh; slab[in1] = nhu; slab[in2] = nhv;
+    }
+    if (t == 0 && ti.x0 == 0 && ti.y0 == 0) {
+      PatchTimeDev &T = times[ti.pid];
+      if (tl_greater(dt, 0.0)) {
+        T.time = __dadd_rn(T.time, T.dt);
+        T.dt = dt;
+      }
+      T.est_next = cfl_dt(prm, bitsd(patch_smax[ti.pid]), subcell(P, 0), subcell(P, 1));
+    }
+  }
+}
+
+// Start of a step: group dt <- max_dt, patch max speed <- 0.
+__global__ void k_reset_step(int n_groups, const double *__restrict__ group_max_dt,
+                             unsigned long long *__restrict__ group_dt, int n_patches,
+                             unsigned long long *__restrict__ patch_smax) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_groups) group_dt[i] = dbits(group_max_dt[i]);
+  for (int k = i; k < n_patches; k += gridDim.x * blockDim.x) patch_smax[k] = 0ull;
+}
+
+// Record the dt of every group after a step.
+__global__ void k_record_dt(int n_groups, const unsigned long long *__restrict__ group_dt,
+                            double *__restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_groups) out[i] = bitsd(group_dt[i]);
+}
+
+// ===========================================================================
+// Fused per-patch solve (SWEKernel::solveTimestep), one CTA per patch.
+// Input state: uOld (+ghost).  Net updates live in dynamic shared memory.
+// ===========================================================================
+__global__ void __launch_bounds__(kSweepThreads)
+    k_solve_patch(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                  PatchTimeDev *__restrict__ times, int pid, SweParamsDev prm, double max_dt,
+                  double *__restrict__ out) {
+  __shared__ SweepSmem S;
+  extern __shared__ double net[];  // 3 * nx * ny
+  const PatchDev P = patches[pid];
+  const int nx = P.nx, ny = P.ny;
+  double smax = 0.0;
+  for (int x0 = 0; x0 < nx; x0 += kTile)
+    for (int y0 = 0; y0 < ny; y0 += kTile) {
+      int tw = min(kTile, nx - x0), th = min(kTile, ny - y0);
+      double nh = 0, nhu = 0, nhv = 0;
+      double s = sweep_tile(S, slab, P, prm, x0, y0, tw, th, false, nh, nhu, nhv);
+      smax = fmax(smax, s);
+      int t = threadIdx.x;
+      if (t < tw * th) {
+        int x = x0 + t / th, y = y0 + t % th;
+        long long c = (long long)x * ny + y;
+        net[c] = nh;
+        net[(long long)nx * ny + c] = nhu;
+        net[2LL * nx * ny + c] = nhv;
+      }
+    }
+  __syncthreads();
+  double dx = subcell(P, 0), dy = subcell(P, 1);
+  double block_dt = cfl_dt(prm, smax, dx, dy);
+  double dt = fmin(block_dt, max_dt);
+  for (int c = threadIdx.x; c < nx * ny; c += blockDim.x) {
+    int x = c / ny, y = c - x * ny;
+    long long io0 = idx_uold(P, 0, x, y), io1 = idx_uold(P, 1, x, y), io2 = idx_uold(P, 2, x, y);
+    long long in0 = idx_unew(P, 0, x, y), in1 = idx_unew(P, 1, x, y), in2 = idx_unew(P, 2, x, y);
+    double nh = __fma_rn(-dt, net[c], slab[io0]);
+    double nhu = __fma_rn(-dt, net[(long long)nx * ny + c], slab[io1]);
+    double nhv = __fma_rn(-dt, net[2LL * nx * ny + c], slab[io2]);
+    if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
+    if (nh < 0.0) nh = 0.0;
+    // swapUNewAndUOld: uOld <- previous uNew, uNew <- updated values
+    double o0 = slab[in0], o1 = slab[in1], o2 = slab[in2];
+    slab[io0] = o0; slab[io1] = o1; slab[io2] = o2;
+    slab[in0] = nh; slab[in1] = nhu; slab[in2] = nhv;
+  }
+  if (threadIdx.x == 0) {
+    PatchTimeDev &T = times[pid];
+    if (tl_greater(dt, 0.0)) {
+      T.time = __dadd_rn(T.time, T.dt);
+      T.dt = dt;
+    }
+    T.est_next = block_dt;
+    out[0] = dt;
+    out[1] = block_dt;
+  }
+}
+
+// ===========================================================================
+// Ghost layers
+// ===========================================================================
+__device__ __forceinline__ double transfer_tf(const PatchDev &S, const PatchTimeDev &ST,
+                                              const PatchDev &D, const PatchTimeDev &DT) {
+  double dtu = time_unew(D, DT);
+  if (is_virtual(S)) return __ddiv_rn(__dsub_rn(dtu, 0.0), 1.0);
+  double su = time_unew(S, ST), so = time_uold(S, ST);
+  if (tl_greater(__dsub_rn(su, so), 0.0)) return __ddiv_rn(__dsub_rn(dtu, so), __dsub_rn(su, so));
+  return 1.0;
+}
+
+// DefaultTransferTemplate::transferGhostlayer body for cell k of the region.
+__device__ __forceinline__ void transfer_cell(double *slab, const PatchDev &S, const PatchDev &D,
+                                              const int size[2], const int so[2], const int dof[2],
+                                              double tf, double itf, int k) {
+  int x = k / size[1], y = k - x * size[1];
+  for (int q = 0; q < S.nq; q++) {
+    double vn = slab[idx_unew(S, q, so[0] + x, so[1] + y)];
+    double vo = slab[idx_uold(S, q, so[0] + x, so[1] + y)];
+    slab[idx_uold(D, q, dof[0] + x, dof[1] + y)] = __dadd_rn(__dmul_rn(vn, tf), __dmul_rn(vo, itf));
+  }
+}
+
+__device__ __forceinline__ double interp_tf(const PatchDev &S, const PatchTimeDev &ST,
+                                            const PatchDev &D, const PatchTimeDev &DT,
+                                            bool to_current, bool use_unew_uold) {
+  double tf;
+  if (tl_equals(ST.dt, 0.0)) {
+    tf = 1.0;
+  } else if (use_unew_uold) {
+    double so = time_uold(S, ST), su = time_unew(S, ST);
+    double num = to_current ? __dsub_rn(time_uold(D, DT), so) : __dsub_rn(time_unew(D, DT), so);
+    tf = __ddiv_rn(num, __dsub_rn(su, so));
+  } else {
+    double den = __dsub_rn(__dadd_rn(ST.time, ST.dt), ST.time);
+    double num = to_current ? __dsub_rn(DT.time, ST.time)
+                            : __dsub_rn(__dadd_rn(DT.time, DT.dt), ST.time);
+    tf = __ddiv_rn(num, den);
+  }
+  return fmax(0.0, fmin(1.0, tf));
+}
+
+// DefaultInterpolationTemplate::interpolateSolution body for destination cell
+// k of the region (clear uOld, d-linear stencil with time factor, SWE h+b wrap).
+__device__ void interp_cell(double *slab, const PatchDev &S, const PatchDev &D, const int size[2],
+                            const int dof[2], double tf, bool to_uold, bool swe, int k) {
+  double one_m_tf = __dsub_rn(1.0, tf);
+  int cx = dof[0] + k / size[1], cy = dof[1] + k % size[1];
+  for (int q = 0; q < D.nq; q++) slab[idx_uold(D, q, cx, cy)] = 0.0;
+  double sh[2] = {subcell(S, 0), subcell(S, 1)};
+  double inv[2] = {__ddiv_rn(1.0, sh[0]), __ddiv_rn(1.0, sh[1])};
+  double c[2] = {subcell_center(D, 0, cx), subcell_center(D, 1, cy)};
+  int bi[2];
+  int n[2] = {S.nx, S.ny};
+  for (int d = 0; d < 2; d++) {
+    double sbase = __dadd_rn(S.pos[d], __dmul_rn(sh[d], 0.5));
+    double local = __dsub_rn(c[d], sbase);
+    int v = (int)floor(__dmul_rn(local, inv[d]));
+    v = v < n[d] - 2 ? v : n[d] - 2;
+    bi[d] = v > 0 ? v : 0;
+  }
+  for (int kk = 0; kk < 4; kk++) {
+    int off[2] = {kk & 1, (kk >> 1) & 1};
+    int nxi = bi[0] + off[0], nyi = bi[1] + off[1];
+    double npos[2] = {subcell_center(S, 0, nxi), subcell_center(S, 1, nyi)};
+    double sf = 1.0;
+    for (int d = 0; d < 2; d++) {
+      double sign = (double)(1 - 2 * off[d]);
+      sf = __dmul_rn(sf, __dsub_rn(1.0, __dmul_rn(__dmul_rn(sign, __dsub_rn(c[d], npos[d])), inv[d])));
+    }
+    for (int q = 0; q < D.nq; q++) {
+      double so = slab[idx_uold(S, q, nxi, nyi)];
+      double sn = slab[idx_unew(S, q, nxi, nyi)];
+      if (swe && q == 0) {
+        double bb = slab[idx_pw(S, 0, nxi, nyi)];
+        so = __dadd_rn(so, bb);
+        sn = __dadd_rn(sn, bb);
+      }
+      if (to_uold) {
+        long long id = idx_uold(D, q, cx, cy);
+        slab[id] = __dadd_rn(slab[id], __dmul_rn(sf, __dadd_rn(__dmul_rn(so, one_m_tf), __dmul_rn(sn, tf))));
+      } else {
+        long long id = idx_unew(D, q, cx, cy);
+        slab[id] = __dadd_rn(__dadd_rn(slab[id], __dmul_rn(__dmul_rn(sf, so), one_m_tf)),
+                             __dmul_rn(__dmul_rn(sf, sn), tf));
+      }
+    }
+  }
+  if (swe) {
+    double bb = slab[idx_pw(D, 0, cx, cy)];
+    long long id = to_uold ? idx_uold(D, 0, cx, cy) : idx_unew(D, 0, cx, cy);
+    slab[id] = __dadd_rn(slab[id], __dmul_rn(-1.0, bb));
+  }
+}
+
+// Batched ghost fill: one warp per item.  Items write disjoint ghost cells.
+__global__ void k_ghost_items(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                              const PatchTimeDev *__restrict__ times,
+                              const GhostItemDev *__restrict__ items, int first, int count,
+                              const int *__restrict__ group_active) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int w = warp; w < count; w += nwarps) {
+    GhostItemDev it = items[first + w];
+    PatchDev S = patches[it.src], D = patches[it.dst];
+    if (group_active && !group_active[D.group]) continue;
+    PatchTimeDev ST = times[it.src], DT = times[it.dst];
+    int ncell = it.size[0] * it.size[1];
+    if (it.kind == 0) {
+      double tf = transfer_tf(S, ST, D, DT);
+      double itf = __dsub_rn(1.0, tf);
+      for (int k = lane; k < ncell; k += 32) transfer_cell(slab, S, D, it.size, it.src_off, it.dst_off, tf, itf, k);
+    } else {
+      double tf = interp_tf(S, ST, D, DT, false, true);
+      for (int k = lane; k < ncell; k += 32) interp_cell(slab, S, D, it.size, it.dst_off, tf, true, true, k);
+    }
+  }
+}
+
+// SWEKernel::fillBoundaryLayer for one face; reads interior cells from uNew
+// when `interior_from_unew` (the copy uNew -> uOld of SolveTimestep is implicit
+// in the batched form), ghost cells from uOld.
+__device__ __forceinline__ void wall_face(double *slab, const PatchDev &P, int dim, int up,
+                                          bool interior_from_unew, int lane, int nl) {
+  if (dim == 0) {
+    int xi = up ? P.nx : -1;
+    int sx = xi + (up ? -1 : 1);
+    for (int k = lane; k < (P.ny + 2) * P.nq; k += nl) {
+      int yi = k / P.nq - 1, q = k % P.nq;
+      bool inside = yi >= 0 && yi < P.ny;
+      double v = (interior_from_unew && inside) ? slab[idx_unew(P, q, sx, yi)] : slab[idx_uold(P, q, sx, yi)];
+      slab[idx_uold(P, q, xi, yi)] = (q == dim + 1) ? -v : v;
+    }
+  } else {
+    int yi = up ? P.ny : -1;
+    int sy = yi + (up ? -1 : 1);
+    for (int k = lane; k < (P.nx + 2) * P.nq; k += nl) {
+      int xi = k / P.nq - 1, q = k % P.nq;
+      bool inside = xi >= 0 && xi < P.nx;
+      double v = (interior_from_unew && inside) ? slab[idx_unew(P, q, xi, sy)] : slab[idx_uold(P, q, xi, sy)];
+      slab[idx_uold(P, q, xi, yi)] = (q == dim + 1) ? -v : v;
+    }
+  }
+}
+
+// Walls of the listed patches in the order of SolveTimestep::fillBoundaryLayers:
+// (0,lower), (1,upper), (0,upper), (1,lower).  One warp per patch.
+__global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                        const int *__restrict__ wall_patches, int count,
+                        const int *__restrict__ group_active) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int order[4][2] = {{0, 0}, {1, 1}, {0, 1}, {1, 0}};
+  for (int w = warp; w < count; w += nwarps) {
+    PatchDev P = patches[wall_patches[w]];
+    if (group_active && !group_active[P.group]) continue;
+    for (int f = 0; f < 4; f++) {
+      int d = order[f][0], up = order[f][1];
+      if (P.wall & (1 << (2 * d + up))) wall_face(slab, P, d, up, true, lane, 32);
+      __syncwarp();
+    }
+  }
+}
+
+// Plain form, one launch per patch: the patch's ghost items, then its walls.
+__global__ void k_fill_patch(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                             const PatchTimeDev *__restrict__ times,
+                             const GhostItemDev *__restrict__ items, int first, int count, int pid) {
+  int lane = threadIdx.x;
+  for (int w = 0; w < count; w++) {
+    GhostItemDev it = items[first + w];
+    PatchDev S = patches[it.src], D = patches[it.dst];
+    PatchTimeDev ST = times[it.src], DT = times[it.dst];
+    int ncell = it.size[0] * it.size[1];
+    if (it.kind == 0) {
+      double tf = transfer_tf(S, ST, D, DT);
+      double itf = __dsub_rn(1.0, tf);
+      for (int k = lane; k < ncell; k += blockDim.x) transfer_cell(slab, S, D, it.size, it.src_off, it.dst_off, tf, itf, k);
+    } else {
+      double tf = interp_tf(S, ST, D, DT, false, true);
+      for (int k = lane; k < ncell; k += blockDim.x) interp_cell(slab, S, D, it.size, it.dst_off, tf, true, true, k);
+    }
+  }
+  __syncthreads();
+  PatchDev P = patches[pid];
+  const int order[4][2] = {{0, 0}, {1, 1}, {0, 1}, {1, 0}};
+  for (int f = 0; f < 4; f++) {
+    int d = order[f][0], up = order[f][1];
+    if (P.wall & (1 << (2 * d + up))) wall_face(slab, P, d, up, true, lane, blockDim.x);
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// Single Numerics operations (one launch each)
+// ===========================================================================
+__global__ void k_copy_unew_to_uold(double *slab, const PatchDev *patches, int pid) {
+  PatchDev P = patches[pid];
+  int n = P.nq * P.nx * P.ny;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int q = k / (P.nx * P.ny), r = k - q * P.nx * P.ny, x = r / P.ny, y = r - x * P.ny;
+    slab[idx_uold(P, q, x, y)] = slab[idx_unew(P, q, x, y)];
+  }
+}
+
+__global__ void k_fill_boundary_layer(double *slab, const PatchDev *patches, int pid, int dim, int up) {
+  PatchDev P = patches[pid];
+  wall_face(slab, P, dim, up, false, threadIdx.x, blockDim.x);
+}
+
+__global__ void k_transfer(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                           GhostItemDev it) {
+  PatchDev S = patches[it.src], D = patches[it.dst];
+  double tf = transfer_tf(S, times[it.src], D, times[it.dst]);
+  double itf = __dsub_rn(1.0, tf);
+  int ncell = it.size[0] * it.size[1];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ncell; k += gridDim.x * blockDim.x)
+    transfer_cell(slab, S, D, it.size, it.src_off, it.dst_off, tf, itf, k);
+}
+
+__global__ void k_interpolate(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                              GhostItemDev it, int to_uold, int to_current, int use_unew_uold, int swe) {
+  PatchDev S = patches[it.src], D = patches[it.dst];
+  double tf = interp_tf(S, times[it.src], D, times[it.dst], to_current != 0, use_unew_uold != 0);
+  int ncell = it.size[0] * it.size[1];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ncell; k += gridDim.x * blockDim.x)
+    interp_cell(slab, S, D, it.size, it.dst_off, tf, to_uold != 0, swe != 0, k);
+}
+
+// ---------------------------------------------------------------------------
+// Restriction
+// ---------------------------------------------------------------------------
+// Region::getRegionsOverlappedByNeighboringGhostlayers (Region.cpp:247-315)
+__device__ int regions_overlapped(const double lower[2], const double upper[2], const double sp[2],
+                                  const double ss[2], const double sub[2], const int n[2],
+                                  int off[8], int sz[8]) {
+  bool one_greater = false, one_ge = false, all_greater = true;
+  for (int d = 0; d < 2; d++) {
+    if (tl_greater(__dadd_rn(upper[d], sub[d]), lower[d])) one_greater = true;
+    if (__dsub_rn(upper[d], __dadd_rn(sp[d], ss[d])) >= -kTarchEps) one_ge = true;
+    if (!tl_greater(lower[d], sp[d])) all_greater = false;
+  }
+  if (one_greater || one_ge || !all_greater) {
+    for (int k = 0; k < 8; k++) { off[k] = 0; sz[k] = 0; }
+    sz[0] = n[0]; sz[1] = n[1];
+    return 1;
+  }
+  const double eps = 1e-12;
+  int lo[2], up[2];
+  for (int d = 0; d < 2; d++) {
+    double dl = __dadd_rn(__dmul_rn(__dsub_rn(lower[d], sp[d]), __ddiv_rn(1.0, sub[d])), eps);
+    double du = __dsub_rn(__dmul_rn(__dsub_rn(upper[d], sp[d]), __ddiv_rn(1.0, sub[d])), eps);
+    dl = fmin(2147483647.0, dl);
+    du = fmax(-2147483648.0, du);
+    int a = (int)floor(dl), b = (int)floor(du);
+    a = a < n[d] ? a : n[d];
+    b = b < n[d] ? b : n[d];
+    lo[d] = a > -1 ? a : -1;
+    up[d] = b > -1 ? b : -1;
+  }
+  for (int d = 0; d < 2; d++) {
+    int r0 = 2 * d, r1 = 2 * d + 1;
+    sz[2 * r0 + d] = up[d] + 1; off[2 * r0 + d] = 0;
+    sz[2 * r1 + d] = n[d] - lo[d]; off[2 * r1 + d] = lo[d];
+    for (int i = 0; i < d; i++) {
+      sz[2 * r0 + i] = -up[i] - 1 + lo[i]; off[2 * r0 + i] = up[i] + 1;
+      sz[2 * r1 + i] = sz[2 * r0 + i]; off[2 * r1 + i] = off[2 * r0 + i];
+    }
+    for (int i = d + 1; i < 2; i++) {
+      sz[2 * r0 + i] = n[i]; off[2 * r0 + i] = 0;
+      sz[2 * r1 + i] = n[i]; off[2 * r1 + i] = 0;
+    }
+  }
+  return 4;
+}
+
+// Region::mapToPatch (Region.cpp:174-206)
+__device__ void map_to_patch(const int roff[2], const int rsz[2], const PatchDev &S,
+                             const PatchDev &D, double eps, int ooff[2], int osz[2]) {
+  for (int d = 0; d < 2; d++) {
+    double ss = subcell(S, d), ds = subcell(D, d);
+    double position = __dmul_rn(ss, (double)roff[d]);
+    position = __dadd_rn(position, __dsub_rn(S.pos[d], D.pos[d]));
+    double ot = __ddiv_rn(__dadd_rn(position, eps), ds);
+    ooff[d] = (int)ot;
+    double size = __dmul_rn(ss, (double)(roff[d] + rsz[d]));
+    size = __dadd_rn(size, __dsub_rn(S.pos[d], D.pos[d]));
+    double st = __ddiv_rn(__dsub_rn(size, eps), ds);
+    st = __dsub_rn(st, (double)ooff[d]);
+    st = __dadd_rn(st, 1.0);
+    osz[d] = (int)st;
+  }
+}
+
+// One restriction of src into dst (DefaultRestrictionTemplate::restrictSolution),
+// executed by the whole CTA; regions are processed in order.
+__device__ void restrict_block(double *slab, const PatchDev &S, const PatchTimeDev &ST,
+                               const PatchDev &D, const PatchTimeDev &DT, bool only_overlapped,
+                               bool swe) {
+  int roff[8], rsz[8], nr;
+  int n[2] = {S.nx, S.ny};
+  if (only_overlapped) {
+    double sp[2] = {S.pos[0], S.pos[1]}, ss[2] = {S.size[0], S.size[1]};
+    double sub[2] = {subcell(S, 0), subcell(S, 1)};
+    nr = regions_overlapped(DT.rl, DT.ru, sp, ss, sub, n, roff, rsz);
+  } else {
+    nr = 1;
+    roff[0] = 0; roff[1] = 0; rsz[0] = n[0]; rsz[1] = n[1];
+  }
+  const double eps = 1e-12;
+  double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
+  double dsub[2] = {iter_sub(D, 0), iter_sub(D, 1)};
+  double dvol = __dmul_rn(dsub[0], dsub[1]);
+  double tfo = 1.0, tfn = 1.0;
+  if (tl_greater(ST.dt, 0.0)) {
+    double so = time_uold(S, ST), su = time_unew(S, ST);
+    tfo = __ddiv_rn(__dsub_rn(0.0, so), __dsub_rn(su, so));
+    tfn = __ddiv_rn(__dsub_rn(1.0, so), __dsub_rn(su, so));
+  }
+  for (int r = 0; r < nr; r++) {
+    const int *ro = &roff[2 * r], *rs = &rsz[2 * r];
+    if (only_overlapped && !(rs[0] > 0 && rs[1] > 0)) continue;
+    int doff[2], dsz[2];
+    map_to_patch(ro, rs, S, D, eps, doff, dsz);
+    int ncell = dsz[0] > 0 && dsz[1] > 0 ? dsz[0] * dsz[1] : 0;
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) {
+      int x = doff[0] + k / dsz[1], y = doff[1] + k % dsz[1];
+      double dpos[2] = {iter_pos(D, 0, x), iter_pos(D, 1, y)};
+      int coff[2], csz[2];
+      for (int d = 0; d < 2; d++) {
+        double ot = __ddiv_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
+        int o = (int)ot;
+        double st = __ddiv_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
+        st = __dsub_rn(st, ot);
+        st = __dadd_rn(st, 1.0);
+        int up = o + (int)st;
+        int rup = ro[d] + rs[d];
+        int oo = o > ro[d] ? o : ro[d];
+        int uu = up < rup ? up : rup;
+        coff[d] = oo;
+        csz[d] = uu - oo;
+      }
+      for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++)
+        for (int sy = coff[1]; sy < coff[1] + csz[1]; sy++) {
+          double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
+          double region = 1.0;
+          for (int d = 0; d < 2; d++) {
+            double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
+            double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
+            region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
+            region = fmax(region, 0.0);
+          }
+          for (int q = 0; q < D.nq; q++) {
+            double vo = slab[idx_uold(S, q, sx, sy)];
+            double vn = slab[idx_unew(S, q, sx, sy)];
+            if (swe && q == 0) {
+              double bb = slab[idx_pw(S, 0, sx, sy)];
+              vo = __dadd_rn(vo, bb);
+              vn = __dadd_rn(vn, bb);
+            }
+            double d_o = __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, __dsub_rn(1.0, tfo)), __dmul_rn(vn, tfo)), region), dvol);
+            double d_n = __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, __dsub_rn(1.0, tfn)), __dmul_rn(vn, tfn)), region), dvol);
+            long long io = idx_uold(D, q, x, y), in = idx_unew(D, q, x, y);
+            slab[io] = __dadd_rn(slab[io], d_o);
+            slab[in] = __dadd_rn(slab[in], d_n);
+          }
+        }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_restrict(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                           int src, int dst, int only_overlapped, int swe) {
+  restrict_block(slab, patches[src], times[src], patches[dst], times[dst], only_overlapped != 0, swe != 0);
+}
+
+// Batched restriction: block b handles the items [begin[b], begin[b+1]) that
+// all share one destination, in list order.
+__global__ void k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                 const int4 *items, const int *begin) {
+  for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
+    int4 it = items[k];  // src, dst, only_overlapped, swe
+    restrict_block(slab, patches[it.x], times[it.x], patches[it.y], times[it.y], it.z != 0, it.w != 0);
+    __syncthreads();
+  }
+}
+
+__global__ void k_post_process_restriction(double *slab, const PatchDev *patches, const int *ids, int count) {
+  PatchDev P = patches[ids[blockIdx.x % count]];
+  if ((int)blockIdx.x >= count) return;
+  for (int c = threadIdx.x; c < P.nx * P.ny; c += blockDim.x) {
+    int x = c / P.ny, y = c % P.ny;
+    double bb = slab[idx_pw(P, 0, x, y)];
+    long long io = idx_uold(P, 0, x, y), in = idx_unew(P, 0, x, y);
+    slab[io] = __dadd_rn(slab[io], __dmul_rn(-1.0, bb));
+    slab[in] = __dadd_rn(slab[in], __dmul_rn(-1.0, bb));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Flux correction
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void compute_flux(int dim, const double u[3], double gf, double f[3]) {
+  double m = u[1 + dim];
+  f[0] = __dmul_rn(u[0], m);
+  f[1] = __dmul_rn(u[1], m);
+  f[2] = __dmul_rn(u[2], m);
+  f[1] = __dmul_rn(f[1], u[0]);
+  f[2] = __dmul_rn(f[2], u[0]);
+  double pr = __dmul_rn(__dmul_rn(__dmul_rn(0.5, gf), u[0]), u[0]);
+  f[1 + dim] = __dadd_rn(f[1 + dim], pr);
+}
+
+__global__ void k_compute_fluxes(double *slab, const PatchDev *patches, const int *ids, int count, double gf) {
+  if ((int)blockIdx.x >= count) return;
+  PatchDev P = patches[ids[blockIdx.x]];
+  int n[2] = {P.nx, P.ny};
+  int total = 2 * (n[1] + n[0]);
+  for (int k = threadIdx.x; k < total; k += blockDim.x) {
+    int dim, dir, c;
+    if (k < 2 * n[1]) { dim = 0; dir = (k < n[1]) ? -1 : 1; c = k % n[1]; }
+    else { int r = k - 2 * n[1]; dim = 1; dir = (r < n[0]) ? -1 : 1; c = r % n[0]; }
+    int inner = (dir == -1) ? 0 : n[dim] - 1;
+    int ghost = (dir == -1) ? -1 : n[dim];
+    double gu[3], iu[3], gfx[3], ifx[3];
+    for (int q = 0; q < 3; q++) {
+      int gx = dim == 0 ? ghost : c, gy = dim == 0 ? c : ghost;
+      int ix = dim == 0 ? inner : c, iy = dim == 0 ? c : inner;
+      gu[q] = slab[idx_uold(P, q, gx, gy)];
+      iu[q] = slab[idx_uold(P, q, ix, iy)];
+    }
+    compute_flux(dim, gu, gf, gfx);
+    compute_flux(dim, iu, gf, ifx);
+    for (int q = 0; q < 3; q++) slab[idx_flux(P, q, c, dim, dir)] = __dmul_rn(0.5, __dadd_rn(gfx[q], ifx[q]));
+  }
+}
+
+// DefaultFluxCorrectionTemplate::applyCorrection; the corrections of several
+// source cells can land in one destination cell, so a single thread applies
+// them in the reference's order.
+__global__ void k_flux_correction(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                  int src, int dst, int dim, int dir) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  PatchDev S = patches[src], D = patches[dst];
+  PatchTimeDev ST = times[src], DT = times[dst];
+  double lo = fmax(ST.time, DT.time);
+  double hi = fmin(__dadd_rn(ST.time, ST.dt), __dadd_rn(DT.time, DT.dt));
+  double tov = __dsub_rn(hi, lo);
+  int rdim = 0;
+  for (int d = 0; d < 2; d++) {
+    if (tl_greater(D.pos[d], S.pos[d])) rdim = d;
+    else if (tl_greater(S.pos[d], D.pos[d])) rdim = d;
+  }
+  double ssub[2] = {subcell(S, 0), subcell(S, 1)}, dsub[2] = {subcell(D, 0), subcell(D, 1)};
+  double dvol = __dmul_rn(dsub[0], dsub[1]);
+  int sn[2] = {S.nx, S.ny}, dn[2] = {D.nx, D.ny};
+  int other = 1 - dim;
+  const double heps = 1e-10;
+  for (int cs = 0; cs < sn[other]; cs++) {
+    int po = 1 - rdim;
+    double npos = __dadd_rn(S.pos[po], __dmul_rn(ssub[po], (double)cs));
+    double lb = fmax(D.pos[po], npos);
+    double ub = fmin(__dadd_rn(D.pos[po], dsub[po]), __dadd_rn(npos, ssub[po]));
+    int lbc = (int)__ddiv_rn(__dadd_rn(__dsub_rn(lb, D.pos[po]), heps), dsub[po]);
+    int ubc = (int)ceil(__ddiv_rn(__dsub_rn(__dsub_rn(ub, D.pos[po]), heps), dsub[po]));
+    double sF[3];
+    for (int q = 0; q < 3; q++) sF[q] = slab[idx_flux(S, q, cs, dim, dir)];
+    int dinner = (-dir == -1) ? 0 : dn[dim] - 1;
+    for (int cd = lbc; cd < ubc; cd++) {
+      double dF[3];
+      for (int q = 0; q < 3; q++) dF[q] = slab[idx_flux(D, q, cd, dim, -dir)];
+      double a1 = __dadd_rn(S.pos[other], __dmul_rn(__dadd_rn((double)cs, 1.0), ssub[other]));
+      double a2 = __dadd_rn(D.pos[other], __dmul_rn(__dadd_rn((double)cd, 1.0), dsub[other]));
+      double b1 = __dadd_rn(S.pos[other], __dmul_rn((double)cs, ssub[other]));
+      double b2 = __dadd_rn(D.pos[other], __dmul_rn((double)cd, dsub[other]));
+      double area = __dmul_rn(1.0, __dsub_rn(a1 < a2 ? a1 : a2, b1 > b2 ? b1 : b2));
+      if (area < 0.0) area = 0.0;
+      int ux = dim == 0 ? dinner : cd, uy = dim == 0 ? cd : dinner;
+      if (ux < 0 || uy < 0 || ux >= D.nx || uy >= D.ny) continue;
+      for (int q = 0; q < 3; q++) {
+        double corr = __ddiv_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF[q], dF[q]), tov), area), dvol);
+        long long id = idx_unew(D, q, ux, uy);
+        slab[id] = __dadd_rn(slab[id], corr);
+      }
+    }
+  }
+}
+
+// ===========================================================================
+// Host-side launchers
+// ===========================================================================
+cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                         const TileItem *tiles, int first, int count, const SweParamsDev &prm,
+                         unsigned long long *patch_smax, unsigned long long *group_dt,
+                         const int *group_active) {
+  if (count <= 0) return cudaSuccess;
+  k_sweep_tiles<<<grid, kSweepThreads, 0, st>>>(slab, patches, tiles, first, count, prm, patch_smax,
+                                                group_dt, group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                          PatchTimeDev *times, const TileItem *tiles, int first, int count,
+                          const SweParamsDev &prm, const unsigned long long *patch_smax,
+                          const unsigned long long *group_dt, const int *group_active) {
+  if (count <= 0) return cudaSuccess;
+  k_update_tiles<<<grid, kSweepThreads, 0, st>>>(slab, patches, times, tiles, first, count, prm,
+                                                 patch_smax, group_dt, group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_dt,
+                         unsigned long long *group_dt, int n_patches,
+                         unsigned long long *patch_smax) {
+  int n = n_groups > n_patches ? n_groups : n_patches;
+  int grid = (n + 255) / 256;
+  if (grid > 1024) grid = 1024;
+  if (grid < 1) grid = 1;
+  k_reset_step<<<grid, 256, 0, st>>>(n_groups, group_max_dt, group_dt, n_patches, patch_smax);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_record_dt(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
+                             double *out) {
+  k_record_dt<<<(n_groups + 127) / 128, 128, 0, st>>>(n_groups, group_dt, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_items(cudaStream_t st, double *slab, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev *items, int first,
+                               int count, const int *group_active) {
+  if (count <= 0) return cudaSuccess;
+  int warps_per_block = 8;
+  int grid = (count + warps_per_block - 1) / warps_per_block;
+  if (grid > 152 * 16) grid = 152 * 16;
+  k_ghost_items<<<grid, 32 * warps_per_block, 0, st>>>(slab, patches, times, items, first, count,
+                                                       group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
+                         const int *wall_patches, int count, const int *group_active) {
+  if (count <= 0) return cudaSuccess;
+  int grid = (count + 7) / 8;
+  if (grid > 152 * 16) grid = 152 * 16;
+  k_walls<<<grid, 256, 0, st>>>(slab, patches, wall_patches, count, group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,
+                              const PatchTimeDev *times, const GhostItemDev *items, int first,
+                              int count, int pid) {
+  k_fill_patch<<<1, 128, 0, st>>>(slab, patches, times, items, first, count, pid);
+  return cudaGetLastError();
+}
+
+cudaError_t sweep_occupancy(int *blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_tiles, kSweepThreads, 0);
+}
+
+size_t solve_patch_smem(int nx, int ny) { return sizeof(double) * 3 * (size_t)nx * ny; }
+
+cudaError_t prepare_solve_patch(size_t max_dynamic_smem) {
+  return cudaFuncSetAttribute(k_solve_patch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)max_dynamic_smem);
+}
+
+cudaError_t launch_solve_patch(cudaStream_t st, double *slab, const PatchDev *patches,
+                               PatchTimeDev *times, int pid, int nx, int ny,
+                               const SweParamsDev &prm, double max_dt, double *out) {
+  k_solve_patch<<<1, kSweepThreads, solve_patch_smem(nx, ny), st>>>(slab, patches, times, pid, prm,
+                                                                    max_dt, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_unew_to_uold(cudaStream_t st, double *slab, const PatchDev *patches, int pid,
+                                     int n) {
+  k_copy_unew_to_uold<<<(n + 255) / 256, 256, 0, st>>>(slab, patches, pid);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_boundary_layer(cudaStream_t st, double *slab, const PatchDev *patches,
+                                       int pid, int dim, int up) {
+  k_fill_boundary_layer<<<1, 128, 0, st>>>(slab, patches, pid, dim, up);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transfer(cudaStream_t st, double *slab, const PatchDev *patches,
+                            const PatchTimeDev *times, const GhostItemDev &it) {
+  int n = it.size[0] * it.size[1];
+  k_transfer<<<(n + 127) / 128, 128, 0, st>>>(slab, patches, times, it);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_interpolate(cudaStream_t st, double *slab, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev &it, int to_uold,
+                               int to_current, int use_unew_uold, int swe) {
+  int n = it.size[0] * it.size[1];
+  k_interpolate<<<(n + 127) / 128, 128, 0, st>>>(slab, patches, times, it, to_uold, to_current,
+                                                 use_unew_uold, swe);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patches,
+                            const PatchTimeDev *times, int src, int dst, int only_overlapped, int swe) {
+  k_restrict<<<1, 256, 0, st>>>(slab, patches, times, src, dst, only_overlapped, swe);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
+                                  const PatchTimeDev *times, const int4 *items, const int *begin,
+                                  int n_dst) {
+  if (n_dst <= 0) return cudaSuccess;
+  k_restrict_items<<<n_dst, 256, 0, st>>>(slab, patches, times, items, begin);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
+                                            const int *ids, int count) {
+  if (count <= 0) return cudaSuccess;
+  k_post_process_restriction<<<count, 256, 0, st>>>(slab, patches, ids, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
+                                  const int *ids, int count, double gf) {
+  if (count <= 0) return cudaSuccess;
+  k_compute_fluxes<<<count, 128, 0, st>>>(slab, patches, ids, count, gf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev *patches,
+                                   const PatchTimeDev *times, int src, int dst, int dim, int dir) {
+  k_flux_correction<<<1, 32, 0, st>>>(slab, patches, times, src, dst, dim, dir);
+  return cudaGetLastError();
+}
+
+}  // namespace pcg

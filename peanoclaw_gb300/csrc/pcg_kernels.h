@@ -1,0 +1,58 @@
+// pcg_kernels.h -- host-side launchers of the kernels in pcg_kernels.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pcg_device.cuh"
+
+namespace pcg {
+
+cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                         const TileItem *tiles, int first, int count, const SweParamsDev &prm,
+                         unsigned long long *patch_smax, unsigned long long *group_dt,
+                         const int *group_active);
+cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                          PatchTimeDev *times, const TileItem *tiles, int first, int count,
+                          const SweParamsDev &prm, const unsigned long long *patch_smax,
+                          const unsigned long long *group_dt, const int *group_active);
+cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_dt,
+                         unsigned long long *group_dt, int n_patches,
+                         unsigned long long *patch_smax);
+cudaError_t launch_record_dt(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
+                             double *out);
+cudaError_t launch_ghost_items(cudaStream_t st, double *slab, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev *items, int first,
+                               int count, const int *group_active);
+cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
+                         const int *wall_patches, int count, const int *group_active);
+cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,
+                              const PatchTimeDev *times, const GhostItemDev *items, int first,
+                              int count, int pid);
+size_t solve_patch_smem(int nx, int ny);
+cudaError_t sweep_occupancy(int *blocks_per_sm);
+cudaError_t prepare_solve_patch(size_t max_dynamic_smem);
+cudaError_t launch_solve_patch(cudaStream_t st, double *slab, const PatchDev *patches,
+                               PatchTimeDev *times, int pid, int nx, int ny,
+                               const SweParamsDev &prm, double max_dt, double *out);
+cudaError_t launch_copy_unew_to_uold(cudaStream_t st, double *slab, const PatchDev *patches, int pid,
+                                     int n);
+cudaError_t launch_fill_boundary_layer(cudaStream_t st, double *slab, const PatchDev *patches,
+                                       int pid, int dim, int up);
+cudaError_t launch_transfer(cudaStream_t st, double *slab, const PatchDev *patches,
+                            const PatchTimeDev *times, const GhostItemDev &it);
+cudaError_t launch_interpolate(cudaStream_t st, double *slab, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev &it, int to_uold,
+                               int to_current, int use_unew_uold, int swe);
+cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patches,
+                            const PatchTimeDev *times, int src, int dst, int only_overlapped, int swe);
+cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
+                                  const PatchTimeDev *times, const int4 *items, const int *begin,
+                                  int n_dst);
+cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
+                                            const int *ids, int count);
+cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
+                                  const int *ids, int count, double gf);
+cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev *patches,
+                                   const PatchTimeDev *times, int src, int dst, int dim, int dir);
+
+}  // namespace pcg

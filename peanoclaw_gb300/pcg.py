@@ -1,0 +1,270 @@
+"""ctypes binding of libpcg.so (include/pcg.h).
+
+The library is built in-tree by peanoclaw_gb300.build; importing this module
+never builds anything and never falls back to a CPU implementation: if the
+shared library is missing the import of `lib()` raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libpcg.so")
+
+PCG_OK = 0
+PCG_E_INVALID = -1
+PCG_E_NOMEM = -2
+PCG_E_CUDA = -3
+PCG_E_TIMEOUT = -4
+PCG_E_STATE = -5
+PCG_E_NUMERIC = -6
+
+PCG_PATCH_LEAF = 1
+PCG_PATCH_VIRTUAL = 2
+PCG_GHOST_COPY = 0
+PCG_GHOST_INTERP = 1
+PCG_MODE_PLAIN = 0
+PCG_MODE_BATCHED = 1
+
+FLT_MAX = float(np.finfo(np.float32).max)
+
+
+class SweParams(C.Structure):
+    _fields_ = [("g", C.c_double), ("cfl", C.c_double), ("dry_tol", C.c_double),
+                ("dry_tol_update", C.c_double), ("s_min", C.c_double), ("dt_inf", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_patches", C.c_int32), ("max_groups", C.c_int32),
+                ("reserved_", C.c_int32), ("slab_doubles", C.c_int64), ("params", SweParams)]
+
+
+class PatchDesc(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("ghost", C.c_int32), ("nq", C.c_int32),
+                ("np_wo", C.c_int32), ("np_w", C.c_int32), ("level", C.c_int32),
+                ("flags", C.c_int32), ("pos", C.c_double * 2), ("size", C.c_double * 2)]
+
+
+class PatchTime(C.Structure):
+    _fields_ = [("time", C.c_double), ("dt", C.c_double), ("est_next", C.c_double),
+                ("min_neighbor_time", C.c_double), ("max_neighbor_dt", C.c_double),
+                ("restr_lower", C.c_double * 2), ("restr_upper", C.c_double * 2)]
+
+
+class GhostItem(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("src", C.c_int32), ("dst", C.c_int32),
+                ("size", C.c_int32 * 2), ("src_offset", C.c_int32 * 2),
+                ("dst_offset", C.c_int32 * 2)]
+
+
+# every entry point declared in include/pcg.h: name -> (restype, argtypes)
+_CTX = C.c_void_p
+_I2 = C.POINTER(C.c_int32)
+_D = C.POINTER(C.c_double)
+SIGNATURES = {
+    "pcg_create": (C.c_int, [C.POINTER(Config), C.POINTER(_CTX)]),
+    "pcg_destroy": (C.c_int, [_CTX]),
+    "pcg_last_error": (C.c_char_p, []),
+    "pcg_slab_info": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "pcg_set_params": (C.c_int, [_CTX, C.POINTER(SweParams)]),
+    "pcg_patch_alloc": (C.c_int, [_CTX, C.POINTER(PatchDesc), C.POINTER(C.c_int32)]),
+    "pcg_patch_free": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_patch_vector_size": (C.c_int64, [C.POINTER(PatchDesc)]),
+    "pcg_patch_upload": (C.c_int, [_CTX, C.c_int32, _D, C.c_int64]),
+    "pcg_patch_download": (C.c_int, [_CTX, C.c_int32, _D, C.c_int64]),
+    "pcg_patches_upload": (C.c_int, [_CTX, C.c_int32, _I2, _D]),
+    "pcg_patches_download": (C.c_int, [_CTX, C.c_int32, _I2, _D]),
+    "pcg_patch_set_desc_flags": (C.c_int, [_CTX, C.c_int32, C.c_int32]),
+    "pcg_patch_set_time": (C.c_int, [_CTX, C.c_int32, C.POINTER(PatchTime)]),
+    "pcg_patch_get_time": (C.c_int, [_CTX, C.c_int32, C.POINTER(PatchTime)]),
+    "pcg_patch_set_boundary": (C.c_int, [_CTX, C.c_int32, C.c_uint32]),
+    "pcg_patch_set_group": (C.c_int, [_CTX, C.c_int32, C.c_int32]),
+    "pcg_copy_unew_to_uold": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_fill_boundary_layer": (C.c_int, [_CTX, C.c_int32, C.c_int32, C.c_int32]),
+    "pcg_solve_timestep": (C.c_int, [_CTX, C.c_int32, C.c_double, _D, _D]),
+    "pcg_transfer_ghostlayer": (C.c_int, [_CTX, _I2, _I2, _I2, C.c_int32, C.c_int32]),
+    "pcg_interpolate_solution": (C.c_int, [_CTX, _I2, _I2, C.c_int32, C.c_int32, C.c_int32,
+                                           C.c_int32, C.c_int32, C.c_int32]),
+    "pcg_restrict_solution": (C.c_int, [_CTX, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "pcg_post_process_restriction": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_compute_fluxes": (C.c_int, [_CTX, C.c_int32, C.c_double]),
+    "pcg_apply_flux_correction": (C.c_int, [_CTX, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "pcg_set_ghost_items": (C.c_int, [_CTX, C.POINTER(GhostItem), C.c_int32]),
+    "pcg_set_group_max_dt": (C.c_int, [_CTX, C.c_int32, C.c_double]),
+    "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
+    "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
+    "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "pcg_synchronize": (C.c_int, [_CTX]),
+}
+
+_lib = None
+
+
+class PcgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("pcg error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libpcg.so; raises if the CUDA library has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libpcg.so not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != PCG_OK:
+        raise PcgError(rc, lib().pcg_last_error().decode())
+    return rc
+
+
+def i2(v):
+    return (C.c_int32 * 2)(*[int(x) for x in v])
+
+
+def dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def swe_params(g=9.81, cfl=0.4, dry_tol=0.01, dry_tol_update=0.1, s_min=1e-5, dt_inf=FLT_MAX):
+    return SweParams(g, cfl, dry_tol, dry_tol_update, s_min, dt_inf)
+
+
+def vector_size(n, ghost=1, nq=3, np_wo=0, np_w=1):
+    nx, ny = (n, n) if np.isscalar(n) else n
+    vn, vo = nx * ny, (nx + 2 * ghost) * (ny + 2 * ghost)
+    return nq * vn + nq * vo + np_wo * vn + np_w * vo + 2 * nq * (nx + ny)
+
+
+class Context:
+    """A device context: one HBM slab with every patch vector resident."""
+
+    def __init__(self, slab_doubles, max_patches=1024, max_groups=1, params=None, device=0):
+        cfg = Config()
+        cfg.device = device
+        cfg.max_patches = max_patches
+        cfg.max_groups = max_groups
+        cfg.slab_doubles = int(slab_doubles)
+        cfg.params = params if params is not None else swe_params()
+        self.max_groups = max_groups
+        h = C.c_void_p()
+        check(lib().pcg_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().pcg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # patches --------------------------------------------------------------
+    def alloc(self, n, ghost=1, nq=3, np_wo=0, np_w=1, pos=(0.0, 0.0), size=(1.0, 1.0),
+              level=0, leaf=True, virtual=False):
+        nx, ny = (n, n) if np.isscalar(n) else n
+        size = (size, size) if np.isscalar(size) else size
+        d = PatchDesc(nx, ny, ghost, nq, np_wo, np_w, level,
+                      (PCG_PATCH_LEAF if leaf else 0) | (PCG_PATCH_VIRTUAL if virtual else 0),
+                      (C.c_double * 2)(*pos), (C.c_double * 2)(*size))
+        pid = C.c_int32()
+        check(lib().pcg_patch_alloc(self.h, C.byref(d), C.byref(pid)))
+        return pid.value
+
+    def free(self, pid):
+        check(lib().pcg_patch_free(self.h, pid))
+
+    def upload(self, pid, vec):
+        vec = np.ascontiguousarray(vec, dtype=np.float64)
+        check(lib().pcg_patch_upload(self.h, pid, dptr(vec), vec.size))
+
+    def download(self, pid, n):
+        out = np.empty(n, dtype=np.float64)
+        check(lib().pcg_patch_download(self.h, pid, dptr(out), n))
+        return out
+
+    def upload_many(self, ids, packed):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        packed = np.ascontiguousarray(packed, dtype=np.float64)
+        check(lib().pcg_patches_upload(self.h, len(ids), ids.ctypes.data_as(_I2), dptr(packed)))
+
+    def download_many(self, ids, total):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        out = np.empty(total, dtype=np.float64)
+        check(lib().pcg_patches_download(self.h, len(ids), ids.ctypes.data_as(_I2), dptr(out)))
+        return out
+
+    def set_time(self, pid, time=0.0, dt=0.0, est_next=0.0, min_neighbor_time=0.0,
+                 max_neighbor_dt=0.0, restr_lower=None, restr_upper=None):
+        big = np.finfo(np.float64).max
+        rl = restr_lower if restr_lower is not None else (big, big)
+        ru = restr_upper if restr_upper is not None else (-big, -big)
+        t = PatchTime(time, dt, est_next, min_neighbor_time, max_neighbor_dt,
+                      (C.c_double * 2)(*rl), (C.c_double * 2)(*ru))
+        check(lib().pcg_patch_set_time(self.h, pid, C.byref(t)))
+
+    def get_time(self, pid):
+        t = PatchTime()
+        check(lib().pcg_patch_get_time(self.h, pid, C.byref(t)))
+        return {"time": t.time, "dt": t.dt, "est_next": t.est_next,
+                "min_neighbor_time": t.min_neighbor_time, "max_neighbor_dt": t.max_neighbor_dt}
+
+    def set_boundary(self, pid, mask):
+        check(lib().pcg_patch_set_boundary(self.h, pid, int(mask)))
+
+    def set_group(self, pid, group):
+        check(lib().pcg_patch_set_group(self.h, pid, int(group)))
+
+    def set_flags(self, pid, leaf=True, virtual=False):
+        check(lib().pcg_patch_set_desc_flags(
+            self.h, pid, (PCG_PATCH_LEAF if leaf else 0) | (PCG_PATCH_VIRTUAL if virtual else 0)))
+
+    def slab_info(self):
+        f, t = C.c_int64(), C.c_int64()
+        check(lib().pcg_slab_info(self.h, C.byref(f), C.byref(t)))
+        return f.value, t.value
+
+    # batched ----------------------------------------------------------------
+    def set_ghost_items(self, items):
+        arr = (GhostItem * max(1, len(items)))()
+        for k, it in enumerate(items):
+            a = arr[k]
+            a.kind, a.src, a.dst = it["kind"], it["src"], it["dst"]
+            a.size[0], a.size[1] = it["size"]
+            a.src_offset[0], a.src_offset[1] = it.get("src_offset", (0, 0))
+            a.dst_offset[0], a.dst_offset[1] = it["dst_offset"]
+        check(lib().pcg_set_ghost_items(self.h, arr, len(items)))
+
+    def set_group_max_dt(self, group, max_dt):
+        check(lib().pcg_set_group_max_dt(self.h, group, float(max_dt)))
+
+    def step(self, mode=PCG_MODE_BATCHED):
+        out = np.zeros(self.max_groups)
+        check(lib().pcg_step(self.h, mode, dptr(out)))
+        return out
+
+    def run(self, steps, mode=PCG_MODE_BATCHED):
+        hist = np.zeros(steps * self.max_groups)
+        check(lib().pcg_run(self.h, steps, mode, dptr(hist)))
+        return hist.reshape(steps, self.max_groups)
+
+    def stats(self):
+        cu, ms = C.c_int64(), C.c_double()
+        check(lib().pcg_stats(self.h, C.byref(cu), C.byref(ms)))
+        return cu.value, ms.value
+
+    def synchronize(self):
+        check(lib().pcg_synchronize(self.h))

@@ -1,0 +1,195 @@
+"""Synthetic SWE workloads (patch sets, initial states, face-pair lists).
+
+A workload is a `PatchSet`: per patch its subdivision, position, size, level
+and domain-wall mask, the initial data vector of every patch in the
+reference layout (uNew holds h, hu, hv; the bathymetry b is a parameter with
+ghost layer, filled on the ghost ring too so that lake-at-rest states stay
+exactly still across patch faces), and the ghost-layer items a Peano
+traversal would issue for it (GhostlayerCompositorFunctors.cpp:23-221):
+same-size neighbours copy (transferGhostlayer), neighbours of another size
+interpolate (SWE interpolateSolution, h+b wrapped).
+
+Layout of one patch vector (src/peanoclaw/grid/LinearizationZYXQ.h:20-88):
+  [uNew 3*n*n][uOld 3*(n+2)^2][b (n+2)^2][fluxes 2*3*(n+n)]
+"""
+import numpy as np
+
+from .pcg import PCG_GHOST_COPY, PCG_GHOST_INTERP, vector_size
+
+NQ = 3
+
+
+class PatchSet:
+    def __init__(self):
+        self.n = []          # subdivision (square patches)
+        self.pos = []
+        self.size = []
+        self.level = []
+        self.wall = []
+        self.offsets = None  # start of each patch vector in `packed`
+        self.packed = None   # all patch vectors back to back
+        self.items = []
+        self.meta = {}
+
+    def __len__(self):
+        return len(self.n)
+
+    def vec_len(self, p):
+        return vector_size(self.n[p])
+
+    def vector(self, p):
+        o = self.offsets[p]
+        return self.packed[o: o + self.vec_len(p)]
+
+    def finalize_layout(self):
+        lens = np.array([vector_size(n) for n in self.n], dtype=np.int64)
+        self.offsets = np.zeros(len(lens), dtype=np.int64)
+        if len(lens) > 1:
+            self.offsets[1:] = np.cumsum(lens)[:-1]
+        self.packed = np.zeros(int(lens.sum()), dtype=np.float64)
+        return self
+
+    def views(self, p):
+        """uNew (3,n,n), uOld (3,n+2,n+2), b (n+2,n+2) views into packed."""
+        n = self.n[p]
+        v = self.vector(p)
+        a = NQ * n * n
+        o = NQ * (n + 2) * (n + 2)
+        return (v[:a].reshape(NQ, n, n), v[a:a + o].reshape(NQ, n + 2, n + 2),
+                v[a + o:a + o + (n + 2) * (n + 2)].reshape(n + 2, n + 2))
+
+    def cells(self):
+        return int(sum(n * n for n in self.n))
+
+
+def _centers(pos, size, n, ghost=True):
+    """Cell centres (Patch::getSubcellCenter) of the patch, with ghost ring."""
+    h0 = size[0] / n
+    h1 = size[1] / n
+    r = np.arange(-1, n + 1) if ghost else np.arange(n)
+    xs = (pos[0] + h0 * r) + h0 * 0.5
+    ys = (pos[1] + h1 * r) + h1 * 0.5
+    return np.meshgrid(xs, ys, indexing="ij")
+
+
+def _build_grid_items(ps, grid_index, nslots_x, nslots_y):
+    """Face and corner items for a regular grid of equally sized slots holding
+    patches of different subdivision.  Same subdivision: copy; otherwise
+    interpolation from the neighbour (its subcells are larger or smaller)."""
+    items = []
+    for sx in range(nslots_x):
+        for sy in range(nslots_y):
+            d = grid_index[sx, sy]
+            nd = ps.n[d]
+            for dx, dy in ((-1, 0), (1, 0), (0, -1), (0, 1), (-1, -1), (1, -1), (-1, 1), (1, 1)):
+                tx, ty = sx + dx, sy + dy
+                if not (0 <= tx < nslots_x and 0 <= ty < nslots_y):
+                    continue
+                s = grid_index[tx, ty]
+                ns = ps.n[s]
+                # direction from source to destination (functor convention)
+                dirv = (-dx, -dy)
+                size = [nd if v == 0 else 1 for v in dirv]
+                dst_off = [0 if v == 0 else (-1 if v == 1 else nd) for v in dirv]
+                if ns == nd:
+                    src_off = [0 if v == 0 else (nd - 1 if v == 1 else 0) for v in dirv]
+                    items.append({"kind": PCG_GHOST_COPY, "src": s, "dst": d, "size": size,
+                                  "src_offset": src_off, "dst_offset": dst_off})
+                else:
+                    items.append({"kind": PCG_GHOST_INTERP, "src": s, "dst": d, "size": size,
+                                  "src_offset": [0, 0], "dst_offset": dst_off})
+    return items
+
+
+def radial_dam_break(npx=9, n=16, radius=0.15, h_in=2.0, h_out=1.0):
+    """Regular grid of npx x npx patches of n x n cells on [0,1]^2, flat
+    bathymetry, h = h_in inside `radius` around the centre, reflecting walls."""
+    ps = PatchSet()
+    L = 1.0 / npx
+    grid = np.zeros((npx, npx), dtype=np.int64)
+    for i in range(npx):
+        for j in range(npx):
+            grid[i, j] = len(ps.n)
+            ps.n.append(n)
+            ps.pos.append((i * L, j * L))
+            ps.size.append((L, L))
+            ps.level.append(0)
+            m = 0
+            if i == 0: m |= 1
+            if i == npx - 1: m |= 2
+            if j == 0: m |= 4
+            if j == npx - 1: m |= 8
+            ps.wall.append(m)
+    ps.finalize_layout()
+    for p in range(len(ps)):
+        unew, uold, b = ps.views(p)
+        X, Y = _centers(ps.pos[p], ps.size[p], n, ghost=False)
+        r = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2)
+        unew[0] = np.where(r <= radius, h_in, h_out)
+        b[:] = 0.0
+    ps.items = _build_grid_items(ps, grid, npx, npx)
+    ps.meta = {"workload": "radial dam break, %dx%d patches of %dx%d cells" % (npx, npx, n, n)}
+    return ps
+
+
+def gaussian_sum_bathymetry(seed, k=32, amp=(-0.5, 0.5), sigma=(0.01, 0.1)):
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(amp[0], amp[1], k)
+    S = rng.uniform(sigma[0], sigma[1], k)
+    Cc = rng.uniform(0.0, 1.0, (k, 2))
+    return A, S, Cc
+
+
+def eval_bathymetry(X, Y, A, S, Cc):
+    b = np.zeros_like(X)
+    for a, s, c in zip(A, S, Cc):
+        b += a * np.exp(-((X - c[0]) ** 2 + (Y - c[1]) ** 2) / (2.0 * s * s))
+    return b
+
+
+def uneven_patches(grid=224, sizes=(8, 16, 32, 64), seed_sizes=1234, seed_bathy=1235,
+                   seed_perturb=1236, perturb=0.1):
+    """Mosaic of grid x grid equally sized slots on [0,1]^2, each holding one
+    patch whose subdivision is drawn uniformly from `sizes`; bathymetry is a sum
+    of 32 Gaussians, h = max(0, 1 - b) + perturb*U[-1,1] clamped >= 0, hu = hv = 0.
+    grid = 224 gives 50,176 patches (about 68 M cells)."""
+    rng = np.random.default_rng(seed_sizes)
+    choice = rng.integers(0, len(sizes), grid * grid)
+    ps = PatchSet()
+    L = 1.0 / grid
+    gi = np.zeros((grid, grid), dtype=np.int64)
+    k = 0
+    for i in range(grid):
+        for j in range(grid):
+            gi[i, j] = len(ps.n)
+            ps.n.append(int(sizes[choice[k]]))
+            k += 1
+            ps.pos.append((i * L, j * L))
+            ps.size.append((L, L))
+            ps.level.append(0)
+            m = 0
+            if i == 0: m |= 1
+            if i == grid - 1: m |= 2
+            if j == 0: m |= 4
+            if j == grid - 1: m |= 8
+            ps.wall.append(m)
+    ps.finalize_layout()
+    A, S, Cc = gaussian_sum_bathymetry(seed_bathy)
+    prng = np.random.default_rng(seed_perturb)
+    dry = 0
+    total = 0
+    for p in range(len(ps)):
+        n = ps.n[p]
+        unew, uold, b = ps.views(p)
+        X, Y = _centers(ps.pos[p], ps.size[p], n, ghost=True)
+        bb = eval_bathymetry(X, Y, A, S, Cc)
+        b[:] = bb
+        h = np.maximum(0.0, 1.0 - bb[1:-1, 1:-1]) + perturb * prng.uniform(-1.0, 1.0, (n, n))
+        h = np.maximum(h, 0.0)
+        unew[0] = h
+        dry += int(np.count_nonzero(h <= 0.01))
+        total += n * n
+    ps.items = _build_grid_items(ps, gi, grid, grid)
+    ps.meta = {"workload": "uneven patches %d x {%s}^2 cells" % (len(ps), ",".join(map(str, sizes))),
+               "dry_fraction": dry / max(1, total)}
+    return ps

@@ -1,0 +1,81 @@
+"""Shared test helpers: identical inputs for the CUDA path and the oracle."""
+import numpy as np
+
+from oracle import oracle as O
+from peanoclaw_gb300 import pcg as P
+
+
+def oracle_params(prm):
+    return O.swe_params(prm.g, prm.cfl, prm.dry_tol, prm.dry_tol_update, prm.s_min, prm.dt_inf)
+
+
+def random_swe_vector(rng, n, dry_fraction=0.2, lake=False, ghost_b=True):
+    """Patch vector (reference layout, ghost 1, 3 unknowns, b with ghost) with a
+    random wet/dry state in uNew and uOld (incl. ghost ring)."""
+    ln = P.vector_size(n)
+    v = np.zeros(ln)
+    a = 3 * n * n
+    o = 3 * (n + 2) ** 2
+    unew = v[:a].reshape(3, n, n)
+    uold = v[a:a + o].reshape(3, n + 2, n + 2)
+    b = v[a + o:a + o + (n + 2) ** 2].reshape(n + 2, n + 2)
+    b[:] = rng.uniform(-0.3, 0.6, (n + 2, n + 2))
+    if lake:
+        # dyadic values so that h + b is exact: a lake at rest with dry cells
+        b[:] = np.round(b * 64.0) / 64.0
+        eta = 0.5
+        h = np.maximum(0.0, eta - b)
+        uold[0] = h
+        unew[0] = h[1:-1, 1:-1]
+        return v
+    h = rng.uniform(0.0, 2.0, (n + 2, n + 2))
+    dry = rng.uniform(0, 1, (n + 2, n + 2)) < dry_fraction
+    h[dry] = rng.uniform(0.0, 0.02, dry.sum())
+    hu = rng.normal(0.0, 0.5, (n + 2, n + 2))
+    hv = rng.normal(0.0, 0.5, (n + 2, n + 2))
+    uold[0], uold[1], uold[2] = h, hu, hv
+    unew[0] = rng.uniform(0.0, 2.0, (n, n))
+    unew[1] = rng.normal(0.0, 0.5, (n, n))
+    unew[2] = rng.normal(0.0, 0.5, (n, n))
+    v[a + o + (n + 2) ** 2:] = rng.normal(0.0, 1.0, v.size - (a + o + (n + 2) ** 2))
+    return v
+
+
+def oracle_patch_from(vec, n, pos=(0.0, 0.0), size=(1.0, 1.0), level=0, time=0.0, dt=0.0,
+                      ghost=1, nq=3, np_wo=0, np_w=1, leaf=True, virtual=False,
+                      min_neighbor_time=0.0, max_neighbor_dt=0.0):
+    p = O.Patch(n, ghost=ghost, nq=nq, np_wo=np_wo, np_w=np_w, pos=pos, size=size, level=level,
+                time=time, dt=dt, is_leaf=leaf, is_virtual=virtual,
+                min_neighbor_time=min_neighbor_time, max_neighbor_dt=max_neighbor_dt)
+    assert p.u.size == vec.size
+    p.u[:] = vec
+    return p
+
+
+def oracle_patchset(ps):
+    pats = []
+    for p in range(len(ps)):
+        pats.append(oracle_patch_from(ps.vector(p).copy(), ps.n[p], ps.pos[p], ps.size[p],
+                                      ps.level[p]))
+    return pats
+
+
+def gpu_patchset(ctx, ps):
+    ids = []
+    for p in range(len(ps)):
+        pid = ctx.alloc(ps.n[p], pos=ps.pos[p], size=ps.size[p], level=ps.level[p])
+        ids.append(pid)
+        ctx.set_boundary(pid, ps.wall[p])
+    ctx.upload_many(ids, ps.packed)
+    items = []
+    for it in ps.items:
+        it2 = dict(it)
+        it2["src"] = ids[it["src"]]
+        it2["dst"] = ids[it["dst"]]
+        items.append(it2)
+    ctx.set_ghost_items(items)
+    return ids
+
+
+def slab_for(ps, slack=1.2):
+    return int(sum(P.vector_size(n) + 32 for n in ps.n) * slack) + 4096
