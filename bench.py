@@ -1,0 +1,338 @@
+"""Benchmark: SWE cell-updates/s of the batched GPU form on 50k uneven patches.
+
+Workload (the batching configuration): 224 x 224 = 50,176 patches with
+subdivision drawn uniformly from {8, 16, 32, 64}^2 (67.8 M cells, FP64), sum of
+32 Gaussians bathymetry with ~20% dry area, h = max(0, 1-b) + 0.1 U[-1,1],
+reflecting walls, g = 9.81, CFL 0.5.  A step is one synchronous timestep of
+every patch (ghost fill + f-wave sweep with CFL reduction + update), replayed
+from a captured CUDA graph.  The 4.1 GB of patch state is far larger than L2,
+so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--grid G] [--plain-steps P] [--no-e2e]
+
+`--impl reference` times the CPU restatement of the reference path (the
+reference's own SWE path cannot be built: Peano 3 and the TUM SWE sources are
+absent) with all host threads on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SWE cell-updates/s batched vs per-patch on 1 GB300; p50/p99 scenario latency"
+UNIT = "cell-updates/s"
+
+# Algorithmic FP64 work of one cell update (wet cell, subsonic edges), counted
+# from the f-wave operation list of pcg_device.cuh (FMA = 2 flops, divide and
+# square root = 1 flop each): per cell 6 ops (sqrt, 1/s, p, q, p^2, q^2); per
+# edge 19 plain ops + 3 FMA (2 edges per cell); accumulation 8 FMA; update 3 FMA.
+FLOP_PER_CELL = 6 + 2 * (19 + 2 * 3) + 2 * 8 + 2 * 3
+# Algorithmic bytes per patch step: read h, hu, hv, b with halo, write h, hu, hv.
+def bytes_per_patch(n):
+    return 8 * (4 * (n + 2) ** 2 + 3 * n * n)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", type=int, default=224)
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample-grid", type=int, default=48)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def dist_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def build_context(ps, prm):
+    from peanoclaw_gb300 import pcg as P
+    slab = int(sum(P.vector_size(n) + 32 for n in ps.n)) + 4096
+    ctx = P.Context(slab_doubles=slab, max_patches=len(ps) + 16, max_groups=1, params=prm)
+    ids = []
+    for p in range(len(ps)):
+        pid = ctx.alloc(ps.n[p], pos=ps.pos[p], size=ps.size[p], level=ps.level[p])
+        if ps.wall[p]:
+            ctx.set_boundary(pid, ps.wall[p])
+        ids.append(pid)
+    items = [dict(it, src=ids[it["src"]], dst=ids[it["dst"]]) for it in ps.items]
+    ctx.set_ghost_items(items)
+    return ctx, ids
+
+
+def cpu_baseline(args, prm, seconds_target=15.0):
+    """The oracle (CPU restatement, OpenMP over patches, all host threads) on a
+    bounded sample of the same generator: a G x G slot mosaic."""
+    from oracle import oracle as O
+    from peanoclaw_gb300 import scenarios as S
+    ps = S.uneven_patches(grid=args.cpu_sample_grid)
+    pats = []
+    for p in range(len(ps)):
+        op = O.Patch(ps.n[p], pos=ps.pos[p], size=ps.size[p])
+        op.u[:] = ps.vector(p)
+        pats.append(op)
+    oprm = O.swe_params(prm.g, prm.cfl, prm.dry_tol, prm.dry_tol_update, prm.s_min, prm.dt_inf)
+    threads = os.cpu_count() or 1
+    O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=threads)  # warm-up
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > seconds_target or steps >= 200:
+            break
+    cells = ps.cells()
+    return {"value": cells * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%dx%d-slot mosaic of the same generator (%d patches, %d cells), %d steps, %.1f s"
+                      % (args.cpu_sample_grid, args.cpu_sample_grid, len(ps), cells, steps, el)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    from peanoclaw_gb300 import pcg as P
+    prm = P.swe_params(g=9.81, cfl=0.5)
+    cb = cpu_baseline(args, prm, seconds_target=max(5.0, min(60.0, 2.0 * args.steps)))
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "uneven patches, sample of the 224x224-slot mosaic",
+                       "sample_grid": args.cpu_sample_grid},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    ws, rank, local = dist_info()
+    dist = dist_init(ws)
+    from peanoclaw_gb300 import pcg as P
+    from peanoclaw_gb300 import scenarios as S
+    prm = P.swe_params(g=9.81, cfl=0.5)
+    ps = S.uneven_patches(grid=args.grid)
+    cells = ps.cells()
+    ctx, ids = build_context(ps, prm)
+    ctx.upload_many(ids, ps.packed)
+    ctx.set_group_max_dt(0, 1e9)
+
+    # warm-up (also instantiates the graph)
+    ctx.run(max(1, args.warmup), P.PCG_MODE_BATCHED)
+    dist_barrier(dist)
+    ctx.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    cu0, ms0 = ctx.stats()
+    t0 = time.perf_counter()
+    ctx.run(args.steps, P.PCG_MODE_BATCHED)
+    ctx.synchronize()
+    wall = time.perf_counter() - t0
+    cu1, ms1 = ctx.stats()
+    dev_ms = ms1 - ms0
+    clk = clocks.stop()
+    dist_barrier(dist)
+    dev_s = dist_max(dist, dev_ms / 1e3)
+    value = ws * cells * args.steps / dev_s
+    ms_per_step = dev_s * 1e3 / args.steps
+
+    # per-phase device time of the batched step (CUDA events on the launch stream)
+    phases = np.array([ctx.profile_step() for _ in range(5)])
+    ph = phases.mean(axis=0)
+    sweep_ms = float(ph[3])
+    update_ms = float(ph[4])
+    fp64_peak = ctx.fp64_peak_tflops()
+    flops = FLOP_PER_CELL * cells
+    # the FP64 work sits in the sweep (and 3 FMA/cell in the update)
+    achieved = (flops / 1e12) / ((sweep_ms + update_ms) / 1e3)
+    alg_bytes = sum(bytes_per_patch(n) for n in ps.n)
+    hbm_peak = None
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        hbm_peak = mp.get("hbm_gbs")
+    except Exception:
+        pass
+    step_ms_phase = float(ph.sum())
+
+    # plain per-patch form (one launch per patch per phase), same workload
+    plain = None
+    if args.plain_steps > 0:
+        ctx.run(1, P.PCG_MODE_PLAIN)
+        ctx.synchronize()
+        c0, m0 = ctx.stats()
+        ctx.run(args.plain_steps, P.PCG_MODE_PLAIN)
+        c1, m1 = ctx.stats()
+        plain = cells * args.plain_steps / ((m1 - m0) / 1e3)
+
+    # end to end through the C ABI with host buffers: pinned upload of the
+    # state, `steps` timesteps (the dt of every step read back), download.
+    e2e = None
+    if not args.no_e2e:
+        import torch
+        pinned = torch.empty(ps.packed.size, dtype=torch.float64, pin_memory=True).numpy()
+        pinned[:] = ps.packed
+        out = torch.empty(ps.packed.size, dtype=torch.float64, pin_memory=True).numpy()
+        import ctypes as C
+        idarr = np.ascontiguousarray(ids, dtype=np.int32)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        P.check(P.lib().pcg_patches_upload(ctx.h, len(ids), idarr.ctypes.data_as(C.POINTER(C.c_int32)),
+                                           pinned.ctypes.data_as(C.POINTER(C.c_double))))
+        hist = ctx.run(args.steps, P.PCG_MODE_BATCHED)
+        P.check(P.lib().pcg_patches_download(ctx.h, len(ids), idarr.ctypes.data_as(C.POINTER(C.c_int32)),
+                                             out.ctypes.data_as(C.POINTER(C.c_double))))
+        e2e_s = time.perf_counter() - t0
+        e2e_s = dist_max(dist, e2e_s)
+        nbytes = int(ps.packed.nbytes)
+        e2e = {"value": ws * cells * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": nbytes // args.steps,
+               "d2h_bytes_per_step": nbytes // args.steps + 8,
+               "note": "one job = pinned upload of all patch vectors + %d timesteps (dt read back "
+                       "each step) + download; bytes are per timestep" % args.steps}
+        assert np.isfinite(hist).all()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and ws == 1:
+        cpu = cpu_baseline(args, prm)
+    ctx.close()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "batched persistent form, 50k uneven patches "
+                                   "(%d patches, {8,16,32,64}^2 cells, %d cells, %.1f%% dry), "
+                                   "radial-free random Gaussian bathymetry, 200-step config "
+                                   "timed over %d steps" % (len(ps), cells, 100 * ps.meta["dry_fraction"], args.steps),
+                       "patches": len(ps), "cells": cells, "grid_slots": args.grid,
+                       "l2": "inputs (%.1f GB) larger than L2, no flush" % (ps.packed.nbytes / 1e9),
+                       "parallelism": "replicas x%d" % ws if ws > 1 else "1 GPU"},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp64_peak, "traffic": None,
+                         "peak_source": "measured live (DFMA chain probe, FMA = 2 flops)",
+                         "flop_per_cell": FLOP_PER_CELL,
+                         "kernels": "k_sweep_tiles + k_update_tiles",
+                         "hbm": {"achieved_gbs": alg_bytes / (step_ms_phase / 1e3) / 1e9,
+                                 "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json",
+                                 "alg_bytes_per_step": alg_bytes}},
+            "phase_ms": {"reset": ph[0], "ghost_items": ph[1], "walls": ph[2], "sweep": ph[3],
+                         "update": ph[4]},
+            "plain_per_patch_value": plain,
+            "batched_over_plain": (value / ws) / plain if plain else None,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": 6 * args.steps,
+            "wall_s": wall,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

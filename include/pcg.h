@@ -197,6 +197,17 @@ int pcg_stats(pcg_context *ctx, int64_t *cell_updates, double *device_ms);
 /* Block until all work issued on the context has finished. */
 int pcg_synchronize(pcg_context *ctx);
 
+/* ----------------------------------------------------------- diagnostics */
+
+/* No counterpart in the reference.  One BATCHED step with CUDA events between
+ * its phases on the context stream; ms[5] receives the device time of
+ * reset, ghost items, walls, sweep and update. */
+int pcg_profile_step(pcg_context *ctx, double *ms);
+/* No counterpart in the reference.  Measures the FP64 FMA throughput of the
+ * context's device (dependent-chain loop on every SM); returns TFLOP/s with an
+ * FMA counted as two flops. */
+int pcg_probe_fp64_peak(pcg_context *ctx, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,17 @@ __global__ void k_record_hist(int n_groups, const unsigned long long *group_dt, 
   if (threadIdx.x == 0) *counter = idx + 1;
 }
 
+// FP64 FMA throughput probe: 8 independent dependent chains per thread.
+__global__ void k_fp64_probe(double *out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = __fma_rn(x0, a, b); x1 = __fma_rn(x1, a, b); x2 = __fma_rn(x2, a, b); x3 = __fma_rn(x3, a, b);
+    x4 = __fma_rn(x4, a, b); x5 = __fma_rn(x5, a, b); x6 = __fma_rn(x6, a, b); x7 = __fma_rn(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
 constexpr int64_t kAlign = 32;  // doubles (256 B)
 
 int64_t vector_size(const pcg_patch_desc &d) {
@@ -76,6 +87,7 @@ struct pcg_context {
   std::map<int64_t, int64_t> free_list;  // offset -> length
 
   int max_patches = 0, max_groups = 1;
+  int slot_hint = 0;
   std::vector<pcg::PatchDev> h_patches;
   std::vector<int64_t> h_len;
   std::vector<char> used;
@@ -467,8 +479,10 @@ int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
   if (!(d->size[0] > 0.0) || !(d->size[1] > 0.0)) return fail(PCG_E_INVALID, "patch size must be positive");
   std::lock_guard<std::mutex> lk(c->mu);
   int slot = -1;
-  for (int p = 0; p < c->max_patches; p++)
+  for (int k = 0; k < c->max_patches; k++) {
+    int p = (c->slot_hint + k) % c->max_patches;
     if (!c->used[p]) { slot = p; break; }
+  }
   if (slot < 0) return fail(PCG_E_NOMEM, "patch table full");
   int64_t len = vector_size(*d), off = 0;
   int rc = slab_alloc(c, len, &off);
@@ -489,9 +503,10 @@ int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
   const double big = 1.7976931348623157e308;
   t.rl[0] = t.rl[1] = big;
   t.ru[0] = t.ru[1] = -big;
+  // pageable source: the copy is staged before cudaMemcpyAsync returns
   PCG_CUDA(cudaMemcpyAsync(c->d_times + slot, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream));
-  PCG_CUDA(cudaStreamSynchronize(c->stream));
   c->patches_dirty = c->topo_dirty = true;
+  c->slot_hint = slot + 1;
   *id = slot;
   return PCG_OK;
 }
@@ -502,6 +517,7 @@ int pcg_patch_free(pcg_context *c, int32_t id) {
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   slab_free(c, c->h_patches[id].off, c->h_len[id]);
   c->used[id] = 0;
+  if (id < c->slot_hint) c->slot_hint = id;
   c->h_patches[id] = pcg::PatchDev{};
   c->patches_dirty = c->topo_dirty = true;
   return PCG_OK;
@@ -852,6 +868,67 @@ int pcg_stats(pcg_context *c, int64_t *cell_updates, double *device_ms) {
   if (!c) return fail(PCG_E_INVALID, "null context");
   if (cell_updates) *cell_updates = c->cell_updates;
   if (device_ms) *device_ms = c->device_ms;
+  return PCG_OK;
+}
+
+int pcg_profile_step(pcg_context *c, double *ms) {
+  if (!c || !ms) return fail(PCG_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  if ((rc = check_solvable(c)) != PCG_OK) return rc;
+  if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  cudaEvent_t ev[6];
+  for (int i = 0; i < 6; i++) PCG_CUDA(cudaEventCreate(&ev[i]));
+  using namespace pcg;
+  PCG_CUDA(cudaEventRecord(ev[0], c->stream));
+  PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
+                        c->d_patch_smax));
+  PCG_CUDA(cudaEventRecord(ev[1], c->stream));
+  PCG_CUDA(launch_ghost_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, 0,
+                              (int)c->h_items.size(), nullptr));
+  PCG_CUDA(cudaEventRecord(ev[2], c->stream));
+  PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
+  PCG_CUDA(cudaEventRecord(ev[3], c->stream));
+  PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
+                        (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+  PCG_CUDA(cudaEventRecord(ev[4], c->stream));
+  PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
+                         (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+  PCG_CUDA(cudaEventRecord(ev[5], c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < 5; i++) {
+    float t = 0.f;
+    PCG_CUDA(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+    ms[i] = t;
+  }
+  for (int i = 0; i < 6; i++) cudaEventDestroy(ev[i]);
+  c->cell_updates += c->cells_per_step;
+  return PCG_OK;
+}
+
+int pcg_probe_fp64_peak(pcg_context *c, double *tflops) {
+  if (!c || !tflops) return fail(PCG_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int blocks = c->num_sms * 8, threads = 256, iters = 4096;
+  double *buf = nullptr;
+  PCG_CUDA(cudaMalloc(&buf, sizeof(double) * (size_t)blocks * threads));
+  k_fp64_probe<<<blocks, threads, 0, c->stream>>>(buf, 64, 1.0000001, 1e-9);
+  PCG_CUDA(cudaGetLastError());
+  float best = 1e30f;
+  for (int r = 0; r < 3; r++) {
+    PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+    k_fp64_probe<<<blocks, threads, 0, c->stream>>>(buf, iters, 1.0000001, 1e-9);
+    PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+    PCG_CUDA(cudaEventSynchronize(c->ev1));
+    float t = 0.f;
+    PCG_CUDA(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+    best = std::min(best, t);
+  }
+  PCG_CUDA(cudaFree(buf));
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
   return PCG_OK;
 }
 

@@ -96,6 +96,8 @@ SIGNATURES = {
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "pcg_synchronize": (C.c_int, [_CTX]),
+    "pcg_profile_step": (C.c_int, [_CTX, _D]),
+    "pcg_probe_fp64_peak": (C.c_int, [_CTX, _D]),
 }
 
 _lib = None
@@ -268,3 +270,14 @@ class Context:
 
     def synchronize(self):
         check(lib().pcg_synchronize(self.h))
+
+    def profile_step(self):
+        """Device ms of (reset, ghost items, walls, sweep, update) of one batched step."""
+        ms = np.zeros(5)
+        check(lib().pcg_profile_step(self.h, dptr(ms)))
+        return ms
+
+    def fp64_peak_tflops(self):
+        v = C.c_double()
+        check(lib().pcg_probe_fp64_peak(self.h, C.byref(v)))
+        return v.value

@@ -147,11 +147,21 @@ def eval_bathymetry(X, Y, A, S, Cc):
     return b
 
 
+def bathymetry_lift(A, S, Cc, dry_area=0.2, samples=1024):
+    """Constant added to the Gaussian sum so that `dry_area` of the domain lies
+    above the still-water level 1 (the amplitude range alone keeps b < 1)."""
+    t = (np.arange(samples) + 0.5) / samples
+    X, Y = np.meshgrid(t, t, indexing="ij")
+    b = eval_bathymetry(X, Y, A, S, Cc)
+    return float(1.0 - np.quantile(b, 1.0 - dry_area))
+
+
 def uneven_patches(grid=224, sizes=(8, 16, 32, 64), seed_sizes=1234, seed_bathy=1235,
-                   seed_perturb=1236, perturb=0.1):
+                   seed_perturb=1236, perturb=0.1, dry_area=0.2):
     """Mosaic of grid x grid equally sized slots on [0,1]^2, each holding one
     patch whose subdivision is drawn uniformly from `sizes`; bathymetry is a sum
-    of 32 Gaussians, h = max(0, 1 - b) + perturb*U[-1,1] clamped >= 0, hu = hv = 0.
+    of 32 Gaussians lifted so that `dry_area` of the domain is above the still
+    water level, h = max(0, 1 - b) + perturb*U[-1,1] clamped >= 0, hu = hv = 0.
     grid = 224 gives 50,176 patches (about 68 M cells)."""
     rng = np.random.default_rng(seed_sizes)
     choice = rng.integers(0, len(sizes), grid * grid)
@@ -175,21 +185,38 @@ def uneven_patches(grid=224, sizes=(8, 16, 32, 64), seed_sizes=1234, seed_bathy=
             ps.wall.append(m)
     ps.finalize_layout()
     A, S, Cc = gaussian_sum_bathymetry(seed_bathy)
-    prng = np.random.default_rng(seed_perturb)
+    lift = bathymetry_lift(A, S, Cc, dry_area) if dry_area > 0 else 0.0
+    nall = np.array(ps.n)
+    cell_start = np.zeros(len(ps) + 1, dtype=np.int64)
+    cell_start[1:] = np.cumsum(nall * nall)
+    # one perturbation draw per interior cell, in patch order
+    pert = np.random.default_rng(seed_perturb).uniform(-1.0, 1.0, int(cell_start[-1]))
+    posx = np.array([q[0] for q in ps.pos])
+    posy = np.array([q[1] for q in ps.pos])
     dry = 0
-    total = 0
-    for p in range(len(ps)):
-        n = ps.n[p]
-        unew, uold, b = ps.views(p)
-        X, Y = _centers(ps.pos[p], ps.size[p], n, ghost=True)
-        bb = eval_bathymetry(X, Y, A, S, Cc)
-        b[:] = bb
-        h = np.maximum(0.0, 1.0 - bb[1:-1, 1:-1]) + perturb * prng.uniform(-1.0, 1.0, (n, n))
-        h = np.maximum(h, 0.0)
-        unew[0] = h
-        dry += int(np.count_nonzero(h <= 0.01))
-        total += n * n
+    for n in sizes:
+        idx = np.nonzero(nall == n)[0]
+        h0 = L / n
+        r = np.arange(-1, n + 1)
+        for c0 in range(0, len(idx), 1024):
+            sel = idx[c0:c0 + 1024]
+            xs = (posx[sel, None] + h0 * r[None, :]) + h0 * 0.5
+            ys = (posy[sel, None] + h0 * r[None, :]) + h0 * 0.5
+            X = np.broadcast_to(xs[:, :, None], (len(sel), n + 2, n + 2))
+            Y = np.broadcast_to(ys[:, None, :], (len(sel), n + 2, n + 2))
+            bb = eval_bathymetry(X, Y, A, S, Cc) + lift
+            pr = np.stack([pert[cell_start[p]:cell_start[p + 1]].reshape(n, n) for p in sel])
+            h = np.maximum(np.maximum(0.0, 1.0 - bb[:, 1:-1, 1:-1]) + perturb * pr, 0.0)
+            dry += int(np.count_nonzero(h <= 0.01))
+            base = ps.offsets[sel]
+            a = 3 * n * n
+            o = 3 * (n + 2) * (n + 2)
+            hi = base[:, None] + np.arange(n * n)[None, :]
+            ps.packed[hi] = h.reshape(len(sel), n * n)
+            bi = base[:, None] + a + o + np.arange((n + 2) * (n + 2))[None, :]
+            ps.packed[bi] = bb.reshape(len(sel), (n + 2) * (n + 2))
+    total = int(cell_start[-1])
     ps.items = _build_grid_items(ps, gi, grid, grid)
     ps.meta = {"workload": "uneven patches %d x {%s}^2 cells" % (len(ps), ",".join(map(str, sizes))),
-               "dry_fraction": dry / max(1, total)}
+               "dry_fraction": dry / max(1, total), "bathymetry_lift": lift}
     return ps
