@@ -111,8 +111,8 @@ double pco_time_unew(const pco_patch *p) {
 /* eigenvectors (1, ubar -+ cbar).                                           */
 /*                                                                           */
 /* Defined details (identical in the CUDA kernels):                          */
-/*  - a cell is wet iff h > dry_tol; dry cells carry zero velocity and zero  */
-/*    Roe weight (s = 0, p = 0, F = 0, hu = 0);                              */
+/*  - a cell is wet iff h > dry_tol; dry cells carry zero velocity, zero    */
+/*    Roe weight (s = 0, p = 0, F = 0, hu = 0) and depth max(h, 0);          */
 /*  - wet|dry edge where the wet surface h+b does not reach the dry cell's   */
 /*    bathymetry: reflecting wall (dry side replaced by the mirrored wet     */
 /*    state), and the update of the dry cell is dropped;                     */
@@ -141,6 +141,9 @@ static void cell_derived(const pco_swe_params *prm, double h, double hu, double 
     c->F = p * p;
     c->hu = hu;
   } else {
+    /* a dry cell enters with zero velocity and a non-negative depth (a ghost
+     * value interpolated across a coastline can be negative) */
+    c->h = h > 0.0 ? h : 0.0;
     c->s = 0.0;
     c->p = 0.0;
     c->F = 0.0;

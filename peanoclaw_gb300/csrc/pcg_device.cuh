@@ -123,7 +123,7 @@ __device__ __forceinline__ double bitsd(unsigned long long b) {
 // ---------------------------------------------------------------------------
 // f-wave edge solve (same operation sequence as the oracle's fwave_derived).
 // Cell quantities: h, hu (normal momentum, zero for dry cells), b, s = sqrt(h),
-// p = hu / s, F = p*p; wet = h > dry_tol.
+// p = hu / s, F = p*p; wet = h > dry_tol; a dry cell has h = max(h, 0).
 // ---------------------------------------------------------------------------
 struct CellQ {
   double h, hu, b, s, p, F;
@@ -143,6 +143,9 @@ __device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu
     cx.s = s; cx.p = p; cx.F = __dmul_rn(p, p); cx.hu = hu;
     cy.s = s; cy.p = q; cy.F = __dmul_rn(q, q); cy.hu = hv;
   } else {
+    // dry: zero velocity, depth clamped to >= 0 (interpolated ghosts can be negative)
+    double hd = h > 0.0 ? h : 0.0;
+    cx.h = hd; cy.h = hd;
     cx.s = 0.0; cx.p = 0.0; cx.F = 0.0; cx.hu = 0.0;
     cy.s = 0.0; cy.p = 0.0; cy.F = 0.0; cy.hu = 0.0;
   }

@@ -79,7 +79,7 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
     double b = slab[idx_pw(P, 0, x, y)];
     CellQ qx, qy;
     cell_derived(dry, h, hu, hv, b, qx, qy);
-    S.h[sx][sy] = h; S.b[sx][sy] = b; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
+    S.h[sx][sy] = qx.h; S.b[sx][sy] = b; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
     S.s[sx][sy] = qx.s; S.p[sx][sy] = qx.p; S.q[sx][sy] = qy.p;
     S.F[sx][sy] = qx.F; S.G[sx][sy] = qy.F; S.wet[sx][sy] = qx.wet ? 1 : 0;
   }
