@@ -208,6 +208,25 @@ int pcg_profile_step(pcg_context *ctx, double *ms);
  * FMA counted as two flops. */
 int pcg_probe_fp64_peak(pcg_context *ctx, double *tflops);
 
+/* ----------------------------------------------------- allocation-free solve */
+
+/* No counterpart in the reference.  SWEKernel::solveTimestep for one patch
+ * without a context and without any device allocation, for callers that cannot
+ * call cudaMalloc (a thread working on a patch buffer owned by another
+ * component, or a process whose device memory belongs to another framework's
+ * pool).  d_vector is the patch vector in device memory (reference layout,
+ * ghost width 1, 3 unknowns, b with ghost layer), nx*ny <= 16384 (128 x 128),
+ * larger patches are rejected with PCG_E_INVALID.  dt_used / est_next (host,
+ * may be NULL) receive the dt taken and the CFL estimate; the caller keeps the
+ * time intervals.  stream: a cudaStream_t (NULL = default stream).
+ * Scratch is a fixed 393 KB array inside the library, held by every GPU that
+ * loads it until exit and shared by all calls: calls that overlap on the GPU
+ * race.  The first call on a device resolves that array's device address (a
+ * one-time set-up); make that first call before any stream capture. */
+int pcg_solve_timestep_noalloc(double *d_vector, int32_t nx, int32_t ny, const double size[2],
+                               const pcg_swe_params *params, double max_dt, double *dt_used,
+                               double *est_next, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

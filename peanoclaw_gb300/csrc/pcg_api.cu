@@ -75,6 +75,8 @@ int64_t vector_size(const pcg_patch_desc &d) {
 
 }  // namespace
 
+int pcg_report_error(int code, const std::string &msg) { return fail(code, msg); }
+
 struct pcg_context {
   int device = 0;
   int num_sms = 152;

@@ -933,3 +933,141 @@ cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev
 }
 
 }  // namespace pcg
+
+// ===========================================================================
+// Allocation-free single-patch solve (pcg_solve_timestep_noalloc).
+//
+// Some callers cannot call cudaMalloc: a traversal thread that works on a
+// patch buffer owned by someone else and must not trigger the device-wide
+// synchronisation of an allocation, or a process whose device memory is held
+// by another framework's pool, so that a new allocation can fail at any time.
+// They also cannot create a pcg_context, whose slab is allocated.  For them
+// the solve below keeps its scratch (the net updates of one patch and the two
+// result words) in a fixed array that is part of the library image.
+// ===========================================================================
+
+namespace pcg {
+
+// Largest patch (interior cells) the allocation-free solve accepts: 128 x 128.
+constexpr int kNoAllocMaxCells = 128 * 128;
+
+// 3 net-update fields of up to kNoAllocMaxCells cells + {dt used, next dt}:
+// 393,232 bytes that every GPU which loads this library holds until exit.
+// All calls share it and it keeps the last call's contents; every element a
+// call reads was written earlier by the same call, so nothing needs clearing.
+// Calls whose kernels overlap on the GPU (different streams, no ordering)
+// race on this array.
+static __device__ __align__(256) double g_noalloc_scratch[3 * kNoAllocMaxCells + 2];
+
+__global__ void __launch_bounds__(kSweepThreads)
+    k_solve_patch_noalloc(double *__restrict__ vec, PatchDev P, SweParamsDev prm, double max_dt,
+                          double *__restrict__ scratch) {
+  __shared__ SweepSmem S;
+  const int nx = P.nx, ny = P.ny;
+  double *net = scratch;
+  double smax = 0.0;
+  for (int x0 = 0; x0 < nx; x0 += kTile)
+    for (int y0 = 0; y0 < ny; y0 += kTile) {
+      int tw = min(kTile, nx - x0), th = min(kTile, ny - y0);
+      double nh = 0, nhu = 0, nhv = 0;
+      double s = sweep_tile(S, vec, P, prm, x0, y0, tw, th, false, nh, nhu, nhv);
+      smax = fmax(smax, s);
+      int t = threadIdx.x;
+      if (t < tw * th) {
+        int x = x0 + t / th, y = y0 + t % th;
+        long long c = (long long)x * ny + y;
+        net[c] = nh;
+        net[(long long)nx * ny + c] = nhu;
+        net[2LL * nx * ny + c] = nhv;
+      }
+    }
+  __syncthreads();
+  double dx = subcell(P, 0), dy = subcell(P, 1);
+  double block_dt = cfl_dt(prm, smax, dx, dy);
+  double dt = fmin(block_dt, max_dt);
+  for (int c = threadIdx.x; c < nx * ny; c += blockDim.x) {
+    int x = c / ny, y = c - x * ny;
+    long long io0 = idx_uold(P, 0, x, y), io1 = idx_uold(P, 1, x, y), io2 = idx_uold(P, 2, x, y);
+    long long in0 = idx_unew(P, 0, x, y), in1 = idx_unew(P, 1, x, y), in2 = idx_unew(P, 2, x, y);
+    double nh = __fma_rn(-dt, net[c], vec[io0]);
+    double nhu = __fma_rn(-dt, net[(long long)nx * ny + c], vec[io1]);
+    double nhv = __fma_rn(-dt, net[2LL * nx * ny + c], vec[io2]);
+    if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
+    if (nh < 0.0) nh = 0.0;
+    double o0 = vec[in0], o1 = vec[in1], o2 = vec[in2];
+    vec[io0] = o0; vec[io1] = o1; vec[io2] = o2;
+    vec[in0] = nh; vec[in1] = nhu; vec[in2] = nhv;
+  }
+  if (threadIdx.x == 0) {
+    scratch[3 * kNoAllocMaxCells] = dt;
+    scratch[3 * kNoAllocMaxCells + 1] = block_dt;
+  }
+}
+
+}  // namespace pcg
+
+#include <mutex>
+
+#include "../../include/pcg.h"
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 64;
+double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+extern "C" int pcg_solve_timestep_noalloc(double *d_vector, int32_t nx, int32_t ny,
+                                          const double size[2], const pcg_swe_params *params,
+                                          double max_dt, double *dt_used, double *est_next,
+                                          void *stream) {
+  using namespace pcg;
+  if (!d_vector || !size || !params)
+    return pcg_report_error(PCG_E_INVALID, "pcg_solve_timestep_noalloc: null argument");
+  if (nx < 1 || ny < 1 || (long long)nx * ny > kNoAllocMaxCells)
+    return pcg_report_error(PCG_E_INVALID,
+                            "pcg_solve_timestep_noalloc: patch must have 1..16384 (128 x 128) cells");
+  if (!(size[0] > 0.0) || !(size[1] > 0.0))
+    return pcg_report_error(PCG_E_INVALID, "pcg_solve_timestep_noalloc: patch size must be positive");
+  if (((uintptr_t)d_vector & 7u) != 0)
+    return pcg_report_error(PCG_E_INVALID, "pcg_solve_timestep_noalloc: vector must be 8-byte aligned");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return pcg_report_error(PCG_E_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return pcg_report_error(PCG_E_INVALID, "pcg_solve_timestep_noalloc: device ordinal too large");
+  double *scratch;
+  {
+    // First call on a device: resolve the device address of the scratch
+    // array with that device current (the host-side name is not a device
+    // address).
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      double *p = nullptr;
+      e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p)
+        return pcg_report_error(PCG_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = p;
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  PatchDev P{};
+  P.off = 0;
+  P.nx = nx; P.ny = ny; P.g = 1; P.nq = 3; P.np_wo = 0; P.np_w = 1;
+  P.flags = kFlagLeaf;
+  P.size[0] = size[0]; P.size[1] = size[1];
+  SweParamsDev prm{params->g, params->cfl, params->dry_tol, params->dry_tol_update, params->s_min,
+                   params->dt_inf};
+  cudaStream_t st = (cudaStream_t)stream;
+  k_solve_patch_noalloc<<<1, kSweepThreads, 0, st>>>(d_vector, P, prm, max_dt, scratch);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return pcg_report_error(PCG_E_CUDA, cudaGetErrorString(e));
+  if (dt_used || est_next) {
+    double res[2];
+    e = cudaMemcpyAsync(res, scratch + 3 * kNoAllocMaxCells, sizeof(res), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return pcg_report_error(PCG_E_CUDA, cudaGetErrorString(e));
+    if (dt_used) *dt_used = res[0];
+    if (est_next) *est_next = res[1];
+  }
+  return PCG_OK;
+}

@@ -3,7 +3,13 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "pcg_device.cuh"
+
+// Records the calling thread's last error (returned by pcg_last_error) and
+// returns `code`.
+int pcg_report_error(int code, const std::string &msg);
 
 namespace pcg {
 

@@ -98,6 +98,8 @@ SIGNATURES = {
     "pcg_synchronize": (C.c_int, [_CTX]),
     "pcg_profile_step": (C.c_int, [_CTX, _D]),
     "pcg_probe_fp64_peak": (C.c_int, [_CTX, _D]),
+    "pcg_solve_timestep_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _D,
+                                             C.POINTER(SweParams), C.c_double, _D, _D, C.c_void_p]),
 }
 
 _lib = None
