@@ -151,8 +151,8 @@ def build_context(ps, prm):
         if ps.wall[p]:
             ctx.set_boundary(pid, ps.wall[p])
         ids.append(pid)
-    items = [dict(it, src=ids[it["src"]], dst=ids[it["dst"]]) for it in ps.items]
-    ctx.set_ghost_items(items)
+    from peanoclaw_gb300.scenarios import remap_items
+    ctx.set_ghost_items(remap_items(ps.items, ids))
     return ctx, ids
 
 

@@ -208,25 +208,29 @@ def compute_net_updates(p, prm):
 
 
 def ghost_items(items):
-    arr = (PcoGhostItem * max(1, len(items)))()
-    for k, it in enumerate(items):
-        a = arr[k]
-        a.kind, a.src, a.dst = it["kind"], it["src"], it["dst"]
-        a.size[0], a.size[1] = it["size"]
-        a.src_offset[0], a.src_offset[1] = it["src_offset"]
-        a.dst_offset[0], a.dst_offset[1] = it["dst_offset"]
-    return arr
+    """(N, 9) int32 array (or list of dicts) -> pco_ghost_item array."""
+    if isinstance(items, np.ndarray):
+        arr = np.ascontiguousarray(items, dtype=np.int32).reshape(-1, 9)
+    else:
+        arr = np.array([[it["kind"], it["src"], it["dst"], it["size"][0], it["size"][1],
+                         it.get("src_offset", (0, 0))[0], it.get("src_offset", (0, 0))[1],
+                         it["dst_offset"][0], it["dst_offset"][1]] for it in items],
+                       dtype=np.int32).reshape(-1, 9)
+    if len(arr) == 0:
+        arr = np.zeros((1, 9), dtype=np.int32)
+    arr = np.ascontiguousarray(arr)
+    return arr.ctypes.data_as(C.POINTER(PcoGhostItem)), arr
 
 
 def grid_step(patches, items, wall_mask, prm, max_dt, group=None, n_groups=1, n_threads=0):
     P = C.POINTER(PcoPatch)
     parr = (P * len(patches))(*[C.pointer(p.s) for p in patches])
-    it = ghost_items(items)
+    it, keep = ghost_items(items)
     wm = np.ascontiguousarray(wall_mask, dtype=np.uint8)
     grp = None if group is None else np.ascontiguousarray(group, dtype=np.int32)
     mdt = np.ascontiguousarray(np.broadcast_to(np.asarray(max_dt, dtype=np.float64), (n_groups,)))
     dto = np.zeros(n_groups)
-    lib().pco_grid_step(parr, len(patches), it, len(items),
+    lib().pco_grid_step(parr, len(patches), it, len(keep) if len(items) else 0,
                         wm.ctypes.data_as(C.POINTER(C.c_uint8)),
                         None if grp is None else grp.ctypes.data_as(C.POINTER(C.c_int32)),
                         n_groups, C.byref(prm), mdt.ctypes.data_as(C.POINTER(C.c_double)),
@@ -237,6 +241,7 @@ def grid_step(patches, items, wall_mask, prm, max_dt, group=None, n_groups=1, n_
 def grid_fill(patches, items, wall_mask):
     P = C.POINTER(PcoPatch)
     parr = (P * len(patches))(*[C.pointer(p.s) for p in patches])
-    it = ghost_items(items)
+    it, keep = ghost_items(items)
     wm = np.ascontiguousarray(wall_mask, dtype=np.uint8)
-    lib().pco_grid_fill(parr, len(patches), it, len(items), wm.ctypes.data_as(C.POINTER(C.c_uint8)))
+    lib().pco_grid_fill(parr, len(patches), it, len(keep) if len(items) else 0,
+                        wm.ctypes.data_as(C.POINTER(C.c_uint8)))

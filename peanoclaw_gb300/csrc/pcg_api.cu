@@ -66,6 +66,44 @@ __global__ void k_fp64_probe(double *out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// Self-check of the integer-pipe divide / square root against the hardware
+// IEEE operations on pseudo-random operands (splitmix64 of seed and index).
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void k_check_ieee(long long n, unsigned long long seed, unsigned long long *bad) {
+  using namespace pcg::ieee;
+  unsigned long long local = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    uint64_t A = splitmix64(seed ^ (2 * (uint64_t)i)), B = splitmix64(seed ^ (2 * (uint64_t)i + 1));
+    switch (i & 7) {
+      case 0: break;  // any bit pattern (specials, subnormals included)
+      case 1:  // moderate exponents
+        A = (A & ~(0x7FFull << 52)) | ((uint64_t)(900 + (A >> 53) % 250) << 52);
+        B = (B & ~(0x7FFull << 52)) | ((uint64_t)(900 + (B >> 53) % 250) << 52);
+        break;
+      case 2: B = (B & ~kFrac) | (B & 63); break;                 // divisor near a power of two
+      case 3: B = (B & ~kFrac) | (kFrac - (B & 63)); break;       // divisor mantissa near all ones
+      case 4: A = (A & ~kFrac) | (B & kFrac); break;              // equal mantissas
+      case 5: A = (A & ~kFrac) | (A & 1023); B = (B & ~kFrac) | (B & 1023); break;
+      case 6: A &= ~kSign; A = (A & ~(0x7FFull << 52)) | (1023ull << 52); break;  // [1,2)
+      default: A = (A & ~(0x7FFull << 52)) | ((uint64_t)(1010 + (A >> 53) % 30) << 52); break;
+    }
+    double a = from_bits(A), b = from_bits(B);
+    double q1 = div_rn(a, b), q2 = __ddiv_rn(a, b);
+    bool qbad = bits(q1) != bits(q2) && !(q1 != q1 && q2 != q2);
+    double r1 = sqrt_rn(fabs(a)), r2 = __dsqrt_rn(fabs(a));
+    bool sbad = bits(r1) != bits(r2) && !(r1 != r1 && r2 != r2);
+    local += (qbad ? 1 : 0) + (sbad ? 1 : 0);
+  }
+  if (local) atomicAdd(bad, local);
+}
+
 constexpr int64_t kAlign = 32;  // doubles (256 B)
 
 int64_t vector_size(const pcg_patch_desc &d) {
@@ -110,6 +148,13 @@ struct pcg_context {
   std::vector<int> item_first, item_count;  // per patch (plain form)
   pcg::GhostItemDev *d_items = nullptr;
   size_t d_items_cap = 0;
+  // flat ghost-cell list of the batched fill (copies first) + interpolation plan
+  std::vector<pcg::GhostCellDev> h_gcells;
+  int n_copy_cells = 0, n_interp_cells = 0;
+  pcg::GhostCellDev *d_gcells = nullptr;
+  size_t d_gcells_cap = 0;
+  pcg::InterpPlanDev *d_plan = nullptr;
+  size_t d_plan_cap = 0;
 
   std::vector<pcg::TileItem> h_tiles;
   pcg::TileItem *d_tiles = nullptr;
@@ -253,7 +298,21 @@ int rebuild_topology(pcg_context *c) {
     }
     c->item_count[p] = (int)c->h_items.size() - c->item_first[p];
   }
+  // flat ghost-cell list: every cell of every COPY item, then of every INTERP item
+  c->h_gcells.clear();
+  for (int pass = 0; pass < 2; pass++) {
+    for (size_t k = 0; k < c->h_items.size(); k++) {
+      const pcg::GhostItemDev &it = c->h_items[k];
+      if (it.kind != pass) continue;
+      int nc = it.size[0] * it.size[1];
+      for (int q = 0; q < nc; q++) c->h_gcells.push_back(pcg::GhostCellDev{(int)k, q});
+    }
+    if (pass == 0) c->n_copy_cells = (int)c->h_gcells.size();
+  }
+  c->n_interp_cells = (int)c->h_gcells.size() - c->n_copy_cells;
   int rc;
+  if ((rc = ensure_device(c, &c->d_gcells, &c->d_gcells_cap, c->h_gcells.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_plan, &c->d_plan_cap, (size_t)c->n_interp_cells)) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_tiles, &c->d_tiles_cap, c->h_tiles.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_wall, &c->d_wall_cap, c->h_wall.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_items, &c->d_items_cap, c->h_items.size())) != PCG_OK) return rc;
@@ -266,6 +325,13 @@ int rebuild_topology(pcg_context *c) {
   if (!c->h_items.empty())
     PCG_CUDA(cudaMemcpyAsync(c->d_items, c->h_items.data(), sizeof(pcg::GhostItemDev) * c->h_items.size(),
                              cudaMemcpyHostToDevice, c->stream));
+  if (!c->h_gcells.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_gcells, c->h_gcells.data(), sizeof(pcg::GhostCellDev) * c->h_gcells.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+  c->patches_dirty = true;
+  if ((rc = upload_patches(c)) != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_build_interp_plan(c->stream, c->d_patches, c->d_items, c->d_gcells + c->n_copy_cells,
+                                         c->n_interp_cells, c->d_plan));
   int per_sm = 0;
   PCG_CUDA(pcg::sweep_occupancy(&per_sm));
   if (per_sm < 1) per_sm = 1;
@@ -288,8 +354,8 @@ int enqueue_step(pcg_context *c, int mode) {
   PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
                         c->d_patch_smax));
   if (mode == PCG_MODE_BATCHED) {
-    PCG_CUDA(launch_ghost_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, 0,
-                                (int)c->h_items.size(), nullptr));
+    PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, c->d_gcells,
+                                c->n_copy_cells, c->n_interp_cells, c->d_plan, nullptr));
     PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
     PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
@@ -442,6 +508,8 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_group_max_dt);
   cudaFree(c->d_dt_out);
   cudaFree(c->d_items);
+  cudaFree(c->d_gcells);
+  cudaFree(c->d_plan);
   cudaFree(c->d_tiles);
   cudaFree(c->d_wall);
   cudaFree(c->d_solve_out);
@@ -759,7 +827,7 @@ int pcg_set_ghost_items(pcg_context *c, const pcg_ghost_item *items, int32_t n) 
     if (!region_inside(D, it.dst_offset, it.size, true) ||
         (it.kind == 0 && !region_inside(S, it.src_offset, it.size, false)))
       return fail(PCG_E_INVALID, "ghost item " + std::to_string(k) + ": region outside the patches");
-    if (it.kind == 1 && (S.nx < 2 || S.ny < 2 || S.np_w < 1 || D.np_w < 1))
+    if (it.kind == 1 && (S.nx < 2 || S.ny < 2 || S.np_w < 1 || D.np_w < 1 || S.nq != 3))
       return fail(PCG_E_INVALID, "ghost item " + std::to_string(k) + ": interpolation source unsupported");
   }
   c->items_user.assign(items, items + n);
@@ -888,8 +956,8 @@ int pcg_profile_step(pcg_context *c, double *ms) {
   PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
                         c->d_patch_smax));
   PCG_CUDA(cudaEventRecord(ev[1], c->stream));
-  PCG_CUDA(launch_ghost_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, 0,
-                              (int)c->h_items.size(), nullptr));
+  PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, c->d_gcells,
+                              c->n_copy_cells, c->n_interp_cells, c->d_plan, nullptr));
   PCG_CUDA(cudaEventRecord(ev[2], c->stream));
   PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
   PCG_CUDA(cudaEventRecord(ev[3], c->stream));
@@ -931,6 +999,23 @@ int pcg_probe_fp64_peak(pcg_context *c, double *tflops) {
   }
   PCG_CUDA(cudaFree(buf));
   *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return PCG_OK;
+}
+
+int pcg_check_ieee_emulation(pcg_context *c, int64_t samples, uint64_t seed, int64_t *mismatches) {
+  if (!c || !mismatches || samples < 0) return fail(PCG_E_INVALID, "bad argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  unsigned long long *d = nullptr;
+  PCG_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
+  PCG_CUDA(cudaMemsetAsync(d, 0, sizeof(unsigned long long), c->stream));
+  k_check_ieee<<<c->num_sms * 8, 256, 0, c->stream>>>(samples, seed, d);
+  PCG_CUDA(cudaGetLastError());
+  unsigned long long h = 0;
+  PCG_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  PCG_CUDA(cudaFree(d));
+  *mismatches = (int64_t)h;
   return PCG_OK;
 }
 

@@ -10,6 +10,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pcg_ieee.cuh"
+
 namespace pcg {
 
 // Patch table entry.  `off` is the offset (in doubles) of the patch's data
@@ -46,6 +48,20 @@ struct GhostItemDev {
   int size[2];
   int src_off[2];
   int dst_off[2];
+};
+
+// One ghost cell of the precomputed face-pair list: item and the cell's
+// linear index k inside the item's region.
+struct GhostCellDev {
+  int item, k;
+};
+
+// Static part of a coarse-to-fine interpolation of one ghost cell: base
+// source cell and the four d-linear weights (DefaultInterpolation.cpph:107-151),
+// computed once per grid change.
+struct __align__(8) InterpPlanDev {
+  int bx, by;
+  double sf[4];
 };
 
 constexpr int kTile = 16;           // tile edge of the sweep
@@ -120,8 +136,40 @@ __device__ __forceinline__ double bitsd(unsigned long long b) {
   return __longlong_as_double((long long)b);
 }
 
+// IEEE comparisons evaluated on the bit patterns (integer pipes); each one
+// returns exactly what the FP64 comparison returns, NaN included.
+constexpr unsigned long long kAbsMask = 0x7FFFFFFFFFFFFFFFull;
+constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
+// x < 0.0
+__device__ __forceinline__ bool lt_zero(double x) {
+  long long b = __double_as_longlong(x);
+  unsigned long long m = (unsigned long long)b & kAbsMask;
+  return b < 0 && m != 0ull && m <= kInfBits;
+}
+// x > c for a constant c >= +0.0 (not NaN)
+__device__ __forceinline__ bool gt_nonneg(double x, double c) {
+  long long b = __double_as_longlong(x);
+  return b > __double_as_longlong(c) && ((unsigned long long)b & kAbsMask) <= kInfBits;
+}
+// fmax(fabs(a), fabs(b)) with fmax's NaN rule (a NaN operand is ignored)
+__device__ __forceinline__ double fmax_abs(double a, double b) {
+  unsigned long long ma = (unsigned long long)__double_as_longlong(a) & kAbsMask;
+  unsigned long long mb = (unsigned long long)__double_as_longlong(b) & kAbsMask;
+  unsigned long long r = ma > kInfBits ? mb : (mb > kInfBits ? ma : (ma > mb ? ma : mb));
+  return __longlong_as_double((long long)r);
+}
+// fmax(a, b) for a, b >= +0.0 or NaN
+__device__ __forceinline__ double fmax_nonneg(double a, double b) {
+  unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+  unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+  unsigned long long r = ua > kInfBits ? ub : (ub > kInfBits ? ua : (ua > ub ? ua : ub));
+  return __longlong_as_double((long long)r);
+}
+
 // ---------------------------------------------------------------------------
 // f-wave edge solve (same operation sequence as the oracle's fwave_derived).
+// Divides and square roots go through pcg_ieee.cuh (integer pipes, results
+// identical to the IEEE operations).
 // Cell quantities: h, hu (normal momentum, zero for dry cells), b, s = sqrt(h),
 // p = hu / s, F = p*p; wet = h > dry_tol; a dry cell has h = max(h, 0).
 // ---------------------------------------------------------------------------
@@ -132,23 +180,39 @@ struct CellQ {
 
 __device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu, double hv,
                                              double b, CellQ &cx, CellQ &cy) {
-  bool wet = h > dry_tol;
+  bool wet = gt_nonneg(h, dry_tol);
   cx.h = h; cx.b = b; cx.wet = wet;
   cy.h = h; cy.b = b; cy.wet = wet;
   if (wet) {
-    double s = __dsqrt_rn(h);
-    double rs = __ddiv_rn(1.0, s);
+    double s = ieee::sqrt_rn(h);
+    double rs = ieee::div_rn(1.0, s);
     double p = __dmul_rn(hu, rs);
     double q = __dmul_rn(hv, rs);
     cx.s = s; cx.p = p; cx.F = __dmul_rn(p, p); cx.hu = hu;
     cy.s = s; cy.p = q; cy.F = __dmul_rn(q, q); cy.hu = hv;
   } else {
     // dry: zero velocity, depth clamped to >= 0 (interpolated ghosts can be negative)
-    double hd = h > 0.0 ? h : 0.0;
+    double hd = gt_nonneg(h, 0.0) ? h : 0.0;
     cx.h = hd; cy.h = hd;
     cx.s = 0.0; cx.p = 0.0; cx.F = 0.0; cx.hu = 0.0;
     cy.s = 0.0; cy.p = 0.0; cy.F = 0.0; cy.hu = 0.0;
   }
+}
+
+// IEEE negation as a sign-bit flip (a standalone FP64 negation would take an
+// FP64 issue slot).
+__device__ __forceinline__ double neg(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+
+// Wet|dry edge: decide whether the dry side is a reflecting wall and, if so,
+// replace it by the mirrored wet state.  Out of line so the compiler keeps it
+// behind a branch: only coastline edges execute it.
+static __device__ __noinline__ void coastline(CellQ &L, CellQ &R, bool &wallL, bool &wallR) {
+  wallR = L.wet && (__dadd_rn(L.h, L.b) <= R.b);
+  wallL = R.wet && (__dadd_rn(R.h, R.b) <= L.b);
+  if (wallR) { R.h = L.h; R.hu = neg(L.hu); R.b = L.b; R.s = L.s; R.p = neg(L.p); R.F = L.F; }
+  if (wallL) { L.h = R.h; L.hu = neg(R.hu); L.b = R.b; L.s = R.s; L.p = neg(R.p); L.F = R.F; }
 }
 
 // out: Lh, Lhu, Rh, Rhu (net updates of the left/right cell) and the edge's
@@ -159,25 +223,23 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
     Lh = Lhu = Rh = Rhu = speed = 0.0;
     return;
   }
-  bool wallR = L.wet && !R.wet && (__dadd_rn(L.h, L.b) <= R.b);
-  bool wallL = R.wet && !L.wet && (__dadd_rn(R.h, R.b) <= L.b);
-  if (wallR) { R.h = L.h; R.hu = -L.hu; R.b = L.b; R.s = L.s; R.p = -L.p; R.F = L.F; }
-  if (wallL) { L.h = R.h; L.hu = -R.hu; L.b = R.b; L.s = R.s; L.p = -R.p; L.F = R.F; }
+  bool wallR = false, wallL = false;
+  if (L.wet != R.wet) coastline(L, R, wallL, wallR);  // coastline edges only
   double a = __dmul_rn(halfg, __dadd_rn(L.h, R.h));
-  double cb = __dsqrt_rn(a);
-  double ub = __ddiv_rn(__dadd_rn(L.p, R.p), __dadd_rn(L.s, R.s));
+  double cb = ieee::sqrt_rn(a);
+  double ub = ieee::div_rn(__dadd_rn(L.p, R.p), __dadd_rn(L.s, R.s));
   double l1 = __dsub_rn(ub, cb);
   double l2 = __dadd_rn(ub, cb);
   double df1 = __dsub_rn(R.hu, L.hu);
   double deta = __dadd_rn(__dsub_rn(R.h, L.h), __dsub_rn(R.b, L.b));
   double df2 = __fma_rn(a, deta, __dsub_rn(R.F, L.F));
-  double inv = __ddiv_rn(1.0, __dsub_rn(l2, l1));
+  double inv = ieee::div_rn(1.0, __dsub_rn(l2, l1));
   double b1 = __dmul_rn(__fma_rn(l2, df1, -df2), inv);
   double b2 = __dmul_rn(__fma_rn(-l1, df1, df2), inv);
   double z1 = __dmul_rn(b1, l1);
   double z2 = __dmul_rn(b2, l2);
-  if (l1 < 0.0) {
-    if (l2 < 0.0) {
+  if (lt_zero(l1)) {
+    if (lt_zero(l2)) {
       Lh = __dadd_rn(b1, b2); Lhu = __dadd_rn(z1, z2); Rh = 0.0; Rhu = 0.0;
     } else {
       Lh = b1; Lhu = z1; Rh = b2; Rhu = z2;
@@ -187,7 +249,7 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
   }
   if (wallR) { Rh = 0.0; Rhu = 0.0; }
   if (wallL) { Lh = 0.0; Lhu = 0.0; }
-  speed = fmax(fabs(l1), fabs(l2));
+  speed = fmax_abs(l1, l2);
 }
 
 // CFL timestep of a block whose maximum wave speed is s

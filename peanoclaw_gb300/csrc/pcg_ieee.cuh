@@ -69,6 +69,26 @@ PCG_HD double from_bits(uint64_t u) {
 #endif
 }
 
+PCG_HD float bits_float(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+PCG_HD uint32_t float_bits(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+
 // FP32 seeds: only their accuracy matters (the integer refinement corrects
 // any seed within a few units of 2^-22), not their exact value.
 PCG_HD float rcp_seed(float d) {
@@ -91,7 +111,11 @@ PCG_HD float rsqrt_seed(float d) {
 #endif
 }
 
-PCG_HD double hw_div(double a, double b) {
+// Fallbacks for operands outside the fast path.  Kept out of line on the
+// device so the compiler cannot evaluate them speculatively next to the fast
+// path (that would put the FP64 divide / square root back on the FP64 pipe).
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__ double hw_div(double a, double b) {
 #if defined(__CUDA_ARCH__)
   return __ddiv_rn(a, b);
 #else
@@ -99,13 +123,17 @@ PCG_HD double hw_div(double a, double b) {
 #endif
 }
 
-PCG_HD double hw_sqrt(double a) {
+static __host__ __device__ __noinline__ double hw_sqrt(double a) {
 #if defined(__CUDA_ARCH__)
   return __dsqrt_rn(a);
 #else
   return std::sqrt(a);
 #endif
 }
+#else
+inline double hw_div(double a, double b) { return a / b; }
+inline double hw_sqrt(double a) { return std::sqrt(a); }
+#endif
 
 // One Newton-Raphson step for V ~ 2^116 / m  (m in [2^52, 2^53), V in (2^63, 2^64)).
 PCG_HD uint64_t recip_step(uint64_t m, uint64_t V) {
@@ -139,11 +167,12 @@ PCG_HD double div_rn(double a, double b) {
   if ((B & kFrac) == 0) {
     q = x;  // divisor is a power of two: exact
   } else {
-    float d = (float)(uint32_t)(mb >> 29);  // leading 24 bits, exact
-    float r = rcp_seed(d);                  // ~ 2^-23.x
-    // V0 = r * 2^87, kept below 2^64
-    float t = r * 77371252455336267181195264.0f;  // r * 2^86 <= 2^63
-    uint64_t V = (t >= 9223372036854775808.0f ? 0x7FFFFFFFFFFFFFFFull : (uint64_t)t) << 1;
+    // leading 23 fraction bits of the divisor as a float in [1, 2); its
+    // reciprocal r in (0.5, 1] gives V0 = r * 2^64 straight from r's bits
+    float d = bits_float(0x3F800000u | (uint32_t)((mb >> 29) & 0x7FFFFFu));
+    uint32_t rb = float_bits(rcp_seed(d));
+    uint64_t V = ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u)) << ((int)((rb >> 23) & 0xFFu) - 86);
+    if (((rb >> 23) & 0xFFu) >= 127u) V = 0xFFFFFFFFFFFFFFFFull;  // r == 1: clamp below 2^64
     V = recip_step(mb, V);
     V = recip_step(mb, V);
     q = mulhi(x, V);
@@ -186,11 +215,13 @@ PCG_HD double sqrt_rn(double a) {
   if (M == kHidden) {
     s = kHidden;  // power of four: exact
   } else {
-    float f = (float)(uint32_t)(M >> 30);  // leading 24 bits, exact
-    float r = rsqrt_seed(f);
-    // Y0 = r * 2^75, kept below 2^64
-    float t = r * 18889465931478580854784.0f;  // r * 2^74 <= 2^63
-    uint64_t Y = (t >= 9223372036854775808.0f ? 0x7FFFFFFFFFFFFFFFull : (uint64_t)t) << 1;
+    // M / 2^52 in [1, 4) as a float (leading 24 bits); its reciprocal square
+    // root r in (0.5, 1] gives Y0 = r * 2^64 straight from r's bits
+    float f = bits_float(((M >> 53) ? 0x40000000u : 0x3F800000u) |
+                         (uint32_t)((M >> ((M >> 53) ? 30 : 29)) & 0x7FFFFFu));
+    uint32_t rb = float_bits(rsqrt_seed(f));
+    uint64_t Y = ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u)) << ((int)((rb >> 23) & 0xFFu) - 86);
+    if (((rb >> 23) & 0xFFu) >= 127u) Y = 0xFFFFFFFFFFFFFFFFull;  // r == 1: clamp below 2^64
     Y = rsqrt_step(M, Y);
     Y = rsqrt_step(M, Y);
     s = mulhi(M, Y);

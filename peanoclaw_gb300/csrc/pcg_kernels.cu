@@ -32,6 +32,7 @@ struct SweepSmem {
   double xl_h[kTile][kTile], xl_hu[kTile][kTile];  // left-going parts of x-edges
   double yl_h[kTile][kTile], yl_hv[kTile][kTile];  // down-going parts of y-edges
   double red[kSweepThreads / 32];
+  double dxi, dyi;  // 1 / subcell size of the tile's patch
 };
 
 __device__ __forceinline__ CellQ load_x(const SweepSmem &S, int i, int j) {
@@ -58,6 +59,10 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
                                              double &nh, double &nhu, double &nhv) {
   const int t = threadIdx.x;
   const double dry = prm.dry_tol;
+  if (t == 0) {
+    S.dxi = __ddiv_rn(1.0, subcell(P, 0));
+    S.dyi = __ddiv_rn(1.0, subcell(P, 1));
+  }
   // ---- stage tile + halo (corners skipped: the 5-point sweep never reads them)
   const int sw = tw + 2, sh = th + 2;
   for (int k = t; k < sw * sh; k += blockDim.x) {
@@ -93,33 +98,34 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
     double Lh, Lhu, Rh, Rhu, sp;
     // x-edge between (lx-1, ly) and (lx, ly)
     fwave_edge(halfg, load_x(S, lx, ly + 1), load_x(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
-    smax = fmax(smax, sp);
+    smax = fmax_nonneg(smax, sp);
     xr_h = Rh; xr_hu = Rhu;
     if (lx >= 1) { S.xl_h[lx - 1][ly] = Lh; S.xl_hu[lx - 1][ly] = Lhu; }
     // y-edge between (lx, ly-1) and (lx, ly)
     fwave_edge(halfg, load_y(S, lx + 1, ly), load_y(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
-    smax = fmax(smax, sp);
+    smax = fmax_nonneg(smax, sp);
     yr_h = Rh; yr_hv = Rhu;
     if (ly >= 1) { S.yl_h[lx][ly - 1] = Lh; S.yl_hv[lx][ly - 1] = Lhu; }
   }
-  // closing edges on the upper x and y side of the tile
-  if (t < th + tw) {
+  // closing edges on the upper x and y side of the tile, done by the last
+  // threads (the first ones stage the second round of halo cells)
+  const int ce = t - ((int)blockDim.x - (th + tw));
+  if (ce >= 0) {
     double Lh, Lhu, Rh, Rhu, sp;
-    if (t < th) {
-      int j = t;
+    if (ce < th) {
+      int j = ce;
       fwave_edge(halfg, load_x(S, tw, j + 1), load_x(S, tw + 1, j + 1), Lh, Lhu, Rh, Rhu, sp);
       S.xl_h[tw - 1][j] = Lh; S.xl_hu[tw - 1][j] = Lhu;
     } else {
-      int i = t - th;
+      int i = ce - th;
       fwave_edge(halfg, load_y(S, i + 1, th), load_y(S, i + 1, th + 1), Lh, Lhu, Rh, Rhu, sp);
       S.yl_h[i][th - 1] = Lh; S.yl_hv[i][th - 1] = Lhu;
     }
-    smax = fmax(smax, sp);
+    smax = fmax_nonneg(smax, sp);
   }
   __syncthreads();
   if (active) {
-    double dx = subcell(P, 0), dy = subcell(P, 1);
-    double dxi = __ddiv_rn(1.0, dx), dyi = __ddiv_rn(1.0, dy);
+    const double dxi = S.dxi, dyi = S.dyi;
     // accumulation order of computeNumericalFluxes: x-edges (own left edge,
     // then right edge), then y-edges (own lower edge, then upper edge)
     double a = __fma_rn(dxi, xr_h, 0.0);
@@ -151,7 +157,7 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
 // Batched sweep: tiles [first, first + count) of the work list, grid-strided.
 // Net updates go to the uOld interior (free between the ghost fill and the
 // update), the tile's max speed to the patch and its CFL dt to the group.
-__global__ void __launch_bounds__(kSweepThreads)
+__global__ void __launch_bounds__(kSweepThreads, 4)
     k_sweep_tiles(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                   const TileItem *__restrict__ tiles, int first, int count, SweParamsDev prm,
                   unsigned long long *__restrict__ patch_smax,
@@ -297,9 +303,9 @@ __global__ void __launch_bounds__(kSweepThreads)
 __device__ __forceinline__ double transfer_tf(const PatchDev &S, const PatchTimeDev &ST,
                                               const PatchDev &D, const PatchTimeDev &DT) {
   double dtu = time_unew(D, DT);
-  if (is_virtual(S)) return __ddiv_rn(__dsub_rn(dtu, 0.0), 1.0);
+  if (is_virtual(S)) return ieee::div_rn(__dsub_rn(dtu, 0.0), 1.0);
   double su = time_unew(S, ST), so = time_uold(S, ST);
-  if (tl_greater(__dsub_rn(su, so), 0.0)) return __ddiv_rn(__dsub_rn(dtu, so), __dsub_rn(su, so));
+  if (tl_greater(__dsub_rn(su, so), 0.0)) return ieee::div_rn(__dsub_rn(dtu, so), __dsub_rn(su, so));
   return 1.0;
 }
 
@@ -324,12 +330,12 @@ __device__ __forceinline__ double interp_tf(const PatchDev &S, const PatchTimeDe
   } else if (use_unew_uold) {
     double so = time_uold(S, ST), su = time_unew(S, ST);
     double num = to_current ? __dsub_rn(time_uold(D, DT), so) : __dsub_rn(time_unew(D, DT), so);
-    tf = __ddiv_rn(num, __dsub_rn(su, so));
+    tf = ieee::div_rn(num, __dsub_rn(su, so));
   } else {
     double den = __dsub_rn(__dadd_rn(ST.time, ST.dt), ST.time);
     double num = to_current ? __dsub_rn(DT.time, ST.time)
                             : __dsub_rn(__dadd_rn(DT.time, DT.dt), ST.time);
-    tf = __ddiv_rn(num, den);
+    tf = ieee::div_rn(num, den);
   }
   return fmax(0.0, fmin(1.0, tf));
 }
@@ -384,6 +390,95 @@ __device__ void interp_cell(double *slab, const PatchDev &S, const PatchDev &D, 
     double bb = slab[idx_pw(D, 0, cx, cy)];
     long long id = to_uold ? idx_uold(D, 0, cx, cy) : idx_unew(D, 0, cx, cy);
     slab[id] = __dadd_rn(slab[id], __dmul_rn(-1.0, bb));
+  }
+}
+
+// Static interpolation geometry of ghost cell k of an INTERP item: the same
+// operations as interp_cell, evaluated once per grid change.
+__device__ void interp_plan_cell(const PatchDev &S, const PatchDev &D, const int size[2],
+                                 const int dof[2], int k, InterpPlanDev &pl) {
+  int cx = dof[0] + k / size[1], cy = dof[1] + k % size[1];
+  double sh[2] = {subcell(S, 0), subcell(S, 1)};
+  double inv[2] = {__ddiv_rn(1.0, sh[0]), __ddiv_rn(1.0, sh[1])};
+  double c[2] = {subcell_center(D, 0, cx), subcell_center(D, 1, cy)};
+  int bi[2];
+  int n[2] = {S.nx, S.ny};
+  for (int d = 0; d < 2; d++) {
+    double sbase = __dadd_rn(S.pos[d], __dmul_rn(sh[d], 0.5));
+    double local = __dsub_rn(c[d], sbase);
+    int v = (int)floor(__dmul_rn(local, inv[d]));
+    v = v < n[d] - 2 ? v : n[d] - 2;
+    bi[d] = v > 0 ? v : 0;
+  }
+  pl.bx = bi[0];
+  pl.by = bi[1];
+  for (int kk = 0; kk < 4; kk++) {
+    int off[2] = {kk & 1, (kk >> 1) & 1};
+    double npos[2] = {subcell_center(S, 0, bi[0] + off[0]), subcell_center(S, 1, bi[1] + off[1])};
+    double sf = 1.0;
+    for (int d = 0; d < 2; d++) {
+      double sign = (double)(1 - 2 * off[d]);
+      sf = __dmul_rn(sf, __dsub_rn(1.0, __dmul_rn(__dmul_rn(sign, __dsub_rn(c[d], npos[d])), inv[d])));
+    }
+    pl.sf[kk] = sf;
+  }
+}
+
+__global__ void k_build_interp_plan(const PatchDev *__restrict__ patches,
+                                    const GhostItemDev *__restrict__ items,
+                                    const GhostCellDev *__restrict__ cells, int count,
+                                    InterpPlanDev *__restrict__ plan) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    GhostCellDev gc = cells[e];
+    GhostItemDev it = items[gc.item];
+    interp_plan_cell(patches[it.src], patches[it.dst], it.size, it.dst_off, gc.k, plan[e]);
+  }
+}
+
+// Batched ghost fill over the flat ghost-cell list: entries [0, ncopy) copy,
+// [ncopy, ncopy + ninterp) interpolate with their precomputed plan.  Items
+// write disjoint ghost cells, one thread per ghost cell.
+__global__ void __launch_bounds__(256)
+    k_ghost_cells(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                  const PatchTimeDev *__restrict__ times, const GhostItemDev *__restrict__ items,
+                  const GhostCellDev *__restrict__ cells, int ncopy, int ninterp,
+                  const InterpPlanDev *__restrict__ plan, const int *__restrict__ group_active) {
+  const int total = ncopy + ninterp;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    GhostCellDev gc = cells[e];
+    GhostItemDev it = items[gc.item];
+    const PatchDev S = patches[it.src], D = patches[it.dst];
+    if (group_active && !group_active[D.group]) continue;
+    const PatchTimeDev ST = times[it.src], DT = times[it.dst];
+    if (e < ncopy) {
+      double tf = transfer_tf(S, ST, D, DT);
+      double itf = __dsub_rn(1.0, tf);
+      transfer_cell(slab, S, D, it.size, it.src_off, it.dst_off, tf, itf, gc.k);
+      continue;
+    }
+    const InterpPlanDev pl = plan[e - ncopy];
+    double tf = interp_tf(S, ST, D, DT, false, true);
+    double one_m_tf = __dsub_rn(1.0, tf);
+    int cx = it.dst_off[0] + gc.k / it.size[1], cy = it.dst_off[1] + gc.k % it.size[1];
+    double acc[3];
+    const int nq = D.nq < 3 ? D.nq : 3;
+    for (int q = 0; q < nq; q++) acc[q] = 0.0;
+    for (int kk = 0; kk < 4; kk++) {
+      int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
+      double sf = pl.sf[kk];
+      for (int q = 0; q < nq; q++) {
+        double so = slab[idx_uold(S, q, nxi, nyi)];
+        double sn = slab[idx_unew(S, q, nxi, nyi)];
+        if (q == 0) {
+          double bb = slab[idx_pw(S, 0, nxi, nyi)];
+          so = __dadd_rn(so, bb);
+          sn = __dadd_rn(sn, bb);
+        }
+        acc[q] = __dadd_rn(acc[q], __dmul_rn(sf, __dadd_rn(__dmul_rn(so, one_m_tf), __dmul_rn(sn, tf))));
+      }
+    }
+    acc[0] = __dadd_rn(acc[0], __dmul_rn(-1.0, slab[idx_pw(D, 0, cx, cy)]));
+    for (int q = 0; q < nq; q++) slab[idx_uold(D, q, cx, cy)] = acc[q];
   }
 }
 
@@ -832,6 +927,29 @@ cudaError_t launch_ghost_items(cudaStream_t st, double *slab, const PatchDev *pa
   if (grid > 152 * 16) grid = 152 * 16;
   k_ghost_items<<<grid, 32 * warps_per_block, 0, st>>>(slab, patches, times, items, first, count,
                                                        group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
+                                     const GhostItemDev *items, const GhostCellDev *cells, int count,
+                                     InterpPlanDev *plan) {
+  if (count <= 0) return cudaSuccess;
+  int grid = (count + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  k_build_interp_plan<<<grid, 256, 0, st>>>(patches, items, cells, count, plan);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev *items,
+                               const GhostCellDev *cells, int ncopy, int ninterp,
+                               const InterpPlanDev *plan, const int *group_active) {
+  int total = ncopy + ninterp;
+  if (total <= 0) return cudaSuccess;
+  int grid = (total + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  k_ghost_cells<<<grid, 256, 0, st>>>(slab, patches, times, items, cells, ncopy, ninterp, plan,
+                                      group_active);
   return cudaGetLastError();
 }
 

@@ -29,6 +29,13 @@ cudaError_t launch_record_dt(cudaStream_t st, int n_groups, const unsigned long 
 cudaError_t launch_ghost_items(cudaStream_t st, double *slab, const PatchDev *patches,
                                const PatchTimeDev *times, const GhostItemDev *items, int first,
                                int count, const int *group_active);
+cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
+                                     const GhostItemDev *items, const GhostCellDev *cells, int count,
+                                     InterpPlanDev *plan);
+cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev *items,
+                               const GhostCellDev *cells, int ncopy, int ninterp,
+                               const InterpPlanDev *plan, const int *group_active);
 cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
                          const int *wall_patches, int count, const int *group_active);
 cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,

@@ -98,6 +98,7 @@ SIGNATURES = {
     "pcg_synchronize": (C.c_int, [_CTX]),
     "pcg_profile_step": (C.c_int, [_CTX, _D]),
     "pcg_probe_fp64_peak": (C.c_int, [_CTX, _D]),
+    "pcg_check_ieee_emulation": (C.c_int, [_CTX, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "pcg_solve_timestep_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _D,
                                              C.POINTER(SweParams), C.c_double, _D, _D, C.c_void_p]),
 }
@@ -148,6 +149,16 @@ def vector_size(n, ghost=1, nq=3, np_wo=0, np_w=1):
     nx, ny = (n, n) if np.isscalar(n) else n
     vn, vo = nx * ny, (nx + 2 * ghost) * (ny + 2 * ghost)
     return nq * vn + nq * vo + np_wo * vn + np_w * vo + 2 * nq * (nx + ny)
+
+
+def items_array(items):
+    """Ghost items as a contiguous (N, 9) int32 array in pcg_ghost_item layout."""
+    if isinstance(items, np.ndarray):
+        return np.ascontiguousarray(items, dtype=np.int32).reshape(-1, 9)
+    rows = [[it["kind"], it["src"], it["dst"], it["size"][0], it["size"][1],
+             it.get("src_offset", (0, 0))[0], it.get("src_offset", (0, 0))[1],
+             it["dst_offset"][0], it["dst_offset"][1]] for it in items]
+    return np.array(rows, dtype=np.int32).reshape(-1, 9)
 
 
 class Context:
@@ -243,14 +254,11 @@ class Context:
 
     # batched ----------------------------------------------------------------
     def set_ghost_items(self, items):
-        arr = (GhostItem * max(1, len(items)))()
-        for k, it in enumerate(items):
-            a = arr[k]
-            a.kind, a.src, a.dst = it["kind"], it["src"], it["dst"]
-            a.size[0], a.size[1] = it["size"]
-            a.src_offset[0], a.src_offset[1] = it.get("src_offset", (0, 0))
-            a.dst_offset[0], a.dst_offset[1] = it["dst_offset"]
-        check(lib().pcg_set_ghost_items(self.h, arr, len(items)))
+        """items: (N, 9) int32 array (kind, src, dst, size[2], src_offset[2],
+        dst_offset[2]) or a list of dicts with those keys."""
+        arr = items_array(items)
+        ptr = arr.ctypes.data_as(C.POINTER(GhostItem)) if len(arr) else None
+        check(lib().pcg_set_ghost_items(self.h, ptr, len(arr)))
 
     def set_group_max_dt(self, group, max_dt):
         check(lib().pcg_set_group_max_dt(self.h, group, float(max_dt)))
@@ -278,6 +286,11 @@ class Context:
         ms = np.zeros(5)
         check(lib().pcg_profile_step(self.h, dptr(ms)))
         return ms
+
+    def check_ieee_emulation(self, samples, seed=1):
+        bad = C.c_int64()
+        check(lib().pcg_check_ieee_emulation(self.h, int(samples), int(seed), C.byref(bad)))
+        return bad.value
 
     def fp64_peak_tflops(self):
         v = C.c_double()

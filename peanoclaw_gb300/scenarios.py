@@ -28,7 +28,7 @@ class PatchSet:
         self.wall = []
         self.offsets = None  # start of each patch vector in `packed`
         self.packed = None   # all patch vectors back to back
-        self.items = []
+        self.items = np.zeros((0, 9), dtype=np.int32)
         self.meta = {}
 
     def __len__(self):
@@ -75,17 +75,19 @@ def _centers(pos, size, n, ghost=True):
 def _build_grid_items(ps, grid_index, nslots_x, nslots_y):
     """Face and corner items for a regular grid of equally sized slots holding
     patches of different subdivision.  Same subdivision: copy; otherwise
-    interpolation from the neighbour (its subcells are larger or smaller)."""
-    items = []
+    interpolation from the neighbour (its subcells are larger or smaller).
+    Returns an (N, 9) int32 array: kind, src, dst, size[2], src_offset[2],
+    dst_offset[2] (the pcg_ghost_item layout)."""
+    rows = []
     for sx in range(nslots_x):
         for sy in range(nslots_y):
-            d = grid_index[sx, sy]
+            d = int(grid_index[sx, sy])
             nd = ps.n[d]
             for dx, dy in ((-1, 0), (1, 0), (0, -1), (0, 1), (-1, -1), (1, -1), (-1, 1), (1, 1)):
                 tx, ty = sx + dx, sy + dy
                 if not (0 <= tx < nslots_x and 0 <= ty < nslots_y):
                     continue
-                s = grid_index[tx, ty]
+                s = int(grid_index[tx, ty])
                 ns = ps.n[s]
                 # direction from source to destination (functor convention)
                 dirv = (-dx, -dy)
@@ -93,12 +95,19 @@ def _build_grid_items(ps, grid_index, nslots_x, nslots_y):
                 dst_off = [0 if v == 0 else (-1 if v == 1 else nd) for v in dirv]
                 if ns == nd:
                     src_off = [0 if v == 0 else (nd - 1 if v == 1 else 0) for v in dirv]
-                    items.append({"kind": PCG_GHOST_COPY, "src": s, "dst": d, "size": size,
-                                  "src_offset": src_off, "dst_offset": dst_off})
+                    rows.append([PCG_GHOST_COPY, s, d] + size + src_off + dst_off)
                 else:
-                    items.append({"kind": PCG_GHOST_INTERP, "src": s, "dst": d, "size": size,
-                                  "src_offset": [0, 0], "dst_offset": dst_off})
-    return items
+                    rows.append([PCG_GHOST_INTERP, s, d] + size + [0, 0] + dst_off)
+    return np.array(rows, dtype=np.int32).reshape(-1, 9)
+
+
+def remap_items(items, ids):
+    """Items with patch indices replaced by the ids `ids[index]`."""
+    out = np.array(items, dtype=np.int32, copy=True).reshape(-1, 9)
+    ids = np.asarray(ids, dtype=np.int32)
+    out[:, 1] = ids[out[:, 1]]
+    out[:, 2] = ids[out[:, 2]]
+    return out
 
 
 def radial_dam_break(npx=9, n=16, radius=0.15, h_in=2.0, h_out=1.0):

@@ -67,13 +67,8 @@ def gpu_patchset(ctx, ps):
         ids.append(pid)
         ctx.set_boundary(pid, ps.wall[p])
     ctx.upload_many(ids, ps.packed)
-    items = []
-    for it in ps.items:
-        it2 = dict(it)
-        it2["src"] = ids[it["src"]]
-        it2["dst"] = ids[it["dst"]]
-        items.append(it2)
-    ctx.set_ghost_items(items)
+    from peanoclaw_gb300.scenarios import remap_items
+    ctx.set_ghost_items(remap_items(ps.items, ids))
     return ids
 
 

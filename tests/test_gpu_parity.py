@@ -277,3 +277,9 @@ def test_mass_conservation_closed_basin():
     m1 = mass()
     c.close()
     assert abs(m1 - m0) / m0 < 1e-13
+
+
+def test_integer_pipe_divide_and_sqrt_match_ieee(ctx):
+    """The sweep's divide / square root (integer pipes) equal the hardware
+    IEEE results bit for bit on 2^26 pseudo-random operand pairs."""
+    assert ctx.check_ieee_emulation(1 << 26, seed=20261203) == 0
