@@ -182,6 +182,23 @@ int pcg_apply_flux_correction(pcg_context *ctx, int32_t src, int32_t dst, int32_
  * (replaces the per-vertex GhostLayerCompositor traversal,
  * GhostLayerCompositor.cpp:280-320).  Items must write disjoint ghost cells. */
 int pcg_set_ghost_items(pcg_context *ctx, const pcg_ghost_item *items, int32_t n);
+/* Restriction into virtual (refined) patches, run after the update of every
+ * grid step: each destination's uNew and uOld interior is cleared
+ * (GridLevelTransfer::switchToAndAddVirtualSubgrid), then
+ * SWEKernel::restrictSolution(src[k], dst[k], only_overlapped) runs in list
+ * order per destination (GridLevelTransfer::restrictToOverlappingVirtualSubgrids,
+ * GridLevelTransfer.cpp:140-210), then SWEKernel::postProcessRestriction on
+ * every destination (finalizeVirtualSubgrid, :212-275). */
+int pcg_set_restriction_items(pcg_context *ctx, int32_t n, const int32_t *src, const int32_t *dst,
+                              int32_t only_overlapped);
+/* Flux correction after the update of every grid step: computeFluxes of every
+ * leaf (g_flux as in Numerics::computeFlux), then
+ * applyFluxCorrection(src[k], dst[k], dim[k], dir[k]) in list order per
+ * destination (SolveTimestep.cpp:674-679, FluxCorrectionFunctor). */
+int pcg_set_flux_correction_items(pcg_context *ctx, int32_t n, const int32_t *src, const int32_t *dst,
+                                  const int32_t *dim, const int32_t *dir, double g_flux);
+/* Run the restriction list once (fills the virtual patches at start-up). */
+int pcg_restrict_all(pcg_context *ctx);
 /* Upper bound for the dt of a group (maximumTimestepSize). */
 int pcg_set_group_max_dt(pcg_context *ctx, int32_t group, double max_dt);
 /* One synchronous step of every leaf patch: fill ghost layers (items, then

@@ -169,6 +169,15 @@ struct pcg_context {
   double *d_solve_out = nullptr;
   size_t solve_smem_set = 0;
 
+  // restriction / flux-correction phases after the update (AMR)
+  std::vector<int4> restr_user, flux_user;
+  std::vector<int4> h_restr, h_flux;      // grouped by destination
+  std::vector<int> restr_begin, flux_begin, restr_dsts;
+  int4 *d_restr = nullptr, *d_flux = nullptr;
+  int *d_restr_begin = nullptr, *d_flux_begin = nullptr, *d_restr_dsts = nullptr, *d_leaf_ids = nullptr;
+  size_t d_restr_cap = 0, d_flux_cap = 0, d_rb_cap = 0, d_fb_cap = 0, d_rd_cap = 0, d_leaf_cap = 0;
+  double g_flux = 1.0;
+
   // graph of one batched step
   cudaGraphExec_t graph = nullptr;
   bool graph_valid = false;
@@ -310,7 +319,43 @@ int rebuild_topology(pcg_context *c) {
     if (pass == 0) c->n_copy_cells = (int)c->h_gcells.size();
   }
   c->n_interp_cells = (int)c->h_gcells.size() - c->n_copy_cells;
+  // restriction and flux-correction items grouped by destination, list order kept
+  auto group_by_dst = [&](const std::vector<int4> &in, std::vector<int4> &out, std::vector<int> &begin,
+                          std::vector<int> *dsts) {
+    std::vector<int> order;
+    std::map<int, std::vector<int>> by;
+    for (size_t k = 0; k < in.size(); k++) {
+      if (!valid_id(c, in[k].x) || !valid_id(c, in[k].y)) continue;
+      if (!by.count(in[k].y)) order.push_back(in[k].y);
+      by[in[k].y].push_back((int)k);
+    }
+    out.clear();
+    begin.assign(1, 0);
+    if (dsts) dsts->clear();
+    for (int d : order) {
+      for (int k : by[d]) out.push_back(in[k]);
+      begin.push_back((int)out.size());
+      if (dsts) dsts->push_back(d);
+    }
+  };
+  group_by_dst(c->restr_user, c->h_restr, c->restr_begin, &c->restr_dsts);
+  group_by_dst(c->flux_user, c->h_flux, c->flux_begin, nullptr);
   int rc;
+  if ((rc = ensure_device(c, &c->d_restr, &c->d_restr_cap, c->h_restr.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_flux, &c->d_flux_cap, c->h_flux.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_restr_begin, &c->d_rb_cap, c->restr_begin.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_flux_begin, &c->d_fb_cap, c->flux_begin.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_restr_dsts, &c->d_rd_cap, c->restr_dsts.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_leaf_ids, &c->d_leaf_cap, c->leaf_ids.size())) != PCG_OK) return rc;
+  auto up = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) : cudaSuccess;
+  };
+  PCG_CUDA(up(c->d_restr, c->h_restr.data(), sizeof(int4) * c->h_restr.size()));
+  PCG_CUDA(up(c->d_flux, c->h_flux.data(), sizeof(int4) * c->h_flux.size()));
+  PCG_CUDA(up(c->d_restr_begin, c->restr_begin.data(), sizeof(int) * c->restr_begin.size()));
+  PCG_CUDA(up(c->d_flux_begin, c->flux_begin.data(), sizeof(int) * c->flux_begin.size()));
+  PCG_CUDA(up(c->d_restr_dsts, c->restr_dsts.data(), sizeof(int) * c->restr_dsts.size()));
+  PCG_CUDA(up(c->d_leaf_ids, c->leaf_ids.data(), sizeof(int) * c->leaf_ids.size()));
   if ((rc = ensure_device(c, &c->d_gcells, &c->d_gcells_cap, c->h_gcells.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_plan, &c->d_plan_cap, (size_t)c->n_interp_cells)) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_tiles, &c->d_tiles_cap, c->h_tiles.size())) != PCG_OK) return rc;
@@ -348,6 +393,27 @@ int upload_group_max_dt(pcg_context *c) {
   return PCG_OK;
 }
 
+// Flux correction (computeFluxes of every leaf, then the correction list) and
+// restriction into the virtual patches (clear, restrict list, post-process),
+// the order in which SolveTimestep::enterCell and Remesh::leaveCell run them.
+int enqueue_post_update(pcg_context *c) {
+  using namespace pcg;
+  if (!c->h_flux.empty()) {
+    PCG_CUDA(launch_compute_fluxes(c->stream, c->slab, c->d_patches, c->d_leaf_ids, (int)c->leaf_ids.size(),
+                                   c->g_flux));
+    PCG_CUDA(launch_flux_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_flux, c->d_flux_begin,
+                               (int)c->flux_begin.size() - 1));
+  }
+  if (!c->h_restr.empty()) {
+    int nd = (int)c->restr_dsts.size();
+    PCG_CUDA(launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
+    PCG_CUDA(launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
+                                   c->d_restr_begin, nd));
+    PCG_CUDA(launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
+  }
+  return PCG_OK;
+}
+
 // Enqueue one synchronous step (no synchronisation, capturable in BATCHED mode).
 int enqueue_step(pcg_context *c, int mode) {
   using namespace pcg;
@@ -376,7 +442,7 @@ int enqueue_step(pcg_context *c, int mode) {
                              P.tile_begin, P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
     }
   }
-  return PCG_OK;
+  return enqueue_post_update(c);
 }
 
 int ensure_staging(pcg_context *c, size_t doubles, size_t metas) {
@@ -509,6 +575,12 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_dt_out);
   cudaFree(c->d_items);
   cudaFree(c->d_gcells);
+  cudaFree(c->d_restr);
+  cudaFree(c->d_flux);
+  cudaFree(c->d_restr_begin);
+  cudaFree(c->d_flux_begin);
+  cudaFree(c->d_restr_dsts);
+  cudaFree(c->d_leaf_ids);
   cudaFree(c->d_plan);
   cudaFree(c->d_tiles);
   cudaFree(c->d_wall);
@@ -832,6 +904,59 @@ int pcg_set_ghost_items(pcg_context *c, const pcg_ghost_item *items, int32_t n) 
   }
   c->items_user.assign(items, items + n);
   c->topo_dirty = true;
+  return PCG_OK;
+}
+
+int pcg_set_restriction_items(pcg_context *c, int32_t n, const int32_t *src, const int32_t *dst,
+                              int32_t only_overlapped) {
+  if (!c || n < 0 || (n > 0 && (!src || !dst))) return fail(PCG_E_INVALID, "bad restriction list");
+  std::lock_guard<std::mutex> lk(c->mu);
+  std::vector<int4> v;
+  for (int k = 0; k < n; k++) {
+    if (!valid_id(c, src[k]) || !valid_id(c, dst[k]) || src[k] == dst[k])
+      return fail(PCG_E_INVALID, "restriction item " + std::to_string(k) + ": bad ids");
+    const pcg::PatchDev &S = c->h_patches[src[k]], &D = c->h_patches[dst[k]];
+    if (S.nq != D.nq || S.np_w < 1 || D.np_w < 1)
+      return fail(PCG_E_INVALID, "restriction item " + std::to_string(k) + ": not SWE patches");
+    v.push_back(make_int4(src[k], dst[k], only_overlapped ? 1 : 0, 1));
+  }
+  c->restr_user = v;
+  c->topo_dirty = true;
+  return PCG_OK;
+}
+
+int pcg_set_flux_correction_items(pcg_context *c, int32_t n, const int32_t *src, const int32_t *dst,
+                                  const int32_t *dim, const int32_t *dir, double g_flux) {
+  if (!c || n < 0 || (n > 0 && (!src || !dst || !dim || !dir))) return fail(PCG_E_INVALID, "bad flux list");
+  std::lock_guard<std::mutex> lk(c->mu);
+  std::vector<int4> v;
+  for (int k = 0; k < n; k++) {
+    if (!valid_id(c, src[k]) || !valid_id(c, dst[k]) || dim[k] < 0 || dim[k] > 1 || (dir[k] != 1 && dir[k] != -1))
+      return fail(PCG_E_INVALID, "flux item " + std::to_string(k) + ": bad arguments");
+    if (c->h_patches[src[k]].nq != 3 || c->h_patches[dst[k]].nq != 3)
+      return fail(PCG_E_INVALID, "flux item " + std::to_string(k) + ": needs 3 unknowns");
+    v.push_back(make_int4(src[k], dst[k], dim[k], dir[k]));
+  }
+  c->flux_user = v;
+  c->g_flux = g_flux;
+  c->topo_dirty = true;
+  return PCG_OK;
+}
+
+int pcg_restrict_all(pcg_context *c) {
+  if (!c) return fail(PCG_E_INVALID, "null context");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  if (!c->h_restr.empty()) {
+    int nd = (int)c->restr_dsts.size();
+    PCG_CUDA(pcg::launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
+    PCG_CUDA(pcg::launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
+                                        c->d_restr_begin, nd));
+    PCG_CUDA(pcg::launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
+  }
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
   return PCG_OK;
 }
 

@@ -830,9 +830,8 @@ __global__ void k_compute_fluxes(double *slab, const PatchDev *patches, const in
 // DefaultFluxCorrectionTemplate::applyCorrection; the corrections of several
 // source cells can land in one destination cell, so a single thread applies
 // them in the reference's order.
-__global__ void k_flux_correction(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                                  int src, int dst, int dim, int dir) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void flux_correction_one(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                    int src, int dst, int dim, int dir) {
   PatchDev S = patches[src], D = patches[dst];
   PatchTimeDev ST = times[src], DT = times[dst];
   double lo = fmax(ST.time, DT.time);
@@ -875,6 +874,37 @@ __global__ void k_flux_correction(double *slab, const PatchDev *patches, const P
         slab[id] = __dadd_rn(slab[id], corr);
       }
     }
+  }
+}
+
+__global__ void k_flux_correction(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                  int src, int dst, int dim, int dir) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  flux_correction_one(slab, patches, times, src, dst, dim, dir);
+}
+
+// Batched flux correction: block b applies the items [begin[b], begin[b+1])
+// (all with the same destination) in list order.
+__global__ void k_flux_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                             const int4 *items, const int *begin) {
+  if (threadIdx.x != 0) return;
+  for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
+    int4 it = items[k];  // src, dst, dim, dir
+    flux_correction_one(slab, patches, times, it.x, it.y, it.z, it.w);
+  }
+}
+
+// Clears uNew and the uOld interior of the listed (virtual) patches before
+// the restriction accumulates into them (Patch accessor clearRegion, called
+// from GridLevelTransfer::switchToAndAddVirtualSubgrid).
+__global__ void k_clear_interior(double *slab, const PatchDev *patches, const int *ids, int count) {
+  if ((int)blockIdx.x >= count) return;
+  PatchDev P = patches[ids[blockIdx.x]];
+  int n = P.nx * P.ny;
+  for (int k = threadIdx.x; k < P.nq * n; k += blockDim.x) {
+    int q = k / n, c = k - q * n, x = c / P.ny, y = c - x * P.ny;
+    slab[idx_unew(P, q, x, y)] = 0.0;
+    slab[idx_uold(P, q, x, y)] = 0.0;
   }
 }
 
@@ -1041,6 +1071,21 @@ cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev 
                                   const int *ids, int count, double gf) {
   if (count <= 0) return cudaSuccess;
   k_compute_fluxes<<<count, 128, 0, st>>>(slab, patches, ids, count, gf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *patches,
+                              const PatchTimeDev *times, const int4 *items, const int *begin,
+                              int n_dst) {
+  if (n_dst <= 0) return cudaSuccess;
+  k_flux_items<<<n_dst, 32, 0, st>>>(slab, patches, times, items, begin);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev *patches,
+                                  const int *ids, int count) {
+  if (count <= 0) return cudaSuccess;
+  k_clear_interior<<<count, 256, 0, st>>>(slab, patches, ids, count);
   return cudaGetLastError();
 }
 

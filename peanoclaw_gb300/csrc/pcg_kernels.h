@@ -65,6 +65,11 @@ cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const
                                             const int *ids, int count);
 cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const int *ids, int count, double gf);
+cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *patches,
+                              const PatchTimeDev *times, const int4 *items, const int *begin,
+                              int n_dst);
+cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev *patches,
+                                  const int *ids, int count);
 cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev *patches,
                                    const PatchTimeDev *times, int src, int dst, int dim, int dir);
 

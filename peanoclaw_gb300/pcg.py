@@ -92,6 +92,9 @@ SIGNATURES = {
     "pcg_apply_flux_correction": (C.c_int, [_CTX, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "pcg_set_ghost_items": (C.c_int, [_CTX, C.POINTER(GhostItem), C.c_int32]),
     "pcg_set_group_max_dt": (C.c_int, [_CTX, C.c_int32, C.c_double]),
+    "pcg_set_restriction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, C.c_int32]),
+    "pcg_set_flux_correction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, _I2, _I2, C.c_double]),
+    "pcg_restrict_all": (C.c_int, [_CTX]),
     "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
@@ -259,6 +262,20 @@ class Context:
         arr = items_array(items)
         ptr = arr.ctypes.data_as(C.POINTER(GhostItem)) if len(arr) else None
         check(lib().pcg_set_ghost_items(self.h, ptr, len(arr)))
+
+    def set_restriction_items(self, src, dst, only_overlapped=True):
+        src = np.ascontiguousarray(src, dtype=np.int32)
+        dst = np.ascontiguousarray(dst, dtype=np.int32)
+        check(lib().pcg_set_restriction_items(self.h, len(src), src.ctypes.data_as(_I2),
+                                              dst.ctypes.data_as(_I2), int(only_overlapped)))
+
+    def set_flux_correction_items(self, src, dst, dim, direction, g_flux=1.0):
+        arrs = [np.ascontiguousarray(a, dtype=np.int32) for a in (src, dst, dim, direction)]
+        check(lib().pcg_set_flux_correction_items(self.h, len(arrs[0]),
+                                                  *[a.ctypes.data_as(_I2) for a in arrs], float(g_flux)))
+
+    def restrict_all(self):
+        check(lib().pcg_restrict_all(self.h))
 
     def set_group_max_dt(self, group, max_dt):
         check(lib().pcg_set_group_max_dt(self.h, group, float(max_dt)))

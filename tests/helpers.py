@@ -74,3 +74,65 @@ def gpu_patchset(ctx, ps):
 
 def slab_for(ps, slack=1.2):
     return int(sum(P.vector_size(n) + 32 for n in ps.n) * slack) + 4096
+
+
+def oracle_amr_patchset(ps):
+    pats = []
+    for p in range(len(ps)):
+        leaf = bool(ps.leaf[p])
+        op = oracle_patch_from(ps.vector(p).copy(), ps.n[p], ps.pos[p], ps.size[p], ps.level[p],
+                               leaf=leaf, virtual=not leaf)
+        op.s.restr_lower[0], op.s.restr_lower[1] = ps.restr_lower[p]
+        op.s.restr_upper[0], op.s.restr_upper[1] = ps.restr_upper[p]
+        pats.append(op)
+    return pats
+
+
+def oracle_restrict_all(pats, ps):
+    """Clear every destination, restrict in list order, post-process."""
+    dsts = []
+    for s, d in ps.restrict_items:
+        if d not in dsts:
+            dsts.append(int(d))
+    for d in dsts:
+        pats[d].unew()[:] = 0.0
+        g = pats[d].s.ghost
+        pats[d].uold()[:, g:-g, g:-g] = 0.0
+    for s, d in ps.restrict_items:
+        O.restrict(pats[s], pats[d], only_overlapped=True, swe=True)
+    for d in dsts:
+        O.lib().pco_swe_post_process_restriction(pats[d].ptr())
+
+
+def oracle_amr_step(pats, ps, prm, max_dt, g_flux=1.0, flux=True):
+    dt = O.grid_step(pats, ps.items, ps.wall, prm, max_dt)[0]
+    if flux and len(ps.flux_items):
+        for p in range(len(ps)):
+            if ps.leaf[p]:
+                O.lib().pco_compute_fluxes(pats[p].ptr(), g_flux)
+        for s, d, dim, direction in ps.flux_items:
+            O.lib().pco_apply_flux_correction(pats[s].ptr(), pats[d].ptr(), int(dim), int(direction))
+    oracle_restrict_all(pats, ps)
+    return dt
+
+
+def gpu_amr_patchset(ctx, ps, flux=True, g_flux=1.0):
+    from peanoclaw_gb300.scenarios import remap_items
+    ids = []
+    for p in range(len(ps)):
+        leaf = bool(ps.leaf[p])
+        pid = ctx.alloc(ps.n[p], pos=ps.pos[p], size=ps.size[p], level=ps.level[p], leaf=leaf,
+                        virtual=not leaf)
+        ids.append(pid)
+        if ps.wall[p]:
+            ctx.set_boundary(pid, ps.wall[p])
+        if not leaf:
+            ctx.set_time(pid, restr_lower=ps.restr_lower[p], restr_upper=ps.restr_upper[p])
+    ids = np.array(ids, dtype=np.int32)
+    ctx.upload_many(ids, ps.packed)
+    ctx.set_ghost_items(remap_items(ps.items, ids))
+    ctx.set_restriction_items(ids[ps.restrict_items[:, 0]], ids[ps.restrict_items[:, 1]], True)
+    if flux and len(ps.flux_items):
+        f = ps.flux_items
+        ctx.set_flux_correction_items(ids[f[:, 0]], ids[f[:, 1]], f[:, 2], f[:, 3], g_flux)
+    return ids
