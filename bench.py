@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--cpu-sample-grid", type=int, default=48)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the secondary configurations (dam break, AMR, serving)")
+    ap.add_argument("--amr-steps", type=int, default=100)
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rate", type=float, default=1.0)
     return ap.parse_args()
 
 
@@ -184,6 +189,71 @@ def cpu_baseline(args, prm, seconds_target=15.0):
                       % (args.cpu_sample_grid, args.cpu_sample_grid, len(ps), cells, steps, el)}
 
 
+def bench_radial(prm):
+    """9 x 9 patches of 16 x 16 cells, radial dam break, 100 steps: batched and plain."""
+    from peanoclaw_gb300 import pcg as P
+    from peanoclaw_gb300 import scenarios as S
+    out = {}
+    for mode, name in ((P.PCG_MODE_BATCHED, "batched"), (P.PCG_MODE_PLAIN, "plain")):
+        ps = S.radial_dam_break(npx=9, n=16)
+        ctx, ids = build_context(ps, prm)
+        ctx.upload_many(ids, ps.packed)
+        ctx.set_group_max_dt(0, 1e9)
+        c0, m0 = ctx.stats()
+        ctx.run(100, mode)
+        c1, m1 = ctx.stats()
+        ctx.close()
+        out[name] = ps.cells() * 100 / ((m1 - m0) / 1e3)
+    out["cells"] = 81 * 256
+    out["steps"] = 100
+    return out
+
+
+def bench_amr(prm, steps):
+    """Adaptive breaking dam: 3 levels of 3x refinement, 27 x 27 cells per patch,
+    ghost interpolation, flux correction and restriction in every step."""
+    from peanoclaw_gb300 import pcg as P
+    from peanoclaw_gb300 import scenarios as S
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    ps = S.breaking_dam_amr(base=9, n=27, levels=3)
+    slab = int(sum(P.vector_size(n) + 32 for n in ps.n)) + 4096
+    res = {"patches": len(ps), "leaves": int(sum(ps.leaf)), "leaf_cells": ps.meta["leaf_cells"]}
+    for mode, name, k in ((P.PCG_MODE_BATCHED, "batched", steps), (P.PCG_MODE_PLAIN, "plain", 5)):
+        ctx = P.Context(slab_doubles=slab, max_patches=len(ps) + 16, max_groups=1, params=prm)
+        from helpers import gpu_amr_patchset
+        gpu_amr_patchset(ctx, ps)
+        ctx.restrict_all()
+        ctx.set_group_max_dt(0, 1e9)
+        ctx.run(3, mode)
+        c0, m0 = ctx.stats()
+        ctx.run(k, mode)
+        c1, m1 = ctx.stats()
+        ctx.close()
+        res[name] = ps.meta["leaf_cells"] * k / ((m1 - m0) / 1e3)
+        res[name + "_ms_per_step"] = (m1 - m0) / k
+    return res
+
+
+def bench_serving(args, prm):
+    """Scenario stream with Poisson arrivals (seed 42): radial dam breaks and
+    Gaussian-hump tsunamis, 1e4..4e6 cells, end time U[0.05, 0.5]."""
+    from peanoclaw_gb300 import serving as SV
+    reqs = SV.make_requests(args.serve_requests, rate=args.serve_rate, seed=42, n=32)
+    need = sum(int(r.cells * 1.4) for r in reqs)
+    srv = SV.Server(slab_doubles=int(need * 8) + (1 << 24), max_groups=16, max_patches=60000, params=prm)
+    try:
+        done, wall = srv.serve(reqs, max_wall=240.0)
+    finally:
+        srv.close()
+    lat = np.array([r.finished - r.arrival for r in done])
+    cu = sum(r.cell_updates for r in done)
+    return {"requests": len(reqs), "completed": len(done), "rate_per_s": args.serve_rate,
+            "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "cell_updates_per_s": cu / wall, "wall_s": wall,
+            "max_concurrent_groups": 16}
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -293,10 +363,15 @@ def main():
                        "each step) + download; bytes are per timestep" % args.steps}
         assert np.isfinite(hist).all()
 
+    ctx.close()
     cpu = None
     if rank == 0 and not args.no_cpu and ws == 1:
         cpu = cpu_baseline(args, prm)
-    ctx.close()
+    configs = None
+    if rank == 0 and not args.no_configs:
+        configs = {"radial_dam_break_9x9x16": bench_radial(prm),
+                   "adaptive_breaking_dam_3_levels": bench_amr(prm, args.amr_steps),
+                   "serving_stream": bench_serving(args, prm)}
 
     if rank == 0:
         line = {
@@ -324,6 +399,7 @@ def main():
             "batched_over_plain": (value / ws) / plain if plain else None,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "configs": configs,
             "clocks": clk,
             "gpu_launches": 6 * args.steps,
             "wall_s": wall,
