@@ -89,6 +89,42 @@ PCG_HD uint32_t float_bits(float f) {
 #endif
 }
 
+PCG_HD float fma_f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+  return __fmaf_rn(a, b, c);
+#else
+  return std::fmaf(a, b, c);
+#endif
+}
+
+PCG_HD float mul_f(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+
+PCG_HD int32_t rint_f(float a) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rn(a);
+#else
+  return (int32_t)std::lrintf(a);
+#endif
+}
+
+// 2^64 * v as a signed 64-bit integer for |v| < 2^-2 (v = 0 gives 0), read
+// straight from the float's bits.
+PCG_HD int64_t scaled64(float v) {
+  uint32_t fb = float_bits(v);
+  int e = (int)((fb >> 23) & 0xFFu);
+  if (e == 0) return 0;
+  uint64_t m = (uint64_t)((fb & 0x7FFFFFu) | 0x800000u);
+  int sh = e - 86;  // 2^64 * 1.m * 2^(e-127) = m << (e - 86)
+  uint64_t mag = sh >= 0 ? (m << sh) : (sh > -64 ? (m >> (-sh)) : 0ull);
+  return (fb >> 31) ? -(int64_t)mag : (int64_t)mag;
+}
+
 // FP32 seeds: only their accuracy matters (the integer refinement corrects
 // any seed within a few units of 2^-22), not their exact value.
 PCG_HD float rcp_seed(float d) {
@@ -167,16 +203,30 @@ PCG_HD double div_rn(double a, double b) {
   if ((B & kFrac) == 0) {
     q = x;  // divisor is a power of two: exact
   } else {
-    // leading 23 fraction bits of the divisor as a float in [1, 2); its
-    // reciprocal r in (0.5, 1] gives V0 = r * 2^64 straight from r's bits
-    float d = bits_float(0x3F800000u | (uint32_t)((mb >> 29) & 0x7FFFFFu));
-    uint32_t rb = float_bits(rcp_seed(d));
+    // 1/D for D = mb / 2^52 in [1, 2): FP32 seed refined once with the
+    // divisor split into two floats (d_hi exact 24 bits, d_lo the rest),
+    // 1/D ~ r0 (1 + e + e^2) with e = 1 - D r0, accurate to ~2^-45
+    float d_hi = bits_float(0x3F800000u | (uint32_t)((mb >> 29) & 0x7FFFFFu));
+    float d_lo = mul_f((float)(uint32_t)(mb & 0x1FFFFFFFull), 2.220446049250313e-16f);  // * 2^-52
+    // After the FP32 Newton step r0 is 1/d_hi to float precision; for
+    // d_hi == 1 that is r0 == 1 exactly (any seed within 2^-12 of it), so V
+    // below is clamped under 2^64 and corr <= 0 keeps it there.
+    float r0 = rcp_seed(d_hi);
+    r0 = fma_f(r0, fma_f(-d_hi, r0, 1.0f), r0);
+    float er = fma_f(-d_hi, r0, 1.0f);
+    er = fma_f(-d_lo, r0, er);
+    float corr = mul_f(r0, fma_f(er, er, er));
+    uint32_t rb = float_bits(r0);
     uint64_t V = ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u)) << ((int)((rb >> 23) & 0xFFu) - 86);
-    if (((rb >> 23) & 0xFFu) >= 127u) V = 0xFFFFFFFFFFFFFFFFull;  // r == 1: clamp below 2^64
-    V = recip_step(mb, V);
-    V = recip_step(mb, V);
-    q = mulhi(x, V);
+    if (((rb >> 23) & 0xFFu) >= 127u) V = 0xFFFFFFFFFFFFFFFFull;  // r0 == 1: clamp below 2^64
+    V = (uint64_t)((int64_t)V + scaled64(corr));
+    q = mulhi(x, V);  // within a few hundred units of the quotient
     int64_t rem = (int64_t)((x << 52) - q * mb);
+    // one FP32 correction step: delta = rem / mb, then exact fix-up
+    float dq = mul_f(mul_f((float)(int32_t)(rem >> 32), r0), 9.5367431640625e-07f);  // * 2^-20
+    int64_t di = (int64_t)rint_f(dq);
+    q = (uint64_t)((int64_t)q + di);
+    rem -= di * (int64_t)mb;
     if (rem < 0) { q -= 1; rem += (int64_t)mb; }
     if (rem < 0) { q -= 1; rem += (int64_t)mb; }
     if (rem >= (int64_t)mb) { q += 1; rem -= (int64_t)mb; }
@@ -215,17 +265,32 @@ PCG_HD double sqrt_rn(double a) {
   if (M == kHidden) {
     s = kHidden;  // power of four: exact
   } else {
-    // M / 2^52 in [1, 4) as a float (leading 24 bits); its reciprocal square
-    // root r in (0.5, 1] gives Y0 = r * 2^64 straight from r's bits
-    float f = bits_float(((M >> 53) ? 0x40000000u : 0x3F800000u) |
-                         (uint32_t)((M >> ((M >> 53) ? 30 : 29)) & 0x7FFFFFu));
-    uint32_t rb = float_bits(rsqrt_seed(f));
+    // 1/sqrt(F) for F = M / 2^52 in [1, 4): FP32 seed refined once with F
+    // split into two floats, 1/sqrt(F) ~ r0 (1 + e/2 + 3e^2/8), e = 1 - F r0^2
+    const bool hi = (M >> 53) != 0;
+    const int sh = hi ? 30 : 29;
+    float f_hi = bits_float((hi ? 0x40000000u : 0x3F800000u) | (uint32_t)((M >> sh) & 0x7FFFFFu));
+    float f_lo = mul_f((float)(uint32_t)(M & ((1ull << sh) - 1)), 2.220446049250313e-16f);  // * 2^-52
+    float r0 = rsqrt_seed(f_hi);
+    // FP32 Newton step: r0 to float precision
+    r0 = fma_f(mul_f(r0, 0.5f), fma_f(-mul_f(f_hi, r0), r0, 1.0f), r0);
+    float s0 = mul_f(f_hi, r0);
+    float s0e = fma_f(f_hi, r0, -s0);          // f_hi * r0 = s0 + s0e exactly
+    float er = fma_f(-s0, r0, 1.0f);
+    er = fma_f(-s0e, r0, er);
+    er = fma_f(-mul_f(f_lo, r0), r0, er);
+    float corr = mul_f(r0, fma_f(mul_f(er, 0.375f), er, mul_f(er, 0.5f)));
+    uint32_t rb = float_bits(r0);
     uint64_t Y = ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u)) << ((int)((rb >> 23) & 0xFFu) - 86);
-    if (((rb >> 23) & 0xFFu) >= 127u) Y = 0xFFFFFFFFFFFFFFFFull;  // r == 1: clamp below 2^64
-    Y = rsqrt_step(M, Y);
-    Y = rsqrt_step(M, Y);
-    s = mulhi(M, Y);
+    if (((rb >> 23) & 0xFFu) >= 127u) Y = 0xFFFFFFFFFFFFFFFFull;  // r0 == 1: clamp below 2^64
+    Y = (uint64_t)((int64_t)Y + scaled64(corr));
+    s = mulhi(M, Y);  // within a few hundred units of floor(sqrt(M * 2^52))
     int64_t rem = (int64_t)((M << 52) - s * s);
+    // one FP32 correction step: delta = rem / (2 s), 1/(2 s) ~ r0 * 2^-53
+    float ds = mul_f(mul_f((float)(int32_t)(rem >> 32), r0), 4.76837158203125e-07f);  // * 2^-21
+    int64_t di = (int64_t)rint_f(ds);
+    rem -= di * (int64_t)(2 * s) + di * di;
+    s = (uint64_t)((int64_t)s + di);
     if (rem < 0) { s -= 1; rem += (int64_t)(2 * s + 1); }
     if (rem < 0) { s -= 1; rem += (int64_t)(2 * s + 1); }
     if (rem > (int64_t)(2 * s)) { rem -= (int64_t)(2 * s + 1); s += 1; }
