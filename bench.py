@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--cpu-sample-grid", type=int, default=48)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default batched schedule instead of autotuning it")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the secondary configurations (dam break, AMR, serving)")
     ap.add_argument("--amr-steps", type=int, default=100)
@@ -289,8 +291,14 @@ def main():
     ctx.upload_many(ids, ps.packed)
     ctx.set_group_max_dt(0, 1e9)
 
-    # warm-up (also instantiates the graph)
+    # warm-up, the schedule autotuner (untimed; it advances the simulation by
+    # one or two steps per candidate) and the graph instantiation
     ctx.run(max(1, args.warmup), P.PCG_MODE_BATCHED)
+    tuned = None
+    if not args.no_autotune:
+        tuned = ctx.autotune(reps=2)
+        ctx.run(2, P.PCG_MODE_BATCHED)
+    sched = ctx.get_schedule()
     dist_barrier(dist)
     ctx.synchronize()
     clocks = ClockSampler(local)
@@ -389,12 +397,17 @@ def main():
                          "frac": achieved / fp64_peak, "traffic": None,
                          "peak_source": "measured live (DFMA chain probe, FMA = 2 flops)",
                          "flop_per_cell": FLOP_PER_CELL,
-                         "kernels": "k_sweep_tiles + k_update_tiles",
+                         "kernels": ("k_sweep_tiles + k_update_tiles" if sched[0] == P.SCHED_TILES
+                                     else "k_sweep_strips + k_update_strips"),
                          "hbm": {"achieved_gbs": alg_bytes / (step_ms_phase / 1e3) / 1e9,
                                  "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json",
                                  "alg_bytes_per_step": alg_bytes}},
             "phase_ms": {"reset": ph[0], "ghost_items": ph[1], "walls": ph[2], "sweep": ph[3],
                          "update": ph[4]},
+            "schedule": {"kind": "tiles" if sched[0] == P.SCHED_TILES else "strips",
+                         "variant": sched[1], "chunk": sched[2],
+                         "autotune_ms_per_step": ({"%s/%d/%d" % ("tiles" if k[0] == 0 else "strips", k[1], k[2]): m
+                                                   for k, m in tuned} if tuned else None)},
             "plain_per_patch_value": plain,
             "batched_over_plain": (value / ws) / plain if plain else None,
             "e2e": e2e,

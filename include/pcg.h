@@ -214,6 +214,38 @@ int pcg_stats(pcg_context *ctx, int64_t *cell_updates, double *device_ms);
 /* Block until all work issued on the context has finished. */
 int pcg_synchronize(pcg_context *ctx);
 
+/* --------------------------------------------- batched schedule + autotuner */
+
+/* No counterpart in the reference (its block sweep is one loop nest).  How the
+ * BATCHED sweep and update map patches onto the GPU; every schedule computes
+ * bit-identical results.
+ *   kind 0: one 16x16 tile of a patch per CTA iteration (256 threads);
+ *   kind 1: warp strips: a warp marches strips of up to 32 rows and `chunk`
+ *           columns (1..32) of one or more patches along x; `variant` picks
+ *           the CTA size / register budget (0..3: 4 warps x 4 CTAs/SM,
+ *           4 x 6, 8 x 2, 8 x 3). */
+typedef struct pcg_schedule {
+  int32_t kind;
+  int32_t variant;
+  int32_t chunk;
+  int32_t reserved_;
+} pcg_schedule;
+#define PCG_SCHED_TILES 0
+#define PCG_SCHED_STRIPS 1
+/* Fix the schedule of the context (overrides any tuned choice). */
+int pcg_set_schedule(pcg_context *ctx, const pcg_schedule *s);
+int pcg_get_schedule(pcg_context *ctx, pcg_schedule *s);
+/* Autotuner: runs `reps` BATCHED steps with each candidate schedule (tiles;
+ * strips x 4 variants x chunk 32 / 16), times each candidate's steps with
+ * CUDA events, keeps the fastest for this context and caches it for the
+ * process under the key (SM count, histogram of leaf patch shapes), so later
+ * contexts with the same patch mix start with it.  The simulation advances by
+ * reps x n_candidates steps (each group by its own dt, as in pcg_step); the
+ * patch time intervals record them.  tried[cap] / ms[cap] (may be NULL)
+ * receive the candidates and their mean step time; *n_tried their number. */
+int pcg_autotune(pcg_context *ctx, int32_t reps, pcg_schedule *tried, double *ms, int32_t cap,
+                 int32_t *n_tried);
+
 /* ----------------------------------------------------------- diagnostics */
 
 /* No counterpart in the reference.  One BATCHED step with CUDA events between

@@ -166,6 +166,17 @@ struct pcg_context {
   int64_t cells_per_step = 0;
   int sweep_grid = 0;
 
+  // batched sweep/update schedule (pcg_schedule); warp-strip work list
+  pcg_schedule sched{PCG_SCHED_STRIPS, 0, 32, 0};
+  bool sched_fixed = false;          // set by pcg_set_schedule / pcg_autotune
+  std::string shape_key;             // SM count + leaf shape histogram
+  std::vector<pcg::StripItem> h_sitems;
+  std::vector<pcg::StripGroup> h_sgroups;
+  pcg::StripItem *d_sitems = nullptr;
+  pcg::StripGroup *d_sgroups = nullptr;
+  size_t d_sitems_cap = 0, d_sgroups_cap = 0;
+  int strip_grid = 0, update_grid = 0;
+
   double *d_solve_out = nullptr;
   size_t solve_smem_set = 0;
 
@@ -251,6 +262,93 @@ int upload_patches(pcg_context *c) {
                            sizeof(pcg::PatchDev) * c->max_patches, cudaMemcpyHostToDevice, c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   c->patches_dirty = false;
+  return PCG_OK;
+}
+
+// Schedules picked by pcg_autotune, per (SM count, leaf shape histogram).
+std::mutex g_tuned_mu;
+std::map<std::string, pcg_schedule> g_tuned;
+
+std::string shape_key(pcg_context *c) {
+  std::map<std::pair<int, int>, int64_t> hist;
+  for (int p : c->leaf_ids) hist[{c->h_patches[p].nx, c->h_patches[p].ny}]++;
+  std::string k = "sm" + std::to_string(c->num_sms);
+  for (auto &e : hist)
+    k += ";" + std::to_string(e.first.first) + "x" + std::to_string(e.first.second) + ":" +
+         std::to_string(e.second);
+  return k;
+}
+
+// Warp-strip work list: every leaf patch is cut into strips of at most 32 rows
+// (balanced heights) and `chunk` columns (balanced widths); strips of equal
+// (rows, columns) are packed floor(32 / max(rows, columns)) to a warp item.
+// Items are ordered by decreasing work so that grid-strided warps get an even
+// mix.
+void build_strips(pcg_context *c, int chunk) {
+  std::map<std::pair<int, int>, std::vector<pcg::StripGroup>> cls;
+  for (int p : c->leaf_ids) {
+    const pcg::PatchDev &P = c->h_patches[p];
+    const int nsy = (P.ny + 31) / 32;
+    for (int ky = 0; ky < nsy; ky++) {
+      const int y0 = (int)((int64_t)ky * P.ny / nsy), y1 = (int)((int64_t)(ky + 1) * P.ny / nsy);
+      const int hs = y1 - y0;
+      const int wcap = std::min(chunk, 32 / (32 / hs));
+      const int nsx = (P.nx + wcap - 1) / wcap;
+      for (int kx = 0; kx < nsx; kx++) {
+        const int x0 = (int)((int64_t)kx * P.nx / nsx), x1 = (int)((int64_t)(kx + 1) * P.nx / nsx);
+        cls[{hs, x1 - x0}].push_back(pcg::StripGroup{p, (short)x0, (short)y0});
+      }
+    }
+  }
+  std::vector<std::pair<int64_t, std::pair<int, int>>> order;
+  for (auto &e : cls) {
+    const int hs = e.first.first, w = e.first.second;
+    const int G = std::max(1, std::min(32 / hs, 32 / w));
+    order.push_back({(int64_t)G * hs * w, e.first});
+  }
+  std::sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+  c->h_sitems.clear();
+  c->h_sgroups.clear();
+  for (auto &o : order) {
+    const int hs = o.second.first, w = o.second.second;
+    const int G = std::max(1, std::min(32 / hs, 32 / w));
+    const std::vector<pcg::StripGroup> &gs = cls[o.second];
+    for (size_t k = 0; k < gs.size(); k += G) {
+      pcg::StripItem it;
+      it.g0 = (int)c->h_sgroups.size();
+      it.ngroups = (unsigned char)std::min<size_t>(G, gs.size() - k);
+      it.hs = (unsigned char)hs;
+      it.w = (unsigned char)w;
+      it.pad_ = 0;
+      for (int g = 0; g < it.ngroups; g++) c->h_sgroups.push_back(gs[k + g]);
+      c->h_sitems.push_back(it);
+    }
+  }
+}
+
+// Upload the strip list of the current schedule and size its grids.
+int apply_schedule(pcg_context *c) {
+  build_strips(c, c->sched.chunk);
+  int rc;
+  if ((rc = ensure_device(c, &c->d_sitems, &c->d_sitems_cap, c->h_sitems.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_sgroups, &c->d_sgroups_cap, c->h_sgroups.size())) != PCG_OK) return rc;
+  if (!c->h_sitems.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_sitems, c->h_sitems.data(), sizeof(pcg::StripItem) * c->h_sitems.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+  if (!c->h_sgroups.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_sgroups, c->h_sgroups.data(),
+                             sizeof(pcg::StripGroup) * c->h_sgroups.size(), cudaMemcpyHostToDevice,
+                             c->stream));
+  const int v = c->sched.variant;
+  int per_sm = 0;
+  PCG_CUDA(pcg::strip_occupancy(v, &per_sm));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t warps = pcg::kStripVariants[v].warps;
+  const int64_t need = std::max<int64_t>(1, ((int64_t)c->h_sitems.size() + warps - 1) / warps);
+  c->strip_grid = (int)std::min<int64_t>((int64_t)c->num_sms * per_sm, need);
+  c->update_grid = (int)std::min<int64_t>((int64_t)c->num_sms * 8,
+                                          std::max<int64_t>(1, ((int64_t)c->h_sitems.size() + 7) / 8));
+  c->graph_valid = false;
   return PCG_OK;
 }
 
@@ -381,6 +479,13 @@ int rebuild_topology(pcg_context *c) {
   PCG_CUDA(pcg::sweep_occupancy(&per_sm));
   if (per_sm < 1) per_sm = 1;
   c->sweep_grid = (int)std::min<int64_t>((int64_t)c->num_sms * per_sm, std::max<int64_t>(1, (int64_t)c->h_tiles.size()));
+  c->shape_key = shape_key(c);
+  if (!c->sched_fixed) {
+    std::lock_guard<std::mutex> lk(g_tuned_mu);
+    auto it = g_tuned.find(c->shape_key);
+    if (it != g_tuned.end()) c->sched = it->second;
+  }
+  if ((rc = apply_schedule(c)) != PCG_OK) return rc;
   c->patches_dirty = true;
   c->topo_dirty = false;
   c->graph_valid = false;
@@ -414,6 +519,31 @@ int enqueue_post_update(pcg_context *c) {
   return PCG_OK;
 }
 
+// Batched sweep and update with the context's schedule.
+int enqueue_sweep(pcg_context *c) {
+  using namespace pcg;
+  if (c->sched.kind == PCG_SCHED_TILES)
+    PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
+                          (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+  else
+    PCG_CUDA(launch_sweep_strips(c->stream, c->sched.variant, c->strip_grid, c->slab, c->d_patches,
+                                 c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
+                                 c->d_patch_smax, c->d_group_dt));
+  return PCG_OK;
+}
+
+int enqueue_update(pcg_context *c) {
+  using namespace pcg;
+  if (c->sched.kind == PCG_SCHED_TILES)
+    PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
+                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+  else
+    PCG_CUDA(launch_update_strips(c->stream, c->update_grid, c->slab, c->d_patches, c->d_times,
+                                  c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
+                                  c->d_patch_smax, c->d_group_dt));
+  return PCG_OK;
+}
+
 // Enqueue one synchronous step (no synchronisation, capturable in BATCHED mode).
 int enqueue_step(pcg_context *c, int mode) {
   using namespace pcg;
@@ -423,10 +553,9 @@ int enqueue_step(pcg_context *c, int mode) {
     PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, c->d_gcells,
                                 c->n_copy_cells, c->n_interp_cells, c->d_plan, nullptr));
     PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
-    PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
-                          (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
-    PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
-                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+    int rc;
+    if ((rc = enqueue_sweep(c)) != PCG_OK) return rc;
+    if ((rc = enqueue_update(c)) != PCG_OK) return rc;
   } else {
     for (int p : c->leaf_ids)
       PCG_CUDA(launch_fill_patch(c->stream, c->slab, c->d_patches, c->d_times, c->d_items,
@@ -583,6 +712,8 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_leaf_ids);
   cudaFree(c->d_plan);
   cudaFree(c->d_tiles);
+  cudaFree(c->d_sitems);
+  cudaFree(c->d_sgroups);
   cudaFree(c->d_wall);
   cudaFree(c->d_solve_out);
   cudaFree(c->d_hist);
@@ -972,6 +1103,8 @@ static int check_solvable(pcg_context *c) {
     const pcg::PatchDev &P = c->h_patches[p];
     if (P.g != 1 || P.nq != 3 || P.np_w < 1)
       return fail(PCG_E_INVALID, "leaf patch " + std::to_string(p) + " is not an SWE patch (ghost 1, 3 unknowns, b)");
+    if (P.nx > 32767 || P.ny > 32767)  // tile / strip coordinates are 16-bit
+      return fail(PCG_E_INVALID, "leaf patch " + std::to_string(p) + " has more than 32767 cells per edge");
   }
   return PCG_OK;
 }
@@ -1059,6 +1192,94 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   return PCG_OK;
 }
 
+namespace {
+
+int check_schedule(const pcg_schedule *s) {
+  if (!s) return fail(PCG_E_INVALID, "null schedule");
+  if (s->kind == PCG_SCHED_TILES) return PCG_OK;
+  if (s->kind != PCG_SCHED_STRIPS) return fail(PCG_E_INVALID, "schedule kind must be 0 or 1");
+  if (s->variant < 0 || s->variant >= pcg::kNumStripVariants)
+    return fail(PCG_E_INVALID, "strip variant out of range");
+  if (s->chunk < 1 || s->chunk > 32) return fail(PCG_E_INVALID, "strip chunk must be in 1..32");
+  return PCG_OK;
+}
+
+}  // namespace
+
+int pcg_set_schedule(pcg_context *c, const pcg_schedule *s) {
+  if (!c) return fail(PCG_E_INVALID, "null context");
+  int rc = check_schedule(s);
+  if (rc != PCG_OK) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  c->sched = *s;
+  c->sched.reserved_ = 0;
+  if (c->sched.kind == PCG_SCHED_TILES) { c->sched.variant = 0; c->sched.chunk = 32; }
+  c->sched_fixed = true;
+  c->graph_valid = false;
+  if (!c->topo_dirty) return apply_schedule(c);
+  return PCG_OK;
+}
+
+int pcg_get_schedule(pcg_context *c, pcg_schedule *s) {
+  if (!c || !s) return fail(PCG_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  *s = c->sched;
+  return PCG_OK;
+}
+
+int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, int32_t cap,
+                 int32_t *n_tried) {
+  if (!c || reps < 1 || cap < 0) return fail(PCG_E_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  if ((rc = check_solvable(c)) != PCG_OK) return rc;
+  if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  std::vector<pcg_schedule> cand;
+  cand.push_back(pcg_schedule{PCG_SCHED_TILES, 0, 32, 0});
+  for (int chunk : {32, 16})
+    for (int v = 0; v < pcg::kNumStripVariants; v++) cand.push_back(pcg_schedule{PCG_SCHED_STRIPS, v, chunk, 0});
+  std::vector<double> t(cand.size(), 0.0);
+  for (size_t k = 0; k < cand.size(); k++) {
+    c->sched = cand[k];
+    if ((rc = apply_schedule(c)) != PCG_OK) return rc;
+    for (int r = 0; r < reps; r++) {
+      PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+      if ((rc = enqueue_step(c, PCG_MODE_BATCHED)) != PCG_OK) return rc;
+      PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+      PCG_CUDA(cudaStreamSynchronize(c->stream));
+      float e = 0.f;
+      PCG_CUDA(cudaEventElapsedTime(&e, c->ev0, c->ev1));
+      t[k] += e;
+      c->device_ms += e;
+      c->cell_updates += c->cells_per_step;
+    }
+    t[k] /= reps;
+  }
+  size_t best = 0;
+  for (size_t k = 1; k < cand.size(); k++)
+    if (t[k] < t[best]) best = k;
+  c->sched = cand[best];
+  c->sched_fixed = true;
+  if ((rc = apply_schedule(c)) != PCG_OK) return rc;
+  {
+    std::lock_guard<std::mutex> g(g_tuned_mu);
+    g_tuned[c->shape_key] = c->sched;
+  }
+  const int32_t n = (int32_t)cand.size();
+  for (int32_t k = 0; k < std::min(n, cap); k++) {
+    if (tried) tried[k] = cand[k];
+    if (ms) ms[k] = t[k];
+  }
+  if (n_tried) *n_tried = n;
+  return PCG_OK;
+}
+
 int pcg_stats(pcg_context *c, int64_t *cell_updates, double *device_ms) {
   if (!c) return fail(PCG_E_INVALID, "null context");
   if (cell_updates) *cell_updates = c->cell_updates;
@@ -1086,11 +1307,9 @@ int pcg_profile_step(pcg_context *c, double *ms) {
   PCG_CUDA(cudaEventRecord(ev[2], c->stream));
   PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
   PCG_CUDA(cudaEventRecord(ev[3], c->stream));
-  PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
-                        (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+  if ((rc = enqueue_sweep(c)) != PCG_OK) return rc;
   PCG_CUDA(cudaEventRecord(ev[4], c->stream));
-  PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
-                         (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+  if ((rc = enqueue_update(c)) != PCG_OK) return rc;
   PCG_CUDA(cudaEventRecord(ev[5], c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   for (int i = 0; i < 5; i++) {

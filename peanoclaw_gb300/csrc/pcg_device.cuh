@@ -39,6 +39,20 @@ struct __align__(16) TileItem {
   int pad_;
 };
 
+// Warp-strip work item of the batched sweep/update: `ngroups` lane groups,
+// each a strip of `hs` rows and `w` columns of one patch (the StripGroup
+// entries g0 .. g0 + ngroups - 1), with ngroups * hs <= 32 and
+// ngroups * w <= 32.
+struct __align__(8) StripItem {
+  int g0;
+  unsigned char ngroups, hs, w, pad_;
+};
+
+struct __align__(8) StripGroup {
+  int pid;
+  short x0, y0;
+};
+
 struct SweParamsDev {
   double g, cfl, dry_tol, dry_tol_update, s_min, dt_inf;
 };
@@ -206,9 +220,8 @@ __device__ __forceinline__ double neg(double x) {
 }
 
 // Wet|dry edge: decide whether the dry side is a reflecting wall and, if so,
-// replace it by the mirrored wet state.  Out of line so the compiler keeps it
-// behind a branch: only coastline edges execute it.
-static __device__ __noinline__ void coastline(CellQ &L, CellQ &R, bool &wallL, bool &wallR) {
+// replace it by the mirrored wet state.
+__device__ __forceinline__ void coastline(CellQ &L, CellQ &R, bool &wallL, bool &wallR) {
   wallR = L.wet && (__dadd_rn(L.h, L.b) <= R.b);
   wallL = R.wet && (__dadd_rn(R.h, R.b) <= L.b);
   if (wallR) { R.h = L.h; R.hu = neg(L.hu); R.b = L.b; R.s = L.s; R.p = neg(L.p); R.F = L.F; }
@@ -224,7 +237,12 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
     return;
   }
   bool wallR = false, wallL = false;
-  if (L.wet != R.wet) coastline(L, R, wallL, wallR);  // coastline edges only
+  // coastline edges only; the branch is taken per warp (a vote), so warps
+  // without a wet|dry edge skip its FP64 additions and nothing is spilled
+  const bool coast = L.wet != R.wet;
+  if (__any_sync(__activemask(), coast)) {
+    if (coast) coastline(L, R, wallL, wallR);
+  }
   double a = __dmul_rn(halfg, __dadd_rn(L.h, R.h));
   double cb = ieee::sqrt_rn(a);
   double ub = ieee::div_rn(__dadd_rn(L.p, R.p), __dadd_rn(L.s, R.s));

@@ -73,4 +73,22 @@ cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev 
 cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev *patches,
                                    const PatchTimeDev *times, int src, int dst, int dim, int dir);
 
+// Warp-strip sweep variants: warps per CTA and minimum resident CTAs per SM
+// (the register budget the compiler is held to).
+struct StripVariant {
+  int warps, min_blocks;
+};
+constexpr int kNumStripVariants = 4;
+extern const StripVariant kStripVariants[kNumStripVariants];
+cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *slab,
+                                const PatchDev *patches, const StripItem *items,
+                                const StripGroup *groups, int count, const SweParamsDev &prm,
+                                unsigned long long *patch_smax, unsigned long long *group_dt);
+cudaError_t strip_occupancy(int variant, int *blocks_per_sm);
+cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                                 PatchTimeDev *times, const StripItem *items, const StripGroup *groups,
+                                 int count, const SweParamsDev &prm,
+                                 const unsigned long long *patch_smax,
+                                 const unsigned long long *group_dt);
+
 }  // namespace pcg

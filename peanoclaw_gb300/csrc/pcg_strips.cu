@@ -1,0 +1,277 @@
+// pcg_strips.cu -- warp-strip form of the batched sweep and update.
+//
+// Same arithmetic as k_sweep_tiles / k_update_tiles (and so as
+// SWE_WaveAccumulationBlock::computeNumericalFluxes + updateUnknowns,
+// tools/SWE_WaveAccumulationBlock.cpp:84-296), with another work
+// decomposition: a warp owns up to G "lane groups", each a strip of hs rows
+// (one row per lane, hs <= 32) and w columns of one patch, and marches the
+// strip along x.  The x-edge between two columns is solved with the previous
+// column's cell quantities kept in registers, the y-edges of a column with
+// the lower neighbour taken from the next lane down (warp shuffle).  No CTA
+// barrier is involved: warps are independent and the FP64 pipe is fed by
+// whichever warp has work.  The two strip-boundary rows are handled per warp
+// before the march: the cells just below each group (derived once, kept in
+// shared memory) and the edges just above each group (solved once, their
+// lower-cell parts kept in shared memory for the top lane).
+#include "pcg_device.cuh"
+#include "pcg_kernels.h"
+
+namespace pcg {
+
+namespace {
+
+// Per-warp shared memory: one entry per (group, column), G * w <= 32.
+struct StripWarpSmem {
+  double h[32], b[32], hv[32], s[32], q[32], G[32];  // cell below the group's first row
+  double top_h[32], top_hv[32], top_sp[32];            // edge above the group's last row
+  unsigned char wet[32];
+};
+
+__device__ __forceinline__ void load_state(const double *__restrict__ slab, const PatchDev &P, int x,
+                                           int y, double &h, double &hu, double &hv, double &b) {
+  const bool inside = x >= 0 && x < P.nx && y >= 0 && y < P.ny;
+  if (inside) {
+    h = slab[idx_unew(P, 0, x, y)];
+    hu = slab[idx_unew(P, 1, x, y)];
+    hv = slab[idx_unew(P, 2, x, y)];
+  } else {
+    h = slab[idx_uold(P, 0, x, y)];
+    hu = slab[idx_uold(P, 1, x, y)];
+    hv = slab[idx_uold(P, 2, x, y)];
+  }
+  b = slab[idx_pw(P, 0, x, y)];
+}
+
+__device__ __forceinline__ double shfl_up_d(double v, int d) {
+  return __shfl_up_sync(0xffffffffu, v, d);
+}
+__device__ __forceinline__ double shfl_down_d(double v, int d) {
+  return __shfl_down_sync(0xffffffffu, v, d);
+}
+
+// 1 / subcell size of a patch in dimension d, correctly rounded on the
+// integer pipes (same value as 1.0 / (size / n) in IEEE arithmetic).
+__device__ __forceinline__ double inv_subcell(const PatchDev &P, int d) {
+  return ieee::div_rn(1.0, ieee::div_rn(P.size[d], (double)(d == 0 ? P.nx : P.ny)));
+}
+
+}  // namespace
+
+template <int kWarps, int kMinBlocks>
+__global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
+    k_sweep_strips(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                   const StripItem *__restrict__ items, const StripGroup *__restrict__ groups,
+                   int count, SweParamsDev prm, unsigned long long *__restrict__ patch_smax,
+                   unsigned long long *__restrict__ group_dt) {
+  __shared__ StripWarpSmem SM[kWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  StripWarpSmem &S = SM[wid];
+  const double dry = prm.dry_tol;
+  const double halfg = __dmul_rn(0.5, prm.g);
+  for (int it = blockIdx.x * kWarps + wid; it < count; it += gridDim.x * kWarps) {
+    const StripItem I = items[it];
+    const int hs = I.hs, w = I.w, G = I.ngroups;
+    const int gi = lane / hs, j = lane - gi * hs;
+    const bool act = gi < G;
+    const StripGroup SG = groups[I.g0 + (act ? gi : 0)];
+    const PatchDev P = patches[SG.pid];
+    const int y = SG.y0 + j;
+
+    // ---- boundary rows: lane l < G*w takes (group l / w, column l % w)
+    if (lane < G * w) {
+      const int gh = lane / w, c = lane - gh * w;
+      const StripGroup HG = groups[I.g0 + gh];
+      const PatchDev &PH = patches[HG.pid];
+      const int x = HG.x0 + c;
+      double h, hu, hv, b;
+      CellQ cx, cy, ty, ay;
+      load_state(slab, PH, x, HG.y0 - 1, h, hu, hv, b);
+      cell_derived(dry, h, hu, hv, b, cx, cy);
+      S.h[lane] = cy.h; S.b[lane] = cy.b; S.hv[lane] = cy.hu; S.s[lane] = cy.s;
+      S.q[lane] = cy.p; S.G[lane] = cy.F; S.wet[lane] = cy.wet ? 1 : 0;
+      load_state(slab, PH, x, HG.y0 + hs - 1, h, hu, hv, b);
+      cell_derived(dry, h, hu, hv, b, cx, ty);
+      load_state(slab, PH, x, HG.y0 + hs, h, hu, hv, b);
+      cell_derived(dry, h, hu, hv, b, cx, ay);
+      double Lh, Lhv, Rh, Rhv, sp;
+      fwave_edge(halfg, ty, ay, Lh, Lhv, Rh, Rhv, sp);
+      S.top_h[lane] = Lh; S.top_hv[lane] = Lhv; S.top_sp[lane] = sp;
+    }
+    __syncwarp();
+
+    const double dxi = inv_subcell(P, 0), dyi = inv_subcell(P, 1);
+    double smax = 0.0;
+    double h = 0.0, hu = 0.0, hv = 0.0, b = 0.0;
+    CellQ px, py;
+    if (act) load_state(slab, P, SG.x0 - 1, y, h, hu, hv, b);
+    cell_derived(dry, h, hu, hv, b, px, py);
+    // parts of the previous column's cell: left edge (xr), lower edge (yr),
+    // upper edge (yl)
+    double p_xrh = 0.0, p_xrhu = 0.0, p_yrh = 0.0, p_yrhv = 0.0, p_ylh = 0.0, p_ylhv = 0.0;
+    for (int c = 0; c <= w; c++) {
+      const int x = SG.x0 + c;
+      h = hu = hv = b = 0.0;
+      if (act) load_state(slab, P, x, y, h, hu, hv, b);
+      CellQ cx, cy;
+      cell_derived(dry, h, hu, hv, b, cx, cy);
+      double Lh, Lhu, Rh, Rhu, sp;
+      fwave_edge(halfg, px, cx, Lh, Lhu, Rh, Rhu, sp);
+      smax = fmax_nonneg(smax, sp);
+      if (c > 0 && act) {
+        // accumulation order of computeNumericalFluxes: x-edges (left, then
+        // right), then y-edges (lower, then upper)
+        double a = __fma_rn(dxi, p_xrh, 0.0);
+        a = __fma_rn(dxi, Lh, a);
+        a = __fma_rn(dyi, p_yrh, a);
+        const double nh = __fma_rn(dyi, p_ylh, a);
+        const double nhu = __fma_rn(dxi, Lhu, __fma_rn(dxi, p_xrhu, 0.0));
+        const double nhv = __fma_rn(dyi, p_ylhv, __fma_rn(dyi, p_yrhv, 0.0));
+        slab[idx_uold(P, 0, x - 1, y)] = nh;
+        slab[idx_uold(P, 1, x - 1, y)] = nhu;
+        slab[idx_uold(P, 2, x - 1, y)] = nhv;
+      }
+      if (c == w) break;
+      // y-edge below this lane's cell; the lower cell comes from the next
+      // lane down, or from shared memory for a group's first row
+      CellQ dn;
+      dn.h = shfl_up_d(cy.h, 1);
+      dn.b = shfl_up_d(cy.b, 1);
+      dn.hu = shfl_up_d(cy.hu, 1);
+      dn.s = shfl_up_d(cy.s, 1);
+      dn.p = shfl_up_d(cy.p, 1);
+      dn.F = shfl_up_d(cy.F, 1);
+      dn.wet = __shfl_up_sync(0xffffffffu, (int)cy.wet, 1) != 0;
+      const int sl = gi * w + c;
+      if (j == 0 && act) {
+        dn.h = S.h[sl]; dn.b = S.b[sl]; dn.hu = S.hv[sl]; dn.s = S.s[sl];
+        dn.p = S.q[sl]; dn.F = S.G[sl]; dn.wet = S.wet[sl] != 0;
+      }
+      double yLh, yLhv, yRh, yRhv, sp2;
+      fwave_edge(halfg, dn, cy, yLh, yLhv, yRh, yRhv, sp2);
+      smax = fmax_nonneg(smax, sp2);
+      double uh = shfl_down_d(yLh, 1), uhv = shfl_down_d(yLhv, 1);
+      if (j == hs - 1 && act) {
+        uh = S.top_h[sl];
+        uhv = S.top_hv[sl];
+        smax = fmax_nonneg(smax, S.top_sp[sl]);
+      }
+      p_xrh = Rh; p_xrhu = Rhu; p_yrh = yRh; p_yrhv = yRhv; p_ylh = uh; p_ylhv = uhv;
+      px = cx;
+    }
+    __syncwarp();  // S is reused by the next item
+
+    // ---- per-group max wave speed (speeds >= 0: bit patterns order like values)
+    unsigned long long m = act ? dbits(smax) : 0ull;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long other = __shfl_down_sync(0xffffffffu, m, o);
+      if (j + o < hs) m = other > m ? other : m;
+    }
+    if (act && j == 0) {
+      atomicMax(&patch_smax[SG.pid], m);
+      const double dtc = cfl_dt(prm, bitsd(m), subcell(P, 0), subcell(P, 1));
+      atomicMin(&group_dt[P.group], dbits(dtc));
+    }
+  }
+}
+
+// Update in strip order (same per-cell arithmetic as k_update_tiles).
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32)
+    k_update_strips(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                    PatchTimeDev *__restrict__ times, const StripItem *__restrict__ items,
+                    const StripGroup *__restrict__ groups, int count, SweParamsDev prm,
+                    const unsigned long long *__restrict__ patch_smax,
+                    const unsigned long long *__restrict__ group_dt) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int it = blockIdx.x * kWarps + wid; it < count; it += gridDim.x * kWarps) {
+    const StripItem I = items[it];
+    const int hs = I.hs, w = I.w, G = I.ngroups;
+    const int gi = lane / hs, j = lane - gi * hs;
+    if (gi >= G) continue;
+    const StripGroup SG = groups[I.g0 + gi];
+    const PatchDev P = patches[SG.pid];
+    const double dt = bitsd(group_dt[P.group]);
+    const int y = SG.y0 + j;
+    const long long vn = vol_new(P), vo = vol_old(P);
+    long long in0 = idx_unew(P, 0, SG.x0, y), io0 = idx_uold(P, 0, SG.x0, y);
+    const int sn = P.ny, so = P.ny + 2 * P.g;
+#pragma unroll 4
+    for (int c = 0; c < w; c++) {
+      const double h = slab[in0], hu = slab[in0 + vn], hv = slab[in0 + 2 * vn];
+      const double fh = slab[io0], fhu = slab[io0 + vo], fhv = slab[io0 + 2 * vo];
+      double nh = __fma_rn(-dt, fh, h);
+      double nhu = __fma_rn(-dt, fhu, hu);
+      double nhv = __fma_rn(-dt, fhv, hv);
+      if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
+      if (nh < 0.0) nh = 0.0;
+      slab[io0] = h; slab[io0 + vo] = hu; slab[io0 + 2 * vo] = hv;
+      slab[in0] = nh; slab[in0 + vn] = nhu; slab[in0 + 2 * vn] = nhv;
+      in0 += sn;
+      io0 += so;
+    }
+    if (j == 0 && SG.x0 == 0 && SG.y0 == 0) {
+      PatchTimeDev &T = times[SG.pid];
+      if (tl_greater(dt, 0.0)) {
+        T.time = __dadd_rn(T.time, T.dt);
+        T.dt = dt;
+      }
+      T.est_next = cfl_dt(prm, bitsd(patch_smax[SG.pid]), subcell(P, 0), subcell(P, 1));
+    }
+  }
+}
+
+namespace {
+
+template <int kWarps, int kMinBlocks>
+cudaError_t sweep_strips_t(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                           const StripItem *items, const StripGroup *groups, int count,
+                           const SweParamsDev &prm, unsigned long long *patch_smax,
+                           unsigned long long *group_dt) {
+  if (count <= 0) return cudaSuccess;
+  k_sweep_strips<kWarps, kMinBlocks><<<grid, kWarps * 32, 0, st>>>(slab, patches, items, groups, count,
+                                                                   prm, patch_smax, group_dt);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Variants of the strip sweep (CTA size, minimum resident CTAs per SM).
+const StripVariant kStripVariants[kNumStripVariants] = {
+    {4, 4}, {4, 6}, {8, 2}, {8, 3},
+};
+
+cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *slab,
+                                const PatchDev *patches, const StripItem *items,
+                                const StripGroup *groups, int count, const SweParamsDev &prm,
+                                unsigned long long *patch_smax, unsigned long long *group_dt) {
+  switch (variant) {
+    case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
+    case 1: return sweep_strips_t<4, 6>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
+    case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
+    case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t strip_occupancy(int variant, int *blocks_per_sm) {
+  switch (variant) {
+    case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<4, 4>, 128, 0);
+    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<4, 6>, 128, 0);
+    case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<8, 2>, 256, 0);
+    case 3: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<8, 3>, 256, 0);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                                 PatchTimeDev *times, const StripItem *items, const StripGroup *groups,
+                                 int count, const SweParamsDev &prm,
+                                 const unsigned long long *patch_smax,
+                                 const unsigned long long *group_dt) {
+  if (count <= 0) return cudaSuccess;
+  k_update_strips<8><<<grid, 256, 0, st>>>(slab, patches, times, items, groups, count, prm, patch_smax,
+                                           group_dt);
+  return cudaGetLastError();
+}
+
+}  // namespace pcg

@@ -58,6 +58,18 @@ class GhostItem(C.Structure):
                 ("dst_offset", C.c_int32 * 2)]
 
 
+class Schedule(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("variant", C.c_int32), ("chunk", C.c_int32),
+                ("reserved_", C.c_int32)]
+
+    def as_tuple(self):
+        return (self.kind, self.variant, self.chunk)
+
+
+SCHED_TILES = 0
+SCHED_STRIPS = 1
+
+
 # every entry point declared in include/pcg.h: name -> (restype, argtypes)
 _CTX = C.c_void_p
 _I2 = C.POINTER(C.c_int32)
@@ -99,6 +111,10 @@ SIGNATURES = {
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "pcg_synchronize": (C.c_int, [_CTX]),
+    "pcg_set_schedule": (C.c_int, [_CTX, C.POINTER(Schedule)]),
+    "pcg_get_schedule": (C.c_int, [_CTX, C.POINTER(Schedule)]),
+    "pcg_autotune": (C.c_int, [_CTX, C.c_int32, C.POINTER(Schedule), _D, C.c_int32,
+                               C.POINTER(C.c_int32)]),
     "pcg_profile_step": (C.c_int, [_CTX, _D]),
     "pcg_probe_fp64_peak": (C.c_int, [_CTX, _D]),
     "pcg_check_ieee_emulation": (C.c_int, [_CTX, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
@@ -297,6 +313,27 @@ class Context:
 
     def synchronize(self):
         check(lib().pcg_synchronize(self.h))
+
+    def set_schedule(self, kind, variant=0, chunk=32):
+        """Fix the batched sweep/update schedule (SCHED_TILES or SCHED_STRIPS)."""
+        s = Schedule(kind, variant, chunk, 0)
+        check(lib().pcg_set_schedule(self.h, C.byref(s)))
+
+    def get_schedule(self):
+        s = Schedule()
+        check(lib().pcg_get_schedule(self.h, C.byref(s)))
+        return s.as_tuple()
+
+    def autotune(self, reps=2):
+        """Time every candidate schedule over `reps` batched steps each (the
+        simulation advances by those steps) and keep the fastest.  Returns
+        [((kind, variant, chunk), mean ms per step), ...]."""
+        cap = 64
+        tried = (Schedule * cap)()
+        ms = np.zeros(cap)
+        n = C.c_int32()
+        check(lib().pcg_autotune(self.h, int(reps), tried, dptr(ms), cap, C.byref(n)))
+        return [(tried[k].as_tuple(), float(ms[k])) for k in range(min(n.value, cap))]
 
     def profile_step(self):
         """Device ms of (reset, ghost items, walls, sweep, update) of one batched step."""
