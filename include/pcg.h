@@ -223,7 +223,7 @@ int pcg_synchronize(pcg_context *ctx);
  *   kind 1: warp strips: a warp marches strips of up to 32 rows and `chunk`
  *           columns (1..32) of one or more patches along x; `variant` picks
  *           the CTA size / register budget (0..3: 4 warps x 4 CTAs/SM,
- *           4 x 6, 8 x 2, 8 x 3). */
+ *           4 x 5, 8 x 2, 8 x 3). */
 typedef struct pcg_schedule {
   int32_t kind;
   int32_t variant;

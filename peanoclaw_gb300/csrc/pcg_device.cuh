@@ -256,14 +256,16 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
   double b2 = __dmul_rn(__fma_rn(-l1, df1, df2), inv);
   double z1 = __dmul_rn(b1, l1);
   double z2 = __dmul_rn(b2, l2);
-  if (lt_zero(l1)) {
-    if (lt_zero(l2)) {
-      Lh = __dadd_rn(b1, b2); Lhu = __dadd_rn(z1, z2); Rh = 0.0; Rhu = 0.0;
-    } else {
-      Lh = b1; Lhu = z1; Rh = b2; Rhu = z2;
+  // both waves to one side (supersonic edges): their sums go to that side.
+  // Branch per warp (a vote) so that subsonic warps skip the FP64 additions.
+  const bool left1 = lt_zero(l1), split = left1 && !lt_zero(l2);
+  Lh = b1; Lhu = z1; Rh = b2; Rhu = z2;
+  if (__any_sync(__activemask(), !split)) {
+    if (!split) {
+      const double sh = __dadd_rn(b1, b2), shu = __dadd_rn(z1, z2);
+      if (left1) { Lh = sh; Lhu = shu; Rh = 0.0; Rhu = 0.0; }
+      else { Lh = 0.0; Lhu = 0.0; Rh = sh; Rhu = shu; }
     }
-  } else {
-    Lh = 0.0; Lhu = 0.0; Rh = __dadd_rn(b1, b2); Rhu = __dadd_rn(z1, z2);
   }
   if (wallR) { Rh = 0.0; Rhu = 0.0; }
   if (wallL) { Lh = 0.0; Lhu = 0.0; }

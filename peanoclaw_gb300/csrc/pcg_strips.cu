@@ -6,8 +6,9 @@
 // decomposition: a warp owns up to G "lane groups", each a strip of hs rows
 // (one row per lane, hs <= 32) and w columns of one patch, and marches the
 // strip along x.  The x-edge between two columns is solved with the previous
-// column's cell quantities kept in registers, the y-edges of a column with
-// the lower neighbour taken from the next lane down (warp shuffle).  No CTA
+// column's cell quantities kept in a per-lane shared-memory slot, the y-edges
+// of a column with the lower neighbour taken from the next lane down (warp
+// shuffle).  No CTA
 // barrier is involved: warps are independent and the FP64 pipe is fed by
 // whichever warp has work.  The two strip-boundary rows are handled per warp
 // before the march: the cells just below each group (derived once, kept in
@@ -42,6 +43,23 @@ __device__ __forceinline__ void load_state(const double *__restrict__ slab, cons
   b = slab[idx_pw(P, 0, x, y)];
 }
 
+// Per-lane slot for the x-direction quantities of the previous column's cell.
+struct StripLaneSmem {
+  double h[32], hu[32], b[32], s[32], p[32], F[32];
+  unsigned char wet[32];
+};
+
+__device__ __forceinline__ void store_x(StripLaneSmem &L, int lane, const CellQ &c) {
+  L.h[lane] = c.h; L.hu[lane] = c.hu; L.b[lane] = c.b; L.s[lane] = c.s; L.p[lane] = c.p;
+  L.F[lane] = c.F; L.wet[lane] = c.wet ? 1 : 0;
+}
+__device__ __forceinline__ CellQ load_x(const StripLaneSmem &L, int lane) {
+  CellQ c;
+  c.h = L.h[lane]; c.hu = L.hu[lane]; c.b = L.b[lane]; c.s = L.s[lane]; c.p = L.p[lane];
+  c.F = L.F[lane]; c.wet = L.wet[lane] != 0;
+  return c;
+}
+
 __device__ __forceinline__ double shfl_up_d(double v, int d) {
   return __shfl_up_sync(0xffffffffu, v, d);
 }
@@ -64,6 +82,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
                    int count, SweParamsDev prm, unsigned long long *__restrict__ patch_smax,
                    unsigned long long *__restrict__ group_dt) {
   __shared__ StripWarpSmem SM[kWarps];
+  __shared__ StripLaneSmem LS[kWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   StripWarpSmem &S = SM[wid];
   const double dry = prm.dry_tol;
@@ -102,12 +121,20 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     const double dxi = inv_subcell(P, 0), dyi = inv_subcell(P, 1);
     double smax = 0.0;
     double h = 0.0, hu = 0.0, hv = 0.0, b = 0.0;
-    CellQ px, py;
-    if (act) load_state(slab, P, SG.x0 - 1, y, h, hu, hv, b);
-    cell_derived(dry, h, hu, hv, b, px, py);
-    // parts of the previous column's cell: left edge (xr), lower edge (yr),
-    // upper edge (yl)
-    double p_xrh = 0.0, p_xrhu = 0.0, p_yrh = 0.0, p_yrhv = 0.0, p_ylh = 0.0, p_ylhv = 0.0;
+    // x-direction quantities of the previous column's cell live in shared
+    // memory (one slot per lane) to keep the register budget small
+    StripLaneSmem &L = LS[wid];
+    {
+      CellQ cx, cy;
+      if (act) load_state(slab, P, SG.x0 - 1, y, h, hu, hv, b);
+      cell_derived(dry, h, hu, hv, b, cx, cy);
+      store_x(L, lane, cx);
+    }
+    // partial sums of the previous column's cell, in the accumulation order
+    // of computeNumericalFluxes (x-edges left then right, y-edges lower then
+    // upper): a1 = dxi * (left edge part of h), u1 = dxi * (left edge part of
+    // hu); the y parts of h are added after the right edge's
+    double a1 = 0.0, u1 = 0.0, yrh = 0.0, ylh = 0.0;
     for (int c = 0; c <= w; c++) {
       const int x = SG.x0 + c;
       h = hu = hv = b = 0.0;
@@ -115,22 +142,18 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       CellQ cx, cy;
       cell_derived(dry, h, hu, hv, b, cx, cy);
       double Lh, Lhu, Rh, Rhu, sp;
-      fwave_edge(halfg, px, cx, Lh, Lhu, Rh, Rhu, sp);
+      fwave_edge(halfg, load_x(L, lane), cx, Lh, Lhu, Rh, Rhu, sp);
       smax = fmax_nonneg(smax, sp);
       if (c > 0 && act) {
-        // accumulation order of computeNumericalFluxes: x-edges (left, then
-        // right), then y-edges (lower, then upper)
-        double a = __fma_rn(dxi, p_xrh, 0.0);
-        a = __fma_rn(dxi, Lh, a);
-        a = __fma_rn(dyi, p_yrh, a);
-        const double nh = __fma_rn(dyi, p_ylh, a);
-        const double nhu = __fma_rn(dxi, Lhu, __fma_rn(dxi, p_xrhu, 0.0));
-        const double nhv = __fma_rn(dyi, p_ylhv, __fma_rn(dyi, p_yrhv, 0.0));
-        slab[idx_uold(P, 0, x - 1, y)] = nh;
-        slab[idx_uold(P, 1, x - 1, y)] = nhu;
-        slab[idx_uold(P, 2, x - 1, y)] = nhv;
+        double a = __fma_rn(dxi, Lh, a1);
+        a = __fma_rn(dyi, yrh, a);
+        slab[idx_uold(P, 0, x - 1, y)] = __fma_rn(dyi, ylh, a);
+        slab[idx_uold(P, 1, x - 1, y)] = __fma_rn(dxi, Lhu, u1);
       }
       if (c == w) break;
+      a1 = __fma_rn(dxi, Rh, 0.0);
+      u1 = __fma_rn(dxi, Rhu, 0.0);
+      store_x(L, lane, cx);
       // y-edge below this lane's cell; the lower cell comes from the next
       // lane down, or from shared memory for a group's first row
       CellQ dn;
@@ -155,8 +178,10 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
         uhv = S.top_hv[sl];
         smax = fmax_nonneg(smax, S.top_sp[sl]);
       }
-      p_xrh = Rh; p_xrhu = Rhu; p_yrh = yRh; p_yrhv = yRhv; p_ylh = uh; p_ylhv = uhv;
-      px = cx;
+      yrh = yRh;
+      ylh = uh;
+      // hv only has y-edge parts: complete for this column already
+      if (act) slab[idx_uold(P, 2, x, y)] = __fma_rn(dyi, uhv, __fma_rn(dyi, yRhv, 0.0));
     }
     __syncwarp();  // S is reused by the next item
 
@@ -237,7 +262,7 @@ cudaError_t sweep_strips_t(cudaStream_t st, int grid, double *slab, const PatchD
 
 // Variants of the strip sweep (CTA size, minimum resident CTAs per SM).
 const StripVariant kStripVariants[kNumStripVariants] = {
-    {4, 4}, {4, 6}, {8, 2}, {8, 3},
+    {4, 4}, {4, 5}, {8, 2}, {8, 3},
 };
 
 cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *slab,
@@ -246,7 +271,7 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
                                 unsigned long long *patch_smax, unsigned long long *group_dt) {
   switch (variant) {
     case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
-    case 1: return sweep_strips_t<4, 6>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
+    case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
     case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
     case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
     default: return cudaErrorInvalidValue;
@@ -256,7 +281,7 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
 cudaError_t strip_occupancy(int variant, int *blocks_per_sm) {
   switch (variant) {
     case 0: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<4, 4>, 128, 0);
-    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<4, 6>, 128, 0);
+    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<4, 5>, 128, 0);
     case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<8, 2>, 256, 0);
     case 3: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<8, 3>, 256, 0);
     default: return cudaErrorInvalidValue;
