@@ -257,7 +257,7 @@ int pcg_profile_step(pcg_context *ctx, double *ms);
  * FMA counted as two flops. */
 int pcg_probe_fp64_peak(pcg_context *ctx, double *tflops);
 /* No counterpart in the reference.  Compares the library's integer-pipe FP64
- * divide and square root with the hardware IEEE operations on `samples`
+ * divide, reciprocal and square root with the hardware IEEE operations on `samples`
  * pseudo-random operand pairs; *mismatches receives the number of results
  * whose bits differ (0 expected). */
 int pcg_check_ieee_emulation(pcg_context *ctx, int64_t samples, uint64_t seed, int64_t *mismatches);

@@ -97,9 +97,11 @@ __global__ void k_check_ieee(long long n, unsigned long long seed, unsigned long
     double a = from_bits(A), b = from_bits(B);
     double q1 = div_rn(a, b), q2 = __ddiv_rn(a, b);
     bool qbad = bits(q1) != bits(q2) && !(q1 != q1 && q2 != q2);
+    double c1 = rcp_rn(b), c2 = __ddiv_rn(1.0, b);
+    bool cbad = bits(c1) != bits(c2) && !(c1 != c1 && c2 != c2);
     double r1 = sqrt_rn(fabs(a)), r2 = __dsqrt_rn(fabs(a));
     bool sbad = bits(r1) != bits(r2) && !(r1 != r1 && r2 != r2);
-    local += (qbad ? 1 : 0) + (sbad ? 1 : 0);
+    local += (qbad ? 1 : 0) + (cbad ? 1 : 0) + (sbad ? 1 : 0);
   }
   if (local) atomicAdd(bad, local);
 }

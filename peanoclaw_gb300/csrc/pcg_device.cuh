@@ -199,7 +199,7 @@ __device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu
   cy.h = h; cy.b = b; cy.wet = wet;
   if (wet) {
     double s = ieee::sqrt_rn(h);
-    double rs = ieee::div_rn(1.0, s);
+    double rs = ieee::rcp_rn(s);
     double p = __dmul_rn(hu, rs);
     double q = __dmul_rn(hv, rs);
     cx.s = s; cx.p = p; cx.F = __dmul_rn(p, p); cx.hu = hu;
@@ -251,7 +251,7 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
   double df1 = __dsub_rn(R.hu, L.hu);
   double deta = __dadd_rn(__dsub_rn(R.h, L.h), __dsub_rn(R.b, L.b));
   double df2 = __fma_rn(a, deta, __dsub_rn(R.F, L.F));
-  double inv = ieee::div_rn(1.0, __dsub_rn(l2, l1));
+  double inv = ieee::rcp_rn(__dsub_rn(l2, l1));
   double b1 = __dmul_rn(__fma_rn(l2, df1, -df2), inv);
   double b2 = __dmul_rn(__fma_rn(-l1, df1, df2), inv);
   double z1 = __dmul_rn(b1, l1);

@@ -12,13 +12,15 @@
 // Floating-Point Arithmetic, 2nd ed., ch. 9 and 10, and Moller & Granlund,
 // "Improved division by invariant integers", IEEE TC 60(2), 2011):
 //   * significands as 53-bit integers;
-//   * a fixed-point reciprocal (or reciprocal square root) is seeded from the
-//     FP32 approximation of the leading 24 bits and refined by two
-//     Newton-Raphson steps in 64-bit fixed point;
-//   * the candidate quotient (root) comes from one high 64x64 product; its
-//     exact remainder, computed modulo 2^64, corrects it to the truncated
-//     result and decides the rounding (ties to even for the quotient; a
-//     square root of a double is never exactly half way).
+//   * a 64-bit fixed-point reciprocal (or reciprocal square root) from an
+//     FP32 seed of the leading 24 bits, one FP32 Newton step and a
+//     second-order correction computed in FP32 on a two-float split of the
+//     operand (about 46 correct bits);
+//   * the candidate quotient (root) from one high 64x64 product, its exact
+//     remainder modulo 2^64, one FP32 correction step of the remainder and
+//     one fix-up give the truncated result, and the remainder decides the
+//     rounding (ties to even for the quotient; a square root of a double is
+//     never exactly half way).
 // Operands outside the fast path (zero, subnormal, infinite, NaN, results
 // that would leave the normal range) are handed to the hardware operation,
 // so the functions are exact for every input.
@@ -113,20 +115,9 @@ PCG_HD int32_t rint_f(float a) {
 #endif
 }
 
-// 2^64 * v as a signed 64-bit integer for |v| < 2^-2 (v = 0 gives 0), read
-// straight from the float's bits.
-PCG_HD int64_t scaled64(float v) {
-  uint32_t fb = float_bits(v);
-  int e = (int)((fb >> 23) & 0xFFu);
-  if (e == 0) return 0;
-  uint64_t m = (uint64_t)((fb & 0x7FFFFFu) | 0x800000u);
-  int sh = e - 86;  // 2^64 * 1.m * 2^(e-127) = m << (e - 86)
-  uint64_t mag = sh >= 0 ? (m << sh) : (sh > -64 ? (m >> (-sh)) : 0ull);
-  return (fb >> 31) ? -(int64_t)mag : (int64_t)mag;
-}
-
-// FP32 seeds: only their accuracy matters (the integer refinement corrects
-// any seed within a few units of 2^-22), not their exact value.
+// FP32 seeds: only their accuracy matters, not their exact value (one FP32
+// Newton step squares the seed's error; any seed within 2^-12 of the
+// reciprocal (square root) gives exact results).
 PCG_HD float rcp_seed(float d) {
 #if defined(__CUDA_ARCH__)
   float r;
@@ -171,16 +162,46 @@ inline double hw_div(double a, double b) { return a / b; }
 inline double hw_sqrt(double a) { return std::sqrt(a); }
 #endif
 
-// One Newton-Raphson step for V ~ 2^116 / m  (m in [2^52, 2^53), V in (2^63, 2^64)).
-PCG_HD uint64_t recip_step(uint64_t m, uint64_t V) {
-  uint64_t hi = mulhi(m, V), lo = m * V;
-  // E = 2^116 - m*V as a signed 128-bit number (hi part small), then E / 2^52
-  int64_t ehi = (int64_t)(kHidden - hi) - (lo != 0 ? 1 : 0);
-  uint64_t elo = (uint64_t)0 - lo;
-  int64_t e = (int64_t)((uint64_t)ehi << 12) | (int64_t)(elo >> 52);
-  uint64_t ae = e < 0 ? (uint64_t)(-e) : (uint64_t)e;
-  uint64_t d = mulhi(V, ae);
-  return e < 0 ? V - d : V + d;
+// 2^64 / D for D = mb / 2^52 in (1, 2), accurate to about 2^-46 relative and
+// below 2^64, plus the FP32 reciprocal r0 of D's leading 24 bits.
+// r0 = 1 / d_hi to float precision (one FP32 Newton step on the seed), then
+// 1/D = r0 (1 + e + e^2 + ...) with e = 1 - D r0 computed from the two-float
+// split D = d_hi + d_lo.  r0 lies in (0.5, 1]: its significand shifted by 40
+// is r0 * 2^64 (r0 == 1, for d_hi == 1, is clamped to 2^64 - 1; its
+// correction is then <= 0).  The correction r0 (e + e^2) (|.| < 2^-22) is
+// added as a multiple of 2^-50.
+PCG_HD uint64_t recip64(uint64_t mb, float &r0) {
+  const float d_hi = bits_float(0x3F800000u | (uint32_t)((mb >> 29) & 0x7FFFFFu));
+  const float d_lo = mul_f((float)(uint32_t)(mb & 0x1FFFFFFFull), 2.220446049250313e-16f);  // * 2^-52
+  r0 = rcp_seed(d_hi);
+  r0 = fma_f(r0, fma_f(-d_hi, r0, 1.0f), r0);
+  float er = fma_f(-d_hi, r0, 1.0f);
+  er = fma_f(-d_lo, r0, er);
+  const float corr = mul_f(r0, fma_f(er, er, er));
+  const uint32_t rb = float_bits(r0);
+  uint64_t V = rb >= 0x3F800000u ? 0xFFFFFFFFFFFFFFFFull
+                                 : ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << 40);
+  return V + ((uint64_t)(int64_t)rint_f(mul_f(corr, 1.125899906842624e15f)) << 14);  // corr * 2^50
+}
+
+// Quotient significand q = x * 2^52 / mb (x in [mb, 2 mb)) rounded to nearest
+// even, from the estimate q0 (within a few hundred units) and
+// rem = x * 2^52 - q0 * mb (exact modulo 2^64; its true value is small).
+// One FP32 step rem / mb (error < 2^-14) brings the remainder into
+// (-(1/2 + 2^-14) mb, (1/2 + 2^-14) mb); one fix-up makes it the remainder
+// of the truncated quotient.
+PCG_HD uint64_t quot_round(uint64_t q, int64_t rem, uint64_t mb, float r0) {
+  const float dq = mul_f(mul_f((float)(int32_t)(rem >> 32), r0), 9.5367431640625e-07f);  // * 2^-20
+  const int64_t di = (int64_t)rint_f(dq);
+  q = (uint64_t)((int64_t)q + di);
+  rem -= di * (int64_t)mb;
+  if (rem < 0) {
+    q -= 1;
+    rem += (int64_t)mb;
+  }
+  const uint64_t twice = (uint64_t)rem << 1;
+  if (twice > mb || (twice == mb && (q & 1))) q += 1;
+  return q;
 }
 
 // Correctly rounded a / b.
@@ -203,51 +224,28 @@ PCG_HD double div_rn(double a, double b) {
   if ((B & kFrac) == 0) {
     q = x;  // divisor is a power of two: exact
   } else {
-    // 1/D for D = mb / 2^52 in [1, 2): FP32 seed refined once with the
-    // divisor split into two floats (d_hi exact 24 bits, d_lo the rest),
-    // 1/D ~ r0 (1 + e + e^2) with e = 1 - D r0, accurate to ~2^-45
-    float d_hi = bits_float(0x3F800000u | (uint32_t)((mb >> 29) & 0x7FFFFFu));
-    float d_lo = mul_f((float)(uint32_t)(mb & 0x1FFFFFFFull), 2.220446049250313e-16f);  // * 2^-52
-    // After the FP32 Newton step r0 is 1/d_hi to float precision; for
-    // d_hi == 1 that is r0 == 1 exactly (any seed within 2^-12 of it), so V
-    // below is clamped under 2^64 and corr <= 0 keeps it there.
-    float r0 = rcp_seed(d_hi);
-    r0 = fma_f(r0, fma_f(-d_hi, r0, 1.0f), r0);
-    float er = fma_f(-d_hi, r0, 1.0f);
-    er = fma_f(-d_lo, r0, er);
-    float corr = mul_f(r0, fma_f(er, er, er));
-    uint32_t rb = float_bits(r0);
-    uint64_t V = ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u)) << ((int)((rb >> 23) & 0xFFu) - 86);
-    if (((rb >> 23) & 0xFFu) >= 127u) V = 0xFFFFFFFFFFFFFFFFull;  // r0 == 1: clamp below 2^64
-    V = (uint64_t)((int64_t)V + scaled64(corr));
-    q = mulhi(x, V);  // within a few hundred units of the quotient
-    int64_t rem = (int64_t)((x << 52) - q * mb);
-    // one FP32 correction step: delta = rem / mb, then exact fix-up
-    float dq = mul_f(mul_f((float)(int32_t)(rem >> 32), r0), 9.5367431640625e-07f);  // * 2^-20
-    int64_t di = (int64_t)rint_f(dq);
-    q = (uint64_t)((int64_t)q + di);
-    rem -= di * (int64_t)mb;
-    if (rem < 0) { q -= 1; rem += (int64_t)mb; }
-    if (rem < 0) { q -= 1; rem += (int64_t)mb; }
-    if (rem >= (int64_t)mb) { q += 1; rem -= (int64_t)mb; }
-    if (rem >= (int64_t)mb) { q += 1; rem -= (int64_t)mb; }
-    uint64_t twice = (uint64_t)rem << 1;
-    if (twice > mb || (twice == mb && (q & 1))) q += 1;
+    float r0;
+    const uint64_t V = recip64(mb, r0);
+    const uint64_t q0 = mulhi(x, V);
+    q = quot_round(q0, (int64_t)((x << 52) - q0 * mb), mb, r0);
   }
   return from_bits(sign | ((uint64_t)e << 52) | (q - kHidden));
 }
 
-// One Newton-Raphson step for Y ~ 2^90 / sqrt(M)  (M in [2^52, 2^54), Y in (2^63, 2^64)).
-PCG_HD uint64_t rsqrt_step(uint64_t M, uint64_t Y) {
-  uint64_t y2 = mulhi(Y, Y);  // Y^2 / 2^64 ~ 2^116 / M
-  uint64_t hi = mulhi(M, y2), lo = M * y2;
-  int64_t ehi = (int64_t)(kHidden - hi) - (lo != 0 ? 1 : 0);
-  uint64_t elo = (uint64_t)0 - lo;
-  // Y' = Y + Y * E / 2^117 with E = 2^116 - M*y2; E / 2^53 first
-  int64_t e = (int64_t)((uint64_t)ehi << 11) | (int64_t)(elo >> 53);
-  uint64_t ae = e < 0 ? (uint64_t)(-e) : (uint64_t)e;
-  uint64_t d = mulhi(Y, ae);
-  return e < 0 ? Y - d : Y + d;
+// Correctly rounded 1 / b (div_rn(1.0, b) with the dividend's work folded in).
+PCG_HD double rcp_rn(double b) {
+  const uint64_t B = bits(b);
+  const uint32_t eb = (uint32_t)(B >> 52) & 0x7FFu;
+  if (eb - 1u >= 2044u) return hw_div(1.0, b);  // zero, subnormal, huge, inf, NaN
+  const uint64_t sign = B & kSign;
+  if ((B & kFrac) == 0) return from_bits(sign | ((uint64_t)(2046u - eb) << 52));  // 2^-k
+  const uint64_t mb = (B & kFrac) | kHidden;
+  float r0;
+  const uint64_t V = recip64(mb, r0);
+  // x = 2^53 (1 < mb / 2^52): q0 = 2^53 V / 2^64, and x * 2^52 = 2^105 is 0 mod 2^64
+  const uint64_t q0 = V >> 11;
+  const uint64_t q = quot_round(q0, (int64_t)(0ull - q0 * mb), mb, r0);
+  return from_bits(sign | ((uint64_t)(2045u - eb) << 52) | (q - kHidden));
 }
 
 // Correctly rounded sqrt(a).
@@ -265,37 +263,41 @@ PCG_HD double sqrt_rn(double a) {
   if (M == kHidden) {
     s = kHidden;  // power of four: exact
   } else {
-    // 1/sqrt(F) for F = M / 2^52 in [1, 4): FP32 seed refined once with F
-    // split into two floats, 1/sqrt(F) ~ r0 (1 + e/2 + 3e^2/8), e = 1 - F r0^2
+    // 1/sqrt(F) for F = M / 2^52 in [1, 4): r0 = 1/sqrt(f_hi) to float
+    // precision (one FP32 Newton step on the seed), refined with the
+    // two-float split F = f_hi + f_lo: 1/sqrt(F) ~ r0 (1 + e/2 + 3e^2/8),
+    // e = 1 - F r0^2.  r0 lies in (0.5, 1]: Y = r0 * 2^64 is its significand
+    // shifted by 40 (r0 == 1 clamped to 2^64 - 1), the correction is added as
+    // a multiple of 2^-50.
     const bool hi = (M >> 53) != 0;
     const int sh = hi ? 30 : 29;
-    float f_hi = bits_float((hi ? 0x40000000u : 0x3F800000u) | (uint32_t)((M >> sh) & 0x7FFFFFu));
-    float f_lo = mul_f((float)(uint32_t)(M & ((1ull << sh) - 1)), 2.220446049250313e-16f);  // * 2^-52
+    const float f_hi = bits_float((hi ? 0x40000000u : 0x3F800000u) | (uint32_t)((M >> sh) & 0x7FFFFFu));
+    const float f_lo = mul_f((float)(uint32_t)(M & ((1ull << sh) - 1)), 2.220446049250313e-16f);  // * 2^-52
     float r0 = rsqrt_seed(f_hi);
-    // FP32 Newton step: r0 to float precision
     r0 = fma_f(mul_f(r0, 0.5f), fma_f(-mul_f(f_hi, r0), r0, 1.0f), r0);
-    float s0 = mul_f(f_hi, r0);
-    float s0e = fma_f(f_hi, r0, -s0);          // f_hi * r0 = s0 + s0e exactly
+    const float s0 = mul_f(f_hi, r0);
+    const float s0e = fma_f(f_hi, r0, -s0);  // f_hi * r0 = s0 + s0e exactly
     float er = fma_f(-s0, r0, 1.0f);
     er = fma_f(-s0e, r0, er);
     er = fma_f(-mul_f(f_lo, r0), r0, er);
-    float corr = mul_f(r0, fma_f(mul_f(er, 0.375f), er, mul_f(er, 0.5f)));
-    uint32_t rb = float_bits(r0);
-    uint64_t Y = ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u)) << ((int)((rb >> 23) & 0xFFu) - 86);
-    if (((rb >> 23) & 0xFFu) >= 127u) Y = 0xFFFFFFFFFFFFFFFFull;  // r0 == 1: clamp below 2^64
-    Y = (uint64_t)((int64_t)Y + scaled64(corr));
+    const float corr = mul_f(r0, fma_f(mul_f(er, 0.375f), er, mul_f(er, 0.5f)));
+    const uint32_t rb = float_bits(r0);
+    uint64_t Y = rb >= 0x3F800000u ? 0xFFFFFFFFFFFFFFFFull
+                                   : ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << 40);
+    Y += (uint64_t)(int64_t)rint_f(mul_f(corr, 1.125899906842624e15f)) << 14;  // corr * 2^50
     s = mulhi(M, Y);  // within a few hundred units of floor(sqrt(M * 2^52))
     int64_t rem = (int64_t)((M << 52) - s * s);
-    // one FP32 correction step: delta = rem / (2 s), 1/(2 s) ~ r0 * 2^-53
-    float ds = mul_f(mul_f((float)(int32_t)(rem >> 32), r0), 4.76837158203125e-07f);  // * 2^-21
-    int64_t di = (int64_t)rint_f(ds);
+    // one FP32 step delta = rem / (2 s), 1/(2 s) ~ r0 * 2^-53 (error < 2^-14),
+    // then one fix-up gives floor(sqrt) and its remainder
+    const float ds = mul_f(mul_f((float)(int32_t)(rem >> 32), r0), 4.76837158203125e-07f);  // * 2^-21
+    const int64_t di = (int64_t)rint_f(ds);
     rem -= di * (int64_t)(2 * s) + di * di;
     s = (uint64_t)((int64_t)s + di);
-    if (rem < 0) { s -= 1; rem += (int64_t)(2 * s + 1); }
-    if (rem < 0) { s -= 1; rem += (int64_t)(2 * s + 1); }
-    if (rem > (int64_t)(2 * s)) { rem -= (int64_t)(2 * s + 1); s += 1; }
-    if (rem > (int64_t)(2 * s)) { rem -= (int64_t)(2 * s + 1); s += 1; }
-    if (rem > (int64_t)s) s += 1;
+    if (rem < 0) {
+      s -= 1;
+      rem += (int64_t)(2 * s + 1);
+    }
+    if (rem > (int64_t)s) s += 1;  // never a tie
   }
   return from_bits(((uint64_t)(k / 2 + 1023) << 52) | (s - kHidden));
 }

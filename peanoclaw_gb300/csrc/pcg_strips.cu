@@ -70,7 +70,7 @@ __device__ __forceinline__ double shfl_down_d(double v, int d) {
 // 1 / subcell size of a patch in dimension d, correctly rounded on the
 // integer pipes (same value as 1.0 / (size / n) in IEEE arithmetic).
 __device__ __forceinline__ double inv_subcell(const PatchDev &P, int d) {
-  return ieee::div_rn(1.0, ieee::div_rn(P.size[d], (double)(d == 0 ? P.nx : P.ny)));
+  return ieee::rcp_rn(ieee::div_rn(P.size[d], (double)(d == 0 ? P.nx : P.ny)));
 }
 
 }  // namespace
