@@ -157,6 +157,10 @@ struct pcg_context {
   size_t d_gcells_cap = 0;
   pcg::InterpPlanDev *d_plan = nullptr;
   size_t d_plan_cap = 0;
+  pcg::CopyPlanDev *d_copy_plan = nullptr;
+  size_t d_copy_plan_cap = 0;
+  pcg::GhostItemStepDev *d_item_step = nullptr;
+  size_t d_item_step_cap = 0;
 
   std::vector<pcg::TileItem> h_tiles;
   pcg::TileItem *d_tiles = nullptr;
@@ -169,7 +173,7 @@ struct pcg_context {
   int sweep_grid = 0;
 
   // batched sweep/update schedule (pcg_schedule); warp-strip work list
-  pcg_schedule sched{PCG_SCHED_STRIPS, 0, 32, 0};
+  pcg_schedule sched{PCG_SCHED_STRIPS, 2, 32, 0};
   bool sched_fixed = false;          // set by pcg_set_schedule / pcg_autotune
   std::string shape_key;             // SM count + leaf shape histogram
   std::vector<pcg::StripItem> h_sitems;
@@ -348,7 +352,10 @@ int apply_schedule(pcg_context *c) {
   const int64_t warps = pcg::kStripVariants[v].warps;
   const int64_t need = std::max<int64_t>(1, ((int64_t)c->h_sitems.size() + warps - 1) / warps);
   c->strip_grid = (int)std::min<int64_t>((int64_t)c->num_sms * per_sm, need);
-  c->update_grid = (int)std::min<int64_t>((int64_t)c->num_sms * 8,
+  int upd_sm = 0;
+  PCG_CUDA(pcg::update_strips_occupancy(&upd_sm));
+  if (upd_sm < 1) upd_sm = 1;
+  c->update_grid = (int)std::min<int64_t>((int64_t)c->num_sms * upd_sm,
                                           std::max<int64_t>(1, ((int64_t)c->h_sitems.size() + 7) / 8));
   c->graph_valid = false;
   return PCG_OK;
@@ -458,6 +465,8 @@ int rebuild_topology(pcg_context *c) {
   PCG_CUDA(up(c->d_leaf_ids, c->leaf_ids.data(), sizeof(int) * c->leaf_ids.size()));
   if ((rc = ensure_device(c, &c->d_gcells, &c->d_gcells_cap, c->h_gcells.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_plan, &c->d_plan_cap, (size_t)c->n_interp_cells)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_copy_plan, &c->d_copy_plan_cap, (size_t)c->n_copy_cells)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_item_step, &c->d_item_step_cap, c->h_items.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_tiles, &c->d_tiles_cap, c->h_tiles.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_wall, &c->d_wall_cap, c->h_wall.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_items, &c->d_items_cap, c->h_items.size())) != PCG_OK) return rc;
@@ -477,6 +486,8 @@ int rebuild_topology(pcg_context *c) {
   if ((rc = upload_patches(c)) != PCG_OK) return rc;
   PCG_CUDA(pcg::launch_build_interp_plan(c->stream, c->d_patches, c->d_items, c->d_gcells + c->n_copy_cells,
                                          c->n_interp_cells, c->d_plan));
+  PCG_CUDA(pcg::launch_build_copy_plan(c->stream, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
+                                       c->d_copy_plan));
   int per_sm = 0;
   PCG_CUDA(pcg::sweep_occupancy(&per_sm));
   if (per_sm < 1) per_sm = 1;
@@ -552,8 +563,10 @@ int enqueue_step(pcg_context *c, int mode) {
   PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
                         c->d_patch_smax));
   if (mode == PCG_MODE_BATCHED) {
-    PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, c->d_gcells,
-                                c->n_copy_cells, c->n_interp_cells, c->d_plan, nullptr));
+    PCG_CUDA(launch_item_step(c->stream, c->d_patches, c->d_times, c->d_items, (int)c->h_items.size(),
+                              c->d_item_step));
+    PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
+                                c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step));
     PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
     int rc;
     if ((rc = enqueue_sweep(c)) != PCG_OK) return rc;
@@ -713,6 +726,8 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_restr_dsts);
   cudaFree(c->d_leaf_ids);
   cudaFree(c->d_plan);
+  cudaFree(c->d_copy_plan);
+  cudaFree(c->d_item_step);
   cudaFree(c->d_tiles);
   cudaFree(c->d_sitems);
   cudaFree(c->d_sgroups);
@@ -1304,8 +1319,10 @@ int pcg_profile_step(pcg_context *c, double *ms) {
   PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
                         c->d_patch_smax));
   PCG_CUDA(cudaEventRecord(ev[1], c->stream));
-  PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_times, c->d_items, c->d_gcells,
-                              c->n_copy_cells, c->n_interp_cells, c->d_plan, nullptr));
+  PCG_CUDA(launch_item_step(c->stream, c->d_patches, c->d_times, c->d_items, (int)c->h_items.size(),
+                            c->d_item_step));
+  PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
+                              c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step));
   PCG_CUDA(cudaEventRecord(ev[2], c->stream));
   PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
   PCG_CUDA(cudaEventRecord(ev[3], c->stream));

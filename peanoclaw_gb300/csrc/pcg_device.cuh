@@ -78,6 +78,20 @@ struct __align__(8) InterpPlanDev {
   double sf[4];
 };
 
+// Precomputed source/destination offsets of one ghost cell of a COPY item
+// (offsets of unknown 0; the other unknowns follow at the item's strides).
+struct __align__(16) CopyPlanDev {
+  long long src_new, src_old, dst;
+  int item, pad_;
+};
+
+// Per-step data of one ghost item: its time factor (and 1 - tf) and the
+// unknown strides of its source (uNew, uOld) and destination (uOld).
+struct __align__(16) GhostItemStepDev {
+  double tf, itf;
+  int vn_src, vo_src, vo_dst, nq;
+};
+
 constexpr int kTile = 16;           // tile edge of the sweep
 constexpr int kSweepThreads = 256;  // kTile * kTile
 constexpr int kFlagLeaf = 1;

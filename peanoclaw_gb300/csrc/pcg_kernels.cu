@@ -435,33 +435,92 @@ __global__ void k_build_interp_plan(const PatchDev *__restrict__ patches,
   }
 }
 
-// Batched ghost fill over the flat ghost-cell list: entries [0, ncopy) copy,
-// [ncopy, ncopy + ninterp) interpolate with their precomputed plan.  Items
-// write disjoint ghost cells, one thread per ghost cell.
+// Copy plan of the batched ghost fill: offsets of every COPY ghost cell,
+// computed once per grid change.
+__global__ void k_build_copy_plan(const PatchDev *__restrict__ patches,
+                                  const GhostItemDev *__restrict__ items,
+                                  const GhostCellDev *__restrict__ cells, int count,
+                                  CopyPlanDev *__restrict__ plan) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    const GhostCellDev gc = cells[e];
+    const GhostItemDev it = items[gc.item];
+    const PatchDev &S = patches[it.src], &D = patches[it.dst];
+    const int x = gc.k / it.size[1], y = gc.k - x * it.size[1];
+    CopyPlanDev pl;
+    pl.src_new = idx_unew(S, 0, it.src_off[0] + x, it.src_off[1] + y);
+    pl.src_old = idx_uold(S, 0, it.src_off[0] + x, it.src_off[1] + y);
+    pl.dst = idx_uold(D, 0, it.dst_off[0] + x, it.dst_off[1] + y);
+    pl.item = gc.item;
+    pl.pad_ = 0;
+    plan[e] = pl;
+  }
+}
+
+// Start of a batched fill: the time factor of every item (it is the same for
+// all cells of the item) and its unknown strides.
+__global__ void k_item_step(const PatchDev *__restrict__ patches,
+                            const PatchTimeDev *__restrict__ times,
+                            const GhostItemDev *__restrict__ items, int count,
+                            GhostItemStepDev *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const GhostItemDev it = items[i];
+    const PatchDev &S = patches[it.src], &D = patches[it.dst];
+    const PatchTimeDev &ST = times[it.src], &DT = times[it.dst];
+    GhostItemStepDev r;
+    r.tf = it.kind == 0 ? transfer_tf(S, ST, D, DT) : interp_tf(S, ST, D, DT, false, true);
+    r.itf = __dsub_rn(1.0, r.tf);
+    r.vn_src = (int)vol_new(S);
+    r.vo_src = (int)vol_old(S);
+    r.vo_dst = (int)vol_old(D);
+    r.nq = it.kind == 0 ? S.nq : (D.nq < 3 ? D.nq : 3);
+    out[i] = r;
+  }
+}
+
+// Batched ghost fill over the flat ghost-cell list: entries [0, ncopy) copy
+// (DefaultTransfer's time-interpolated copy, offsets from the copy plan),
+// [ncopy, ncopy + ninterp) interpolate with their precomputed d-linear plan
+// (SWE interpolation with the h+b wrap).  Items write disjoint ghost cells,
+// one thread per ghost cell.
 __global__ void __launch_bounds__(256)
     k_ghost_cells(double *__restrict__ slab, const PatchDev *__restrict__ patches,
-                  const PatchTimeDev *__restrict__ times, const GhostItemDev *__restrict__ items,
-                  const GhostCellDev *__restrict__ cells, int ncopy, int ninterp,
-                  const InterpPlanDev *__restrict__ plan, const int *__restrict__ group_active) {
+                  const GhostItemDev *__restrict__ items, const GhostCellDev *__restrict__ cells,
+                  int ncopy, int ninterp, const CopyPlanDev *__restrict__ copy_plan,
+                  const InterpPlanDev *__restrict__ plan,
+                  const GhostItemStepDev *__restrict__ item_step) {
   const int total = ncopy + ninterp;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    GhostCellDev gc = cells[e];
-    GhostItemDev it = items[gc.item];
-    const PatchDev S = patches[it.src], D = patches[it.dst];
-    if (group_active && !group_active[D.group]) continue;
-    const PatchTimeDev ST = times[it.src], DT = times[it.dst];
     if (e < ncopy) {
-      double tf = transfer_tf(S, ST, D, DT);
-      double itf = __dsub_rn(1.0, tf);
-      transfer_cell(slab, S, D, it.size, it.src_off, it.dst_off, tf, itf, gc.k);
+      const CopyPlanDev pl = copy_plan[e];
+      const GhostItemStepDev I = item_step[pl.item];
+      double vn[3], vo[3];
+      const int nq = I.nq < 3 ? I.nq : 3;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        if (q < nq) {
+          vn[q] = slab[pl.src_new + (long long)q * I.vn_src];
+          vo[q] = slab[pl.src_old + (long long)q * I.vo_src];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+        if (q < nq)
+          slab[pl.dst + (long long)q * I.vo_dst] = __dadd_rn(__dmul_rn(vn[q], I.tf), __dmul_rn(vo[q], I.itf));
+      for (int q = 3; q < I.nq; q++)  // more than three unknowns (not the SWE case)
+        slab[pl.dst + (long long)q * I.vo_dst] =
+            __dadd_rn(__dmul_rn(slab[pl.src_new + (long long)q * I.vn_src], I.tf),
+                      __dmul_rn(slab[pl.src_old + (long long)q * I.vo_src], I.itf));
       continue;
     }
+    const GhostCellDev gc = cells[e];
+    const GhostItemDev it = items[gc.item];
+    const PatchDev S = patches[it.src], D = patches[it.dst];
     const InterpPlanDev pl = plan[e - ncopy];
-    double tf = interp_tf(S, ST, D, DT, false, true);
-    double one_m_tf = __dsub_rn(1.0, tf);
+    const GhostItemStepDev I = item_step[gc.item];
+    const double tf = I.tf, one_m_tf = I.itf;
     int cx = it.dst_off[0] + gc.k / it.size[1], cy = it.dst_off[1] + gc.k % it.size[1];
     double acc[3];
-    const int nq = D.nq < 3 ? D.nq : 3;
+    const int nq = I.nq;
     for (int q = 0; q < nq; q++) acc[q] = 0.0;
     for (int kk = 0; kk < 4; kk++) {
       int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
@@ -971,15 +1030,33 @@ cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
 }
 
 cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
-                               const PatchTimeDev *times, const GhostItemDev *items,
-                               const GhostCellDev *cells, int ncopy, int ninterp,
-                               const InterpPlanDev *plan, const int *group_active) {
+                               const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
+                               int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
+                               const GhostItemStepDev *item_step) {
   int total = ncopy + ninterp;
   if (total <= 0) return cudaSuccess;
   int grid = (total + 255) / 256;
   if (grid > 152 * 32) grid = 152 * 32;
-  k_ghost_cells<<<grid, 256, 0, st>>>(slab, patches, times, items, cells, ncopy, ninterp, plan,
-                                      group_active);
+  k_ghost_cells<<<grid, 256, 0, st>>>(slab, patches, items, cells, ncopy, ninterp, copy_plan, plan,
+                                      item_step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
+                                   const GhostCellDev *cells, int count, CopyPlanDev *plan) {
+  if (count <= 0) return cudaSuccess;
+  int grid = (count + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  k_build_copy_plan<<<grid, 256, 0, st>>>(patches, items, cells, count, plan);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
+                             const GhostItemDev *items, int count, GhostItemStepDev *out) {
+  if (count <= 0) return cudaSuccess;
+  int grid = (count + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  k_item_step<<<grid, 256, 0, st>>>(patches, times, items, count, out);
   return cudaGetLastError();
 }
 

@@ -33,9 +33,13 @@ cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
                                      const GhostItemDev *items, const GhostCellDev *cells, int count,
                                      InterpPlanDev *plan);
 cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
-                               const PatchTimeDev *times, const GhostItemDev *items,
-                               const GhostCellDev *cells, int ncopy, int ninterp,
-                               const InterpPlanDev *plan, const int *group_active);
+                               const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
+                               int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
+                               const GhostItemStepDev *item_step);
+cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
+                                   const GhostCellDev *cells, int count, CopyPlanDev *plan);
+cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
+                             const GhostItemDev *items, int count, GhostItemStepDev *out);
 cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
                          const int *wall_patches, int count, const int *group_active);
 cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,
@@ -85,6 +89,7 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
                                 const StripGroup *groups, int count, const SweParamsDev &prm,
                                 unsigned long long *patch_smax, unsigned long long *group_dt);
 cudaError_t strip_occupancy(int variant, int *blocks_per_sm);
+cudaError_t update_strips_occupancy(int *blocks_per_sm);
 cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                                  PatchTimeDev *times, const StripItem *items, const StripGroup *groups,
                                  int count, const SweParamsDev &prm,

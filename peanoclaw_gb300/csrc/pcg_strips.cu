@@ -220,19 +220,34 @@ __global__ void __launch_bounds__(kWarps * 32)
     const long long vn = vol_new(P), vo = vol_old(P);
     long long in0 = idx_unew(P, 0, SG.x0, y), io0 = idx_uold(P, 0, SG.x0, y);
     const int sn = P.ny, so = P.ny + 2 * P.g;
-#pragma unroll 4
-    for (int c = 0; c < w; c++) {
-      const double h = slab[in0], hu = slab[in0 + vn], hv = slab[in0 + 2 * vn];
-      const double fh = slab[io0], fhu = slab[io0 + vo], fhv = slab[io0 + 2 * vo];
-      double nh = __fma_rn(-dt, fh, h);
-      double nhu = __fma_rn(-dt, fhu, hu);
-      double nhv = __fma_rn(-dt, fhv, hv);
-      if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
-      if (nh < 0.0) nh = 0.0;
-      slab[io0] = h; slab[io0 + vo] = hu; slab[io0 + 2 * vo] = hv;
-      slab[in0] = nh; slab[in0 + vn] = nhu; slab[in0 + 2 * vn] = nhv;
-      in0 += sn;
-      io0 += so;
+    // loads of kBatch columns are issued before their stores (loads and
+    // stores go through the same pointer, so the compiler cannot reorder them)
+    constexpr int kBatch = 4;
+    for (int c0 = 0; c0 < w; c0 += kBatch) {
+      double st[kBatch][3], nt[kBatch][3];
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        if (c0 + k < w) {
+          const long long a = in0 + (long long)k * sn, o = io0 + (long long)k * so;
+          st[k][0] = slab[a]; st[k][1] = slab[a + vn]; st[k][2] = slab[a + 2 * vn];
+          nt[k][0] = slab[o]; nt[k][1] = slab[o + vo]; nt[k][2] = slab[o + 2 * vo];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        if (c0 + k < w) {
+          const long long a = in0 + (long long)k * sn, o = io0 + (long long)k * so;
+          double nh = __fma_rn(-dt, nt[k][0], st[k][0]);
+          double nhu = __fma_rn(-dt, nt[k][1], st[k][1]);
+          double nhv = __fma_rn(-dt, nt[k][2], st[k][2]);
+          if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
+          if (nh < 0.0) nh = 0.0;
+          slab[o] = st[k][0]; slab[o + vo] = st[k][1]; slab[o + 2 * vo] = st[k][2];
+          slab[a] = nh; slab[a + vn] = nhu; slab[a + 2 * vn] = nhv;
+        }
+      }
+      in0 += (long long)kBatch * sn;
+      io0 += (long long)kBatch * so;
     }
     if (j == 0 && SG.x0 == 0 && SG.y0 == 0) {
       PatchTimeDev &T = times[SG.pid];
@@ -286,6 +301,10 @@ cudaError_t strip_occupancy(int variant, int *blocks_per_sm) {
     case 3: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<8, 3>, 256, 0);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t update_strips_occupancy(int *blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_update_strips<8>, 256, 0);
 }
 
 cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
