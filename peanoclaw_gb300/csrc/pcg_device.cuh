@@ -174,6 +174,16 @@ __device__ __forceinline__ bool lt_zero(double x) {
   unsigned long long m = (unsigned long long)b & kAbsMask;
   return b < 0 && m != 0ull && m <= kInfBits;
 }
+// a < b, the IEEE comparison (false if either is NaN; -0 == +0)
+__device__ __forceinline__ bool lt_ieee(double a, double b) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  const unsigned long long ma = (unsigned long long)ia & kAbsMask, mb = (unsigned long long)ib & kAbsMask;
+  if (ma > kInfBits || mb > kInfBits || (ma | mb) == 0ull) return false;
+  // sign-magnitude -> order-preserving two's complement keys
+  const long long ka = ia < 0 ? -(long long)ma : (long long)ma;
+  const long long kb = ib < 0 ? -(long long)mb : (long long)mb;
+  return ka < kb;
+}
 // x > c for a constant c >= +0.0 (not NaN)
 __device__ __forceinline__ bool gt_nonneg(double x, double c) {
   long long b = __double_as_longlong(x);

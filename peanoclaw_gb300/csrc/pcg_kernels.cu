@@ -207,8 +207,8 @@ __global__ void __launch_bounds__(kSweepThreads)
       double nh = __fma_rn(-dt, slab[io0], h);
       double nhu = __fma_rn(-dt, slab[io1], hu);
       double nhv = __fma_rn(-dt, slab[io2], hv);
-      if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
-      if (nh < 0.0) nh = 0.0;
+      if (lt_ieee(nh, prm.dry_tol_update)) { nhu = 0.0; nhv = 0.0; }
+      if (lt_zero(nh)) nh = 0.0;
       slab[io0] = h; slab[io1] = hu; slab[io2] = hv;
       slab[in0] = nh; slab[in1] = nhu; slab[in2] = nhv;
     }
@@ -278,8 +278,8 @@ __global__ void __launch_bounds__(kSweepThreads)
     double nh = __fma_rn(-dt, net[c], slab[io0]);
     double nhu = __fma_rn(-dt, net[(long long)nx * ny + c], slab[io1]);
     double nhv = __fma_rn(-dt, net[2LL * nx * ny + c], slab[io2]);
-    if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
-    if (nh < 0.0) nh = 0.0;
+    if (lt_ieee(nh, prm.dry_tol_update)) { nhu = 0.0; nhv = 0.0; }
+    if (lt_zero(nh)) nh = 0.0;
     // swapUNewAndUOld: uOld <- previous uNew, uNew <- updated values
     double o0 = slab[in0], o1 = slab[in1], o2 = slab[in2];
     slab[io0] = o0; slab[io1] = o1; slab[io2] = o2;
@@ -1232,8 +1232,8 @@ __global__ void __launch_bounds__(kSweepThreads)
     double nh = __fma_rn(-dt, net[c], vec[io0]);
     double nhu = __fma_rn(-dt, net[(long long)nx * ny + c], vec[io1]);
     double nhv = __fma_rn(-dt, net[2LL * nx * ny + c], vec[io2]);
-    if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
-    if (nh < 0.0) nh = 0.0;
+    if (lt_ieee(nh, prm.dry_tol_update)) { nhu = 0.0; nhv = 0.0; }
+    if (lt_zero(nh)) nh = 0.0;
     double o0 = vec[in0], o1 = vec[in1], o2 = vec[in2];
     vec[io0] = o0; vec[io1] = o1; vec[io2] = o2;
     vec[in0] = nh; vec[in1] = nhu; vec[in2] = nhv;

@@ -240,8 +240,8 @@ __global__ void __launch_bounds__(kWarps * 32)
           double nh = __fma_rn(-dt, nt[k][0], st[k][0]);
           double nhu = __fma_rn(-dt, nt[k][1], st[k][1]);
           double nhv = __fma_rn(-dt, nt[k][2], st[k][2]);
-          if (nh < prm.dry_tol_update) { nhu = 0.0; nhv = 0.0; }
-          if (nh < 0.0) nh = 0.0;
+          if (lt_ieee(nh, prm.dry_tol_update)) { nhu = 0.0; nhv = 0.0; }
+          if (lt_zero(nh)) nh = 0.0;
           slab[o] = st[k][0]; slab[o + vo] = st[k][1]; slab[o + 2 * vo] = st[k][2];
           slab[a] = nh; slab[a + vn] = nhu; slab[a + 2 * vn] = nhv;
         }
