@@ -41,6 +41,25 @@ def bytes_per_patch(n):
     return 8 * (4 * (n + 2) ** 2 + 3 * n * n)
 
 
+def profile_figure(name, key):
+    """A figure recorded in a committed ncu summary under profiles/ as
+    `key: value` (None when absent)."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith(key + ":"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+# FP64 instructions per cell update of the strip sweep (ncu count, see
+# profiles/k_sweep_strips_uneven_patches_4k.md) and the FP64 pipe width of
+# GB300 (FP64 lanes per clock per SM; the DFMA probe reaches it).
+FP64_INST_PER_CELL = 60.2
+FP64_LANES_PER_SM_CLK = 2
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -57,8 +76,10 @@ def parse():
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the secondary configurations (dam break, AMR, serving)")
     ap.add_argument("--amr-steps", type=int, default=100)
-    ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--serve-rate", type=float, default=1.0)
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=8.0)
+    ap.add_argument("--serve-batch", type=int, default=8,
+                    help="batched steps per replay of the step graph in the serving loop")
     return ap.parse_args()
 
 
@@ -216,14 +237,12 @@ def bench_amr(prm, steps):
     ghost interpolation, flux correction and restriction in every step."""
     from peanoclaw_gb300 import pcg as P
     from peanoclaw_gb300 import scenarios as S
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
     ps = S.breaking_dam_amr(base=9, n=27, levels=3)
     slab = int(sum(P.vector_size(n) + 32 for n in ps.n)) + 4096
     res = {"patches": len(ps), "leaves": int(sum(ps.leaf)), "leaf_cells": ps.meta["leaf_cells"]}
     for mode, name, k in ((P.PCG_MODE_BATCHED, "batched", steps), (P.PCG_MODE_PLAIN, "plain", 5)):
         ctx = P.Context(slab_doubles=slab, max_patches=len(ps) + 16, max_groups=1, params=prm)
-        from helpers import gpu_amr_patchset
-        gpu_amr_patchset(ctx, ps)
+        S.install_amr(ctx, ps)
         ctx.restrict_all()
         ctx.set_group_max_dt(0, 1e9)
         ctx.run(3, mode)
@@ -242,9 +261,12 @@ def bench_serving(args, prm):
     from peanoclaw_gb300 import serving as SV
     reqs = SV.make_requests(args.serve_requests, rate=args.serve_rate, seed=42, n=32)
     need = sum(int(r.cells * 1.4) for r in reqs)
-    srv = SV.Server(slab_doubles=int(need * 8) + (1 << 24), max_groups=16, max_patches=60000, params=prm)
+    srv = SV.Server(slab_doubles=int(need * 8) + (1 << 24), max_groups=32, max_patches=80000, params=prm,
+                    steps_per_batch=args.serve_batch)
     try:
+        _, ms0 = srv.ctx.stats()
         done, wall = srv.serve(reqs, max_wall=240.0)
+        _, ms1 = srv.ctx.stats()
     finally:
         srv.close()
     lat = np.array([r.finished - r.arrival for r in done])
@@ -253,7 +275,8 @@ def bench_serving(args, prm):
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "cell_updates_per_s": cu / wall, "wall_s": wall,
-            "max_concurrent_groups": 16}
+            "device_busy": (ms1 - ms0) / 1e3 / wall,
+            "max_concurrent_groups": 32, "steps_per_batch": args.serve_batch}
 
 
 def run_reference(args):
@@ -322,6 +345,8 @@ def main():
     sweep_ms = float(ph[3])
     update_ms = float(ph[4])
     fp64_peak = ctx.fp64_peak_tflops()
+    import torch
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     flops = FLOP_PER_CELL * cells
     # the FP64 work sits in the sweep (and 3 FMA/cell in the update)
     achieved = (flops / 1e12) / ((sweep_ms + update_ms) / 1e3)
@@ -333,6 +358,10 @@ def main():
     except Exception:
         pass
     step_ms_phase = float(ph.sum())
+    # DRAM traffic of the dominant kernel (sweep): bytes per cell update from
+    # the ncu capture of the small case, scaled to this launch's cells
+    tpc = profile_figure("k_sweep_strips_uneven_patches_4k.md", "traffic_bytes_per_cell_update")
+    traffic = tpc * cells if (tpc is not None and sched[0] == P.SCHED_STRIPS) else None
 
     # plain per-patch form (one launch per patch per phase), same workload
     plain = None
@@ -394,7 +423,12 @@ def main():
                        "l2": "inputs (%.1f GB) larger than L2, no flush" % (ps.packed.nbytes / 1e9),
                        "parallelism": "replicas x%d" % ws if ws > 1 else "1 GPU"},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp64_peak, "traffic": None,
+                         "frac": achieved / fp64_peak, "traffic": traffic,
+                         "traffic_note": "sweep DRAM bytes per launch: ncu bytes/cell of the 4k-patch "
+                                         "capture x cells (profiles/k_sweep_strips_uneven_patches_4k.md)",
+                         "fp64_pipe_frac_sweep": (FP64_INST_PER_CELL * cells /
+                                                  (sweep_ms / 1e3) /
+                                                  (FP64_LANES_PER_SM_CLK * sm_count * (clk.get("sm_mhz") or 2070.0) * 1e6)),
                          "peak_source": "measured live (DFMA chain probe, FMA = 2 flops)",
                          "flop_per_cell": FLOP_PER_CELL,
                          "kernels": ("k_sweep_tiles + k_update_tiles" if sched[0] == P.SCHED_TILES

@@ -201,6 +201,17 @@ int pcg_set_flux_correction_items(pcg_context *ctx, int32_t n, const int32_t *sr
 int pcg_restrict_all(pcg_context *ctx);
 /* Upper bound for the dt of a group (maximumTimestepSize). */
 int pcg_set_group_max_dt(pcg_context *ctx, int32_t group, double max_dt);
+/* No counterpart in the reference (its driver stops evolveToTime at the end
+ * time).  Sets the group's time to `time` and its end time to `t_end`
+ * (+inf, the default, means none).  Every following step caps the group's dt
+ * at max(0, t_end - time) and adds the dt taken to its time on the device; a
+ * group whose time has reached t_end is inactive: ghost fill, walls, sweep,
+ * update and the flux/restriction phases skip its patches and its state and
+ * time intervals stay unchanged, so many steps can be replayed (pcg_run)
+ * while groups finish at different steps. */
+int pcg_set_group_end_time(pcg_context *ctx, int32_t group, double time, double t_end);
+/* times[max_groups] receives every group's time (see pcg_set_group_end_time). */
+int pcg_get_group_times(pcg_context *ctx, double *times);
 /* One synchronous step of every leaf patch: fill ghost layers (items, then
  * walls), f-wave sweep with per-patch CFL, dt_g = min(max_dt_g, min over the
  * group's patches), update with dt_g, swap, time update.  dt_out (may be NULL)

@@ -140,6 +140,8 @@ struct pcg_context {
 
   unsigned long long *d_patch_smax = nullptr, *d_group_dt = nullptr;
   double *d_group_max_dt = nullptr;
+  double *d_group_t_end = nullptr, *d_group_time = nullptr;  // end time (+inf: none), time
+  int *d_group_active = nullptr;
   double *d_dt_out = nullptr;
   double *h_pinned = nullptr;  // pinned scratch for small D2H/H2D
   std::vector<double> h_group_max_dt;
@@ -332,6 +334,24 @@ void build_strips(pcg_context *c, int chunk) {
   }
 }
 
+// Schedule of a patch mix the autotuner has not seen: small grids (fewer cells
+// than 4096 per SM) have more parallelism in 16x16 tiles (one thread per
+// cell) than in strips (one warp per strip); larger ones use strips of 8
+// warps per CTA with the widest chunk that still gives every SM two CTAs'
+// worth of strip items.
+void default_schedule(pcg_context *c) {
+  if (c->cells_per_step < (int64_t)c->num_sms * 4096) {
+    c->sched = pcg_schedule{PCG_SCHED_TILES, 0, 32, 0};
+    return;
+  }
+  int chunk = 32;
+  for (; chunk > 4; chunk /= 2) {
+    build_strips(c, chunk);
+    if ((int64_t)c->h_sitems.size() >= (int64_t)c->num_sms * 16) break;
+  }
+  c->sched = pcg_schedule{PCG_SCHED_STRIPS, 2, chunk, 0};
+}
+
 // Upload the strip list of the current schedule and size its grids.
 int apply_schedule(pcg_context *c) {
   build_strips(c, c->sched.chunk);
@@ -497,6 +517,7 @@ int rebuild_topology(pcg_context *c) {
     std::lock_guard<std::mutex> lk(g_tuned_mu);
     auto it = g_tuned.find(c->shape_key);
     if (it != g_tuned.end()) c->sched = it->second;
+    else default_schedule(c);
   }
   if ((rc = apply_schedule(c)) != PCG_OK) return rc;
   c->patches_dirty = true;
@@ -516,18 +537,19 @@ int upload_group_max_dt(pcg_context *c) {
 // the order in which SolveTimestep::enterCell and Remesh::leaveCell run them.
 int enqueue_post_update(pcg_context *c) {
   using namespace pcg;
+  const int *ga = c->d_group_active;
   if (!c->h_flux.empty()) {
     PCG_CUDA(launch_compute_fluxes(c->stream, c->slab, c->d_patches, c->d_leaf_ids, (int)c->leaf_ids.size(),
-                                   c->g_flux));
+                                   c->g_flux, ga));
     PCG_CUDA(launch_flux_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_flux, c->d_flux_begin,
-                               (int)c->flux_begin.size() - 1));
+                               (int)c->flux_begin.size() - 1, ga));
   }
   if (!c->h_restr.empty()) {
     int nd = (int)c->restr_dsts.size();
-    PCG_CUDA(launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
+    PCG_CUDA(launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga));
     PCG_CUDA(launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
-                                   c->d_restr_begin, nd));
-    PCG_CUDA(launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
+                                   c->d_restr_begin, nd, ga));
+    PCG_CUDA(launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga));
   }
   return PCG_OK;
 }
@@ -537,11 +559,12 @@ int enqueue_sweep(pcg_context *c) {
   using namespace pcg;
   if (c->sched.kind == PCG_SCHED_TILES)
     PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
-                          (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+                          (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
+                          c->d_group_active));
   else
     PCG_CUDA(launch_sweep_strips(c->stream, c->sched.variant, c->strip_grid, c->slab, c->d_patches,
                                  c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
-                                 c->d_patch_smax, c->d_group_dt));
+                                 c->d_patch_smax, c->d_group_dt, c->d_group_active));
   return PCG_OK;
 }
 
@@ -549,44 +572,53 @@ int enqueue_update(pcg_context *c) {
   using namespace pcg;
   if (c->sched.kind == PCG_SCHED_TILES)
     PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
-                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
+                           c->d_group_active));
   else
     PCG_CUDA(launch_update_strips(c->stream, c->update_grid, c->slab, c->d_patches, c->d_times,
                                   c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
-                                  c->d_patch_smax, c->d_group_dt));
+                                  c->d_patch_smax, c->d_group_dt, c->d_group_active));
   return PCG_OK;
 }
 
 // Enqueue one synchronous step (no synchronisation, capturable in BATCHED mode).
 int enqueue_step(pcg_context *c, int mode) {
   using namespace pcg;
-  PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
+  PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_t_end, c->d_group_time,
+                        c->d_group_dt, c->d_group_active, c->max_patches,
                         c->d_patch_smax));
   if (mode == PCG_MODE_BATCHED) {
     PCG_CUDA(launch_item_step(c->stream, c->d_patches, c->d_times, c->d_items, (int)c->h_items.size(),
                               c->d_item_step));
     PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
-                                c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step));
-    PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
+                                c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step,
+                                c->d_group_active));
+    PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(),
+                          c->d_group_active));
     int rc;
     if ((rc = enqueue_sweep(c)) != PCG_OK) return rc;
     if ((rc = enqueue_update(c)) != PCG_OK) return rc;
   } else {
     for (int p : c->leaf_ids)
       PCG_CUDA(launch_fill_patch(c->stream, c->slab, c->d_patches, c->d_times, c->d_items,
-                                 c->item_first[p], c->item_count[p], p));
+                                 c->item_first[p], c->item_count[p], p, c->d_group_active));
     for (int p : c->leaf_ids) {
       const PatchDev &P = c->h_patches[p];
       PCG_CUDA(launch_sweep(c->stream, P.tile_count, c->slab, c->d_patches, c->d_tiles, P.tile_begin,
-                            P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+                            P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, c->d_group_active));
     }
     for (int p : c->leaf_ids) {
       const PatchDev &P = c->h_patches[p];
       PCG_CUDA(launch_update(c->stream, P.tile_count, c->slab, c->d_patches, c->d_times, c->d_tiles,
-                             P.tile_begin, P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, nullptr));
+                             P.tile_begin, P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt,
+                             c->d_group_active));
     }
   }
-  return enqueue_post_update(c);
+  int rc = enqueue_post_update(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(launch_group_advance(c->stream, c->max_groups, c->d_group_dt, c->d_group_active,
+                                c->d_group_time));
+  return PCG_OK;
 }
 
 int ensure_staging(pcg_context *c, size_t doubles, size_t metas) {
@@ -696,6 +728,15 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->d_patch_smax, sizeof(unsigned long long) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_group_dt, sizeof(unsigned long long) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_group_max_dt, sizeof(double) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_group_t_end, sizeof(double) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_group_time, sizeof(double) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_group_active, sizeof(int) * c->max_groups));
+  {
+    std::vector<double> inf(c->max_groups, HUGE_VAL), zero(c->max_groups, 0.0);
+    CREATE_CK(cudaMemcpy(c->d_group_t_end, inf.data(), sizeof(double) * c->max_groups, cudaMemcpyHostToDevice));
+    CREATE_CK(cudaMemcpy(c->d_group_time, zero.data(), sizeof(double) * c->max_groups, cudaMemcpyHostToDevice));
+    CREATE_CK(cudaMemset(c->d_group_active, 0, sizeof(int) * c->max_groups));
+  }
   CREATE_CK(cudaMalloc(&c->d_dt_out, sizeof(double) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_solve_out, sizeof(double) * 2));
   CREATE_CK(cudaMalloc(&c->d_counter, sizeof(int)));
@@ -716,6 +757,9 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_patch_smax);
   cudaFree(c->d_group_dt);
   cudaFree(c->d_group_max_dt);
+  cudaFree(c->d_group_t_end);
+  cudaFree(c->d_group_time);
+  cudaFree(c->d_group_active);
   cudaFree(c->d_dt_out);
   cudaFree(c->d_items);
   cudaFree(c->d_gcells);
@@ -1108,6 +1152,30 @@ int pcg_restrict_all(pcg_context *c) {
   return PCG_OK;
 }
 
+int pcg_set_group_end_time(pcg_context *c, int32_t group, double time, double t_end) {
+  if (!c || group < 0 || group >= c->max_groups) return fail(PCG_E_INVALID, "group out of range");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  c->h_pinned[0] = time;
+  c->h_pinned[1] = t_end;
+  PCG_CUDA(cudaMemcpyAsync(c->d_group_time + group, c->h_pinned, sizeof(double), cudaMemcpyHostToDevice,
+                           c->stream));
+  PCG_CUDA(cudaMemcpyAsync(c->d_group_t_end + group, c->h_pinned + 1, sizeof(double),
+                           cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+int pcg_get_group_times(pcg_context *c, double *times) {
+  if (!c || !times) return fail(PCG_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  PCG_CUDA(cudaMemcpyAsync(times, c->d_group_time, sizeof(double) * c->max_groups, cudaMemcpyDeviceToHost,
+                           c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
 int pcg_set_group_max_dt(pcg_context *c, int32_t group, double max_dt) {
   if (!c || group < 0 || group >= c->max_groups) return fail(PCG_E_INVALID, "group out of range");
   std::lock_guard<std::mutex> lk(c->mu);
@@ -1316,15 +1384,18 @@ int pcg_profile_step(pcg_context *c, double *ms) {
   for (int i = 0; i < 6; i++) PCG_CUDA(cudaEventCreate(&ev[i]));
   using namespace pcg;
   PCG_CUDA(cudaEventRecord(ev[0], c->stream));
-  PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_dt, c->max_patches,
+  PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_t_end, c->d_group_time,
+                        c->d_group_dt, c->d_group_active, c->max_patches,
                         c->d_patch_smax));
   PCG_CUDA(cudaEventRecord(ev[1], c->stream));
   PCG_CUDA(launch_item_step(c->stream, c->d_patches, c->d_times, c->d_items, (int)c->h_items.size(),
                             c->d_item_step));
   PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
-                              c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step));
+                              c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step,
+                                c->d_group_active));
   PCG_CUDA(cudaEventRecord(ev[2], c->stream));
-  PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), nullptr));
+  PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(),
+                        c->d_group_active));
   PCG_CUDA(cudaEventRecord(ev[3], c->stream));
   if ((rc = enqueue_sweep(c)) != PCG_OK) return rc;
   PCG_CUDA(cudaEventRecord(ev[4], c->stream));

@@ -82,7 +82,7 @@ struct __align__(8) InterpPlanDev {
 // (offsets of unknown 0; the other unknowns follow at the item's strides).
 struct __align__(16) CopyPlanDev {
   long long src_new, src_old, dst;
-  int item, pad_;
+  int item, dst_pid;
 };
 
 // Per-step data of one ghost item: its time factor (and 1 - tf) and the

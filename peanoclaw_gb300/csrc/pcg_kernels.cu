@@ -223,13 +223,31 @@ __global__ void __launch_bounds__(kSweepThreads)
   }
 }
 
-// Start of a step: group dt <- max_dt, patch max speed <- 0.
+// Start of a step: group dt <- min(max_dt, max(0, t_end - t)) (t_end = +inf
+// unless the group has an end time), group active iff t_end - t > 0, patch
+// max speed <- 0.
 __global__ void k_reset_step(int n_groups, const double *__restrict__ group_max_dt,
-                             unsigned long long *__restrict__ group_dt, int n_patches,
-                             unsigned long long *__restrict__ patch_smax) {
+                             const double *__restrict__ group_t_end,
+                             const double *__restrict__ group_time,
+                             unsigned long long *__restrict__ group_dt, int *__restrict__ group_active,
+                             int n_patches, unsigned long long *__restrict__ patch_smax) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n_groups) group_dt[i] = dbits(group_max_dt[i]);
+  if (i < n_groups) {
+    const double rem = __dsub_rn(group_t_end[i], group_time[i]);
+    const bool active = gt_nonneg(rem, 0.0);
+    const double cap = active ? rem : 0.0;
+    const double mx = group_max_dt[i];
+    group_dt[i] = dbits(lt_ieee(cap, mx) ? cap : mx);
+    group_active[i] = active ? 1 : 0;
+  }
   for (int k = i; k < n_patches; k += gridDim.x * blockDim.x) patch_smax[k] = 0ull;
+}
+
+// End of a step: t += dt for the active groups.
+__global__ void k_group_advance(int n_groups, const unsigned long long *__restrict__ group_dt,
+                                const int *__restrict__ group_active, double *__restrict__ group_time) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_groups && group_active[i]) group_time[i] = __dadd_rn(group_time[i], bitsd(group_dt[i]));
 }
 
 // Record the dt of every group after a step.
@@ -451,7 +469,7 @@ __global__ void k_build_copy_plan(const PatchDev *__restrict__ patches,
     pl.src_old = idx_uold(S, 0, it.src_off[0] + x, it.src_off[1] + y);
     pl.dst = idx_uold(D, 0, it.dst_off[0] + x, it.dst_off[1] + y);
     pl.item = gc.item;
-    pl.pad_ = 0;
+    pl.dst_pid = it.dst;
     plan[e] = pl;
   }
 }
@@ -487,11 +505,13 @@ __global__ void __launch_bounds__(256)
                   const GhostItemDev *__restrict__ items, const GhostCellDev *__restrict__ cells,
                   int ncopy, int ninterp, const CopyPlanDev *__restrict__ copy_plan,
                   const InterpPlanDev *__restrict__ plan,
-                  const GhostItemStepDev *__restrict__ item_step) {
+                  const GhostItemStepDev *__restrict__ item_step,
+                  const int *__restrict__ group_active) {
   const int total = ncopy + ninterp;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     if (e < ncopy) {
       const CopyPlanDev pl = copy_plan[e];
+      if (group_active && !group_active[patches[pl.dst_pid].group]) continue;
       const GhostItemStepDev I = item_step[pl.item];
       double vn[3], vo[3];
       const int nq = I.nq < 3 ? I.nq : 3;
@@ -515,6 +535,7 @@ __global__ void __launch_bounds__(256)
     const GhostCellDev gc = cells[e];
     const GhostItemDev it = items[gc.item];
     const PatchDev S = patches[it.src], D = patches[it.dst];
+    if (group_active && !group_active[D.group]) continue;
     const InterpPlanDev pl = plan[e - ncopy];
     const GhostItemStepDev I = item_step[gc.item];
     const double tf = I.tf, one_m_tf = I.itf;
@@ -615,7 +636,9 @@ __global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ 
 // Plain form, one launch per patch: the patch's ghost items, then its walls.
 __global__ void k_fill_patch(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                              const PatchTimeDev *__restrict__ times,
-                             const GhostItemDev *__restrict__ items, int first, int count, int pid) {
+                             const GhostItemDev *__restrict__ items, int first, int count, int pid,
+                             const int *__restrict__ group_active) {
+  if (group_active && !group_active[patches[pid].group]) return;
   int lane = threadIdx.x;
   for (int w = 0; w < count; w++) {
     GhostItemDev it = items[first + w];
@@ -828,7 +851,8 @@ __global__ void k_restrict(double *slab, const PatchDev *patches, const PatchTim
 // Batched restriction: block b handles the items [begin[b], begin[b+1]) that
 // all share one destination, in list order.
 __global__ void k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                                 const int4 *items, const int *begin) {
+                                 const int4 *items, const int *begin, const int *group_active) {
+  if (group_active && !group_active[patches[items[begin[blockIdx.x]].y].group]) return;
   for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
     int4 it = items[k];  // src, dst, only_overlapped, swe
     restrict_block(slab, patches[it.x], times[it.x], patches[it.y], times[it.y], it.z != 0, it.w != 0);
@@ -836,9 +860,11 @@ __global__ void k_restrict_items(double *slab, const PatchDev *patches, const Pa
   }
 }
 
-__global__ void k_post_process_restriction(double *slab, const PatchDev *patches, const int *ids, int count) {
+__global__ void k_post_process_restriction(double *slab, const PatchDev *patches, const int *ids, int count,
+                                           const int *group_active) {
   PatchDev P = patches[ids[blockIdx.x % count]];
   if ((int)blockIdx.x >= count) return;
+  if (group_active && !group_active[P.group]) return;
   for (int c = threadIdx.x; c < P.nx * P.ny; c += blockDim.x) {
     int x = c / P.ny, y = c % P.ny;
     double bb = slab[idx_pw(P, 0, x, y)];
@@ -862,9 +888,11 @@ __device__ __forceinline__ void compute_flux(int dim, const double u[3], double 
   f[1 + dim] = __dadd_rn(f[1 + dim], pr);
 }
 
-__global__ void k_compute_fluxes(double *slab, const PatchDev *patches, const int *ids, int count, double gf) {
+__global__ void k_compute_fluxes(double *slab, const PatchDev *patches, const int *ids, int count, double gf,
+                                 const int *group_active) {
   if ((int)blockIdx.x >= count) return;
   PatchDev P = patches[ids[blockIdx.x]];
+  if (group_active && !group_active[P.group]) return;
   int n[2] = {P.nx, P.ny};
   int total = 2 * (n[1] + n[0]);
   for (int k = threadIdx.x; k < total; k += blockDim.x) {
@@ -945,10 +973,11 @@ __global__ void k_flux_correction(double *slab, const PatchDev *patches, const P
 // Batched flux correction: block b applies the items [begin[b], begin[b+1])
 // (all with the same destination) in list order.
 __global__ void k_flux_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                             const int4 *items, const int *begin) {
+                             const int4 *items, const int *begin, const int *group_active) {
   if (threadIdx.x != 0) return;
   for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
     int4 it = items[k];  // src, dst, dim, dir
+    if (group_active && !group_active[patches[it.y].group]) continue;
     flux_correction_one(slab, patches, times, it.x, it.y, it.z, it.w);
   }
 }
@@ -956,9 +985,11 @@ __global__ void k_flux_items(double *slab, const PatchDev *patches, const PatchT
 // Clears uNew and the uOld interior of the listed (virtual) patches before
 // the restriction accumulates into them (Patch accessor clearRegion, called
 // from GridLevelTransfer::switchToAndAddVirtualSubgrid).
-__global__ void k_clear_interior(double *slab, const PatchDev *patches, const int *ids, int count) {
+__global__ void k_clear_interior(double *slab, const PatchDev *patches, const int *ids, int count,
+                                 const int *group_active) {
   if ((int)blockIdx.x >= count) return;
   PatchDev P = patches[ids[blockIdx.x]];
+  if (group_active && !group_active[P.group]) return;
   int n = P.nx * P.ny;
   for (int k = threadIdx.x; k < P.nq * n; k += blockDim.x) {
     int q = k / n, c = k - q * n, x = c / P.ny, y = c - x * P.ny;
@@ -991,13 +1022,21 @@ cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDe
 }
 
 cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_dt,
-                         unsigned long long *group_dt, int n_patches,
+                         const double *group_t_end, const double *group_time,
+                         unsigned long long *group_dt, int *group_active, int n_patches,
                          unsigned long long *patch_smax) {
   int n = n_groups > n_patches ? n_groups : n_patches;
   int grid = (n + 255) / 256;
   if (grid > 1024) grid = 1024;
   if (grid < 1) grid = 1;
-  k_reset_step<<<grid, 256, 0, st>>>(n_groups, group_max_dt, group_dt, n_patches, patch_smax);
+  k_reset_step<<<grid, 256, 0, st>>>(n_groups, group_max_dt, group_t_end, group_time, group_dt,
+                                     group_active, n_patches, patch_smax);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_group_advance(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
+                                 const int *group_active, double *group_time) {
+  k_group_advance<<<(n_groups + 127) / 128, 128, 0, st>>>(n_groups, group_dt, group_active, group_time);
   return cudaGetLastError();
 }
 
@@ -1032,13 +1071,13 @@ cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
 cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
                                const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
                                int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
-                               const GhostItemStepDev *item_step) {
+                               const GhostItemStepDev *item_step, const int *group_active) {
   int total = ncopy + ninterp;
   if (total <= 0) return cudaSuccess;
   int grid = (total + 255) / 256;
   if (grid > 152 * 32) grid = 152 * 32;
   k_ghost_cells<<<grid, 256, 0, st>>>(slab, patches, items, cells, ncopy, ninterp, copy_plan, plan,
-                                      item_step);
+                                      item_step, group_active);
   return cudaGetLastError();
 }
 
@@ -1071,8 +1110,8 @@ cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
 
 cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,
                               const PatchTimeDev *times, const GhostItemDev *items, int first,
-                              int count, int pid) {
-  k_fill_patch<<<1, 128, 0, st>>>(slab, patches, times, items, first, count, pid);
+                              int count, int pid, const int *group_active) {
+  k_fill_patch<<<1, 128, 0, st>>>(slab, patches, times, items, first, count, pid, group_active);
   return cudaGetLastError();
 }
 
@@ -1131,38 +1170,38 @@ cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patch
 
 cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst) {
+                                  int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
-  k_restrict_items<<<n_dst, 256, 0, st>>>(slab, patches, times, items, begin);
+  k_restrict_items<<<n_dst, 256, 0, st>>>(slab, patches, times, items, begin, group_active);
   return cudaGetLastError();
 }
 
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
-                                            const int *ids, int count) {
+                                            const int *ids, int count, const int *group_active) {
   if (count <= 0) return cudaSuccess;
-  k_post_process_restriction<<<count, 256, 0, st>>>(slab, patches, ids, count);
+  k_post_process_restriction<<<count, 256, 0, st>>>(slab, patches, ids, count, group_active);
   return cudaGetLastError();
 }
 
 cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const int *ids, int count, double gf) {
+                                  const int *ids, int count, double gf, const int *group_active) {
   if (count <= 0) return cudaSuccess;
-  k_compute_fluxes<<<count, 128, 0, st>>>(slab, patches, ids, count, gf);
+  k_compute_fluxes<<<count, 128, 0, st>>>(slab, patches, ids, count, gf, group_active);
   return cudaGetLastError();
 }
 
 cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *patches,
                               const PatchTimeDev *times, const int4 *items, const int *begin,
-                              int n_dst) {
+                              int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
-  k_flux_items<<<n_dst, 32, 0, st>>>(slab, patches, times, items, begin);
+  k_flux_items<<<n_dst, 32, 0, st>>>(slab, patches, times, items, begin, group_active);
   return cudaGetLastError();
 }
 
 cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const int *ids, int count) {
+                                  const int *ids, int count, const int *group_active) {
   if (count <= 0) return cudaSuccess;
-  k_clear_interior<<<count, 256, 0, st>>>(slab, patches, ids, count);
+  k_clear_interior<<<count, 256, 0, st>>>(slab, patches, ids, count, group_active);
   return cudaGetLastError();
 }
 

@@ -22,8 +22,11 @@ cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDe
                           const SweParamsDev &prm, const unsigned long long *patch_smax,
                           const unsigned long long *group_dt, const int *group_active);
 cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_dt,
-                         unsigned long long *group_dt, int n_patches,
+                         const double *group_t_end, const double *group_time,
+                         unsigned long long *group_dt, int *group_active, int n_patches,
                          unsigned long long *patch_smax);
+cudaError_t launch_group_advance(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
+                                 const int *group_active, double *group_time);
 cudaError_t launch_record_dt(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
                              double *out);
 cudaError_t launch_ghost_items(cudaStream_t st, double *slab, const PatchDev *patches,
@@ -35,7 +38,7 @@ cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
 cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
                                const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
                                int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
-                               const GhostItemStepDev *item_step);
+                               const GhostItemStepDev *item_step, const int *group_active);
 cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
                                    const GhostCellDev *cells, int count, CopyPlanDev *plan);
 cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
@@ -44,7 +47,7 @@ cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
                          const int *wall_patches, int count, const int *group_active);
 cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,
                               const PatchTimeDev *times, const GhostItemDev *items, int first,
-                              int count, int pid);
+                              int count, int pid, const int *group_active = nullptr);
 size_t solve_patch_smem(int nx, int ny);
 cudaError_t sweep_occupancy(int *blocks_per_sm);
 cudaError_t prepare_solve_patch(size_t max_dynamic_smem);
@@ -64,16 +67,18 @@ cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patch
                             const PatchTimeDev *times, int src, int dst, int only_overlapped, int swe);
 cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst);
+                                  int n_dst, const int *group_active = nullptr);
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
-                                            const int *ids, int count);
+                                            const int *ids, int count,
+                                            const int *group_active = nullptr);
 cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const int *ids, int count, double gf);
+                                  const int *ids, int count, double gf,
+                                  const int *group_active = nullptr);
 cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *patches,
                               const PatchTimeDev *times, const int4 *items, const int *begin,
-                              int n_dst);
+                              int n_dst, const int *group_active = nullptr);
 cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const int *ids, int count);
+                                  const int *ids, int count, const int *group_active = nullptr);
 cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev *patches,
                                    const PatchTimeDev *times, int src, int dst, int dim, int dir);
 
@@ -87,13 +92,14 @@ extern const StripVariant kStripVariants[kNumStripVariants];
 cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *slab,
                                 const PatchDev *patches, const StripItem *items,
                                 const StripGroup *groups, int count, const SweParamsDev &prm,
-                                unsigned long long *patch_smax, unsigned long long *group_dt);
+                                unsigned long long *patch_smax, unsigned long long *group_dt,
+                                const int *group_active);
 cudaError_t strip_occupancy(int variant, int *blocks_per_sm);
 cudaError_t update_strips_occupancy(int *blocks_per_sm);
 cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                                  PatchTimeDev *times, const StripItem *items, const StripGroup *groups,
                                  int count, const SweParamsDev &prm,
                                  const unsigned long long *patch_smax,
-                                 const unsigned long long *group_dt);
+                                 const unsigned long long *group_dt, const int *group_active);
 
 }  // namespace pcg

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     k_sweep_strips(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                    const StripItem *__restrict__ items, const StripGroup *__restrict__ groups,
                    int count, SweParamsDev prm, unsigned long long *__restrict__ patch_smax,
-                   unsigned long long *__restrict__ group_dt) {
+                   unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active) {
   __shared__ StripWarpSmem SM[kWarps];
   __shared__ StripLaneSmem LS[kWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -91,9 +91,10 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     const StripItem I = items[it];
     const int hs = I.hs, w = I.w, G = I.ngroups;
     const int gi = lane / hs, j = lane - gi * hs;
-    const bool act = gi < G;
-    const StripGroup SG = groups[I.g0 + (act ? gi : 0)];
+    const bool in_group = gi < G;
+    const StripGroup SG = groups[I.g0 + (in_group ? gi : 0)];
     const PatchDev P = patches[SG.pid];
+    const bool act = in_group && (!group_active || group_active[P.group]);
     const int y = SG.y0 + j;
 
     // ---- boundary rows: lane l < G*w takes (group l / w, column l % w)
@@ -206,7 +207,8 @@ __global__ void __launch_bounds__(kWarps * 32)
                     PatchTimeDev *__restrict__ times, const StripItem *__restrict__ items,
                     const StripGroup *__restrict__ groups, int count, SweParamsDev prm,
                     const unsigned long long *__restrict__ patch_smax,
-                    const unsigned long long *__restrict__ group_dt) {
+                    const unsigned long long *__restrict__ group_dt,
+                    const int *__restrict__ group_active) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int it = blockIdx.x * kWarps + wid; it < count; it += gridDim.x * kWarps) {
     const StripItem I = items[it];
@@ -215,6 +217,7 @@ __global__ void __launch_bounds__(kWarps * 32)
     if (gi >= G) continue;
     const StripGroup SG = groups[I.g0 + gi];
     const PatchDev P = patches[SG.pid];
+    if (group_active && !group_active[P.group]) continue;
     const double dt = bitsd(group_dt[P.group]);
     const int y = SG.y0 + j;
     const long long vn = vol_new(P), vo = vol_old(P);
@@ -266,10 +269,11 @@ template <int kWarps, int kMinBlocks>
 cudaError_t sweep_strips_t(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                            const StripItem *items, const StripGroup *groups, int count,
                            const SweParamsDev &prm, unsigned long long *patch_smax,
-                           unsigned long long *group_dt) {
+                           unsigned long long *group_dt, const int *group_active) {
   if (count <= 0) return cudaSuccess;
   k_sweep_strips<kWarps, kMinBlocks><<<grid, kWarps * 32, 0, st>>>(slab, patches, items, groups, count,
-                                                                   prm, patch_smax, group_dt);
+                                                                   prm, patch_smax, group_dt,
+                                                                   group_active);
   return cudaGetLastError();
 }
 
@@ -283,12 +287,13 @@ const StripVariant kStripVariants[kNumStripVariants] = {
 cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *slab,
                                 const PatchDev *patches, const StripItem *items,
                                 const StripGroup *groups, int count, const SweParamsDev &prm,
-                                unsigned long long *patch_smax, unsigned long long *group_dt) {
+                                unsigned long long *patch_smax, unsigned long long *group_dt,
+                                const int *group_active) {
   switch (variant) {
-    case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
-    case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
-    case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
-    case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt);
+    case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
+    case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
+    case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
+    case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -311,10 +316,10 @@ cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const 
                                  PatchTimeDev *times, const StripItem *items, const StripGroup *groups,
                                  int count, const SweParamsDev &prm,
                                  const unsigned long long *patch_smax,
-                                 const unsigned long long *group_dt) {
+                                 const unsigned long long *group_dt, const int *group_active) {
   if (count <= 0) return cudaSuccess;
   k_update_strips<8><<<grid, 256, 0, st>>>(slab, patches, times, items, groups, count, prm, patch_smax,
-                                           group_dt);
+                                           group_dt, group_active);
   return cudaGetLastError();
 }
 

@@ -104,6 +104,8 @@ SIGNATURES = {
     "pcg_apply_flux_correction": (C.c_int, [_CTX, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "pcg_set_ghost_items": (C.c_int, [_CTX, C.POINTER(GhostItem), C.c_int32]),
     "pcg_set_group_max_dt": (C.c_int, [_CTX, C.c_int32, C.c_double]),
+    "pcg_set_group_end_time": (C.c_int, [_CTX, C.c_int32, C.c_double, C.c_double]),
+    "pcg_get_group_times": (C.c_int, [_CTX, _D]),
     "pcg_set_restriction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, C.c_int32]),
     "pcg_set_flux_correction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, _I2, _I2, C.c_double]),
     "pcg_restrict_all": (C.c_int, [_CTX]),
@@ -295,6 +297,15 @@ class Context:
 
     def set_group_max_dt(self, group, max_dt):
         check(lib().pcg_set_group_max_dt(self.h, group, float(max_dt)))
+
+    def set_group_end_time(self, group, time, t_end):
+        """Device-side end time of a group (see pcg_set_group_end_time)."""
+        check(lib().pcg_set_group_end_time(self.h, group, float(time), float(t_end)))
+
+    def group_times(self):
+        out = np.zeros(self.max_groups)
+        check(lib().pcg_get_group_times(self.h, dptr(out)))
+        return out
 
     def step(self, mode=PCG_MODE_BATCHED):
         out = np.zeros(self.max_groups)

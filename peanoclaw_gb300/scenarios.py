@@ -388,3 +388,28 @@ def breaking_dam_amr(base=9, n=27, levels=3, buffers=(1, 2), x_dam=0.5, h_left=1
                            % (levels, len(ps), sum(ps.leaf), n, n),
                "leaf_cells": int(sum(n * n for p in range(len(ps)) if ps.leaf[p]))}
     return ps
+
+
+def install_amr(ctx, ps, flux=True, g_flux=1.0):
+    """Allocate an adaptive PatchSet (breaking_dam_amr) in a pcg.Context:
+    leaves and virtual patches with their restriction bounds, the ghost
+    face-pair list, the restriction list and (flux=True) the flux-correction
+    list.  Returns the patch ids in PatchSet order."""
+    ids = []
+    for p in range(len(ps)):
+        leaf = bool(ps.leaf[p])
+        pid = ctx.alloc(ps.n[p], pos=ps.pos[p], size=ps.size[p], level=ps.level[p], leaf=leaf,
+                        virtual=not leaf)
+        ids.append(pid)
+        if ps.wall[p]:
+            ctx.set_boundary(pid, ps.wall[p])
+        if not leaf:
+            ctx.set_time(pid, restr_lower=ps.restr_lower[p], restr_upper=ps.restr_upper[p])
+    ids = np.array(ids, dtype=np.int32)
+    ctx.upload_many(ids, ps.packed)
+    ctx.set_ghost_items(remap_items(ps.items, ids))
+    ctx.set_restriction_items(ids[ps.restrict_items[:, 0]], ids[ps.restrict_items[:, 1]], True)
+    if flux and len(ps.flux_items):
+        f = ps.flux_items
+        ctx.set_flux_correction_items(ids[f[:, 0]], ids[f[:, 1]], f[:, 2], f[:, 3], g_flux)
+    return ids

@@ -96,19 +96,27 @@ def make_requests(count, rate, seed=42, cells=(1e4, 4e6), t_end=(0.05, 0.5), n=1
 
 
 class Server:
-    """Admits requests by free HBM and group slots, steps all resident groups together."""
+    """Admits requests by free HBM and group slots, steps all resident groups
+    together, `steps_per_batch` batched steps per replay of the step graph.
 
-    def __init__(self, slab_doubles, max_groups=32, max_patches=200_000, params=None):
+    Each scenario's end time lives on the device (pcg_set_group_end_time):
+    its dt is capped at the time left and a finished scenario's group goes
+    inactive (its state stays untouched) until the host retires it after the
+    batch."""
+
+    def __init__(self, slab_doubles, max_groups=32, max_patches=200_000, params=None,
+                 steps_per_batch=8):
         self.prm = params if params is not None else P.swe_params(g=9.81, cfl=0.5)
         self.ctx = P.Context(slab_doubles=slab_doubles, max_patches=max_patches,
                              max_groups=max_groups, params=self.prm)
         self.max_groups = max_groups
+        self.steps_per_batch = max(1, int(steps_per_batch))
         self.free_groups = list(range(max_groups))
-        self.resident = {}      # group -> (Request, PatchSet, times)
+        self.resident = {}      # group -> (Request, PatchSet)
         self.items = {}         # group -> remapped items
-        self.gtime = np.zeros(max_groups)
         for g in range(max_groups):
-            self.ctx.set_group_max_dt(g, 0.0)
+            self.ctx.set_group_max_dt(g, np.inf)
+            self.ctx.set_group_end_time(g, 0.0, 0.0)   # free slots: inactive
 
     def close(self):
         self.ctx.close()
@@ -140,8 +148,7 @@ class Server:
         req.group, req.ids, req.admitted = g, ids, now
         self.items[g] = remap_items(ps.items, ids)
         self.resident[g] = (req, ps)
-        self.gtime[g] = 0.0
-        self.ctx.set_group_max_dt(g, req.t_end)
+        self.ctx.set_group_end_time(g, 0.0, req.t_end)
         self._install_items()
         return True
 
@@ -156,23 +163,23 @@ class Server:
             self.ctx.free(pid)
         req.finished = now
         del self.items[g]
-        self.ctx.set_group_max_dt(g, 0.0)
+        self.ctx.set_group_end_time(g, 0.0, 0.0)
         self.free_groups.append(g)
         self._install_items()
         return req
 
     def step(self):
-        """One batched step of every resident group; returns retired requests."""
-        for g, (req, ps) in self.resident.items():
-            self.ctx.set_group_max_dt(g, max(0.0, req.t_end - self.gtime[g]))
-        dts = self.ctx.step(P.PCG_MODE_BATCHED)
+        """One batch of steps of every resident group; returns the groups that
+        finished (reached their end time, or took a zero step)."""
+        hist = self.ctx.run(self.steps_per_batch, P.PCG_MODE_BATCHED)
+        times = self.ctx.group_times()
         done = []
         for g, (req, ps) in list(self.resident.items()):
-            dt = dts[g]
-            self.gtime[g] += dt
-            req.steps += 1
-            req.cell_updates += ps.cells()
-            if self.gtime[g] >= req.t_end or dt <= 0.0:
+            taken = hist[:, g] > 0.0
+            k = int(np.count_nonzero(taken))
+            req.steps += k
+            req.cell_updates += k * ps.cells()
+            if times[g] >= req.t_end or k < self.steps_per_batch:
                 done.append(g)
         return done
 
@@ -202,9 +209,9 @@ class Server:
         return finished, clock() - t0
 
 
-def run_alone(req, slab_doubles, params=None):
+def run_alone(req, slab_doubles, params=None, steps_per_batch=1):
     """Solve one request as the only resident scenario; returns its final state."""
-    srv = Server(slab_doubles, max_groups=2, params=params)
+    srv = Server(slab_doubles, max_groups=2, params=params, steps_per_batch=steps_per_batch)
     try:
         req2 = Request(**{k: getattr(req, k) for k in ("rid", "kind", "cells", "t_end", "arrival",
                                                      "n", "seed")})

@@ -117,22 +117,5 @@ def oracle_amr_step(pats, ps, prm, max_dt, g_flux=1.0, flux=True):
 
 
 def gpu_amr_patchset(ctx, ps, flux=True, g_flux=1.0):
-    from peanoclaw_gb300.scenarios import remap_items
-    ids = []
-    for p in range(len(ps)):
-        leaf = bool(ps.leaf[p])
-        pid = ctx.alloc(ps.n[p], pos=ps.pos[p], size=ps.size[p], level=ps.level[p], leaf=leaf,
-                        virtual=not leaf)
-        ids.append(pid)
-        if ps.wall[p]:
-            ctx.set_boundary(pid, ps.wall[p])
-        if not leaf:
-            ctx.set_time(pid, restr_lower=ps.restr_lower[p], restr_upper=ps.restr_upper[p])
-    ids = np.array(ids, dtype=np.int32)
-    ctx.upload_many(ids, ps.packed)
-    ctx.set_ghost_items(remap_items(ps.items, ids))
-    ctx.set_restriction_items(ids[ps.restrict_items[:, 0]], ids[ps.restrict_items[:, 1]], True)
-    if flux and len(ps.flux_items):
-        f = ps.flux_items
-        ctx.set_flux_correction_items(ids[f[:, 0]], ids[f[:, 1]], f[:, 2], f[:, 3], g_flux)
-    return ids
+    from peanoclaw_gb300.scenarios import install_amr
+    return install_amr(ctx, ps, flux=flux, g_flux=g_flux)
