@@ -176,6 +176,25 @@ int pcg_compute_fluxes(pcg_context *ctx, int32_t id, double g_flux);
 int pcg_apply_flux_correction(pcg_context *ctx, int32_t src, int32_t dst, int32_t dimension,
                               int32_t direction);
 
+/* ----------------------------------------------------------------- remesh */
+
+/* Patch::getAccessor().clearRegion of uNew and the uOld interior (what
+ * GridLevelTransfer::switchToAndAddVirtualSubgrid does to a virtual patch
+ * before its children restrict into it); used before a full restriction when
+ * a refined patch coarsens. */
+int pcg_clear_subgrid(pcg_context *ctx, int32_t id);
+/* Patch::switchToLeaf (src/peanoclaw/Patch.cpp:793-816): the patch becomes a
+ * leaf and its interior, restricted as values at the times 0 and 1 (the
+ * reference's virtual-patch convention), is re-evaluated at the patch's time
+ * (uOld) and time + dt (uNew).  Set the time interval first. */
+int pcg_switch_to_leaf(pcg_context *ctx, int32_t id);
+/* The BreakingDam refinement criterion of every listed patch
+ * (BreakingDamSWEScenario::computeDemandedMeshWidth,
+ * native/scenarios/BreakingDam.cpp:85-139): out[k] = max over interior
+ * forward differences of |grad h| on uNew.  The scenario refines where it
+ * exceeds 0.1 and coarsens where it is below. */
+int pcg_refinement_indicator(pcg_context *ctx, int32_t n, const int32_t *ids, double *out);
+
 /* ------------------------------------------------------ batched grid step */
 
 /* Install the precomputed face-pair list used by every following grid step

@@ -71,6 +71,7 @@ def lib():
         L.pco_interpolate.argtypes = [I2, I2, P, P, C.c_int, C.c_int, C.c_int, C.c_int]
         L.pco_restrict.argtypes = [P, P, C.c_int, C.c_int]
         L.pco_swe_post_process_restriction.argtypes = [P]
+        L.pco_switch_to_leaf.argtypes = [P]
         L.pco_compute_fluxes.argtypes = [P, C.c_double]
         L.pco_apply_flux_correction.argtypes = [P, P, C.c_int, C.c_int]
         L.pco_region_map_to_patch.argtypes = [I2, I2, P, P, C.c_double, I2, I2]

@@ -577,6 +577,28 @@ double pco_overlap_area(const double p1[2], const double s1[2],
   return region;
 }
 
+/* Patch::switchToLeaf (src/peanoclaw/Patch.cpp:793-816): the reference maps
+ * the virtual patch's interval to [0, 1] (time = 0, timestepSize = 1) and
+ * re-evaluates uOld / uNew of the interior at the patch's own time and
+ * time + dt (switchRegionToMinimalFineGridTimeInterval, :55-76). */
+void pco_switch_to_leaf(pco_patch *p) {
+  p->is_virtual = 0;
+  p->is_leaf = 1;
+  const double time = 0.0, timestep = 1.0;
+  double fo = 1.0, fn = 1.0;
+  if (!tl_equals(timestep, 0.0)) {
+    fo = (p->time - time) / timestep;
+    fn = (p->time + p->dt - time) / timestep;
+  }
+  for (int x = 0; x < p->nx; x++)
+    for (int y = 0; y < p->ny; y++)
+      for (int q = 0; q < p->nq; q++) {
+        double vo = UOLD(p, q, x, y), vn = UNEW(p, q, x, y);
+        UOLD(p, q, x, y) = vo * (1.0 - fo) + vn * fo;
+        UNEW(p, q, x, y) = vo * (1.0 - fn) + vn * fn;
+      }
+}
+
 /* ------------------------------------------------------------------------ */
 /* DefaultRestrictionTemplate::restrictRegion / restrictSolution             */
 /* (src/peanoclaw/interSubgridCommunication/DefaultRestriction.cpph:17-150), */

@@ -113,6 +113,11 @@ void pco_interpolate(const int dst_size[2], const int dst_off[2],
 void pco_restrict(const pco_patch *src, pco_patch *dst, int only_overlapped,
                   int swe_absolute_height);
 void pco_swe_post_process_restriction(pco_patch *dst);
+/* Patch::switchToLeaf data conversion (src/peanoclaw/Patch.cpp:793-816 with
+ * switchRegionToMinimalFineGridTimeInterval, :55-76): a virtual patch holds
+ * its restricted values at the times 0 and 1; the interior is re-evaluated at
+ * the patch's time (uOld) and time + dt (uNew); the patch becomes a leaf. */
+void pco_switch_to_leaf(pco_patch *p);
 void pco_compute_fluxes(pco_patch *p, double g_flux);
 void pco_apply_flux_correction(const pco_patch *src, pco_patch *dst, int dim, int dir);
 

@@ -1047,6 +1047,63 @@ int pcg_post_process_restriction(pcg_context *c, int32_t dst) {
   return PCG_OK;
 }
 
+int pcg_clear_subgrid(pcg_context *c, int32_t id) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  std::lock_guard<std::mutex> lk(c->mu);
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  int *ids = nullptr;
+  size_t cap = 0;
+  rc = ensure_device(c, &ids, &cap, 1);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(ids, &id, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(pcg::launch_clear_interior(c->stream, c->slab, c->d_patches, ids, 1));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  PCG_CUDA(cudaFree(ids));
+  return PCG_OK;
+}
+
+int pcg_switch_to_leaf(pcg_context *c, int32_t id) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  pcg::PatchDev &P = c->h_patches[id];
+  P.flags = (P.flags & ~pcg::kFlagVirtual) | pcg::kFlagLeaf;
+  c->patches_dirty = true;
+  c->topo_dirty = true;
+  c->graph_valid = false;
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_switch_to_leaf(c->stream, c->slab, c->d_patches, c->d_times, id));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+int pcg_refinement_indicator(pcg_context *c, int32_t n, const int32_t *ids, double *out) {
+  if (!c || n < 0 || (n > 0 && (!ids || !out))) return fail(PCG_E_INVALID, "bad arguments");
+  for (int32_t k = 0; k < n; k++) {
+    if (!valid_id(c, ids[k])) return fail(PCG_E_INVALID, "unknown patch id " + std::to_string(ids[k]));
+    if (c->h_patches[ids[k]].nq < 1) return fail(PCG_E_INVALID, "patch without unknowns");
+  }
+  if (n == 0) return PCG_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  int *d_ids = nullptr;
+  double *d_out = nullptr;
+  PCG_CUDA(cudaMalloc(&d_ids, sizeof(int) * n));
+  cudaError_t e = cudaMalloc(&d_out, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_ids, ids, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = pcg::launch_refinement_indicator(c->stream, c->slab, c->d_patches, d_ids, n, d_out);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_ids);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return fail(PCG_E_CUDA, std::string("pcg_refinement_indicator: ") + cudaGetErrorString(e));
+  return PCG_OK;
+}
+
 int pcg_compute_fluxes(pcg_context *c, int32_t id, double g_flux) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   if (c->h_patches[id].nq != 3 || c->h_patches[id].g < 1)

@@ -998,6 +998,62 @@ __global__ void k_clear_interior(double *slab, const PatchDev *patches, const in
   }
 }
 
+// Patch::switchToLeaf data conversion (Patch.cpp:793-816 with
+// switchRegionToMinimalFineGridTimeInterval, :55-76): the restricted values of
+// a virtual patch stand for the times 0 and 1; the interior is re-evaluated
+// at the patch's time (uOld) and time + dt (uNew).  One CTA.
+__global__ void k_switch_to_leaf(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                                 const PatchTimeDev *__restrict__ times, int pid) {
+  const PatchDev P = patches[pid];
+  const PatchTimeDev T = times[pid];
+  const double time = 0.0, timestep = 1.0;
+  double fo = 1.0, fn = 1.0;
+  if (!tl_equals(timestep, 0.0)) {
+    fo = __ddiv_rn(__dsub_rn(T.time, time), timestep);
+    fn = __ddiv_rn(__dsub_rn(__dadd_rn(T.time, T.dt), time), timestep);
+  }
+  const double ofo = __dsub_rn(1.0, fo), ofn = __dsub_rn(1.0, fn);
+  for (int k = threadIdx.x; k < P.nx * P.ny * P.nq; k += blockDim.x) {
+    const int q = k / (P.nx * P.ny), c = k - q * (P.nx * P.ny), x = c / P.ny, y = c - x * P.ny;
+    const long long io = idx_uold(P, q, x, y), in = idx_unew(P, q, x, y);
+    const double vo = slab[io], vn = slab[in];
+    slab[io] = __dadd_rn(__dmul_rn(vo, ofo), __dmul_rn(vn, fo));
+    slab[in] = __dadd_rn(__dmul_rn(vo, ofn), __dmul_rn(vn, fn));
+  }
+}
+
+// BreakingDam refinement criterion (BreakingDamSWEScenario::computeDemandedMeshWidth,
+// native/scenarios/BreakingDam.cpp:85-139): max over xi < nx-1, yi < ny-1 of
+// sqrt(|gx| |gx| + |gy| |gy|), gx = (h[xi+1][yi] - h[xi][yi]) / dx,
+// gy = (h[xi][yi+1] - h[xi][yi]) / dy on uNew; fmax keeps the non-NaN operand.
+// One CTA per listed patch.
+__global__ void k_refinement_indicator(const double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                                       const int *__restrict__ ids, int count, double *__restrict__ out) {
+  if ((int)blockIdx.x >= count) return;
+  const PatchDev P = patches[ids[blockIdx.x]];
+  const double dx = subcell(P, 0), dy = subcell(P, 1);
+  const int mx = P.nx - 1, my = P.ny - 1;
+  double m = 0.0;
+  for (int k = threadIdx.x; k < mx * my; k += blockDim.x) {
+    const int xi = k / my, yi = k - xi * my;
+    const double q0 = slab[idx_unew(P, 0, xi, yi)];
+    const double gx = ieee::div_rn(__dsub_rn(slab[idx_unew(P, 0, xi + 1, yi)], q0), dx);
+    const double gy = ieee::div_rn(__dsub_rn(slab[idx_unew(P, 0, xi, yi + 1)], q0), dy);
+    const double ax = fabs(gx), ay = fabs(gy);
+    m = fmax_nonneg(m, ieee::sqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay))));
+  }
+  __shared__ unsigned long long red[32];
+  // values are >= 0 or NaN; fmax_nonneg ignores NaN, so reduce with it
+  for (int o = 16; o > 0; o >>= 1) m = fmax_nonneg(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dbits(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = fmax_nonneg(r, bitsd(red[w]));
+    out[blockIdx.x] = r;
+  }
+}
+
 // ===========================================================================
 // Host-side launchers
 // ===========================================================================
@@ -1195,6 +1251,19 @@ cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *pat
                               int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
   k_flux_items<<<n_dst, 32, 0, st>>>(slab, patches, times, items, begin, group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_switch_to_leaf(cudaStream_t st, double *slab, const PatchDev *patches,
+                                  const PatchTimeDev *times, int pid) {
+  k_switch_to_leaf<<<1, 256, 0, st>>>(slab, patches, times, pid);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refinement_indicator(cudaStream_t st, const double *slab, const PatchDev *patches,
+                                        const int *ids, int count, double *out) {
+  if (count <= 0) return cudaSuccess;
+  k_refinement_indicator<<<count, 256, 0, st>>>(slab, patches, ids, count, out);
   return cudaGetLastError();
 }
 

@@ -109,6 +109,9 @@ SIGNATURES = {
     "pcg_set_restriction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, C.c_int32]),
     "pcg_set_flux_correction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, _I2, _I2, C.c_double]),
     "pcg_restrict_all": (C.c_int, [_CTX]),
+    "pcg_clear_subgrid": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_switch_to_leaf": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_refinement_indicator": (C.c_int, [_CTX, C.c_int32, _I2, _D]),
     "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
@@ -297,6 +300,20 @@ class Context:
 
     def set_group_max_dt(self, group, max_dt):
         check(lib().pcg_set_group_max_dt(self.h, group, float(max_dt)))
+
+    def clear_subgrid(self, pid):
+        check(lib().pcg_clear_subgrid(self.h, int(pid)))
+
+    def switch_to_leaf(self, pid):
+        check(lib().pcg_switch_to_leaf(self.h, int(pid)))
+
+    def refinement_indicator(self, ids):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        out = np.zeros(len(ids))
+        if len(ids):
+            check(lib().pcg_refinement_indicator(self.h, len(ids), ids.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                 dptr(out)))
+        return out
 
     def set_group_end_time(self, group, time, t_end):
         """Device-side end time of a group (see pcg_set_group_end_time)."""

@@ -265,42 +265,29 @@ def breaking_dam_amr(base=9, n=27, levels=3, buffers=(1, 2), x_dam=0.5, h_left=1
         gy = (h[:-1, 1:] - h[:-1, :-1]) / dx
         return float(np.max(np.sqrt(np.abs(gx) * np.abs(gx) + np.abs(gy) * np.abs(gy)))) > threshold
 
-    exists = [set() for _ in range(levels)]
-    refined = [set() for _ in range(levels)]
-    exists[0] = {(i, j) for i in range(base) for j in range(base)}
-    for l in range(levels - 1):
-        flag = {s for s in exists[l] if needs_refine(l, *s)}
-        buf = buffers[l] if l < len(buffers) else 1
-        grown = set()
-        for (i, j) in flag:
-            for di in range(-buf, buf + 1):
-                for dj in range(-buf, buf + 1):
-                    if (i + di, j + dj) in exists[l]:
-                        grown.add((i + di, j + dj))
-        refined[l] = grown
-        exists[l + 1] = {(3 * i + a, 3 * j + c) for (i, j) in grown for a in range(3) for c in range(3)}
+    from .amr import AmrGrid
+    grid = AmrGrid(base, n, levels, buffers=buffers, threshold=threshold)
+    grid.refine_from(needs_refine)
+    ps = amr_patchset(grid, h_of, b_of)
+    ps.grid = grid
+    ps.h_of, ps.b_of = h_of, b_of
+    return ps
 
+
+def amr_patchset(grid, h_of, b_of):
+    """PatchSet of an AmrGrid: patch order, geometry, leaf flags, walls, the
+    ghost / flux / restriction lists and the restriction bounds; leaves get
+    h = h_of(x) (at rest), every patch b = b_of(x, y) including its ghost ring."""
+    lay = grid.layout()
+    n = grid.n
     ps = PatchSet()
-    ps.leaf = []
-    index = {}
-    for l in range(levels):
-        m = base * 3 ** l
-        L = 1.0 / m
-        for (i, j) in sorted(exists[l]):
-            index[(l, i, j)] = len(ps.n)
-            ps.n.append(n)
-            ps.pos.append((i * L, j * L))
-            ps.size.append((L, L))
-            ps.level.append(l)
-            is_leaf = (i, j) not in refined[l]
-            ps.leaf.append(is_leaf)
-            w = 0
-            if is_leaf:
-                if i == 0: w |= 1
-                if i == m - 1: w |= 2
-                if j == 0: w |= 4
-                if j == m - 1: w |= 8
-            ps.wall.append(w)
+    ps.leaf = list(lay["leaf"])
+    for k in range(len(lay["order"])):
+        ps.n.append(n)
+        ps.pos.append(lay["pos"][k])
+        ps.size.append(lay["size"][k])
+        ps.level.append(lay["level"][k])
+        ps.wall.append(lay["wall"][k])
     ps.finalize_layout()
     for p in range(len(ps)):
         unew, uold, b = ps.views(p)
@@ -308,84 +295,13 @@ def breaking_dam_amr(base=9, n=27, levels=3, buffers=(1, 2), x_dam=0.5, h_left=1
         b[:] = b_of(X, Y)
         if ps.leaf[p]:
             unew[0] = h_of(X[1:-1, 1:-1])
-
-    def owner(l, i, j):
-        """Patch covering slot (l, i, j): the level-l patch or its coarse leaf."""
-        while l >= 0:
-            if (l, i, j) in index:
-                return index[(l, i, j)], l
-            i, j, l = i // 3, j // 3, l - 1
-        return None, None
-
-    rows = []
-    flux = []
-    for l in range(levels):
-        m = base * 3 ** l
-        for (i, j) in sorted(exists[l]):
-            d = index[(l, i, j)]
-            if not ps.leaf[d]:
-                continue
-            for dx, dy in ((-1, 0), (1, 0), (0, -1), (0, 1), (-1, -1), (1, -1), (-1, 1), (1, 1)):
-                tx, ty = i + dx, j + dy
-                if not (0 <= tx < m and 0 <= ty < m):
-                    continue
-                s, ls = owner(l, tx, ty)
-                dirv = (-dx, -dy)
-                size = [n if v == 0 else 1 for v in dirv]
-                dst_off = [0 if v == 0 else (-1 if v == 1 else n) for v in dirv]
-                if ls == l:
-                    src_off = [0 if v == 0 else (n - 1 if v == 1 else 0) for v in dirv]
-                    rows.append([PCG_GHOST_COPY, s, d] + size + src_off + dst_off)
-                else:
-                    rows.append([PCG_GHOST_INTERP, s, d] + size + [0, 0] + dst_off)
-                    if dx == 0 or dy == 0:
-                        dim = 0 if dx != 0 else 1
-                        flux.append([d, s, dim, dx if dx != 0 else dy])
-    ps.items = np.array(rows, dtype=np.int32).reshape(-1, 9)
-    ps.flux_items = np.array(flux, dtype=np.int32).reshape(-1, 4)
-
-    # neighbouring ghost-layer bounds of the virtual patches
-    # (GhostLayerCompositor::updateLower/UpperGhostlayerBound, same-level leaf faces)
-    big = np.finfo(np.float64).max
-    ps.restr_lower = [[big, big] for _ in range(len(ps))]
-    ps.restr_upper = [[-big, -big] for _ in range(len(ps))]
-    for (l, i, j), v in index.items():
-        if ps.leaf[v]:
-            continue
-        for dim in (0, 1):
-            for step in (-1, 1):
-                key = (l, i + step, j) if dim == 0 else (l, i, j + step)
-                if key not in index or not ps.leaf[index[key]]:
-                    continue
-                nb = index[key]
-                sub = ps.size[nb][dim] / n
-                if step < 0:
-                    ps.restr_upper[v][dim] = max(ps.restr_upper[v][dim],
-                                                 ps.pos[nb][dim] + ps.size[nb][dim] + sub)
-                else:
-                    ps.restr_lower[v][dim] = min(ps.restr_lower[v][dim], ps.pos[nb][dim] - sub)
-
-    # leaves restrict into every virtual ancestor whose neighbours' ghost layers
-    # they overlap (GridLevelTransfer::restrictToOverlappingVirtualSubgrids)
-    rest = []
-    for (l, i, j), v in sorted(index.items(), key=lambda kv: kv[1]):
-        if ps.leaf[v]:
-            continue
-        for (l2, i2, j2), s in sorted(index.items(), key=lambda kv: kv[1]):
-            if l2 <= l or not ps.leaf[s]:
-                continue
-            f = 3 ** (l2 - l)
-            if i2 // f != i or j2 // f != j:
-                continue
-            pos, size = ps.pos[s], ps.size[s]
-            lo, up = ps.restr_lower[v], ps.restr_upper[v]
-            overlapped = any(up[d] - pos[d] > 1e-8 for d in (0, 1)) or \
-                any(pos[d] + size[d] - lo[d] > 1e-8 for d in (0, 1))
-            if overlapped:
-                rest.append([s, v])
-    ps.restrict_items = np.array(rest, dtype=np.int32).reshape(-1, 2)
-    ps.meta = {"workload": "adaptive breaking dam, %d levels, %d patches (%d leaves) of %dx%d cells"
-                           % (levels, len(ps), sum(ps.leaf), n, n),
+    ps.items = lay["items"]
+    ps.flux_items = lay["flux_items"]
+    ps.restrict_items = lay["restrict_items"]
+    ps.restr_lower = lay["restr_lower"]
+    ps.restr_upper = lay["restr_upper"]
+    ps.meta = {"workload": "adaptive grid, %d levels, %d patches (%d leaves) of %dx%d cells"
+                           % (grid.levels, len(ps), sum(ps.leaf), n, n),
                "leaf_cells": int(sum(n * n for p in range(len(ps)) if ps.leaf[p]))}
     return ps
 

@@ -119,3 +119,136 @@ def oracle_amr_step(pats, ps, prm, max_dt, g_flux=1.0, flux=True):
 def gpu_amr_patchset(ctx, ps, flux=True, g_flux=1.0):
     from peanoclaw_gb300.scenarios import install_amr
     return install_amr(ctx, ps, flux=flux, g_flux=g_flux)
+
+
+class OracleAmr:
+    """Backend of peanoclaw_gb300.amr.remesh on oracle patches (the CPU side of
+    the remesh parity tests); mirrors DeviceAmr call for call."""
+
+    def __init__(self, grid, ps, b_of, flux=True, g_flux=1.0):
+        self.grid, self.b_of, self.flux, self.g_flux = grid, b_of, flux, g_flux
+        pats = oracle_amr_patchset(ps)
+        self.pat = dict(zip(grid.order(), pats))
+        self.lay = grid.layout()
+        self.walls = {}
+        for s, w in zip(self.lay["order"], self.lay["wall"]):
+            self.walls[s] = w
+
+    def handle(self, slot):
+        return self.pat[slot]
+
+    def forget(self, slot):
+        del self.pat[slot]
+
+    def alloc(self, slot, pos, size, level):
+        p = O.Patch(self.grid.n, pos=pos, size=size, level=level, is_leaf=True)
+        self.pat[slot] = p
+        return p
+
+    def free(self, p):
+        pass
+
+    def set_leaf(self, p, leaf, wall):
+        p.s.is_leaf, p.s.is_virtual = int(leaf), int(not leaf)
+        p.wall = wall
+
+    def times(self, p):
+        return p.s.time, p.s.dt, p.s.est_next
+
+    def set_times(self, p, time, dt, est):
+        big = np.finfo(np.float64).max
+        p.s.time, p.s.dt, p.s.est_next = time, dt, est
+        p.s.min_neighbor_time = p.s.max_neighbor_dt = 0.0
+        p.s.restr_lower[0] = p.s.restr_lower[1] = big
+        p.s.restr_upper[0] = p.s.restr_upper[1] = -big
+
+    def set_b(self, p, b):
+        p.u[:] = 0.0
+        p.param_w()[0] = b
+
+    def interpolate_child(self, parent, child):
+        n = self.grid.n
+        for to_uold, current in ((0, 0), (1, 1)):
+            O.interpolate((n, n), (0, 0), parent, child, to_uold=bool(to_uold),
+                          to_current_time=bool(current), use_time_unew_or_uold=False, swe=True)
+
+    def coarsen(self, parent, children):
+        parent.unew()[:] = 0.0
+        g = parent.s.ghost
+        parent.uold()[:, g:-g, g:-g] = 0.0
+        for k in children:
+            O.restrict(k, parent, only_overlapped=False, swe=True)
+        O.lib().pco_swe_post_process_restriction(parent.ptr())
+
+    def switch_to_leaf(self, p):
+        O.lib().pco_switch_to_leaf(p.ptr())
+
+    def restrict_all(self):
+        pats = self.patches()
+        dsts = []
+        for s, d in self.lay["restrict_items"]:
+            if d not in dsts:
+                dsts.append(int(d))
+        for d in dsts:
+            pats[d].unew()[:] = 0.0
+            g = pats[d].s.ghost
+            pats[d].uold()[:, g:-g, g:-g] = 0.0
+        for s, d in self.lay["restrict_items"]:
+            O.restrict(pats[s], pats[d], only_overlapped=True, swe=True)
+        for d in dsts:
+            O.lib().pco_swe_post_process_restriction(pats[d].ptr())
+
+    def install(self, lay, handles):
+        self.lay = lay
+        for k, p in enumerate(handles):
+            if not lay["leaf"][k]:
+                p.s.restr_lower[0], p.s.restr_lower[1] = lay["restr_lower"][k]
+                p.s.restr_upper[0], p.s.restr_upper[1] = lay["restr_upper"][k]
+
+    # -- driver
+    def patches(self):
+        return [self.pat[s] for s in self.lay["order"]]
+
+    def indicators(self):
+        out = {}
+        for s in self.grid.leaves():
+            p = self.pat[s]
+            h = p.unew()[0]
+            dx, dy = p.s.size[0] / p.s.nx, p.s.size[1] / p.s.ny
+            gx = (h[1:, :-1] - h[:-1, :-1]) / dx
+            gy = (h[:-1, 1:] - h[:-1, :-1]) / dy
+            g = np.sqrt(np.abs(gx) * np.abs(gx) + np.abs(gy) * np.abs(gy))
+            out[s] = float(np.fmax.reduce(g.ravel(), initial=0.0))
+        return out
+
+    def step(self, prm, max_dt):
+        from types import SimpleNamespace
+        lay = self.lay
+        ns = SimpleNamespace(items=lay["items"], wall=lay["wall"], flux_items=lay["flux_items"],
+                             restrict_items=lay["restrict_items"], leaf=lay["leaf"])
+        ns.__len__ = lambda: len(lay["order"])
+        pats = self.patches()
+        dt = O.grid_step(pats, ns.items, ns.wall, prm, max_dt)[0]
+        if self.flux and len(ns.flux_items):
+            for p, lf in zip(pats, ns.leaf):
+                if lf:
+                    O.lib().pco_compute_fluxes(p.ptr(), self.g_flux)
+            for s, d, dim, direction in ns.flux_items:
+                O.lib().pco_apply_flux_correction(pats[s].ptr(), pats[d].ptr(), int(dim), int(direction))
+        dsts = []
+        for s, d in ns.restrict_items:
+            if d not in dsts:
+                dsts.append(int(d))
+        for d in dsts:
+            pats[d].unew()[:] = 0.0
+            g = pats[d].s.ghost
+            pats[d].uold()[:, g:-g, g:-g] = 0.0
+        for s, d in ns.restrict_items:
+            O.restrict(pats[s], pats[d], only_overlapped=True, swe=True)
+        for d in dsts:
+            O.lib().pco_swe_post_process_restriction(pats[d].ptr())
+        return dt
+
+    def remesh(self):
+        from peanoclaw_gb300.amr import remesh
+        return remesh(self.grid, self, self.indicators(), self.b_of)

@@ -1,0 +1,80 @@
+"""Dynamic remeshing (AmrGrid.decide + remesh) on the oracle: the hierarchy
+follows a moving breaking-dam front (refines ahead of it, coarsens behind
+it) and keeps the invariants of the patch lists; refining and coarsening a
+lake at rest keeps it at rest up to round-off (the d-linear interpolation
+weights and the 1/9 area weights of the restriction are not exact in binary,
+and the steps on the refined grid move those ulps around)."""
+import copy
+
+import numpy as np
+
+from helpers import OracleAmr, oracle_params
+from peanoclaw_gb300 import pcg as P
+from peanoclaw_gb300 import scenarios as S
+from peanoclaw_gb300.amr import AmrGrid
+
+PRM = P.swe_params(g=9.81, cfl=0.5)
+
+
+def _check_lists(grid):
+    lay = grid.layout()
+    idx = lay["index"]
+    for (l, i, j) in lay["order"]:
+        if (i, j) in grid.refined[l]:
+            for a in range(3):
+                for c in range(3):
+                    assert (l + 1, 3 * i + a, 3 * j + c) in idx
+        if l > 0:
+            assert (i // 3, j // 3) in grid.refined[l - 1]
+    leaf = lay["leaf"]
+    for row in lay["items"]:
+        assert leaf[row[2]]          # ghost fill writes leaves only
+    for s, d in lay["restrict_items"]:
+        assert leaf[s] and not leaf[d]
+    # leaves cover the domain exactly once
+    area = sum(lay["size"][k][0] * lay["size"][k][1] for k in range(len(leaf)) if leaf[k])
+    assert abs(area - 1.0) < 1e-12
+
+
+def test_remesh_follows_a_moving_front():
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0)
+    grid = ps.grid
+    _check_lists(grid)
+    b_of = ps.b_of
+    be = OracleAmr(grid, ps, b_of)
+    prm = oracle_params(PRM)
+    history = []
+    for r in range(10):
+        for _ in range(4):
+            be.step(prm, 1e9)
+        history.append(be.remesh())
+        _check_lists(grid)
+        assert set(be.pat) == set(grid.order())
+    refined = sum(h[0] for h in history)
+    coarsened = sum(h[1] for h in history)
+    assert refined > 0 and coarsened > 0
+    for p in be.patches():
+        assert np.all(np.isfinite(p.u))
+
+
+def test_remesh_of_a_lake_at_rest_keeps_it_at_rest():
+    # flat surface over a bump: refinement forced everywhere the criterion of
+    # a stepped threshold says so, then everything coarsens again
+    ps = S.breaking_dam_amr(base=3, n=9, levels=2, h_left=1.0, h_right=1.0,
+                            bump=(0.0, 0.05, 0.7, 0.5))
+    grid = ps.grid
+    b_of = ps.b_of
+    be = OracleAmr(grid, ps, b_of)
+    g_all = {s: 1.0 for s in grid.leaves()}   # every leaf asks to refine
+    from peanoclaw_gb300.amr import remesh
+    remesh(grid, be, g_all, b_of)
+    assert len(grid.exists[1]) == 9 * 9
+    prm = oracle_params(PRM)
+    for _ in range(3):
+        be.step(prm, 1e9)
+    g_none = {s: 0.0 for s in grid.leaves()}
+    remesh(grid, be, g_none, b_of)
+    assert len(grid.exists[1]) == 0
+    for p in be.patches():
+        assert np.max(np.abs(p.unew()[0] - 1.0)) <= 1e-14
+        assert np.max(np.abs(p.unew()[1:])) <= 1e-14

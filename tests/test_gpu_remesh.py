@@ -1,0 +1,67 @@
+"""Dynamic remeshing on the GPU (device refinement criterion, new patches by
+interpolation from the coarse patch, coarsening by full restriction and
+switchToLeaf, lists rebuilt) against the same remesh on the oracle: the
+criterion values, the dts, the hierarchy and every patch vector agree bit for
+bit while the grid follows a moving breaking-dam front."""
+import copy
+
+import numpy as np
+import pytest
+
+from helpers import OracleAmr, oracle_params
+from peanoclaw_gb300 import pcg as P
+from peanoclaw_gb300 import scenarios as S
+from peanoclaw_gb300.amr import DeviceAmr
+
+pytestmark = pytest.mark.gpu
+
+PRM = P.swe_params(g=9.81, cfl=0.5)
+
+
+@pytest.mark.parametrize("mode", [P.PCG_MODE_BATCHED, P.PCG_MODE_PLAIN])
+def test_remesh_matches_the_oracle(mode):
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0)
+    ctx = P.Context(slab_doubles=8_000_000, max_patches=1024, max_groups=1, params=PRM)
+    try:
+        ids = S.install_amr(ctx, ps)
+        ctx.restrict_all()
+        ctx.set_group_max_dt(0, 1e9)
+        dev = DeviceAmr(ctx, ps.grid, ps.b_of)
+        dev.pid = dict(zip(ps.grid.order(), (int(i) for i in ids)))
+        ora = OracleAmr(copy.deepcopy(ps.grid), ps, ps.b_of)
+        ora.restrict_all()
+        prm = oracle_params(PRM)
+        changes = []
+        for r in range(8):
+            hist = ctx.run(4, mode)[:, 0]
+            odts = [ora.step(prm, 1e9) for _ in range(4)]
+            assert list(hist) == odts
+            gd, go = dev.indicators(), ora.indicators()
+            assert gd.keys() == go.keys()
+            assert all(np.float64(gd[k]).view(np.int64) == np.float64(go[k]).view(np.int64) for k in gd)
+            cd = dev.remesh()
+            co = ora.remesh()
+            assert cd == co
+            changes.append(cd)
+            assert dev.grid.order() == ora.grid.order()
+        assert sum(c[0] for c in changes) > 0
+        # forced rounds: every leaf below the threshold (everything that can
+        # coarsen does), steps, then every leaf above it (refine everywhere)
+        from peanoclaw_gb300.amr import remesh
+        for val in (0.0, 1e9):
+            cd = remesh(dev.grid, dev, {s: val for s in dev.grid.leaves()}, ps.b_of)
+            co = remesh(ora.grid, ora, {s: val for s in ora.grid.leaves()}, ps.b_of)
+            assert cd == co and cd[1 if val == 0.0 else 0] > 0
+            hist = ctx.run(3, mode)[:, 0]
+            assert list(hist) == [ora.step(prm, 1e9) for _ in range(3)]
+        hist = ctx.run(3, mode)[:, 0]
+        assert list(hist) == [ora.step(prm, 1e9) for _ in range(3)]
+        order = dev.grid.order()
+        for s in order:
+            p = ora.pat[s]
+            got = ctx.download(dev.pid[s], p.u.size)
+            assert np.array_equal(got.view(np.int64), p.u.view(np.int64)), s
+            t = ctx.get_time(dev.pid[s])
+            assert (t["time"], t["dt"]) == (p.s.time, p.s.dt)
+    finally:
+        ctx.close()
