@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the secondary configurations (dam break, AMR, serving)")
     ap.add_argument("--amr-steps", type=int, default=100)
+    ap.add_argument("--remesh-steps", type=int, default=100)
+    ap.add_argument("--remesh-every", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=8.0)
     ap.add_argument("--serve-batch", type=int, default=8,
@@ -255,6 +257,53 @@ def bench_amr(prm, steps):
     return res
 
 
+def bench_remesh(prm, steps, every):
+    """Adaptive tsunami with dynamic remeshing: 3 levels of 3x refinement,
+    27 x 27 cells per patch, base 27 x 27 patches (6561^2 when fully refined),
+    Gaussian hump over a flat seafloor ramping up to a coastline; the device
+    refinement criterion is evaluated and the grid remeshed every `every`
+    steps (new patches interpolated, coarsened ones restricted, lists
+    rebuilt)."""
+    from peanoclaw_gb300 import pcg as P
+    from peanoclaw_gb300 import scenarios as S
+    from peanoclaw_gb300.amr import DeviceAmr
+    ps = S.adaptive_tsunami()
+    full = 729 + 6561 + 59049
+    ctx = P.Context(slab_doubles=int(full * (P.vector_size(27) + 32)) + (1 << 20), max_patches=full + 64,
+                    max_groups=1, params=prm)
+    try:
+        ids = S.install_amr(ctx, ps)
+        ctx.restrict_all()
+        ctx.set_group_max_dt(0, 1e9)
+        dev = DeviceAmr(ctx, ps.grid, ps.b_of)
+        dev.pid = dict(zip(ps.grid.order(), (int(i) for i in ids)))
+        ctx.run(2, P.PCG_MODE_BATCHED)
+        ctx.synchronize()
+        cu = 0
+        leaf_cells, patches, remesh_s = [], [], []
+        _, ms0 = ctx.stats()
+        t0 = time.perf_counter()
+        for r in range(max(1, steps // every)):
+            lc = sum(ps.grid.n ** 2 for _ in ps.grid.leaves())
+            leaf_cells.append(lc)
+            patches.append(len(dev.pid))
+            ctx.run(every, P.PCG_MODE_BATCHED)
+            cu += lc * every
+            t1 = time.perf_counter()
+            dev.remesh()
+            remesh_s.append(time.perf_counter() - t1)
+        ctx.synchronize()
+        wall = time.perf_counter() - t0
+        _, ms1 = ctx.stats()
+    finally:
+        ctx.close()
+    dev_s = (ms1 - ms0) / 1e3
+    return {"steps": steps, "remesh_every": every, "patches_min": min(patches), "patches_max": max(patches),
+            "leaf_cells_min": min(leaf_cells), "leaf_cells_max": max(leaf_cells),
+            "device_cell_updates_per_s": cu / dev_s, "wall_cell_updates_per_s": cu / wall,
+            "remesh_s_mean": float(np.mean(remesh_s)), "wall_s": wall}
+
+
 def bench_serving(args, prm):
     """Scenario stream with Poisson arrivals (seed 42): radial dam breaks and
     Gaussian-hump tsunamis, 1e4..4e6 cells, end time U[0.05, 0.5]."""
@@ -408,6 +457,7 @@ def main():
     if rank == 0 and not args.no_configs:
         configs = {"radial_dam_break_9x9x16": bench_radial(prm),
                    "adaptive_breaking_dam_3_levels": bench_amr(prm, args.amr_steps),
+                   "adaptive_tsunami_remesh": bench_remesh(prm, args.remesh_steps, args.remesh_every),
                    "serving_stream": bench_serving(args, prm)}
 
     if rank == 0:

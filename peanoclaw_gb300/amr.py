@@ -180,21 +180,21 @@ class AmrGrid:
                         upper[v][dim] = max(upper[v][dim], pos[nb][dim] + size[nb][dim] + sub)
                     else:
                         lower[v][dim] = min(lower[v][dim], pos[nb][dim] - sub)
+        # every leaf against its virtual ancestors; list order: virtual patch
+        # index, then leaf index
         rest = []
-        for (l, i, j), v in sorted(index.items(), key=lambda kv: kv[1]):
-            if leaf[v]:
+        for (l2, i2, j2), s in index.items():
+            if not leaf[s]:
                 continue
-            for (l2, i2, j2), s in sorted(index.items(), key=lambda kv: kv[1]):
-                if l2 <= l or not leaf[s]:
-                    continue
+            for l in range(l2 - 1, -1, -1):
                 f = 3 ** (l2 - l)
-                if i2 // f != i or j2 // f != j:
-                    continue
+                v = index[(l, i2 // f, j2 // f)]
                 lo, up = lower[v], upper[v]
                 overlapped = any(up[d] - pos[s][d] > 1e-8 for d in (0, 1)) or \
                     any(pos[s][d] + size[s][d] - lo[d] > 1e-8 for d in (0, 1))
                 if overlapped:
                     rest.append([s, v])
+        rest.sort(key=lambda sv: (sv[1], sv[0]))
         return {"order": order, "index": index, "pos": pos, "size": size, "leaf": leaf,
                 "level": [s[0] for s in order], "wall": [self.wall(*s) for s in order],
                 "items": np.array(rows, dtype=np.int32).reshape(-1, 9),
@@ -248,10 +248,12 @@ def remesh(grid, backend, g, b_of):
                 backend.free(h)
                 backend.forget(k)
             n_crs += 1
+    old_state = {s: (grid.is_leaf(*s), grid.wall(*s)) for s in grid.order()}
     grid.exists, grid.refined = exists, refined
     lay = grid.layout()
     for s, leaf, w in zip(lay["order"], lay["leaf"], lay["wall"]):
-        backend.set_leaf(backend.handle(s), leaf, w)
+        if old_state.get(s) != (leaf, w) or s not in old_state:
+            backend.set_leaf(backend.handle(s), leaf, w)
     backend.install(lay, [backend.handle(s) for s in lay["order"]])
     # virtual patches (new ones included) receive the restriction of the
     # current leaves before the next ghost fill reads them
@@ -266,6 +268,8 @@ class DeviceAmr:
         self.ctx, self.grid, self.b_of = ctx, grid, b_of
         self.flux, self.g_flux = flux, g_flux
         self.pid = {}
+        self._bounds = {}   # restriction bounds last written per virtual patch
+        self.timing = {}
 
     # -- remesh protocol
     def handle(self, slot):
@@ -323,11 +327,17 @@ class DeviceAmr:
 
     def install(self, lay, handles):
         ids = np.asarray(handles, dtype=np.int32)
+        bounds = {}
         for k, pid in enumerate(ids):
             if not lay["leaf"][k]:
+                b = (tuple(lay["restr_lower"][k]), tuple(lay["restr_upper"][k]))
+                bounds[int(pid)] = b
+                if self._bounds.get(int(pid)) == b:
+                    continue
                 t = self.ctx.get_time(int(pid))
                 self.ctx.set_time(int(pid), time=t["time"], dt=t["dt"], est_next=t["est_next"],
-                                  restr_lower=lay["restr_lower"][k], restr_upper=lay["restr_upper"][k])
+                                  restr_lower=b[0], restr_upper=b[1])
+        self._bounds = bounds
         from .scenarios import remap_items
         self.ctx.set_ghost_items(remap_items(lay["items"], ids))
         r = lay["restrict_items"]
@@ -345,4 +355,12 @@ class DeviceAmr:
         return dict(zip(leaves, vals))
 
     def remesh(self):
-        return remesh(self.grid, self, self.indicators(), self.b_of)
+        import time
+        t0 = time.perf_counter()
+        g = self.indicators()
+        t1 = time.perf_counter()
+        r = remesh(self.grid, self, g, self.b_of)
+        self.ctx.synchronize()
+        t2 = time.perf_counter()
+        self.timing = {"indicators_s": t1 - t0, "remesh_s": t2 - t1}
+        return r

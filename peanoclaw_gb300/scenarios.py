@@ -249,7 +249,7 @@ def breaking_dam_amr(base=9, n=27, levels=3, buffers=(1, 2), x_dam=0.5, h_left=1
     `flux_items` ((N,4) src, dst, dim, dir)."""
     a_b, s_b, cx_b, cy_b = bump
 
-    def h_of(X):
+    def h_of(X, Y=None):
         return np.where(X < x_dam, h_left, h_right)
 
     def b_of(X, Y):
@@ -277,7 +277,7 @@ def breaking_dam_amr(base=9, n=27, levels=3, buffers=(1, 2), x_dam=0.5, h_left=1
 def amr_patchset(grid, h_of, b_of):
     """PatchSet of an AmrGrid: patch order, geometry, leaf flags, walls, the
     ghost / flux / restriction lists and the restriction bounds; leaves get
-    h = h_of(x) (at rest), every patch b = b_of(x, y) including its ghost ring."""
+    h = h_of(x, y) (at rest), every patch b = b_of(x, y) including its ghost ring."""
     lay = grid.layout()
     n = grid.n
     ps = PatchSet()
@@ -294,7 +294,7 @@ def amr_patchset(grid, h_of, b_of):
         X, Y = _centers(ps.pos[p], ps.size[p], n, ghost=True)
         b[:] = b_of(X, Y)
         if ps.leaf[p]:
-            unew[0] = h_of(X[1:-1, 1:-1])
+            unew[0] = h_of(X[1:-1, 1:-1], Y[1:-1, 1:-1])
     ps.items = lay["items"]
     ps.flux_items = lay["flux_items"]
     ps.restrict_items = lay["restrict_items"]
@@ -329,3 +329,41 @@ def install_amr(ctx, ps, flux=True, g_flux=1.0):
         f = ps.flux_items
         ctx.set_flux_correction_items(ids[f[:, 0]], ids[f[:, 1]], f[:, 2], f[:, 3], g_flux)
     return ids
+
+
+def adaptive_tsunami(base=27, n=27, levels=3, hump=(0.5, 0.02, 0.4, 0.5), coast=(0.9, 0.95),
+                     threshold=0.1, buffers=(1, 2)):
+    """Gaussian surface hump over a flat seafloor that ramps up to a coastline:
+    b = 0 for x < coast[0], rising linearly to the still-water surface (1.0)
+    at x = coast[1] and above it beyond (dry land).  h = max(0, 1 + A exp(-r^2 /
+    (2 s^2)) - b) with hump = (A, s, cx, cy), at rest.  The hierarchy is
+    refined where the BreakingDam criterion of the initial state exceeds
+    `threshold` (levels of 3x refinement, n x n cells per patch; base = 27,
+    n = 27, levels = 3 is a 6561^2 grid when fully refined)."""
+    from .amr import AmrGrid
+    A, s, cx, cy = hump
+    x0, x1 = coast
+
+    def b_of(X, Y):
+        return np.where(X < x0, 0.0, (X - x0) * (1.0 / (x1 - x0)))
+
+    def h_of(X, Y):
+        eta = 1.0 + A * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2.0 * s * s))
+        return np.maximum(0.0, eta - b_of(X, Y))
+
+    def needs_refine(level, i, j):
+        m = base * 3 ** level
+        L = 1.0 / m
+        X, Y = _centers((i * L, j * L), (L, L), n, ghost=False)
+        h = h_of(X, Y)
+        dx = L / n
+        gx = (h[1:, :-1] - h[:-1, :-1]) / dx
+        gy = (h[:-1, 1:] - h[:-1, :-1]) / dx
+        return float(np.max(np.sqrt(np.abs(gx) * np.abs(gx) + np.abs(gy) * np.abs(gy)))) > threshold
+
+    grid = AmrGrid(base, n, levels, buffers=buffers, threshold=threshold)
+    grid.refine_from(needs_refine)
+    ps = amr_patchset(grid, h_of, b_of)
+    ps.grid = grid
+    ps.h_of, ps.b_of = h_of, b_of
+    return ps
