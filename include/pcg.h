@@ -195,6 +195,17 @@ int pcg_switch_to_leaf(pcg_context *ctx, int32_t id);
  * exceeds 0.1 and coarsens where it is below. */
 int pcg_refinement_indicator(pcg_context *ctx, int32_t n, const int32_t *ids, double *out);
 
+/* ----------------------------------------------------------------- output */
+
+/* No counterpart in the reference (its plotters read the Peano heap on the
+ * host).  Gathers, for every listed patch back to back, uNew (nq planes) and
+ * the interior of the parameters with ghost layer (np_w planes), each plane
+ * nx*ny values in the layout's x-major order, in one device pass and one copy
+ * to `out`; out_len must be sum over the patches of (nq + np_w) * nx * ny. */
+int pcg_gather_cells(pcg_context *ctx, int32_t n, const int32_t *ids, double *out, int64_t out_len);
+/* Time intervals of the listed patches in one call. */
+int pcg_patches_get_time(pcg_context *ctx, int32_t n, const int32_t *ids, pcg_patch_time *out);
+
 /* ------------------------------------------------------ batched grid step */
 
 /* Install the precomputed face-pair list used by every following grid step

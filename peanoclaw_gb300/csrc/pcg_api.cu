@@ -1063,6 +1063,64 @@ int pcg_clear_subgrid(pcg_context *c, int32_t id) {
   return PCG_OK;
 }
 
+int pcg_gather_cells(pcg_context *c, int32_t n, const int32_t *ids, double *out, int64_t out_len) {
+  if (!c || n < 0 || (n > 0 && (!ids || !out))) return fail(PCG_E_INVALID, "bad arguments");
+  std::vector<long long> off(n);
+  int64_t total = 0;
+  for (int32_t k = 0; k < n; k++) {
+    if (!valid_id(c, ids[k])) return fail(PCG_E_INVALID, "unknown patch id " + std::to_string(ids[k]));
+    const pcg::PatchDev &P = c->h_patches[ids[k]];
+    off[k] = total;
+    total += (int64_t)(P.nq + P.np_w) * P.nx * P.ny;
+  }
+  if (total != out_len) return fail(PCG_E_INVALID, "out_len must be " + std::to_string(total));
+  if (n == 0) return PCG_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  int *d_ids = nullptr;
+  long long *d_off = nullptr;
+  double *d_out = nullptr;
+  cudaError_t e = cudaMalloc(&d_ids, sizeof(int) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(long long) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(double) * total);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_ids, ids, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = pcg::launch_gather_cells(c->stream, c->slab, c->d_patches, d_ids, d_off, n, d_out);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(double) * total, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_ids);
+  cudaFree(d_off);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return fail(PCG_E_CUDA, std::string("pcg_gather_cells: ") + cudaGetErrorString(e));
+  return PCG_OK;
+}
+
+int pcg_patches_get_time(pcg_context *c, int32_t n, const int32_t *ids, pcg_patch_time *out) {
+  if (!c || n < 0 || (n > 0 && (!ids || !out))) return fail(PCG_E_INVALID, "bad arguments");
+  for (int32_t k = 0; k < n; k++)
+    if (!valid_id(c, ids[k])) return fail(PCG_E_INVALID, "unknown patch id " + std::to_string(ids[k]));
+  if (n == 0) return PCG_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  std::vector<pcg::PatchTimeDev> all(c->max_patches);
+  PCG_CUDA(cudaMemcpyAsync(all.data(), c->d_times, sizeof(pcg::PatchTimeDev) * c->max_patches,
+                           cudaMemcpyDeviceToHost, c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  for (int32_t k = 0; k < n; k++) {
+    const pcg::PatchTimeDev &T = all[ids[k]];
+    out[k].time = T.time;
+    out[k].dt = T.dt;
+    out[k].est_next = T.est_next;
+    out[k].min_neighbor_time = T.min_nb_time;
+    out[k].max_neighbor_dt = T.max_nb_dt;
+    out[k].restr_lower[0] = T.rl[0]; out[k].restr_lower[1] = T.rl[1];
+    out[k].restr_upper[0] = T.ru[0]; out[k].restr_upper[1] = T.ru[1];
+  }
+  return PCG_OK;
+}
+
 int pcg_switch_to_leaf(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);

@@ -1022,6 +1022,23 @@ __global__ void k_switch_to_leaf(double *__restrict__ slab, const PatchDev *__re
   }
 }
 
+// Output gather: uNew (nq planes) and the interior of the parameters with
+// ghost layer (np_w planes) of every listed patch, back to back, x-major
+// planes of nx*ny values.  One CTA per patch.
+__global__ void k_gather_cells(const double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                               const int *__restrict__ ids, const long long *__restrict__ out_off,
+                               int count, double *__restrict__ out) {
+  if ((int)blockIdx.x >= count) return;
+  const PatchDev P = patches[ids[blockIdx.x]];
+  double *o = out + out_off[blockIdx.x];
+  const int nc = P.nx * P.ny;
+  for (int k = threadIdx.x; k < P.nq * nc; k += blockDim.x) o[k] = slab[P.off + k];
+  for (int k = threadIdx.x; k < P.np_w * nc; k += blockDim.x) {
+    const int q = k / nc, c = k - q * nc, x = c / P.ny, y = c - x * P.ny;
+    o[P.nq * nc + k] = slab[idx_pw(P, q, x, y)];
+  }
+}
+
 // BreakingDam refinement criterion (BreakingDamSWEScenario::computeDemandedMeshWidth,
 // native/scenarios/BreakingDam.cpp:85-139): max over xi < nx-1, yi < ny-1 of
 // sqrt(|gx| |gx| + |gy| |gy|), gx = (h[xi+1][yi] - h[xi][yi]) / dx,
@@ -1251,6 +1268,13 @@ cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *pat
                               int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
   k_flux_items<<<n_dst, 32, 0, st>>>(slab, patches, times, items, begin, group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_cells(cudaStream_t st, const double *slab, const PatchDev *patches,
+                                const int *ids, const long long *out_off, int count, double *out) {
+  if (count <= 0) return cudaSuccess;
+  k_gather_cells<<<count, 256, 0, st>>>(slab, patches, ids, out_off, count, out);
   return cudaGetLastError();
 }
 

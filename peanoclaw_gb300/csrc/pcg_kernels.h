@@ -77,6 +77,8 @@ cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev 
 cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *patches,
                               const PatchTimeDev *times, const int4 *items, const int *begin,
                               int n_dst, const int *group_active = nullptr);
+cudaError_t launch_gather_cells(cudaStream_t st, const double *slab, const PatchDev *patches,
+                                const int *ids, const long long *out_off, int count, double *out);
 cudaError_t launch_switch_to_leaf(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, int pid);
 cudaError_t launch_refinement_indicator(cudaStream_t st, const double *slab, const PatchDev *patches,

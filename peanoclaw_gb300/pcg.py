@@ -110,6 +110,8 @@ SIGNATURES = {
     "pcg_set_flux_correction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, _I2, _I2, C.c_double]),
     "pcg_restrict_all": (C.c_int, [_CTX]),
     "pcg_clear_subgrid": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_gather_cells": (C.c_int, [_CTX, C.c_int32, _I2, _D, C.c_int64]),
+    "pcg_patches_get_time": (C.c_int, [_CTX, C.c_int32, _I2, C.POINTER(PatchTime)]),
     "pcg_switch_to_leaf": (C.c_int, [_CTX, C.c_int32]),
     "pcg_refinement_indicator": (C.c_int, [_CTX, C.c_int32, _I2, _D]),
     "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
@@ -303,6 +305,21 @@ class Context:
 
     def clear_subgrid(self, pid):
         check(lib().pcg_clear_subgrid(self.h, int(pid)))
+
+    def gather_cells(self, ids, shapes):
+        """uNew and the parameter interior of every patch in ids, back to back;
+        shapes: per patch (nq + np_w) * nx * ny."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        out = np.empty(int(sum(shapes)))
+        check(lib().pcg_gather_cells(self.h, len(ids), ids.ctypes.data_as(_I2), dptr(out), out.size))
+        return out
+
+    def times_of(self, ids):
+        """(time, dt) of every patch in ids."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        arr = (PatchTime * max(1, len(ids)))()
+        check(lib().pcg_patches_get_time(self.h, len(ids), ids.ctypes.data_as(_I2), arr))
+        return np.array([[arr[k].time, arr[k].dt] for k in range(len(ids))]).reshape(-1, 2)
 
     def switch_to_leaf(self, pid):
         check(lib().pcg_switch_to_leaf(self.h, int(pid)))
