@@ -263,8 +263,8 @@ int pcg_synchronize(pcg_context *ctx);
  *   kind 0: one 16x16 tile of a patch per CTA iteration (256 threads);
  *   kind 1: warp strips: a warp marches strips of up to 32 rows and `chunk`
  *           columns (1..32) of one or more patches along x; `variant` picks
- *           the CTA size / register budget (0..3: 4 warps x 4 CTAs/SM,
- *           4 x 5, 8 x 2, 8 x 3). */
+ *           the CTA size / register budget (0..4: 4 warps x 4 CTAs/SM,
+ *           4 x 5, 8 x 2, 8 x 3, 6 x 3). */
 typedef struct pcg_schedule {
   int32_t kind;
   int32_t variant;
@@ -277,7 +277,7 @@ typedef struct pcg_schedule {
 int pcg_set_schedule(pcg_context *ctx, const pcg_schedule *s);
 int pcg_get_schedule(pcg_context *ctx, pcg_schedule *s);
 /* Autotuner: runs `reps` BATCHED steps with each candidate schedule (tiles;
- * strips x 4 variants x chunk 32 / 16), times each candidate's steps with
+ * strips x 5 variants x chunk 32 / 16), times each candidate's steps with
  * CUDA events, keeps the fastest for this context and caches it for the
  * process under the key (SM count, histogram of leaf patch shapes), so later
  * contexts with the same patch mix start with it.  The simulation advances by

@@ -93,7 +93,7 @@ cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev
 struct StripVariant {
   int warps, min_blocks;
 };
-constexpr int kNumStripVariants = 4;
+constexpr int kNumStripVariants = 5;
 extern const StripVariant kStripVariants[kNumStripVariants];
 cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *slab,
                                 const PatchDev *patches, const StripItem *items,

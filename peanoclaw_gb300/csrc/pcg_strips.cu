@@ -136,10 +136,13 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     // upper): a1 = dxi * (left edge part of h), u1 = dxi * (left edge part of
     // hu); the y parts of h are added after the right edge's
     double a1 = 0.0, u1 = 0.0, yrh = 0.0, ylh = 0.0;
+    // the loads of column c + 1 are issued before column c is computed
+    double fh = 0.0, fhu = 0.0, fhv = 0.0, fb = 0.0;
+    if (act) load_state(slab, P, SG.x0, y, fh, fhu, fhv, fb);
     for (int c = 0; c <= w; c++) {
       const int x = SG.x0 + c;
-      h = hu = hv = b = 0.0;
-      if (act) load_state(slab, P, x, y, h, hu, hv, b);
+      h = fh; hu = fhu; hv = fhv; b = fb;
+      if (act && c < w) load_state(slab, P, x + 1, y, fh, fhu, fhv, fb);
       CellQ cx, cy;
       cell_derived(dry, h, hu, hv, b, cx, cy);
       double Lh, Lhu, Rh, Rhu, sp;
@@ -281,7 +284,7 @@ cudaError_t sweep_strips_t(cudaStream_t st, int grid, double *slab, const PatchD
 
 // Variants of the strip sweep (CTA size, minimum resident CTAs per SM).
 const StripVariant kStripVariants[kNumStripVariants] = {
-    {4, 4}, {4, 5}, {8, 2}, {8, 3},
+    {4, 4}, {4, 5}, {8, 2}, {8, 3}, {6, 3},
 };
 
 cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *slab,
@@ -294,6 +297,7 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
     case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
     case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
     case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
+    case 4: return sweep_strips_t<6, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -304,6 +308,7 @@ cudaError_t strip_occupancy(int variant, int *blocks_per_sm) {
     case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<4, 5>, 128, 0);
     case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<8, 2>, 256, 0);
     case 3: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<8, 3>, 256, 0);
+    case 4: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_strips<6, 3>, 192, 0);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -44,6 +44,7 @@ SCHEDULES = [
     (P.SCHED_STRIPS, 2, 32),
     (P.SCHED_STRIPS, 3, 7),
     (P.SCHED_STRIPS, 0, 1),
+    (P.SCHED_STRIPS, 4, 32),
 ]
 
 
@@ -64,7 +65,7 @@ def test_schedule_bit_exact_on_ragged_sizes(sched):
 def test_autotuner_picks_a_candidate_and_keeps_results_exact():
     ps = S.uneven_patches(grid=4, sizes=(8, 16, 32, 64))
     out, dts, tuned, got = _gpu_run(ps, 3, autotune_reps=1)
-    assert len(tuned) == 9
+    assert len(tuned) == 11
     assert all(ms > 0.0 for _, ms in tuned)
     best = min(tuned, key=lambda t: t[1])[0]
     assert got == best
@@ -85,7 +86,7 @@ def test_schedule_arguments_are_checked():
     ps = S.radial_dam_break(npx=2, n=8)
     c = P.Context(slab_doubles=slab_for(ps), max_patches=8, max_groups=1, params=PRM)
     try:
-        for bad in [(2, 0, 32), (1, 9, 32), (1, 0, 0), (1, 0, 33)]:
+        for bad in [(2, 0, 32), (1, 9, 32), (1, 5, 32), (1, 0, 0), (1, 0, 33)]:
             with pytest.raises(P.PcgError):
                 c.set_schedule(*bad)
     finally:
