@@ -142,6 +142,11 @@ struct pcg_context {
   double *d_group_max_dt = nullptr;
   double *d_group_t_end = nullptr, *d_group_time = nullptr;  // end time (+inf: none), time
   int *d_group_active = nullptr;
+  // per patch: bit 0 = uOld interior unknowns all below 2^1022 in magnitude,
+  // bit 1 = b interior too (lets the ghost interpolation use uNew alone when
+  // the time factor is 1); rescanned when fin_dirty
+  int *d_fin = nullptr;
+  bool fin_dirty = true;
   double *d_dt_out = nullptr;
   double *h_pinned = nullptr;  // pinned scratch for small D2H/H2D
   std::vector<double> h_group_max_dt;
@@ -554,17 +559,26 @@ int enqueue_post_update(pcg_context *c) {
   return PCG_OK;
 }
 
+// Rescan the finiteness flags of every patch (after anything but a batched
+// step changed patch data).
+int refresh_fin(pcg_context *c) {
+  if (!c->fin_dirty) return PCG_OK;
+  PCG_CUDA(pcg::launch_scan_fin(c->stream, c->slab, c->d_patches, c->max_patches, c->d_fin));
+  c->fin_dirty = false;
+  return PCG_OK;
+}
+
 // Batched sweep and update with the context's schedule.
 int enqueue_sweep(pcg_context *c) {
   using namespace pcg;
   if (c->sched.kind == PCG_SCHED_TILES)
     PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
-                          c->d_group_active));
+                          c->d_group_active, c->d_fin));
   else
     PCG_CUDA(launch_sweep_strips(c->stream, c->sched.variant, c->strip_grid, c->slab, c->d_patches,
                                  c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
-                                 c->d_patch_smax, c->d_group_dt, c->d_group_active));
+                                 c->d_patch_smax, c->d_group_dt, c->d_group_active, c->d_fin));
   return PCG_OK;
 }
 
@@ -573,11 +587,11 @@ int enqueue_update(pcg_context *c) {
   if (c->sched.kind == PCG_SCHED_TILES)
     PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
                            (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
-                           c->d_group_active));
+                           c->d_group_active, c->d_fin));
   else
     PCG_CUDA(launch_update_strips(c->stream, c->update_grid, c->slab, c->d_patches, c->d_times,
                                   c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
-                                  c->d_patch_smax, c->d_group_dt, c->d_group_active));
+                                  c->d_patch_smax, c->d_group_dt, c->d_group_active, c->d_fin));
   return PCG_OK;
 }
 
@@ -592,7 +606,7 @@ int enqueue_step(pcg_context *c, int mode) {
                               c->d_item_step));
     PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
                                 c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step,
-                                c->d_group_active));
+                                c->d_group_active, c->d_fin));
     PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(),
                           c->d_group_active));
     int rc;
@@ -605,14 +619,16 @@ int enqueue_step(pcg_context *c, int mode) {
     for (int p : c->leaf_ids) {
       const PatchDev &P = c->h_patches[p];
       PCG_CUDA(launch_sweep(c->stream, P.tile_count, c->slab, c->d_patches, c->d_tiles, P.tile_begin,
-                            P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, c->d_group_active));
+                            P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt, c->d_group_active,
+                            nullptr));
     }
     for (int p : c->leaf_ids) {
       const PatchDev &P = c->h_patches[p];
       PCG_CUDA(launch_update(c->stream, P.tile_count, c->slab, c->d_patches, c->d_times, c->d_tiles,
                              P.tile_begin, P.tile_count, c->prm, c->d_patch_smax, c->d_group_dt,
-                             c->d_group_active));
+                             c->d_group_active, nullptr));
     }
+    c->fin_dirty = true;
   }
   int rc = enqueue_post_update(c);
   if (rc != PCG_OK) return rc;
@@ -731,6 +747,8 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->d_group_t_end, sizeof(double) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_group_time, sizeof(double) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_group_active, sizeof(int) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_fin, sizeof(int) * c->max_patches));
+  CREATE_CK(cudaMemset(c->d_fin, 0, sizeof(int) * c->max_patches));
   {
     std::vector<double> inf(c->max_groups, HUGE_VAL), zero(c->max_groups, 0.0);
     CREATE_CK(cudaMemcpy(c->d_group_t_end, inf.data(), sizeof(double) * c->max_groups, cudaMemcpyHostToDevice));
@@ -760,6 +778,7 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_group_t_end);
   cudaFree(c->d_group_time);
   cudaFree(c->d_group_active);
+  cudaFree(c->d_fin);
   cudaFree(c->d_dt_out);
   cudaFree(c->d_items);
   cudaFree(c->d_gcells);
@@ -812,6 +831,7 @@ int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
     return fail(PCG_E_INVALID, "invalid patch shape");
   if (!(d->size[0] > 0.0) || !(d->size[1] > 0.0)) return fail(PCG_E_INVALID, "patch size must be positive");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int slot = -1;
   for (int k = 0; k < c->max_patches; k++) {
     int p = (c->slot_hint + k) % c->max_patches;
@@ -848,6 +868,7 @@ int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
 int pcg_patch_free(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   slab_free(c, c->h_patches[id].off, c->h_len[id]);
   c->used[id] = 0;
@@ -860,6 +881,7 @@ int pcg_patch_free(pcg_context *c, int32_t id) {
 int pcg_patch_upload(pcg_context *c, int32_t id, const double *vec, int64_t n) {
   if (!valid_id(c, id) || !vec) return fail(PCG_E_INVALID, "unknown patch id or null vector");
   if (n != c->h_len[id]) return fail(PCG_E_INVALID, "vector length does not match the patch layout");
+  c->fin_dirty = true;
   PCG_CUDA(cudaMemcpyAsync(c->slab + c->h_patches[id].off, vec, sizeof(double) * n,
                            cudaMemcpyHostToDevice, c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
@@ -878,6 +900,7 @@ int pcg_patch_download(pcg_context *c, int32_t id, double *vec, int64_t n) {
 int pcg_patches_upload(pcg_context *c, int32_t n, const int32_t *ids, const double *vecs) {
   if (!c || (n > 0 && (!ids || !vecs))) return fail(PCG_E_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   return multi_copy(c, n, ids, const_cast<double *>(vecs), true);
 }
 
@@ -890,6 +913,7 @@ int pcg_patches_download(pcg_context *c, int32_t n, const int32_t *ids, double *
 int pcg_patch_set_desc_flags(pcg_context *c, int32_t id, int32_t flags) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   c->h_patches[id].flags = flags;
   c->patches_dirty = c->topo_dirty = true;
   return PCG_OK;
@@ -943,6 +967,7 @@ int pcg_patch_set_group(pcg_context *c, int32_t id, int32_t group) {
 int pcg_copy_unew_to_uold(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   const pcg::PatchDev &P = c->h_patches[id];
@@ -955,6 +980,7 @@ int pcg_fill_boundary_layer(pcg_context *c, int32_t id, int32_t dimension, int32
   if (c->h_patches[id].g != 1 || c->h_patches[id].nq < 3)
     return fail(PCG_E_INVALID, "SWE wall boundary needs ghost width 1 and 3 unknowns");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   PCG_CUDA(pcg::launch_fill_boundary_layer(c->stream, c->slab, c->d_patches, id, dimension, set_upper ? 1 : 0));
@@ -969,6 +995,7 @@ int pcg_solve_timestep(pcg_context *c, int32_t id, double max_dt, double *dt_use
   size_t smem = pcg::solve_patch_smem(P.nx, P.ny);
   if (smem > 190 * 1024) return fail(PCG_E_INVALID, "patch too large for the fused per-patch solve");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   if (smem > c->solve_smem_set) {
@@ -992,6 +1019,7 @@ int pcg_transfer_ghostlayer(pcg_context *c, const int32_t size[2], const int32_t
   if (!region_inside(S, so, size, false) || !region_inside(D, dof, size, true))
     return fail(PCG_E_INVALID, "transfer region outside the patches");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   PCG_CUDA(pcg::launch_transfer(c->stream, c->slab, c->d_patches, c->d_times,
@@ -1009,6 +1037,7 @@ int pcg_interpolate_solution(pcg_context *c, const int32_t size[2], const int32_
   if (!region_inside(D, dof, size, to_uold != 0)) return fail(PCG_E_INVALID, "region outside the destination");
   if (swe && (S.np_w < 1 || D.np_w < 1)) return fail(PCG_E_INVALID, "SWE interpolation needs the bathymetry parameter");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   PCG_CUDA(pcg::launch_interpolate(c->stream, c->slab, c->d_patches, c->d_times,
@@ -1023,6 +1052,7 @@ int pcg_restrict_solution(pcg_context *c, int32_t src, int32_t dst, int32_t only
   if (S.nq != D.nq) return fail(PCG_E_INVALID, "unknowns per subcell differ");
   if (swe && S.np_w < 1) return fail(PCG_E_INVALID, "SWE restriction needs the bathymetry parameter");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   PCG_CUDA(pcg::launch_restrict(c->stream, c->slab, c->d_patches, c->d_times, src, dst, only_overlapped, swe));
@@ -1033,6 +1063,7 @@ int pcg_post_process_restriction(pcg_context *c, int32_t dst) {
   if (!valid_id(c, dst)) return fail(PCG_E_INVALID, "unknown patch id");
   if (c->h_patches[dst].np_w < 1) return fail(PCG_E_INVALID, "needs the bathymetry parameter");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   int *ids = nullptr;
@@ -1050,6 +1081,7 @@ int pcg_post_process_restriction(pcg_context *c, int32_t dst) {
 int pcg_clear_subgrid(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   int *ids = nullptr;
@@ -1124,6 +1156,7 @@ int pcg_patches_get_time(pcg_context *c, int32_t n, const int32_t *ids, pcg_patc
 int pcg_switch_to_leaf(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   PCG_CUDA(cudaSetDevice(c->device));
   pcg::PatchDev &P = c->h_patches[id];
   P.flags = (P.flags & ~pcg::kFlagVirtual) | pcg::kFlagLeaf;
@@ -1167,6 +1200,7 @@ int pcg_compute_fluxes(pcg_context *c, int32_t id, double g_flux) {
   if (c->h_patches[id].nq != 3 || c->h_patches[id].g < 1)
     return fail(PCG_E_INVALID, "flux computation needs 3 unknowns and a ghost layer");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   int *ids = nullptr;
@@ -1186,6 +1220,7 @@ int pcg_apply_flux_correction(pcg_context *c, int32_t src, int32_t dst, int32_t 
     return fail(PCG_E_INVALID, "bad dimension/direction");
   if (c->h_patches[src].nq != 3 || c->h_patches[dst].nq != 3) return fail(PCG_E_INVALID, "needs 3 unknowns");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
   PCG_CUDA(pcg::launch_flux_correction(c->stream, c->slab, c->d_patches, c->d_times, src, dst, dimension, direction));
@@ -1253,6 +1288,7 @@ int pcg_set_flux_correction_items(pcg_context *c, int32_t n, const int32_t *src,
 int pcg_restrict_all(pcg_context *c) {
   if (!c) return fail(PCG_E_INVALID, "null context");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
@@ -1317,6 +1353,7 @@ int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
   if ((rc = enqueue_step(c, mode)) != PCG_OK) return rc;
   PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
@@ -1342,6 +1379,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   if (steps > c->hist_cap) {
     if (c->d_hist) PCG_CUDA(cudaFree(c->d_hist));
     PCG_CUDA(cudaMalloc(&c->d_hist, sizeof(double) * (size_t)steps * c->max_groups));
@@ -1440,6 +1478,7 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   std::vector<pcg_schedule> cand;
   cand.push_back(pcg_schedule{PCG_SCHED_TILES, 0, 32, 0});
   for (int chunk : {32, 16})
@@ -1495,6 +1534,7 @@ int pcg_profile_step(pcg_context *c, double *ms) {
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; i++) PCG_CUDA(cudaEventCreate(&ev[i]));
   using namespace pcg;
@@ -1507,7 +1547,7 @@ int pcg_profile_step(pcg_context *c, double *ms) {
                             c->d_item_step));
   PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
                               c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step,
-                                c->d_group_active));
+                                c->d_group_active, c->d_fin));
   PCG_CUDA(cudaEventRecord(ev[2], c->stream));
   PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(),
                         c->d_group_active));

@@ -92,6 +92,13 @@ struct __align__(16) GhostItemStepDev {
   int vn_src, vo_src, vo_dst, nq;
 };
 
+// |x| < 2^1022 (so that x + y of two such values is finite); NaN fails.
+__device__ __forceinline__ bool small_mag(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull) < 0x7FD0000000000000ull;
+}
+constexpr int kFinUOld = 1;  // patch finiteness flags (see k_scan_fin)
+constexpr int kFinB = 2;
+
 constexpr int kTile = 16;           // tile edge of the sweep
 constexpr int kSweepThreads = 256;  // kTile * kTile
 constexpr int kFlagLeaf = 1;

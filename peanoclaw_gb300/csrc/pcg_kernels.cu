@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
     k_sweep_tiles(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                   const TileItem *__restrict__ tiles, int first, int count, SweParamsDev prm,
                   unsigned long long *__restrict__ patch_smax,
-                  unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active) {
+                  unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active, int *__restrict__ fin) {
   __shared__ SweepSmem S;
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
     TileItem ti = tiles[first + it];
@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
       slab[idx_uold(P, 2, x, y)] = nhv;
     }
     if (t == 0) {
+      if (fin) atomicOr(&fin[ti.pid], kFinUOld);
       atomicMax(&patch_smax[ti.pid], dbits(smax));
       double dtc = cfl_dt(prm, smax, subcell(P, 0), subcell(P, 1));
       atomicMin(&group_dt[P.group], dbits(dtc));
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(kSweepThreads)
                    PatchTimeDev *__restrict__ times, const TileItem *__restrict__ tiles, int first,
                    int count, SweParamsDev prm, const unsigned long long *__restrict__ patch_smax,
                    const unsigned long long *__restrict__ group_dt,
-                   const int *__restrict__ group_active) {
+                   const int *__restrict__ group_active, int *__restrict__ fin) {
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
     TileItem ti = tiles[first + it];
     PatchDev P = patches[ti.pid];
@@ -211,6 +212,7 @@ __global__ void __launch_bounds__(kSweepThreads)
       if (lt_zero(nh)) nh = 0.0;
       slab[io0] = h; slab[io1] = hu; slab[io2] = hv;
       slab[in0] = nh; slab[in1] = nhu; slab[in2] = nhv;
+      if (fin && !(small_mag(h) && small_mag(hu) && small_mag(hv))) atomicAnd(&fin[ti.pid], ~kFinUOld);
     }
     if (t == 0 && ti.x0 == 0 && ti.y0 == 0) {
       PatchTimeDev &T = times[ti.pid];
@@ -506,7 +508,7 @@ __global__ void __launch_bounds__(256)
                   int ncopy, int ninterp, const CopyPlanDev *__restrict__ copy_plan,
                   const InterpPlanDev *__restrict__ plan,
                   const GhostItemStepDev *__restrict__ item_step,
-                  const int *__restrict__ group_active) {
+                  const int *__restrict__ group_active, const int *__restrict__ fin) {
   const int total = ncopy + ninterp;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     if (e < ncopy) {
@@ -543,6 +545,23 @@ __global__ void __launch_bounds__(256)
     double acc[3];
     const int nq = I.nq;
     for (int q = 0; q < nq; q++) acc[q] = 0.0;
+    // time factor 1 with a leaf source whose uOld and b interior are below
+    // 2^1022: (uOld [+ b]) * 0 + (uNew [+ b]) * 1 is exactly uNew [+ b] up to
+    // the sign of a zero, which the accumulator (started at +0, never -0)
+    // absorbs, so uOld is not needed
+    if (fin && dbits(tf) == 0x3FF0000000000000ull && is_leaf(S) &&
+        (fin[it.src] & (kFinUOld | kFinB)) == (kFinUOld | kFinB)) {
+      for (int kk = 0; kk < 4; kk++) {
+        const int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
+        const double sf = pl.sf[kk];
+        const double bb = slab[idx_pw(S, 0, nxi, nyi)];
+        acc[0] = __dadd_rn(acc[0], __dmul_rn(sf, __dadd_rn(slab[idx_unew(S, 0, nxi, nyi)], bb)));
+        for (int q = 1; q < nq; q++) acc[q] = __dadd_rn(acc[q], __dmul_rn(sf, slab[idx_unew(S, q, nxi, nyi)]));
+      }
+      acc[0] = __dadd_rn(acc[0], __dmul_rn(-1.0, slab[idx_pw(D, 0, cx, cy)]));
+      for (int q = 0; q < nq; q++) slab[idx_uold(D, q, cx, cy)] = acc[q];
+      continue;
+    }
     for (int kk = 0; kk < 4; kk++) {
       int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
       double sf = pl.sf[kk];
@@ -1022,6 +1041,35 @@ __global__ void k_switch_to_leaf(double *__restrict__ slab, const PatchDev *__re
   }
 }
 
+// Finiteness flags of every patch slot: kFinUOld if every uOld interior
+// unknown and kFinB if every interior value of the first parameter with
+// ghost layer (b) is below 2^1022 in magnitude.  One CTA per slot.
+__global__ void k_scan_fin(const double *__restrict__ slab, const PatchDev *__restrict__ patches, int count,
+                           int *__restrict__ fin) {
+  if ((int)blockIdx.x >= count) return;
+  const PatchDev P = patches[blockIdx.x];
+  __shared__ int bad_u, bad_b;
+  if (threadIdx.x == 0) { bad_u = 0; bad_b = 0; }
+  __syncthreads();
+  if (P.nx > 0 && P.ny > 0) {
+    const int nc = P.nx * P.ny;
+    int bu = 0, bb = 0;
+    for (int k = threadIdx.x; k < P.nq * nc; k += blockDim.x) {
+      const int q = k / nc, c = k - q * nc, x = c / P.ny, y = c - x * P.ny;
+      if (!small_mag(slab[idx_uold(P, q, x, y)])) bu = 1;
+    }
+    for (int k = threadIdx.x; k < (P.np_w > 0 ? nc : 0); k += blockDim.x) {
+      const int x = k / P.ny, y = k - x * P.ny;
+      if (!small_mag(slab[idx_pw(P, 0, x, y)])) bb = 1;
+    }
+    if (bu) atomicOr(&bad_u, 1);
+    if (bb) atomicOr(&bad_b, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    fin[blockIdx.x] = (P.nx > 0 && P.np_w > 0) ? ((bad_u ? 0 : kFinUOld) | (bad_b ? 0 : kFinB)) : 0;
+}
+
 // Output gather: uNew (nq planes) and the interior of the parameters with
 // ghost layer (np_w planes) of every listed patch, back to back, x-major
 // planes of nx*ny values.  One CTA per patch.
@@ -1077,20 +1125,20 @@ __global__ void k_refinement_indicator(const double *__restrict__ slab, const Pa
 cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                          const TileItem *tiles, int first, int count, const SweParamsDev &prm,
                          unsigned long long *patch_smax, unsigned long long *group_dt,
-                         const int *group_active) {
+                         const int *group_active, int *fin) {
   if (count <= 0) return cudaSuccess;
   k_sweep_tiles<<<grid, kSweepThreads, 0, st>>>(slab, patches, tiles, first, count, prm, patch_smax,
-                                                group_dt, group_active);
+                                                group_dt, group_active, fin);
   return cudaGetLastError();
 }
 
 cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                           PatchTimeDev *times, const TileItem *tiles, int first, int count,
                           const SweParamsDev &prm, const unsigned long long *patch_smax,
-                          const unsigned long long *group_dt, const int *group_active) {
+                          const unsigned long long *group_dt, const int *group_active, int *fin) {
   if (count <= 0) return cudaSuccess;
   k_update_tiles<<<grid, kSweepThreads, 0, st>>>(slab, patches, times, tiles, first, count, prm,
-                                                 patch_smax, group_dt, group_active);
+                                                 patch_smax, group_dt, group_active, fin);
   return cudaGetLastError();
 }
 
@@ -1144,13 +1192,14 @@ cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
 cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
                                const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
                                int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
-                               const GhostItemStepDev *item_step, const int *group_active) {
+                               const GhostItemStepDev *item_step, const int *group_active,
+                               const int *fin) {
   int total = ncopy + ninterp;
   if (total <= 0) return cudaSuccess;
   int grid = (total + 255) / 256;
   if (grid > 152 * 32) grid = 152 * 32;
   k_ghost_cells<<<grid, 256, 0, st>>>(slab, patches, items, cells, ncopy, ninterp, copy_plan, plan,
-                                      item_step, group_active);
+                                      item_step, group_active, fin);
   return cudaGetLastError();
 }
 
@@ -1268,6 +1317,13 @@ cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *pat
                               int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
   k_flux_items<<<n_dst, 32, 0, st>>>(slab, patches, times, items, begin, group_active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scan_fin(cudaStream_t st, const double *slab, const PatchDev *patches, int count,
+                            int *fin) {
+  if (count <= 0) return cudaSuccess;
+  k_scan_fin<<<count, 128, 0, st>>>(slab, patches, count, fin);
   return cudaGetLastError();
 }
 

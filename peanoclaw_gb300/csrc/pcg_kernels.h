@@ -16,11 +16,12 @@ namespace pcg {
 cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                          const TileItem *tiles, int first, int count, const SweParamsDev &prm,
                          unsigned long long *patch_smax, unsigned long long *group_dt,
-                         const int *group_active);
+                         const int *group_active, int *fin = nullptr);
 cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                           PatchTimeDev *times, const TileItem *tiles, int first, int count,
                           const SweParamsDev &prm, const unsigned long long *patch_smax,
-                          const unsigned long long *group_dt, const int *group_active);
+                          const unsigned long long *group_dt, const int *group_active,
+                          int *fin = nullptr);
 cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_dt,
                          const double *group_t_end, const double *group_time,
                          unsigned long long *group_dt, int *group_active, int n_patches,
@@ -38,7 +39,10 @@ cudaError_t launch_build_interp_plan(cudaStream_t st, const PatchDev *patches,
 cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *patches,
                                const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
                                int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
-                               const GhostItemStepDev *item_step, const int *group_active);
+                               const GhostItemStepDev *item_step, const int *group_active,
+                               const int *fin);
+cudaError_t launch_scan_fin(cudaStream_t st, const double *slab, const PatchDev *patches, int count,
+                            int *fin);
 cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
                                    const GhostCellDev *cells, int count, CopyPlanDev *plan);
 cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
@@ -99,13 +103,14 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
                                 const PatchDev *patches, const StripItem *items,
                                 const StripGroup *groups, int count, const SweParamsDev &prm,
                                 unsigned long long *patch_smax, unsigned long long *group_dt,
-                                const int *group_active);
+                                const int *group_active, int *fin);
 cudaError_t strip_occupancy(int variant, int *blocks_per_sm);
 cudaError_t update_strips_occupancy(int *blocks_per_sm);
 cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                                  PatchTimeDev *times, const StripItem *items, const StripGroup *groups,
                                  int count, const SweParamsDev &prm,
                                  const unsigned long long *patch_smax,
-                                 const unsigned long long *group_dt, const int *group_active);
+                                 const unsigned long long *group_dt, const int *group_active,
+                                 int *fin);
 
 }  // namespace pcg

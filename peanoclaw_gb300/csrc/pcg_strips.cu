@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     k_sweep_strips(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                    const StripItem *__restrict__ items, const StripGroup *__restrict__ groups,
                    int count, SweParamsDev prm, unsigned long long *__restrict__ patch_smax,
-                   unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active) {
+                   unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active,
+                   int *__restrict__ fin) {
   __shared__ StripWarpSmem SM[kWarps];
   __shared__ StripLaneSmem LS[kWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -196,6 +197,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       if (j + o < hs) m = other > m ? other : m;
     }
     if (act && j == 0) {
+      if (fin) atomicOr(&fin[SG.pid], kFinUOld);
       atomicMax(&patch_smax[SG.pid], m);
       const double dtc = cfl_dt(prm, bitsd(m), subcell(P, 0), subcell(P, 1));
       atomicMin(&group_dt[P.group], dbits(dtc));
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                     const StripGroup *__restrict__ groups, int count, SweParamsDev prm,
                     const unsigned long long *__restrict__ patch_smax,
                     const unsigned long long *__restrict__ group_dt,
-                    const int *__restrict__ group_active) {
+                    const int *__restrict__ group_active, int *__restrict__ fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int it = blockIdx.x * kWarps + wid; it < count; it += gridDim.x * kWarps) {
     const StripItem I = items[it];
@@ -229,6 +231,7 @@ __global__ void __launch_bounds__(kWarps * 32)
     // loads of kBatch columns are issued before their stores (loads and
     // stores go through the same pointer, so the compiler cannot reorder them)
     constexpr int kBatch = 4;
+    bool big = false;  // an old value written to uOld is 2^1022 or more (or NaN)
     for (int c0 = 0; c0 < w; c0 += kBatch) {
       double st[kBatch][3], nt[kBatch][3];
 #pragma unroll
@@ -250,11 +253,13 @@ __global__ void __launch_bounds__(kWarps * 32)
           if (lt_zero(nh)) nh = 0.0;
           slab[o] = st[k][0]; slab[o + vo] = st[k][1]; slab[o + 2 * vo] = st[k][2];
           slab[a] = nh; slab[a + vn] = nhu; slab[a + 2 * vn] = nhv;
+          big |= !(small_mag(st[k][0]) && small_mag(st[k][1]) && small_mag(st[k][2]));
         }
       }
       in0 += (long long)kBatch * sn;
       io0 += (long long)kBatch * so;
     }
+    if (fin && big) atomicAnd(&fin[SG.pid], ~kFinUOld);
     if (j == 0 && SG.x0 == 0 && SG.y0 == 0) {
       PatchTimeDev &T = times[SG.pid];
       if (tl_greater(dt, 0.0)) {
@@ -272,11 +277,11 @@ template <int kWarps, int kMinBlocks>
 cudaError_t sweep_strips_t(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                            const StripItem *items, const StripGroup *groups, int count,
                            const SweParamsDev &prm, unsigned long long *patch_smax,
-                           unsigned long long *group_dt, const int *group_active) {
+                           unsigned long long *group_dt, const int *group_active, int *fin) {
   if (count <= 0) return cudaSuccess;
   k_sweep_strips<kWarps, kMinBlocks><<<grid, kWarps * 32, 0, st>>>(slab, patches, items, groups, count,
                                                                    prm, patch_smax, group_dt,
-                                                                   group_active);
+                                                                   group_active, fin);
   return cudaGetLastError();
 }
 
@@ -291,13 +296,13 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
                                 const PatchDev *patches, const StripItem *items,
                                 const StripGroup *groups, int count, const SweParamsDev &prm,
                                 unsigned long long *patch_smax, unsigned long long *group_dt,
-                                const int *group_active) {
+                                const int *group_active, int *fin) {
   switch (variant) {
-    case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
-    case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
-    case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
-    case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
-    case 4: return sweep_strips_t<6, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active);
+    case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
+    case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
+    case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
+    case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
+    case 4: return sweep_strips_t<6, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -321,10 +326,11 @@ cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const 
                                  PatchTimeDev *times, const StripItem *items, const StripGroup *groups,
                                  int count, const SweParamsDev &prm,
                                  const unsigned long long *patch_smax,
-                                 const unsigned long long *group_dt, const int *group_active) {
+                                 const unsigned long long *group_dt, const int *group_active,
+                                 int *fin) {
   if (count <= 0) return cudaSuccess;
   k_update_strips<8><<<grid, 256, 0, st>>>(slab, patches, times, items, groups, count, prm, patch_smax,
-                                           group_dt, group_active);
+                                           group_dt, group_active, fin);
   return cudaGetLastError();
 }
 
