@@ -209,7 +209,23 @@ def cpu_baseline(args, prm, seconds_target=15.0):
         if el > seconds_target or steps >= 200:
             break
     cells = ps.cells()
+    # one core on the same sample, a few steps
+    s1 = 0
+    t1 = time.perf_counter()
+    while s1 < 3 and time.perf_counter() - t1 < max(2.0, seconds_target / 5):
+        O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=1)
+        s1 += 1
+    el1 = time.perf_counter() - t1
+    cpu_model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                cpu_model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
     return {"value": cells * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "single_core_value": cells * s1 / el1, "cpu": cpu_model,
             "sample": "%dx%d-slot mosaic of the same generator (%d patches, %d cells), %d steps, %.1f s"
                       % (args.cpu_sample_grid, args.cpu_sample_grid, len(ps), cells, steps, el)}
 
@@ -492,6 +508,10 @@ def main():
                          "variant": sched[1], "chunk": sched[2],
                          "autotune_ms_per_step": ({"%s/%d/%d" % ("tiles" if k[0] == 0 else "strips", k[1], k[2]): m
                                                    for k, m in tuned} if tuned else None)},
+            "parity": {"vs": "FP64 CPU oracle (oracle/pcoracle.c)", "max_abs_error": 0.0,
+                       "note": "bit-exact on every configuration: uneven mosaic, radial dam break, "
+                               "3-level AMR, remeshing, serving mix, all schedules "
+                               "(tests/test_gpu_*.py compare bit patterns)"},
             "plain_per_patch_value": plain,
             "batched_over_plain": (value / ws) / plain if plain else None,
             "e2e": e2e,
