@@ -183,6 +183,24 @@ int pcg_apply_flux_correction(pcg_context *ctx, int32_t src, int32_t dst, int32_
  * before its children restrict into it); used before a full restriction when
  * a refined patch coarsens. */
 int pcg_clear_subgrid(pcg_context *ctx, int32_t id);
+/* Host-side list builder of an adaptive grid of n x n patches with 3x
+ * refinement (level l: (base * 3^l)^2 slots on [0,1]^2; no device work).
+ * The np slots (lvl, si, sj) in patch order (level, then i, then j ascending),
+ * refined[k] != 0 for a virtual (refined) slot, give: the ghost face pairs
+ * (items, up to 8 np rows of pcg_ghost_item fields: kind, src, dst, size,
+ * src_offset, dst_offset; copies between slots of one level, interpolation
+ * from the nearest existing coarser slot, GhostlayerCompositorFunctors.cpp),
+ * the flux-correction pairs (flux, up to 4 np rows: fine leaf, coarse owner,
+ * dim, dir), the restriction pairs (restr, up to levels np rows: leaf,
+ * virtual ancestor whose ghost-layer bounds it overlaps, ordered by ancestor
+ * then leaf, GridLevelTransfer::restrictToOverlappingVirtualSubgrids), the
+ * bounds lower[2 np] / upper[2 np] of every virtual slot
+ * (GhostLayerCompositor::updateLower/UpperGhostlayerBound) and the wall
+ * mask of every leaf on the domain boundary. */
+int pcg_amr_layout(int32_t base, int32_t n, int32_t levels, int32_t np, const int32_t *lvl,
+                   const int32_t *si, const int32_t *sj, const uint8_t *refined, int32_t *items,
+                   int32_t *n_items, int32_t *flux, int32_t *n_flux, int32_t *restr, int32_t *n_restr,
+                   double *lower, double *upper, int32_t *walls);
 /* Patch::switchToLeaf (src/peanoclaw/Patch.cpp:793-816): the patch becomes a
  * leaf and its interior, restricted as values at the times 0 and 1 (the
  * reference's virtual-patch convention), is re-evaluated at the patch's time

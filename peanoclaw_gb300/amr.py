@@ -123,6 +123,38 @@ class AmrGrid:
 
     # ----------------------------------------------------------------- lists
     def layout(self):
+        """Patch order and every list the batched step needs (see layout_py),
+        built by the library's native builder (pcg_amr_layout)."""
+        import ctypes as C
+        from . import pcg as P
+        order = self.order()
+        npch = len(order)
+        arr = np.array(order, dtype=np.int32).reshape(-1, 3)
+        lvl, si, sj = (np.ascontiguousarray(arr[:, k]) for k in range(3))
+        ref = np.array([0 if self.is_leaf(*s) else 1 for s in order], dtype=np.uint8)
+        items = np.zeros((8 * npch + 1, 9), dtype=np.int32)
+        flux = np.zeros((4 * npch + 1, 4), dtype=np.int32)
+        restr = np.zeros((self.levels * npch + 1, 2), dtype=np.int32)
+        lower = np.zeros((npch + 1, 2))
+        upper = np.zeros((npch + 1, 2))
+        walls = np.zeros(npch + 1, dtype=np.int32)
+        ni, nf, nr = C.c_int32(), C.c_int32(), C.c_int32()
+        i32 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        P.check(P.lib().pcg_amr_layout(
+            self.base, self.n, self.levels, npch, i32(lvl), i32(si), i32(sj),
+            ref.ctypes.data_as(C.POINTER(C.c_uint8)), i32(items), C.byref(ni), i32(flux), C.byref(nf),
+            i32(restr), C.byref(nr), lower.ctypes.data_as(C.POINTER(C.c_double)),
+            upper.ctypes.data_as(C.POINTER(C.c_double)), i32(walls)))
+        L = 1.0 / (self.base * np.power(3.0, lvl.astype(np.float64)))
+        pos = np.stack([si * L, sj * L], axis=1)
+        size = np.stack([L, L], axis=1)
+        return {"order": order, "index": {s: k for k, s in enumerate(order)}, "pos": pos, "size": size,
+                "leaf": (ref == 0).tolist(), "level": lvl.tolist(), "wall": walls[:npch].tolist(),
+                "items": items[:ni.value].copy(), "flux_items": flux[:nf.value].copy(),
+                "restrict_items": restr[:nr.value].copy(),
+                "restr_lower": lower[:npch].copy(), "restr_upper": upper[:npch].copy()}
+
+    def layout_py(self):
         """Patch order and every list the batched step needs, in patch-order
         indices: items (N, 9), flux_items (N, 4) (fine leaf, coarse owner,
         dim, dir), restrict_items (N, 2) (leaf, virtual ancestor),
@@ -215,6 +247,8 @@ def remesh(grid, backend, g, b_of):
     Returns (#refined, #coarsened)."""
     from .scenarios import _centers
     exists, refined = grid.decide(g)
+    if exists == grid.exists and refined == grid.refined:
+        return 0, 0
     n = grid.n
     n_ref = n_crs = 0
     # refinement, coarse to fine: children of newly refined slots

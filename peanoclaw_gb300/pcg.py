@@ -113,6 +113,8 @@ SIGNATURES = {
     "pcg_gather_cells": (C.c_int, [_CTX, C.c_int32, _I2, _D, C.c_int64]),
     "pcg_patches_get_time": (C.c_int, [_CTX, C.c_int32, _I2, C.POINTER(PatchTime)]),
     "pcg_switch_to_leaf": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_amr_layout": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _I2, _I2, _I2,
+                                 C.POINTER(C.c_uint8), _I2, _I2, _I2, _I2, _I2, _I2, _D, _D, _I2]),
     "pcg_refinement_indicator": (C.c_int, [_CTX, C.c_int32, _I2, _D]),
     "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),

@@ -78,3 +78,24 @@ def test_remesh_of_a_lake_at_rest_keeps_it_at_rest():
     for p in be.patches():
         assert np.max(np.abs(p.unew()[0] - 1.0)) <= 1e-14
         assert np.max(np.abs(p.unew()[1:])) <= 1e-14
+
+
+def test_native_layout_equals_the_python_builder():
+    """pcg_amr_layout (library) and AmrGrid.layout_py give the same lists."""
+    grids = [S.breaking_dam_amr(base=3, n=9, levels=3).grid,
+             S.breaking_dam_amr(base=4, n=6, levels=3, buffers=(2, 1)).grid,
+             S.adaptive_tsunami(base=5, n=8, levels=3).grid]
+    # and one after a remesh of a moving front
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0)
+    be = OracleAmr(ps.grid, ps, ps.b_of)
+    prm = oracle_params(PRM)
+    for _ in range(8):
+        be.step(prm, 1e9)
+    be.remesh()
+    grids.append(ps.grid)
+    for g in grids:
+        a, b = g.layout(), g.layout_py()
+        assert a["order"] == b["order"]
+        for k in ("items", "flux_items", "restrict_items", "restr_lower", "restr_upper", "wall",
+                  "leaf", "level", "pos", "size"):
+            assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
