@@ -273,6 +273,29 @@ int pcg_stats(pcg_context *ctx, int64_t *cell_updates, double *device_ms);
 /* Block until all work issued on the context has finished. */
 int pcg_synchronize(pcg_context *ctx);
 
+/* ----------------------------------------------------- local time stepping */
+
+/* Replaces the reference's adaptive (local) time stepping of SolveTimestep:
+ * a leaf advances in a grid iteration when its end time is not reached and
+ * its uNew time does not lie ahead of the minimal uNew time of its ghost
+ * sources by more than the time tolerance (TimeIntervals.cpp:24-99,
+ * isAllowedToAdvanceInTime / isBlockedByNeighbors).  With PCG_TS_LOCAL every
+ * BATCHED pcg_step / pcg_run iteration decides which leaves advance (on the
+ * device, from the times before the iteration), fills the ghost layers of
+ * those leaves only (time-interpolated from their sources,
+ * DefaultTransfer.cpph:27-50), and solves each of them with its own dt =
+ * min(block CFL dt, group max_dt, end time - uNew time) (SolveTimestep.cpp:
+ * 591-700).  The recorded dt of a group is the minimal dt taken by its
+ * leaves in the iteration (0 if none advanced); its time
+ * (pcg_get_group_times) becomes the minimal uNew time of its leaves.  The
+ * end time of pcg_set_group_end_time bounds every leaf.  Local time stepping
+ * runs in the BATCHED form only and takes no flux-correction or restriction
+ * lists (PCG_E_STATE otherwise); PCG_TS_GLOBAL (default) is the synchronous
+ * step. */
+#define PCG_TS_GLOBAL 0
+#define PCG_TS_LOCAL 1
+int pcg_set_time_stepping(pcg_context *ctx, int32_t mode);
+
 /* --------------------------------------------- batched schedule + autotuner */
 
 /* No counterpart in the reference (its block sweep is one loop nest).  How the

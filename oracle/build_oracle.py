@@ -4,7 +4,7 @@ Compiles oracle/pcoracle.c into oracle/_build/libpcoracle.so with
 -ffp-contract=off (so every fused multiply-add is an explicit fma() call) and
 OpenMP (for the timed CPU baseline).  The reference's own SWE path cannot be
 compiled (Peano 3, the TUM SWE sources and scons are absent), so there is no
-oracle/_ref build; see the design doc.
+oracle/_ref build.
 """
 import os
 import subprocess

@@ -86,6 +86,10 @@ def lib():
         L.pco_grid_step.argtypes = [C.POINTER(P), C.c_int, C.POINTER(PcoGhostItem), C.c_int,
                                     C.POINTER(C.c_uint8), C.POINTER(C.c_int32), C.c_int,
                                     C.POINTER(PcoSweParams), D, D, C.c_int]
+        L.pco_grid_step_lts.restype = C.c_int
+        L.pco_grid_step_lts.argtypes = [C.POINTER(P), C.c_int, C.POINTER(PcoGhostItem), C.c_int,
+                                        C.POINTER(C.c_uint8), C.POINTER(PcoSweParams), C.c_double,
+                                        C.c_double, D, C.c_int]
         _lib = L
     return _lib
 
@@ -246,3 +250,17 @@ def grid_fill(patches, items, wall_mask):
     wm = np.ascontiguousarray(wall_mask, dtype=np.uint8)
     lib().pco_grid_fill(parr, len(patches), it, len(keep) if len(items) else 0,
                         wm.ctypes.data_as(C.POINTER(C.c_uint8)))
+
+
+def grid_step_lts(patches, items, wall_mask, prm, max_dt, t_end, n_threads=0):
+    """One local-time-stepping iteration; returns (number advanced, dt per patch)."""
+    P = C.POINTER(PcoPatch)
+    parr = (P * len(patches))(*[C.pointer(p.s) for p in patches])
+    it, keep = ghost_items(items)
+    wm = np.ascontiguousarray(wall_mask, dtype=np.uint8)
+    dto = np.zeros(len(patches))
+    n = lib().pco_grid_step_lts(parr, len(patches), it, len(keep) if len(items) else 0,
+                                wm.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(prm), float(max_dt),
+                                float(t_end), dto.ctypes.data_as(C.POINTER(C.c_double)), n_threads)
+    return n, dto
+

@@ -846,3 +846,80 @@ void pco_grid_step(pco_patch **patches, int n_patches,
   free(nets);
   free(own);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Local time stepping (the semantics of the batched GPU form with per-patch */
+/* time steps), one grid iteration in two phases.  The reference decides per */
+/* leaf in the traversal whether it may advance (TimeIntervals.cpp:24-99:    */
+/* the global end time is not reached and the patch is not blocked by its    */
+/* neighbours, i.e. time + dt does not exceed the minimal uNew time of the   */
+/* neighbouring subgrids) and then solves with max_dt = end time - (time +   */
+/* dt) (SolveTimestep.cpp:591-700).  Here every decision and every ghost     */
+/* fill of an iteration uses the times at its start (fill all, then solve    */
+/* all): a leaf's neighbours are the sources of its ghost items; the ghost   */
+/* layers of the advancing leaves are filled with the time factors of their */
+/* uNew time (DefaultTransfer / interpolation time interpolation); the       */
+/* leaves then step with dt = min(block CFL dt, max_dt).                     */
+/* dt_out[p] receives the dt taken (0 for a leaf that did not advance);      */
+/* returns the number of leaves that advanced.                               */
+/* ------------------------------------------------------------------------ */
+int pco_grid_step_lts(pco_patch **patches, int n_patches, const pco_ghost_item *items, int n_items,
+                      const uint8_t *wall_mask, const pco_swe_params *prm, double max_dt,
+                      double t_end, double *dt_out, int n_threads) {
+  double *nbmin = (double *)malloc(sizeof(double) * (size_t)n_patches);
+  char *active = (char *)calloc((size_t)n_patches, 1);
+  double *maxdt = (double *)malloc(sizeof(double) * (size_t)n_patches);
+  for (int p = 0; p < n_patches; p++) nbmin[p] = INFINITY;
+  for (int k = 0; k < n_items; k++) {
+    double tu = pco_time_unew(patches[items[k].src]);
+    if (tu < nbmin[items[k].dst]) nbmin[items[k].dst] = tu;
+  }
+  int n_active = 0;
+  for (int p = 0; p < n_patches; p++) {
+    pco_patch *pp = patches[p];
+    dt_out[p] = 0.0;
+    if (!pp->is_leaf) continue;
+    double tu = pco_time_unew(pp);
+    double rem = t_end - tu;
+    maxdt[p] = rem < max_dt ? rem : max_dt;
+    active[p] = tl_greater(maxdt[p], 0.0) && !tl_greater(tu, nbmin[p]);
+    n_active += active[p];
+  }
+  for (int k = 0; k < n_items; k++) {
+    const pco_ghost_item *it = &items[k];
+    if (!active[it->dst]) continue;
+    pco_patch *src = patches[it->src], *dst = patches[it->dst];
+    if (it->kind == PCO_GHOST_COPY)
+      pco_transfer_ghostlayer(it->size, it->src_offset, it->dst_offset, src, dst);
+    else
+      pco_interpolate(it->size, it->dst_offset, src, dst, 1, 0, 1, 1);
+  }
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+  for (int p = 0; p < n_patches; p++) {
+    pco_patch *pp = patches[p];
+    if (!active[p]) continue;
+    pco_copy_unew_to_uold(pp);
+    fill_walls(pp, wall_mask ? wall_mask[p] : 0);
+    int64_t A = (int64_t)(pp->nx + 2) * (pp->ny + 2);
+    double *net = (double *)malloc(sizeof(double) * 3 * A);
+    double own = pco_swe_compute_net_updates(pp, prm, net, NULL);
+    double dt = fmin(own, maxdt[p]);
+    pco_swe_update_unknowns(pp, prm, net, dt);
+    pco_swap_unew_uold(pp);
+    if (tl_greater(dt, 0.0)) {
+      pp->time = pp->time + pp->dt;
+      pp->dt = dt;
+    }
+    pp->est_next = own;
+    dt_out[p] = dt;
+    free(net);
+  }
+  free(nbmin);
+  free(active);
+  free(maxdt);
+  return n_active;
+}
+

@@ -136,6 +136,10 @@ double pco_overlap_area(const double p1[2], const double s1[2],
  * fill ghost layers (items in order, then walls), compute every leaf patch's
  * net updates and own CFL dt, dt = min(max_dt, min over the patches of each
  * group), update every leaf patch with its group's dt.  wall_mask bit (2*dim+upper). */
+/* One local-time-stepping grid iteration (see pcoracle.c). */
+int pco_grid_step_lts(pco_patch **patches, int n_patches, const pco_ghost_item *items, int n_items,
+                      const uint8_t *wall_mask, const pco_swe_params *prm, double max_dt,
+                      double t_end, double *dt_out, int n_threads);
 void pco_grid_step(pco_patch **patches, int n_patches,
                    const pco_ghost_item *items, int n_items,
                    const uint8_t *wall_mask, const int32_t *group, int n_groups,

@@ -147,6 +147,13 @@ struct pcg_context {
   // the time factor is 1); rescanned when fin_dirty
   int *d_fin = nullptr;
   bool fin_dirty = true;
+  // local time stepping (pcg_set_time_stepping): per-patch activity, max dt,
+  // dt taken, neighbours' minimal uNew time (order-preserving keys); per
+  // group minimal uNew time after the iteration
+  bool ts_local = false;
+  int *d_pact = nullptr;
+  double *d_pmaxdt = nullptr;
+  unsigned long long *d_pdt = nullptr, *d_nbmin = nullptr, *d_group_tmin = nullptr;
   double *d_dt_out = nullptr;
   double *h_pinned = nullptr;  // pinned scratch for small D2H/H2D
   std::vector<double> h_group_max_dt;
@@ -574,11 +581,12 @@ int enqueue_sweep(pcg_context *c) {
   if (c->sched.kind == PCG_SCHED_TILES)
     PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
-                          c->d_group_active, c->d_fin));
+                          c->d_group_active, c->d_fin, c->ts_local ? c->d_pact : nullptr));
   else
     PCG_CUDA(launch_sweep_strips(c->stream, c->sched.variant, c->strip_grid, c->slab, c->d_patches,
                                  c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
-                                 c->d_patch_smax, c->d_group_dt, c->d_group_active, c->d_fin));
+                                 c->d_patch_smax, c->d_group_dt, c->d_group_active, c->d_fin,
+                                 c->ts_local ? c->d_pact : nullptr));
   return PCG_OK;
 }
 
@@ -587,31 +595,48 @@ int enqueue_update(pcg_context *c) {
   if (c->sched.kind == PCG_SCHED_TILES)
     PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
                            (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
-                           c->d_group_active, c->d_fin));
+                           c->d_group_active, c->d_fin, c->ts_local ? c->d_pact : nullptr,
+                           c->ts_local ? c->d_pdt : nullptr));
   else
     PCG_CUDA(launch_update_strips(c->stream, c->update_grid, c->slab, c->d_patches, c->d_times,
                                   c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
-                                  c->d_patch_smax, c->d_group_dt, c->d_group_active, c->d_fin));
+                                  c->d_patch_smax, c->d_group_dt, c->d_group_active, c->d_fin,
+                                  c->ts_local ? c->d_pact : nullptr, c->ts_local ? c->d_pdt : nullptr));
   return PCG_OK;
 }
 
-// Enqueue one synchronous step (no synchronisation, capturable in BATCHED mode).
+// One local-time-stepping phase (0: activity, 1: dts, 2: group times).
+int enqueue_lts(pcg_context *c, int phase) {
+  PCG_CUDA(pcg::launch_lts(c->stream, phase, c->max_patches, c->max_groups, c->d_patches, c->d_times,
+                           c->d_items, (int)c->h_items.size(), c->d_nbmin, c->d_patch_smax,
+                           c->d_group_tmin, c->d_group_dt, c->d_group_max_dt, c->d_group_t_end,
+                           c->d_group_active, c->d_pact, c->d_pmaxdt, c->d_pdt, c->d_group_time, c->prm));
+  return PCG_OK;
+}
+
+// Enqueue one synchronous step (no synchronisation, capturable in BATCHED
+// mode); with local time stepping one iteration in which only the leaves
+// that may advance are filled and solved, each with its own dt.
 int enqueue_step(pcg_context *c, int mode) {
   using namespace pcg;
   PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_t_end, c->d_group_time,
                         c->d_group_dt, c->d_group_active, c->max_patches,
                         c->d_patch_smax));
+  int rc;
   if (mode == PCG_MODE_BATCHED) {
+    const int *pact = c->ts_local ? c->d_pact : nullptr;
+    if (c->ts_local && (rc = enqueue_lts(c, 0)) != PCG_OK) return rc;
     PCG_CUDA(launch_item_step(c->stream, c->d_patches, c->d_times, c->d_items, (int)c->h_items.size(),
                               c->d_item_step));
     PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
                                 c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step,
-                                c->d_group_active, c->d_fin));
+                                c->d_group_active, c->d_fin, pact));
     PCG_CUDA(launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(),
-                          c->d_group_active));
-    int rc;
+                          c->d_group_active, pact));
     if ((rc = enqueue_sweep(c)) != PCG_OK) return rc;
+    if (c->ts_local && (rc = enqueue_lts(c, 1)) != PCG_OK) return rc;
     if ((rc = enqueue_update(c)) != PCG_OK) return rc;
+    if (c->ts_local) return enqueue_lts(c, 2);
   } else {
     for (int p : c->leaf_ids)
       PCG_CUDA(launch_fill_patch(c->stream, c->slab, c->d_patches, c->d_times, c->d_items,
@@ -630,7 +655,7 @@ int enqueue_step(pcg_context *c, int mode) {
     }
     c->fin_dirty = true;
   }
-  int rc = enqueue_post_update(c);
+  rc = enqueue_post_update(c);
   if (rc != PCG_OK) return rc;
   PCG_CUDA(launch_group_advance(c->stream, c->max_groups, c->d_group_dt, c->d_group_active,
                                 c->d_group_time));
@@ -749,6 +774,12 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->d_group_active, sizeof(int) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_fin, sizeof(int) * c->max_patches));
   CREATE_CK(cudaMemset(c->d_fin, 0, sizeof(int) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_pact, sizeof(int) * c->max_patches));
+  CREATE_CK(cudaMemset(c->d_pact, 0, sizeof(int) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_pmaxdt, sizeof(double) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_pdt, sizeof(unsigned long long) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_nbmin, sizeof(unsigned long long) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_group_tmin, sizeof(unsigned long long) * c->max_groups));
   {
     std::vector<double> inf(c->max_groups, HUGE_VAL), zero(c->max_groups, 0.0);
     CREATE_CK(cudaMemcpy(c->d_group_t_end, inf.data(), sizeof(double) * c->max_groups, cudaMemcpyHostToDevice));
@@ -779,6 +810,11 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_group_time);
   cudaFree(c->d_group_active);
   cudaFree(c->d_fin);
+  cudaFree(c->d_pact);
+  cudaFree(c->d_pmaxdt);
+  cudaFree(c->d_pdt);
+  cudaFree(c->d_nbmin);
+  cudaFree(c->d_group_tmin);
   cudaFree(c->d_dt_out);
   cudaFree(c->d_items);
   cudaFree(c->d_gcells);
@@ -1345,6 +1381,27 @@ static int check_solvable(pcg_context *c) {
   return PCG_OK;
 }
 
+// Local time stepping runs in the batched form only, without flux-correction
+// or restriction lists (those follow the synchronous step of a group).
+static int check_mode(pcg_context *c, int mode) {
+  if (!c->ts_local) return PCG_OK;
+  if (mode != PCG_MODE_BATCHED) return fail(PCG_E_STATE, "local time stepping runs in the batched form only");
+  if (!c->h_flux.empty() || !c->h_restr.empty())
+    return fail(PCG_E_STATE, "local time stepping takes no flux-correction or restriction lists");
+  return PCG_OK;
+}
+
+int pcg_set_time_stepping(pcg_context *c, int32_t mode) {
+  if (!c || (mode != PCG_TS_GLOBAL && mode != PCG_TS_LOCAL)) return fail(PCG_E_INVALID, "bad time-stepping mode");
+  std::lock_guard<std::mutex> lk(c->mu);
+  const bool local = mode == PCG_TS_LOCAL;
+  if (local != c->ts_local) {
+    c->ts_local = local;
+    c->graph_valid = false;
+  }
+  return PCG_OK;
+}
+
 int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
   if (!c || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED)) return fail(PCG_E_INVALID, "bad mode");
   std::lock_guard<std::mutex> lk(c->mu);
@@ -1352,6 +1409,7 @@ int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
+  if ((rc = check_mode(c, mode)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
   if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
@@ -1378,6 +1436,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
+  if ((rc = check_mode(c, mode)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
   if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   if (steps > c->hist_cap) {
@@ -1477,6 +1536,7 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
+  if ((rc = check_mode(c, PCG_MODE_BATCHED)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
   if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   std::vector<pcg_schedule> cand;
@@ -1529,6 +1589,7 @@ int pcg_stats(pcg_context *c, int64_t *cell_updates, double *device_ms) {
 int pcg_profile_step(pcg_context *c, double *ms) {
   if (!c || !ms) return fail(PCG_E_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(c->mu);
+  if (c->ts_local) return fail(PCG_E_STATE, "the phase profile times the global step only");
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;

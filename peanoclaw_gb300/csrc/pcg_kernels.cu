@@ -161,12 +161,14 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
     k_sweep_tiles(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                   const TileItem *__restrict__ tiles, int first, int count, SweParamsDev prm,
                   unsigned long long *__restrict__ patch_smax,
-                  unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active, int *__restrict__ fin) {
+                  unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active, int *__restrict__ fin,
+                  const int *__restrict__ pact) {
   __shared__ SweepSmem S;
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
     TileItem ti = tiles[first + it];
     PatchDev P = patches[ti.pid];
     if (group_active && !group_active[P.group]) continue;
+    if (pact && !pact[ti.pid]) continue;
     double nh = 0, nhu = 0, nhv = 0;
     double smax = sweep_tile(S, slab, P, prm, ti.x0, ti.y0, ti.tw, ti.th, true, nh, nhu, nhv);
     int t = threadIdx.x;
@@ -193,12 +195,15 @@ __global__ void __launch_bounds__(kSweepThreads)
                    PatchTimeDev *__restrict__ times, const TileItem *__restrict__ tiles, int first,
                    int count, SweParamsDev prm, const unsigned long long *__restrict__ patch_smax,
                    const unsigned long long *__restrict__ group_dt,
-                   const int *__restrict__ group_active, int *__restrict__ fin) {
+                   const int *__restrict__ group_active, int *__restrict__ fin,
+                   const int *__restrict__ pact,
+                   const unsigned long long *__restrict__ pdt) {
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
     TileItem ti = tiles[first + it];
     PatchDev P = patches[ti.pid];
     if (group_active && !group_active[P.group]) continue;
-    double dt = bitsd(group_dt[P.group]);
+    if (pact && !pact[ti.pid]) continue;
+    double dt = bitsd(pdt ? pdt[ti.pid] : group_dt[P.group]);
     int t = threadIdx.x;
     if (t < ti.tw * ti.th) {
       int x = ti.x0 + t / ti.th, y = ti.y0 + t % ti.th;
@@ -250,6 +255,101 @@ __global__ void k_group_advance(int n_groups, const unsigned long long *__restri
                                 const int *__restrict__ group_active, double *__restrict__ group_time) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n_groups && group_active[i]) group_time[i] = __dadd_rn(group_time[i], bitsd(group_dt[i]));
+}
+
+// ---------------------------------------------------------------------------
+// Local time stepping (one grid iteration in two phases; see pcg.h):
+// order-preserving keys of doubles for integer atomicMin over any sign.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long okey(double x) {
+  const unsigned long long b = dbits(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unokey(unsigned long long k) {
+  return (k >> 63) ? bitsd(k & 0x7FFFFFFFFFFFFFFFull) : bitsd(~k);
+}
+
+__global__ void k_lts_begin(int n_patches, unsigned long long *__restrict__ nbmin,
+                            unsigned long long *__restrict__ patch_smax, int n_groups,
+                            unsigned long long *__restrict__ group_tmin,
+                            unsigned long long *__restrict__ group_dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int k = i; k < n_patches; k += gridDim.x * blockDim.x) {
+    nbmin[k] = okey(INFINITY);
+    patch_smax[k] = 0ull;
+  }
+  if (i < n_groups) {
+    group_tmin[i] = okey(INFINITY);
+    group_dt[i] = dbits(INFINITY);
+  }
+}
+
+// Minimal uNew time of the ghost-item sources of every destination.
+__global__ void k_lts_nbmin(const GhostItemDev *__restrict__ items, int count,
+                            const PatchDev *__restrict__ patches, const PatchTimeDev *__restrict__ times,
+                            unsigned long long *__restrict__ nbmin) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    const GhostItemDev it = items[k];
+    atomicMin(&nbmin[it.dst], okey(time_unew(patches[it.src], times[it.src])));
+  }
+}
+
+// Which leaves advance: the end time is not reached (max_dt = min(group
+// max_dt, end time - uNew time) > tarch eps) and uNew time does not exceed
+// the neighbours' minimal uNew time by more than eps
+// (TimeIntervals::isAllowedToAdvanceInTime / isBlockedByNeighbors).
+__global__ void k_lts_activity(const PatchDev *__restrict__ patches, const PatchTimeDev *__restrict__ times,
+                               int n_patches, const unsigned long long *__restrict__ nbmin,
+                               const double *__restrict__ group_max_dt, const double *__restrict__ group_t_end,
+                               const int *__restrict__ group_active, int *__restrict__ pact,
+                               double *__restrict__ pmaxdt) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_patches; p += gridDim.x * blockDim.x) {
+    const PatchDev P = patches[p];
+    if (P.nx <= 0 || !is_leaf(P)) {
+      pact[p] = 0;
+      continue;
+    }
+    const double tu = time_unew(P, times[p]);
+    const double rem = __dsub_rn(group_t_end[P.group], tu);
+    const double mx = group_max_dt[P.group];
+    const double maxdt = rem < mx ? rem : mx;
+    pact[p] = group_active[P.group] && tl_greater(maxdt, 0.0) && !tl_greater(tu, unokey(nbmin[p]));
+    pmaxdt[p] = maxdt;
+  }
+}
+
+// dt of every advancing leaf (min of its block CFL dt and its max_dt), the
+// group's minimal dt taken and minimal uNew time after the step.
+__global__ void k_lts_dt(const PatchDev *__restrict__ patches, const PatchTimeDev *__restrict__ times,
+                         int n_patches, const int *__restrict__ pact, const double *__restrict__ pmaxdt,
+                         const unsigned long long *__restrict__ patch_smax, SweParamsDev prm,
+                         unsigned long long *__restrict__ pdt, unsigned long long *__restrict__ group_dt,
+                         unsigned long long *__restrict__ group_tmin) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_patches; p += gridDim.x * blockDim.x) {
+    const PatchDev P = patches[p];
+    if (P.nx <= 0 || !is_leaf(P)) continue;
+    const PatchTimeDev T = times[p];
+    double tnext = time_unew(P, T);
+    if (pact[p]) {
+      const double own = cfl_dt(prm, bitsd(patch_smax[p]), subcell(P, 0), subcell(P, 1));
+      const double dt = fmin(own, pmaxdt[p]);
+      pdt[p] = dbits(dt);
+      atomicMin(&group_dt[P.group], dbits(dt));
+      if (tl_greater(dt, 0.0)) tnext = __dadd_rn(__dadd_rn(T.time, T.dt), dt);
+    }
+    atomicMin(&group_tmin[P.group], okey(tnext));
+  }
+}
+
+// End of an iteration: group time = minimal uNew time of its leaves; the
+// recorded dt of a group without an advancing leaf is 0.
+__global__ void k_lts_end(int n_groups, const unsigned long long *__restrict__ group_tmin,
+                          double *__restrict__ group_time, unsigned long long *__restrict__ group_dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_groups) return;
+  const double t = unokey(group_tmin[i]);
+  if (t != INFINITY) group_time[i] = t;
+  if (bitsd(group_dt[i]) == INFINITY) group_dt[i] = dbits(0.0);
 }
 
 // Record the dt of every group after a step.
@@ -508,12 +608,14 @@ __global__ void __launch_bounds__(256)
                   int ncopy, int ninterp, const CopyPlanDev *__restrict__ copy_plan,
                   const InterpPlanDev *__restrict__ plan,
                   const GhostItemStepDev *__restrict__ item_step,
-                  const int *__restrict__ group_active, const int *__restrict__ fin) {
+                  const int *__restrict__ group_active, const int *__restrict__ fin,
+                  const int *__restrict__ pact) {
   const int total = ncopy + ninterp;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     if (e < ncopy) {
       const CopyPlanDev pl = copy_plan[e];
       if (group_active && !group_active[patches[pl.dst_pid].group]) continue;
+      if (pact && !pact[pl.dst_pid]) continue;
       const GhostItemStepDev I = item_step[pl.item];
       double vn[3], vo[3];
       const int nq = I.nq < 3 ? I.nq : 3;
@@ -538,6 +640,7 @@ __global__ void __launch_bounds__(256)
     const GhostItemDev it = items[gc.item];
     const PatchDev S = patches[it.src], D = patches[it.dst];
     if (group_active && !group_active[D.group]) continue;
+    if (pact && !pact[it.dst]) continue;
     const InterpPlanDev pl = plan[e - ncopy];
     const GhostItemStepDev I = item_step[gc.item];
     const double tf = I.tf, one_m_tf = I.itf;
@@ -636,7 +739,7 @@ __device__ __forceinline__ void wall_face(double *slab, const PatchDev &P, int d
 // (0,lower), (1,upper), (0,upper), (1,lower).  One warp per patch.
 __global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                         const int *__restrict__ wall_patches, int count,
-                        const int *__restrict__ group_active) {
+                        const int *__restrict__ group_active, const int *__restrict__ pact) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -644,6 +747,7 @@ __global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ 
   for (int w = warp; w < count; w += nwarps) {
     PatchDev P = patches[wall_patches[w]];
     if (group_active && !group_active[P.group]) continue;
+    if (pact && !pact[wall_patches[w]]) continue;
     for (int f = 0; f < 4; f++) {
       int d = order[f][0], up = order[f][1];
       if (P.wall & (1 << (2 * d + up))) wall_face(slab, P, d, up, true, lane, 32);
@@ -1125,20 +1229,21 @@ __global__ void k_refinement_indicator(const double *__restrict__ slab, const Pa
 cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                          const TileItem *tiles, int first, int count, const SweParamsDev &prm,
                          unsigned long long *patch_smax, unsigned long long *group_dt,
-                         const int *group_active, int *fin) {
+                         const int *group_active, int *fin, const int *pact) {
   if (count <= 0) return cudaSuccess;
   k_sweep_tiles<<<grid, kSweepThreads, 0, st>>>(slab, patches, tiles, first, count, prm, patch_smax,
-                                                group_dt, group_active, fin);
+                                                group_dt, group_active, fin, pact);
   return cudaGetLastError();
 }
 
 cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                           PatchTimeDev *times, const TileItem *tiles, int first, int count,
                           const SweParamsDev &prm, const unsigned long long *patch_smax,
-                          const unsigned long long *group_dt, const int *group_active, int *fin) {
+                          const unsigned long long *group_dt, const int *group_active, int *fin,
+                          const int *pact, const unsigned long long *pdt) {
   if (count <= 0) return cudaSuccess;
   k_update_tiles<<<grid, kSweepThreads, 0, st>>>(slab, patches, times, tiles, first, count, prm,
-                                                 patch_smax, group_dt, group_active, fin);
+                                                 patch_smax, group_dt, group_active, fin, pact, pdt);
   return cudaGetLastError();
 }
 
@@ -1152,6 +1257,35 @@ cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_
   if (grid < 1) grid = 1;
   k_reset_step<<<grid, 256, 0, st>>>(n_groups, group_max_dt, group_t_end, group_time, group_dt,
                                      group_active, n_patches, patch_smax);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lts(cudaStream_t st, int phase, int n_patches, int n_groups, const PatchDev *patches,
+                       const PatchTimeDev *times, const GhostItemDev *items, int n_items,
+                       unsigned long long *nbmin, unsigned long long *patch_smax,
+                       unsigned long long *group_tmin, unsigned long long *group_dt,
+                       const double *group_max_dt, const double *group_t_end, const int *group_active,
+                       int *pact, double *pmaxdt, unsigned long long *pdt, double *group_time,
+                       const SweParamsDev &prm) {
+  const int np = n_patches > 0 ? n_patches : 1;
+  const int gp = (np + 255) / 256 < 1024 ? (np + 255) / 256 : 1024;
+  switch (phase) {
+    case 0:
+      k_lts_begin<<<gp, 256, 0, st>>>(n_patches, nbmin, patch_smax, n_groups, group_tmin, group_dt);
+      if (n_items > 0)
+        k_lts_nbmin<<<(n_items + 255) / 256 < 4096 ? (n_items + 255) / 256 : 4096, 256, 0, st>>>(
+            items, n_items, patches, times, nbmin);
+      k_lts_activity<<<gp, 256, 0, st>>>(patches, times, n_patches, nbmin, group_max_dt, group_t_end,
+                                         group_active, pact, pmaxdt);
+      break;
+    case 1:
+      k_lts_dt<<<gp, 256, 0, st>>>(patches, times, n_patches, pact, pmaxdt, patch_smax, prm, pdt, group_dt,
+                                   group_tmin);
+      break;
+    default:
+      k_lts_end<<<(n_groups + 127) / 128, 128, 0, st>>>(n_groups, group_tmin, group_time, group_dt);
+      break;
+  }
   return cudaGetLastError();
 }
 
@@ -1193,13 +1327,13 @@ cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *pa
                                const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
                                int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
                                const GhostItemStepDev *item_step, const int *group_active,
-                               const int *fin) {
+                               const int *fin, const int *pact) {
   int total = ncopy + ninterp;
   if (total <= 0) return cudaSuccess;
   int grid = (total + 255) / 256;
   if (grid > 152 * 32) grid = 152 * 32;
   k_ghost_cells<<<grid, 256, 0, st>>>(slab, patches, items, cells, ncopy, ninterp, copy_plan, plan,
-                                      item_step, group_active, fin);
+                                      item_step, group_active, fin, pact);
   return cudaGetLastError();
 }
 
@@ -1222,11 +1356,12 @@ cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const Pat
 }
 
 cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
-                         const int *wall_patches, int count, const int *group_active) {
+                         const int *wall_patches, int count, const int *group_active,
+                         const int *pact) {
   if (count <= 0) return cudaSuccess;
   int grid = (count + 7) / 8;
   if (grid > 152 * 16) grid = 152 * 16;
-  k_walls<<<grid, 256, 0, st>>>(slab, patches, wall_patches, count, group_active);
+  k_walls<<<grid, 256, 0, st>>>(slab, patches, wall_patches, count, group_active, pact);
   return cudaGetLastError();
 }
 

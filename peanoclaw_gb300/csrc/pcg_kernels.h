@@ -16,16 +16,27 @@ namespace pcg {
 cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                          const TileItem *tiles, int first, int count, const SweParamsDev &prm,
                          unsigned long long *patch_smax, unsigned long long *group_dt,
-                         const int *group_active, int *fin = nullptr);
+                         const int *group_active, int *fin = nullptr, const int *pact = nullptr);
 cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                           PatchTimeDev *times, const TileItem *tiles, int first, int count,
                           const SweParamsDev &prm, const unsigned long long *patch_smax,
                           const unsigned long long *group_dt, const int *group_active,
-                          int *fin = nullptr);
+                          int *fin = nullptr, const int *pact = nullptr,
+                          const unsigned long long *pdt = nullptr);
 cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_dt,
                          const double *group_t_end, const double *group_time,
                          unsigned long long *group_dt, int *group_active, int n_patches,
                          unsigned long long *patch_smax);
+// Local time stepping phases: 0 = neighbour constraints and activity (before
+// the ghost fill), 1 = per-leaf dt (after the sweep), 2 = group time and dt
+// (after the update).
+cudaError_t launch_lts(cudaStream_t st, int phase, int n_patches, int n_groups, const PatchDev *patches,
+                       const PatchTimeDev *times, const GhostItemDev *items, int n_items,
+                       unsigned long long *nbmin, unsigned long long *patch_smax,
+                       unsigned long long *group_tmin, unsigned long long *group_dt,
+                       const double *group_max_dt, const double *group_t_end, const int *group_active,
+                       int *pact, double *pmaxdt, unsigned long long *pdt, double *group_time,
+                       const SweParamsDev &prm);
 cudaError_t launch_group_advance(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
                                  const int *group_active, double *group_time);
 cudaError_t launch_record_dt(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
@@ -40,7 +51,7 @@ cudaError_t launch_ghost_cells(cudaStream_t st, double *slab, const PatchDev *pa
                                const GhostItemDev *items, const GhostCellDev *cells, int ncopy,
                                int ninterp, const CopyPlanDev *copy_plan, const InterpPlanDev *plan,
                                const GhostItemStepDev *item_step, const int *group_active,
-                               const int *fin);
+                               const int *fin, const int *pact = nullptr);
 cudaError_t launch_scan_fin(cudaStream_t st, const double *slab, const PatchDev *patches, int count,
                             int *fin);
 cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
@@ -48,7 +59,8 @@ cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, con
 cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
                              const GhostItemDev *items, int count, GhostItemStepDev *out);
 cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
-                         const int *wall_patches, int count, const int *group_active);
+                         const int *wall_patches, int count, const int *group_active,
+                         const int *pact = nullptr);
 cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,
                               const PatchTimeDev *times, const GhostItemDev *items, int first,
                               int count, int pid, const int *group_active = nullptr);
@@ -103,7 +115,7 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
                                 const PatchDev *patches, const StripItem *items,
                                 const StripGroup *groups, int count, const SweParamsDev &prm,
                                 unsigned long long *patch_smax, unsigned long long *group_dt,
-                                const int *group_active, int *fin);
+                                const int *group_active, int *fin, const int *pact = nullptr);
 cudaError_t strip_occupancy(int variant, int *blocks_per_sm);
 cudaError_t update_strips_occupancy(int *blocks_per_sm);
 cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
@@ -111,6 +123,7 @@ cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const 
                                  int count, const SweParamsDev &prm,
                                  const unsigned long long *patch_smax,
                                  const unsigned long long *group_dt, const int *group_active,
-                                 int *fin);
+                                 int *fin, const int *pact = nullptr,
+                                 const unsigned long long *pdt = nullptr);
 
 }  // namespace pcg

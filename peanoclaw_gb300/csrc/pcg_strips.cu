@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
                    const StripItem *__restrict__ items, const StripGroup *__restrict__ groups,
                    int count, SweParamsDev prm, unsigned long long *__restrict__ patch_smax,
                    unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active,
-                   int *__restrict__ fin) {
+                   int *__restrict__ fin, const int *__restrict__ pact) {
   __shared__ StripWarpSmem SM[kWarps];
   __shared__ StripLaneSmem LS[kWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     const bool in_group = gi < G;
     const StripGroup SG = groups[I.g0 + (in_group ? gi : 0)];
     const PatchDev P = patches[SG.pid];
-    const bool act = in_group && (!group_active || group_active[P.group]);
+    const bool act = in_group && (!group_active || group_active[P.group]) && (!pact || pact[SG.pid]);
     const int y = SG.y0 + j;
 
     // ---- boundary rows: lane l < G*w takes (group l / w, column l % w)
@@ -213,7 +213,8 @@ __global__ void __launch_bounds__(kWarps * 32)
                     const StripGroup *__restrict__ groups, int count, SweParamsDev prm,
                     const unsigned long long *__restrict__ patch_smax,
                     const unsigned long long *__restrict__ group_dt,
-                    const int *__restrict__ group_active, int *__restrict__ fin) {
+                    const int *__restrict__ group_active, int *__restrict__ fin,
+                    const int *__restrict__ pact, const unsigned long long *__restrict__ pdt) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int it = blockIdx.x * kWarps + wid; it < count; it += gridDim.x * kWarps) {
     const StripItem I = items[it];
@@ -223,7 +224,8 @@ __global__ void __launch_bounds__(kWarps * 32)
     const StripGroup SG = groups[I.g0 + gi];
     const PatchDev P = patches[SG.pid];
     if (group_active && !group_active[P.group]) continue;
-    const double dt = bitsd(group_dt[P.group]);
+    if (pact && !pact[SG.pid]) continue;
+    const double dt = bitsd(pdt ? pdt[SG.pid] : group_dt[P.group]);
     const int y = SG.y0 + j;
     const long long vn = vol_new(P), vo = vol_old(P);
     long long in0 = idx_unew(P, 0, SG.x0, y), io0 = idx_uold(P, 0, SG.x0, y);
@@ -277,11 +279,12 @@ template <int kWarps, int kMinBlocks>
 cudaError_t sweep_strips_t(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                            const StripItem *items, const StripGroup *groups, int count,
                            const SweParamsDev &prm, unsigned long long *patch_smax,
-                           unsigned long long *group_dt, const int *group_active, int *fin) {
+                           unsigned long long *group_dt, const int *group_active, int *fin,
+                           const int *pact) {
   if (count <= 0) return cudaSuccess;
   k_sweep_strips<kWarps, kMinBlocks><<<grid, kWarps * 32, 0, st>>>(slab, patches, items, groups, count,
                                                                    prm, patch_smax, group_dt,
-                                                                   group_active, fin);
+                                                                   group_active, fin, pact);
   return cudaGetLastError();
 }
 
@@ -296,13 +299,13 @@ cudaError_t launch_sweep_strips(cudaStream_t st, int variant, int grid, double *
                                 const PatchDev *patches, const StripItem *items,
                                 const StripGroup *groups, int count, const SweParamsDev &prm,
                                 unsigned long long *patch_smax, unsigned long long *group_dt,
-                                const int *group_active, int *fin) {
+                                const int *group_active, int *fin, const int *pact) {
   switch (variant) {
-    case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
-    case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
-    case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
-    case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
-    case 4: return sweep_strips_t<6, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin);
+    case 0: return sweep_strips_t<4, 4>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin, pact);
+    case 1: return sweep_strips_t<4, 5>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin, pact);
+    case 2: return sweep_strips_t<8, 2>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin, pact);
+    case 3: return sweep_strips_t<8, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin, pact);
+    case 4: return sweep_strips_t<6, 3>(st, grid, slab, patches, items, groups, count, prm, patch_smax, group_dt, group_active, fin, pact);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -327,10 +330,10 @@ cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const 
                                  int count, const SweParamsDev &prm,
                                  const unsigned long long *patch_smax,
                                  const unsigned long long *group_dt, const int *group_active,
-                                 int *fin) {
+                                 int *fin, const int *pact, const unsigned long long *pdt) {
   if (count <= 0) return cudaSuccess;
   k_update_strips<8><<<grid, 256, 0, st>>>(slab, patches, times, items, groups, count, prm, patch_smax,
-                                           group_dt, group_active, fin);
+                                           group_dt, group_active, fin, pact, pdt);
   return cudaGetLastError();
 }
 

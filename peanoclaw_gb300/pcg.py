@@ -68,6 +68,8 @@ class Schedule(C.Structure):
 
 SCHED_TILES = 0
 SCHED_STRIPS = 1
+TS_GLOBAL = 0
+TS_LOCAL = 1
 
 
 # every entry point declared in include/pcg.h: name -> (restype, argtypes)
@@ -105,6 +107,7 @@ SIGNATURES = {
     "pcg_set_ghost_items": (C.c_int, [_CTX, C.POINTER(GhostItem), C.c_int32]),
     "pcg_set_group_max_dt": (C.c_int, [_CTX, C.c_int32, C.c_double]),
     "pcg_set_group_end_time": (C.c_int, [_CTX, C.c_int32, C.c_double, C.c_double]),
+    "pcg_set_time_stepping": (C.c_int, [_CTX, C.c_int32]),
     "pcg_get_group_times": (C.c_int, [_CTX, _D]),
     "pcg_set_restriction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, C.c_int32]),
     "pcg_set_flux_correction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, _I2, _I2, C.c_double]),
@@ -337,6 +340,11 @@ class Context:
     def set_group_end_time(self, group, time, t_end):
         """Device-side end time of a group (see pcg_set_group_end_time)."""
         check(lib().pcg_set_group_end_time(self.h, group, float(time), float(t_end)))
+
+    def set_time_stepping(self, mode):
+        """TS_GLOBAL (synchronous steps) or TS_LOCAL (local time stepping,
+        batched form; see pcg_set_time_stepping)."""
+        check(lib().pcg_set_time_stepping(self.h, int(mode)))
 
     def group_times(self):
         out = np.zeros(self.max_groups)

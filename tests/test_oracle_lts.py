@@ -1,0 +1,56 @@
+"""The oracle's local-time-stepping iteration (pco_grid_step_lts) on the CPU:
+with max_dt below every CFL dt it is the synchronous step; otherwise every
+leaf reaches the end time exactly, no advancing leaf lies ahead of its ghost
+sources, and fewer cell updates are spent than with the synchronous step."""
+import numpy as np
+
+from helpers import oracle_params, oracle_patchset
+from oracle import oracle as O
+from peanoclaw_gb300 import pcg as P
+from peanoclaw_gb300 import scenarios as S
+
+PRM = P.swe_params(g=9.81, cfl=0.5)
+
+
+def _tu(p):
+    return p.s.time + p.s.dt
+
+
+def test_small_max_dt_is_the_synchronous_step():
+    ps = S.uneven_patches(grid=4, sizes=(8, 16))
+    prm = oracle_params(PRM)
+    a, b = oracle_patchset(ps), oracle_patchset(ps)
+    for _ in range(5):
+        dt = O.grid_step(a, ps.items, ps.wall, prm, 1e-5)[0]
+        n, dto = O.grid_step_lts(b, ps.items, ps.wall, prm, 1e-5, np.inf)
+        assert dt == 1e-5 and n == len(b) and np.all(dto == 1e-5)
+    for p, q in zip(a, b):
+        assert np.array_equal(p.u.view(np.int64), q.u.view(np.int64))
+        assert (p.s.time, p.s.dt) == (q.s.time, q.s.dt)
+
+
+def test_every_leaf_reaches_the_end_time_without_running_ahead():
+    ps = S.uneven_patches(grid=5, sizes=(8, 16, 32))
+    prm = oracle_params(PRM)
+    pats = oracle_patchset(ps)
+    t_end = 0.02
+    src = {}
+    for it in ps.items:
+        src.setdefault(int(it[2]), set()).add(int(it[1]))
+    lts_updates = 0
+    for _ in range(1000):
+        before = [_tu(p) for p in pats]
+        n, dto = O.grid_step_lts(pats, ps.items, ps.wall, prm, np.inf, t_end)
+        if n == 0:
+            break
+        for p in np.flatnonzero(dto > 0.0):
+            # an advancing leaf was not ahead of any source (time tolerance 1e-8)
+            assert all(before[p] <= before[s] + 1e-8 for s in src.get(int(p), ()))
+            lts_updates += ps.n[p] ** 2
+    assert all(_tu(p) == t_end for p in pats)
+    glob = oracle_patchset(ps)
+    t, steps = 0.0, 0
+    while t < t_end:
+        t += O.grid_step(glob, ps.items, ps.wall, prm, t_end - t)[0]
+        steps += 1
+    assert lts_updates < steps * sum(n * n for n in ps.n)
