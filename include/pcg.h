@@ -285,16 +285,31 @@ int pcg_synchronize(pcg_context *ctx);
  * those leaves only (time-interpolated from their sources,
  * DefaultTransfer.cpph:27-50), and solves each of them with its own dt =
  * min(block CFL dt, group max_dt, end time - uNew time) (SolveTimestep.cpp:
- * 591-700).  The recorded dt of a group is the minimal dt taken by its
- * leaves in the iteration (0 if none advanced); its time
- * (pcg_get_group_times) becomes the minimal uNew time of its leaves.  The
- * end time of pcg_set_group_end_time bounds every leaf.  Local time stepping
- * runs in the BATCHED form only and takes no flux-correction or restriction
- * lists (PCG_E_STATE otherwise); PCG_TS_GLOBAL (default) is the synchronous
- * step. */
+ * 591-700).  A source's time constraint is its time + dt
+ * (TimeIntervals::getTimeConstraint); before the decision every virtual
+ * patch of the pcg_set_virtual_time_items list takes the intersection of
+ * its leaves' time intervals, and after the update the restriction list
+ * (pcg_set_restriction_items) refills the virtual patches, so coarse leaves
+ * next to a refined region wait for its finest leaves and read their data
+ * through the virtual patches (GridLevelTransfer.cpp:108-275).  The recorded
+ * dt of a group is the minimal dt taken by its leaves in the iteration (0 if
+ * none advanced); its time (pcg_get_group_times) becomes the minimal uNew
+ * time of its leaves.  The end time of pcg_set_group_end_time bounds every
+ * leaf.  Local time stepping runs in the BATCHED form only and takes no
+ * flux-correction list (PCG_E_STATE otherwise); PCG_TS_GLOBAL (default) is
+ * the synchronous step. */
 #define PCG_TS_GLOBAL 0
 #define PCG_TS_LOCAL 1
 int pcg_set_time_stepping(pcg_context *ctx, int32_t mode);
+/* (leaf[k], virt[k]) pairs, each leaf against every virtual ancestor: in
+ * local time stepping each listed virtual patch's time interval becomes,
+ * before every iteration, time = the maximal time of its leaves and dt =
+ * their minimal time + dt minus that time (GridLevelTransfer::stepUp,
+ * GridLevelTransfer.cpp:408-431; TimeIntervals::updateMinimalFineGridTimeInterval,
+ * TimeIntervals.cpp:214-231; Patch.cpp:388-397).  Unused by the synchronous
+ * step.  PCG_E_STATE at the next step if a pair does not join a leaf to a
+ * non-leaf patch. */
+int pcg_set_virtual_time_items(pcg_context *ctx, int32_t n, const int32_t *leaf, const int32_t *virt);
 
 /* --------------------------------------------- batched schedule + autotuner */
 

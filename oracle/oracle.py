@@ -89,7 +89,8 @@ def lib():
         L.pco_grid_step_lts.restype = C.c_int
         L.pco_grid_step_lts.argtypes = [C.POINTER(P), C.c_int, C.POINTER(PcoGhostItem), C.c_int,
                                         C.POINTER(C.c_uint8), C.POINTER(PcoSweParams), C.c_double,
-                                        C.c_double, D, C.c_int]
+                                        C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int,
+                                        D, C.c_int]
         _lib = L
     return _lib
 
@@ -252,15 +253,23 @@ def grid_fill(patches, items, wall_mask):
                         wm.ctypes.data_as(C.POINTER(C.c_uint8)))
 
 
-def grid_step_lts(patches, items, wall_mask, prm, max_dt, t_end, n_threads=0):
-    """One local-time-stepping iteration; returns (number advanced, dt per patch)."""
+def grid_step_lts(patches, items, wall_mask, prm, max_dt, t_end, virtual_time_items=None,
+                  n_threads=0):
+    """One local-time-stepping iteration; returns (number advanced, dt per
+    patch).  virtual_time_items: (N, 2) (leaf, virtual ancestor) pairs whose
+    intervals set the virtual patches' time intervals first."""
     P = C.POINTER(PcoPatch)
     parr = (P * len(patches))(*[C.pointer(p.s) for p in patches])
     it, keep = ghost_items(items)
     wm = np.ascontiguousarray(wall_mask, dtype=np.uint8)
+    vt = np.zeros((0, 2), dtype=np.int32) if virtual_time_items is None else \
+        np.ascontiguousarray(np.asarray(virtual_time_items, dtype=np.int32).reshape(-1, 2))
+    vl, vv = np.ascontiguousarray(vt[:, 0]), np.ascontiguousarray(vt[:, 1])
+    i32 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
     dto = np.zeros(len(patches))
     n = lib().pco_grid_step_lts(parr, len(patches), it, len(keep) if len(items) else 0,
                                 wm.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(prm), float(max_dt),
-                                float(t_end), dto.ctypes.data_as(C.POINTER(C.c_double)), n_threads)
+                                float(t_end), i32(vl), i32(vv), len(vt),
+                                dto.ctypes.data_as(C.POINTER(C.c_double)), n_threads)
     return n, dto
 

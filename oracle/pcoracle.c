@@ -860,19 +860,46 @@ void pco_grid_step(pco_patch **patches, int n_patches,
 /* layers of the advancing leaves are filled with the time factors of their */
 /* uNew time (DefaultTransfer / interpolation time interpolation); the       */
 /* leaves then step with dt = min(block CFL dt, max_dt).                     */
+/* A neighbour's time constraint is its time + dt (TimeIntervals::           */
+/* getTimeConstraint).  Virtual patches first take the intersection of the   */
+/* time intervals of their listed leaves (vt_leaf[k] -> vt_virt[k]): time =  */
+/* the maximal leaf time, dt = the minimal leaf time + dt minus that time    */
+/* (GridLevelTransfer::stepUp, GridLevelTransfer.cpp:408-431, with           */
+/* updateMinimalFineGridTimeInterval, TimeIntervals.cpp:214-231, and         */
+/* Patch::switchValuesAndTimeIntervalToMinimalFineGridTimeInterval,         */
+/* Patch.cpp:388-397).                                                       */
 /* dt_out[p] receives the dt taken (0 for a leaf that did not advance);      */
 /* returns the number of leaves that advanced.                               */
 /* ------------------------------------------------------------------------ */
 int pco_grid_step_lts(pco_patch **patches, int n_patches, const pco_ghost_item *items, int n_items,
                       const uint8_t *wall_mask, const pco_swe_params *prm, double max_dt,
-                      double t_end, double *dt_out, int n_threads) {
+                      double t_end, const int32_t *vt_leaf, const int32_t *vt_virt, int n_vt,
+                      double *dt_out, int n_threads) {
   double *nbmin = (double *)malloc(sizeof(double) * (size_t)n_patches);
   char *active = (char *)calloc((size_t)n_patches, 1);
   double *maxdt = (double *)malloc(sizeof(double) * (size_t)n_patches);
-  for (int p = 0; p < n_patches; p++) nbmin[p] = INFINITY;
+  double *vstart = (double *)malloc(sizeof(double) * (size_t)n_patches);
+  double *vend = (double *)malloc(sizeof(double) * (size_t)n_patches);
+  for (int p = 0; p < n_patches; p++) {
+    nbmin[p] = INFINITY;
+    vstart[p] = -INFINITY;
+    vend[p] = INFINITY;
+  }
+  for (int k = 0; k < n_vt; k++) {
+    const pco_patch *lf = patches[vt_leaf[k]];
+    const double t = lf->time, e = lf->time + lf->dt;
+    if (t > vstart[vt_virt[k]]) vstart[vt_virt[k]] = t;
+    if (e < vend[vt_virt[k]]) vend[vt_virt[k]] = e;
+  }
+  for (int k = 0; k < n_vt; k++) {
+    pco_patch *v = patches[vt_virt[k]];
+    v->time = vstart[vt_virt[k]];
+    v->dt = vend[vt_virt[k]] - v->time;
+  }
   for (int k = 0; k < n_items; k++) {
-    double tu = pco_time_unew(patches[items[k].src]);
-    if (tu < nbmin[items[k].dst]) nbmin[items[k].dst] = tu;
+    const pco_patch *src = patches[items[k].src];
+    double tc = src->time + src->dt;
+    if (tc < nbmin[items[k].dst]) nbmin[items[k].dst] = tc;
   }
   int n_active = 0;
   for (int p = 0; p < n_patches; p++) {
@@ -920,6 +947,8 @@ int pco_grid_step_lts(pco_patch **patches, int n_patches, const pco_ghost_item *
   free(nbmin);
   free(active);
   free(maxdt);
+  free(vstart);
+  free(vend);
   return n_active;
 }
 

@@ -139,7 +139,8 @@ double pco_overlap_area(const double p1[2], const double s1[2],
 /* One local-time-stepping grid iteration (see pcoracle.c). */
 int pco_grid_step_lts(pco_patch **patches, int n_patches, const pco_ghost_item *items, int n_items,
                       const uint8_t *wall_mask, const pco_swe_params *prm, double max_dt,
-                      double t_end, double *dt_out, int n_threads);
+                      double t_end, const int32_t *vt_leaf, const int32_t *vt_virt, int n_vt,
+                      double *dt_out, int n_threads);
 void pco_grid_step(pco_patch **patches, int n_patches,
                    const pco_ghost_item *items, int n_items,
                    const uint8_t *wall_mask, const int32_t *group, int n_groups,

@@ -148,11 +148,14 @@ class AmrGrid:
         L = 1.0 / (self.base * np.power(3.0, lvl.astype(np.float64)))
         pos = np.stack([si * L, sj * L], axis=1)
         size = np.stack([L, L], axis=1)
-        return {"order": order, "index": {s: k for k, s in enumerate(order)}, "pos": pos, "size": size,
-                "leaf": (ref == 0).tolist(), "level": lvl.tolist(), "wall": walls[:npch].tolist(),
+        index = {s: k for k, s in enumerate(order)}
+        leaf = (ref == 0).tolist()
+        return {"order": order, "index": index, "pos": pos, "size": size,
+                "leaf": leaf, "level": lvl.tolist(), "wall": walls[:npch].tolist(),
                 "items": items[:ni.value].copy(), "flux_items": flux[:nf.value].copy(),
                 "restrict_items": restr[:nr.value].copy(),
-                "restr_lower": lower[:npch].copy(), "restr_upper": upper[:npch].copy()}
+                "restr_lower": lower[:npch].copy(), "restr_upper": upper[:npch].copy(),
+                "virtual_time_items": virtual_time_items(order, index, leaf)}
 
     def layout_py(self):
         """Patch order and every list the batched step needs, in patch-order
@@ -232,7 +235,28 @@ class AmrGrid:
                 "items": np.array(rows, dtype=np.int32).reshape(-1, 9),
                 "flux_items": np.array(flux, dtype=np.int32).reshape(-1, 4),
                 "restrict_items": np.array(rest, dtype=np.int32).reshape(-1, 2),
-                "restr_lower": lower, "restr_upper": upper}
+                "restr_lower": lower, "restr_upper": upper,
+                "virtual_time_items": virtual_time_items(order, index, leaf)}
+
+
+def virtual_time_items(order, index, leaf):
+    """(leaf, virtual ancestor) pairs in patch-order indices, every leaf
+    against each refined slot above it, sorted by (virtual, leaf): the list
+    whose intervals give the virtual patches' time intervals in local time
+    stepping (the fine-grid time interval that GridLevelTransfer::stepUp
+    accumulates over the children, applied transitively)."""
+    rows = []
+    for (l2, i2, j2) in order:
+        s = index[(l2, i2, j2)]
+        if not leaf[s]:
+            continue
+        for l in range(l2 - 1, -1, -1):
+            f = 3 ** (l2 - l)
+            v = index.get((l, i2 // f, j2 // f))
+            if v is not None and not leaf[v]:
+                rows.append((v, s))
+    rows.sort()
+    return np.array([(s, v) for v, s in rows], dtype=np.int32).reshape(-1, 2)
 
 
 def remesh(grid, backend, g, b_of):
@@ -376,6 +400,8 @@ class DeviceAmr:
         self.ctx.set_ghost_items(remap_items(lay["items"], ids))
         r = lay["restrict_items"]
         self.ctx.set_restriction_items(ids[r[:, 0]], ids[r[:, 1]], True)
+        vt = lay["virtual_time_items"]
+        self.ctx.set_virtual_time_items(ids[vt[:, 0]], ids[vt[:, 1]])
         f = lay["flux_items"]
         if self.flux and len(f):
             self.ctx.set_flux_correction_items(ids[f[:, 0]], ids[f[:, 1]], f[:, 2], f[:, 3], self.g_flux)

@@ -154,6 +154,14 @@ struct pcg_context {
   int *d_pact = nullptr;
   double *d_pmaxdt = nullptr;
   unsigned long long *d_pdt = nullptr, *d_nbmin = nullptr, *d_group_tmin = nullptr;
+  // (leaf, virtual) pairs of pcg_set_virtual_time_items and the distinct
+  // virtual patches; interval keys per patch
+  std::vector<int2> vt_user, h_vt;
+  std::vector<int> vt_virtuals;
+  int2 *d_vt = nullptr;
+  int *d_vt_virtuals = nullptr;
+  size_t d_vt_cap = 0, d_vtv_cap = 0;
+  unsigned long long *d_vstart = nullptr, *d_vend = nullptr;
   double *d_dt_out = nullptr;
   double *h_pinned = nullptr;  // pinned scratch for small D2H/H2D
   std::vector<double> h_group_max_dt;
@@ -479,7 +487,22 @@ int rebuild_topology(pcg_context *c) {
   };
   group_by_dst(c->restr_user, c->h_restr, c->restr_begin, &c->restr_dsts);
   group_by_dst(c->flux_user, c->h_flux, c->flux_begin, nullptr);
+  c->h_vt.clear();
+  c->vt_virtuals.clear();
+  {
+    std::vector<char> seen(c->max_patches, 0);
+    for (const int2 &pr : c->vt_user) {
+      if (!valid_id(c, pr.x) || !valid_id(c, pr.y)) continue;
+      c->h_vt.push_back(pr);
+      if (!seen[pr.y]) {
+        seen[pr.y] = 1;
+        c->vt_virtuals.push_back(pr.y);
+      }
+    }
+  }
   int rc;
+  if ((rc = ensure_device(c, &c->d_vt, &c->d_vt_cap, c->h_vt.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_vt_virtuals, &c->d_vtv_cap, c->vt_virtuals.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_restr, &c->d_restr_cap, c->h_restr.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_flux, &c->d_flux_cap, c->h_flux.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_restr_begin, &c->d_rb_cap, c->restr_begin.size())) != PCG_OK) return rc;
@@ -495,6 +518,8 @@ int rebuild_topology(pcg_context *c) {
   PCG_CUDA(up(c->d_flux_begin, c->flux_begin.data(), sizeof(int) * c->flux_begin.size()));
   PCG_CUDA(up(c->d_restr_dsts, c->restr_dsts.data(), sizeof(int) * c->restr_dsts.size()));
   PCG_CUDA(up(c->d_leaf_ids, c->leaf_ids.data(), sizeof(int) * c->leaf_ids.size()));
+  PCG_CUDA(up(c->d_vt, c->h_vt.data(), sizeof(int2) * c->h_vt.size()));
+  PCG_CUDA(up(c->d_vt_virtuals, c->vt_virtuals.data(), sizeof(int) * c->vt_virtuals.size()));
   if ((rc = ensure_device(c, &c->d_gcells, &c->d_gcells_cap, c->h_gcells.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_plan, &c->d_plan_cap, (size_t)c->n_interp_cells)) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_copy_plan, &c->d_copy_plan_cap, (size_t)c->n_copy_cells)) != PCG_OK) return rc;
@@ -607,8 +632,15 @@ int enqueue_update(pcg_context *c) {
 
 // One local-time-stepping phase (0: activity, 1: dts, 2: group times).
 int enqueue_lts(pcg_context *c, int phase) {
+  pcg::LtsVirtualDev vt;
+  vt.pairs = c->d_vt;
+  vt.n_pairs = (int)c->h_vt.size();
+  vt.virtuals = c->d_vt_virtuals;
+  vt.n_virtual = (int)c->vt_virtuals.size();
+  vt.start = c->d_vstart;
+  vt.end = c->d_vend;
   PCG_CUDA(pcg::launch_lts(c->stream, phase, c->max_patches, c->max_groups, c->d_patches, c->d_times,
-                           c->d_items, (int)c->h_items.size(), c->d_nbmin, c->d_patch_smax,
+                           c->d_items, (int)c->h_items.size(), vt, c->d_nbmin, c->d_patch_smax,
                            c->d_group_tmin, c->d_group_dt, c->d_group_max_dt, c->d_group_t_end,
                            c->d_group_active, c->d_pact, c->d_pmaxdt, c->d_pdt, c->d_group_time, c->prm));
   return PCG_OK;
@@ -636,7 +668,10 @@ int enqueue_step(pcg_context *c, int mode) {
     if ((rc = enqueue_sweep(c)) != PCG_OK) return rc;
     if (c->ts_local && (rc = enqueue_lts(c, 1)) != PCG_OK) return rc;
     if ((rc = enqueue_update(c)) != PCG_OK) return rc;
-    if (c->ts_local) return enqueue_lts(c, 2);
+    if (c->ts_local) {
+      if ((rc = enqueue_lts(c, 2)) != PCG_OK) return rc;
+      return enqueue_post_update(c);
+    }
   } else {
     for (int p : c->leaf_ids)
       PCG_CUDA(launch_fill_patch(c->stream, c->slab, c->d_patches, c->d_times, c->d_items,
@@ -780,6 +815,8 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->d_pdt, sizeof(unsigned long long) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_nbmin, sizeof(unsigned long long) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_group_tmin, sizeof(unsigned long long) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_vstart, sizeof(unsigned long long) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_vend, sizeof(unsigned long long) * c->max_patches));
   {
     std::vector<double> inf(c->max_groups, HUGE_VAL), zero(c->max_groups, 0.0);
     CREATE_CK(cudaMemcpy(c->d_group_t_end, inf.data(), sizeof(double) * c->max_groups, cudaMemcpyHostToDevice));
@@ -815,6 +852,10 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_pdt);
   cudaFree(c->d_nbmin);
   cudaFree(c->d_group_tmin);
+  cudaFree(c->d_vstart);
+  cudaFree(c->d_vend);
+  cudaFree(c->d_vt);
+  cudaFree(c->d_vt_virtuals);
   cudaFree(c->d_dt_out);
   cudaFree(c->d_items);
   cudaFree(c->d_gcells);
@@ -1381,13 +1422,33 @@ static int check_solvable(pcg_context *c) {
   return PCG_OK;
 }
 
-// Local time stepping runs in the batched form only, without flux-correction
-// or restriction lists (those follow the synchronous step of a group).
+// Local time stepping runs in the batched form only, without a
+// flux-correction list; the virtual-time pairs must join a leaf to a
+// non-leaf patch.
 static int check_mode(pcg_context *c, int mode) {
   if (!c->ts_local) return PCG_OK;
   if (mode != PCG_MODE_BATCHED) return fail(PCG_E_STATE, "local time stepping runs in the batched form only");
-  if (!c->h_flux.empty() || !c->h_restr.empty())
-    return fail(PCG_E_STATE, "local time stepping takes no flux-correction or restriction lists");
+  if (!c->h_flux.empty()) return fail(PCG_E_STATE, "local time stepping takes no flux-correction list");
+  for (size_t k = 0; k < c->h_vt.size(); k++) {
+    const int2 pr = c->h_vt[k];
+    if (!(c->h_patches[pr.x].flags & pcg::kFlagLeaf) || (c->h_patches[pr.y].flags & pcg::kFlagLeaf))
+      return fail(PCG_E_STATE, "virtual-time item " + std::to_string(k) + " does not join a leaf to a non-leaf patch");
+  }
+  return PCG_OK;
+}
+
+int pcg_set_virtual_time_items(pcg_context *c, int32_t n, const int32_t *leaf, const int32_t *virt) {
+  if (!c || n < 0 || (n > 0 && (!leaf || !virt))) return fail(PCG_E_INVALID, "bad virtual-time list");
+  std::lock_guard<std::mutex> lk(c->mu);
+  std::vector<int2> v;
+  v.reserve(n);
+  for (int k = 0; k < n; k++) {
+    if (!valid_id(c, leaf[k]) || !valid_id(c, virt[k]) || leaf[k] == virt[k])
+      return fail(PCG_E_INVALID, "virtual-time item " + std::to_string(k) + ": bad ids");
+    v.push_back(make_int2(leaf[k], virt[k]));
+  }
+  c->vt_user = v;
+  c->topo_dirty = true;
   return PCG_OK;
 }
 

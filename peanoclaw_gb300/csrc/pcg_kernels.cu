@@ -284,13 +284,45 @@ __global__ void k_lts_begin(int n_patches, unsigned long long *__restrict__ nbmi
   }
 }
 
-// Minimal uNew time of the ghost-item sources of every destination.
+// Time intervals of the virtual patches: the intersection of the intervals
+// of their listed leaves (time = maximal leaf time, dt = minimal leaf
+// time + dt minus that time; GridLevelTransfer::stepUp with
+// updateMinimalFineGridTimeInterval and
+// switchValuesAndTimeIntervalToMinimalFineGridTimeInterval).
+__global__ void k_lts_vt_reset(const int *__restrict__ vdsts, int nv, unsigned long long *__restrict__ vstart,
+                               unsigned long long *__restrict__ vend) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += gridDim.x * blockDim.x) {
+    vstart[vdsts[k]] = okey(-INFINITY);
+    vend[vdsts[k]] = okey(INFINITY);
+  }
+}
+__global__ void k_lts_vt_pairs(const int2 *__restrict__ pairs, int n, const PatchTimeDev *__restrict__ times,
+                               unsigned long long *__restrict__ vstart, unsigned long long *__restrict__ vend) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int2 pr = pairs[k];
+    const PatchTimeDev T = times[pr.x];
+    atomicMax(&vstart[pr.y], okey(T.time));
+    atomicMin(&vend[pr.y], okey(__dadd_rn(T.time, T.dt)));
+  }
+}
+__global__ void k_lts_vt_set(const int *__restrict__ vdsts, int nv, const unsigned long long *__restrict__ vstart,
+                             const unsigned long long *__restrict__ vend, PatchTimeDev *__restrict__ times) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += gridDim.x * blockDim.x) {
+    const int v = vdsts[k];
+    const double t = unokey(vstart[v]);
+    times[v].time = t;
+    times[v].dt = __dsub_rn(unokey(vend[v]), t);
+  }
+}
+
+// Minimal time constraint (time + dt, TimeIntervals::getTimeConstraint) of
+// the ghost-item sources of every destination.
 __global__ void k_lts_nbmin(const GhostItemDev *__restrict__ items, int count,
-                            const PatchDev *__restrict__ patches, const PatchTimeDev *__restrict__ times,
-                            unsigned long long *__restrict__ nbmin) {
+                            const PatchTimeDev *__restrict__ times, unsigned long long *__restrict__ nbmin) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
     const GhostItemDev it = items[k];
-    atomicMin(&nbmin[it.dst], okey(time_unew(patches[it.src], times[it.src])));
+    const PatchTimeDev T = times[it.src];
+    atomicMin(&nbmin[it.dst], okey(__dadd_rn(T.time, T.dt)));
   }
 }
 
@@ -1261,20 +1293,26 @@ cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_
 }
 
 cudaError_t launch_lts(cudaStream_t st, int phase, int n_patches, int n_groups, const PatchDev *patches,
-                       const PatchTimeDev *times, const GhostItemDev *items, int n_items,
-                       unsigned long long *nbmin, unsigned long long *patch_smax,
+                       PatchTimeDev *times, const GhostItemDev *items, int n_items,
+                       const LtsVirtualDev &vt, unsigned long long *nbmin, unsigned long long *patch_smax,
                        unsigned long long *group_tmin, unsigned long long *group_dt,
                        const double *group_max_dt, const double *group_t_end, const int *group_active,
                        int *pact, double *pmaxdt, unsigned long long *pdt, double *group_time,
                        const SweParamsDev &prm) {
   const int np = n_patches > 0 ? n_patches : 1;
   const int gp = (np + 255) / 256 < 1024 ? (np + 255) / 256 : 1024;
+  auto grid_for = [](int n) { return (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096; };
   switch (phase) {
     case 0:
       k_lts_begin<<<gp, 256, 0, st>>>(n_patches, nbmin, patch_smax, n_groups, group_tmin, group_dt);
+      if (vt.n_pairs > 0 && vt.n_virtual > 0) {
+        k_lts_vt_reset<<<grid_for(vt.n_virtual), 256, 0, st>>>(vt.virtuals, vt.n_virtual, vt.start, vt.end);
+        k_lts_vt_pairs<<<grid_for(vt.n_pairs), 256, 0, st>>>(vt.pairs, vt.n_pairs, times, vt.start, vt.end);
+        k_lts_vt_set<<<grid_for(vt.n_virtual), 256, 0, st>>>(vt.virtuals, vt.n_virtual, vt.start, vt.end,
+                                                             times);
+      }
       if (n_items > 0)
-        k_lts_nbmin<<<(n_items + 255) / 256 < 4096 ? (n_items + 255) / 256 : 4096, 256, 0, st>>>(
-            items, n_items, patches, times, nbmin);
+        k_lts_nbmin<<<grid_for(n_items), 256, 0, st>>>(items, n_items, times, nbmin);
       k_lts_activity<<<gp, 256, 0, st>>>(patches, times, n_patches, nbmin, group_max_dt, group_t_end,
                                          group_active, pact, pmaxdt);
       break;

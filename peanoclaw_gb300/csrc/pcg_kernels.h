@@ -30,9 +30,19 @@ cudaError_t launch_reset(cudaStream_t st, int n_groups, const double *group_max_
 // Local time stepping phases: 0 = neighbour constraints and activity (before
 // the ghost fill), 1 = per-leaf dt (after the sweep), 2 = group time and dt
 // (after the update).
+// (leaf, virtual) pairs that set the virtual patches' time intervals in
+// local time stepping, the distinct virtual patches and two per-patch key
+// arrays for the interval reduction.
+struct LtsVirtualDev {
+  const int2 *pairs = nullptr;
+  int n_pairs = 0;
+  const int *virtuals = nullptr;
+  int n_virtual = 0;
+  unsigned long long *start = nullptr, *end = nullptr;
+};
 cudaError_t launch_lts(cudaStream_t st, int phase, int n_patches, int n_groups, const PatchDev *patches,
-                       const PatchTimeDev *times, const GhostItemDev *items, int n_items,
-                       unsigned long long *nbmin, unsigned long long *patch_smax,
+                       PatchTimeDev *times, const GhostItemDev *items, int n_items,
+                       const LtsVirtualDev &vt, unsigned long long *nbmin, unsigned long long *patch_smax,
                        unsigned long long *group_tmin, unsigned long long *group_dt,
                        const double *group_max_dt, const double *group_t_end, const int *group_active,
                        int *pact, double *pmaxdt, unsigned long long *pdt, double *group_time,

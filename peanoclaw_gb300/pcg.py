@@ -108,6 +108,7 @@ SIGNATURES = {
     "pcg_set_group_max_dt": (C.c_int, [_CTX, C.c_int32, C.c_double]),
     "pcg_set_group_end_time": (C.c_int, [_CTX, C.c_int32, C.c_double, C.c_double]),
     "pcg_set_time_stepping": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_set_virtual_time_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2]),
     "pcg_get_group_times": (C.c_int, [_CTX, _D]),
     "pcg_set_restriction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, C.c_int32]),
     "pcg_set_flux_correction_items": (C.c_int, [_CTX, C.c_int32, _I2, _I2, _I2, _I2, C.c_double]),
@@ -345,6 +346,16 @@ class Context:
         """TS_GLOBAL (synchronous steps) or TS_LOCAL (local time stepping,
         batched form; see pcg_set_time_stepping)."""
         check(lib().pcg_set_time_stepping(self.h, int(mode)))
+
+    def set_virtual_time_items(self, leaf, virt):
+        """(leaf, virtual ancestor) pairs that set the virtual patches' time
+        intervals in local time stepping (see pcg_set_virtual_time_items)."""
+        leaf = np.ascontiguousarray(leaf, dtype=np.int32)
+        virt = np.ascontiguousarray(virt, dtype=np.int32)
+        if leaf.shape != virt.shape:
+            raise ValueError("leaf and virt differ in length")
+        check(lib().pcg_set_virtual_time_items(self.h, len(leaf), leaf.ctypes.data_as(_I2),
+                                               virt.ctypes.data_as(_I2)))
 
     def group_times(self):
         out = np.zeros(self.max_groups)

@@ -300,6 +300,7 @@ def amr_patchset(grid, h_of, b_of):
     ps.restrict_items = lay["restrict_items"]
     ps.restr_lower = lay["restr_lower"]
     ps.restr_upper = lay["restr_upper"]
+    ps.virtual_time_items = lay["virtual_time_items"]
     ps.meta = {"workload": "adaptive grid, %d levels, %d patches (%d leaves) of %dx%d cells"
                            % (grid.levels, len(ps), sum(ps.leaf), n, n),
                "leaf_cells": int(sum(n * n for p in range(len(ps)) if ps.leaf[p]))}
@@ -309,8 +310,9 @@ def amr_patchset(grid, h_of, b_of):
 def install_amr(ctx, ps, flux=True, g_flux=1.0):
     """Allocate an adaptive PatchSet (breaking_dam_amr) in a pcg.Context:
     leaves and virtual patches with their restriction bounds, the ghost
-    face-pair list, the restriction list and (flux=True) the flux-correction
-    list.  Returns the patch ids in PatchSet order."""
+    face-pair list, the restriction list, the virtual-time list (local time
+    stepping) and (flux=True) the flux-correction list.  Returns the patch
+    ids in PatchSet order."""
     ids = []
     for p in range(len(ps)):
         leaf = bool(ps.leaf[p])
@@ -325,6 +327,9 @@ def install_amr(ctx, ps, flux=True, g_flux=1.0):
     ctx.upload_many(ids, ps.packed)
     ctx.set_ghost_items(remap_items(ps.items, ids))
     ctx.set_restriction_items(ids[ps.restrict_items[:, 0]], ids[ps.restrict_items[:, 1]], True)
+    vt = getattr(ps, "virtual_time_items", None)
+    if vt is not None and len(vt):
+        ctx.set_virtual_time_items(ids[vt[:, 0]], ids[vt[:, 1]])
     if flux and len(ps.flux_items):
         f = ps.flux_items
         ctx.set_flux_correction_items(ids[f[:, 0]], ids[f[:, 1]], f[:, 2], f[:, 3], g_flux)

@@ -102,3 +102,62 @@ def test_local_time_stepping_arguments_and_states():
         c.step(P.PCG_MODE_PLAIN)
     finally:
         c.close()
+
+
+def test_local_time_stepping_across_levels_matches_the_oracle():
+    # 3-level breaking dam (virtual patches between the levels): coarse leaves
+    # next to a refined region wait for its finest leaves and read them
+    # through the restricted virtual patches
+    from helpers import oracle_amr_patchset, oracle_restrict_all
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0)
+    assert len(ps.virtual_time_items) and not all(ps.leaf)
+    t_end = 0.012
+    c = P.Context(slab_doubles=8_000_000, max_patches=len(ps) + 8, max_groups=1, params=PRM)
+    try:
+        ids = S.install_amr(c, ps, flux=False)
+        c.restrict_all()
+        c.set_group_max_dt(0, np.inf)
+        c.set_group_end_time(0, 0.0, t_end)
+        c.set_time_stepping(P.TS_LOCAL)
+        pats = oracle_amr_patchset(ps)
+        oracle_restrict_all(pats, ps)
+        prm = oracle_params(PRM)
+        iterations = 0
+        done = False
+        while not done:
+            hist = c.run(8)[:, 0]
+            for k in range(8):
+                n, dto = O.grid_step_lts(pats, ps.items, ps.wall, prm, np.inf, t_end,
+                                         ps.virtual_time_items)
+                if n:
+                    oracle_restrict_all(pats, ps)
+                    iterations += 1
+                else:
+                    done = True
+                taken = dto[dto > 0.0]
+                assert hist[k] == (taken.min() if n else 0.0), (iterations, k)
+            assert iterations < 2000
+        assert iterations > 50
+        out = c.download_many(ids, int(ps.packed.size))
+        ref = np.concatenate([p.u for p in pats])
+        assert np.array_equal(out.view(np.int64), ref.view(np.int64))
+        for p, pid in enumerate(ids):
+            t = c.get_time(int(pid))
+            assert (t["time"], t["dt"]) == (pats[p].s.time, pats[p].s.dt), p
+        assert c.group_times()[0] == t_end
+    finally:
+        c.close()
+
+
+def test_local_time_stepping_refuses_flux_correction_lists():
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0)
+    c = P.Context(slab_doubles=8_000_000, max_patches=len(ps) + 8, max_groups=1, params=PRM)
+    try:
+        S.install_amr(c, ps, flux=True)
+        c.set_group_max_dt(0, np.inf)
+        c.set_time_stepping(P.TS_LOCAL)
+        assert len(ps.flux_items)
+        with pytest.raises(P.PcgError):
+            c.run(1)
+    finally:
+        c.close()

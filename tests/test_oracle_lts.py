@@ -54,3 +54,34 @@ def test_every_leaf_reaches_the_end_time_without_running_ahead():
         t += O.grid_step(glob, ps.items, ps.wall, prm, t_end - t)[0]
         steps += 1
     assert lts_updates < steps * sum(n * n for n in ps.n)
+
+
+def test_virtual_patches_take_the_intersection_of_their_leaves_intervals():
+    from helpers import oracle_amr_patchset, oracle_restrict_all
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0)
+    prm = oracle_params(PRM)
+    pats = oracle_amr_patchset(ps)
+    oracle_restrict_all(pats, ps)
+    t_end = 0.01
+    vt = ps.virtual_time_items
+    virtuals = sorted(set(vt[:, 1].tolist()))
+    leaves_of = {v: vt[vt[:, 1] == v, 0] for v in virtuals}
+    assert all(not ps.leaf[v] for v in virtuals) and all(ps.leaf[s] for s in vt[:, 0])
+    # every leaf lies below its virtual ancestors on every level above it
+    assert len(vt) == sum(ps.level[s] for s in range(len(ps)) if ps.leaf[s])
+    iterations = 0
+    for _ in range(3000):
+        before = {s: (pats[s].s.time, _tu(pats[s])) for s in range(len(ps)) if ps.leaf[s]}
+        n, dto = O.grid_step_lts(pats, ps.items, ps.wall, prm, np.inf, t_end, vt)
+        for v in virtuals:
+            start = max(before[s][0] for s in leaves_of[v])
+            end = min(before[s][1] for s in leaves_of[v])
+            assert pats[v].s.time == start and pats[v].s.dt == end - start
+        if n == 0:
+            break
+        iterations += 1
+        oracle_restrict_all(pats, ps)
+    assert iterations > 50
+    for p, lf in zip(pats, ps.leaf):
+        if lf:
+            assert _tu(p) == t_end
