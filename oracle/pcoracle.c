@@ -117,14 +117,18 @@ double pco_time_unew(const pco_patch *p) {
 /*    bathymetry: reflecting wall (dry side replaced by the mirrored wet     */
 /*    state), and the update of the dry cell is dropped;                     */
 /*  - otherwise (inundation) the dry side enters as (h, 0, b);               */
+/*  - per cell: s = sqrt(h), p = hu * (1/s), F = p*p, surface eta = h + b;  */
 /*  - momentum flux jump through the free-surface difference                 */
-/*    df2 = (F_R - F_L) + g/2 (h_L+h_R) ((h_R-h_L) + (b_R-b_L)), so a lake   */
-/*    at rest gives exactly zero;                                            */
+/*    df2 = (F_R - F_L) + g/2 (h_L+h_R) (eta_R - eta_L), so a lake at rest   */
+/*    (equal eta) gives exactly zero;                                        */
+/*  - wave strengths (lambda2 df1 - df2) / (2 cbar) and                      */
+/*    (df2 - lambda1 df1) / (2 cbar), lambda2 - lambda1 = 2 cbar, each as a  */
+/*    product with 1 / (2 cbar);                                             */
 /*  - waves with speed < 0 go left, all others go right.                     */
 /* out = {hNetLeft, huNetLeft, hNetRight, huNetRight, maxEdgeSpeed}          */
 /* ------------------------------------------------------------------------ */
 typedef struct {
-  double h, hu, b, s, p, F;
+  double h, hu, b, eta, s, p, F;
   int wet;
 } cellq;
 
@@ -149,6 +153,7 @@ static void cell_derived(const pco_swe_params *prm, double h, double hu, double 
     c->F = 0.0;
     c->hu = 0.0;
   }
+  c->eta = c->h + b;
 }
 
 static void fwave_derived(const pco_swe_params *prm, cellq L, cellq R, double out[5]) {
@@ -156,13 +161,13 @@ static void fwave_derived(const pco_swe_params *prm, cellq L, cellq R, double ou
     out[0] = out[1] = out[2] = out[3] = out[4] = 0.0;
     return;
   }
-  int wallR = L.wet && !R.wet && (L.h + L.b <= R.b);
-  int wallL = R.wet && !L.wet && (R.h + R.b <= L.b);
+  int wallR = L.wet && !R.wet && (L.eta <= R.b);
+  int wallL = R.wet && !L.wet && (R.eta <= L.b);
   if (wallR) {
-    R.h = L.h; R.hu = -L.hu; R.b = L.b; R.s = L.s; R.p = -L.p; R.F = L.F;
+    R.h = L.h; R.hu = -L.hu; R.b = L.b; R.eta = L.eta; R.s = L.s; R.p = -L.p; R.F = L.F;
   }
   if (wallL) {
-    L.h = R.h; L.hu = -R.hu; L.b = R.b; L.s = R.s; L.p = -R.p; L.F = R.F;
+    L.h = R.h; L.hu = -R.hu; L.b = R.b; L.eta = R.eta; L.s = R.s; L.p = -R.p; L.F = R.F;
   }
   double halfg = 0.5 * prm->g;
   double a = halfg * (L.h + R.h);
@@ -171,9 +176,9 @@ static void fwave_derived(const pco_swe_params *prm, cellq L, cellq R, double ou
   double l1 = ub - cb;
   double l2 = ub + cb;
   double df1 = R.hu - L.hu;
-  double deta = (R.h - L.h) + (R.b - L.b);
+  double deta = R.eta - L.eta;
   double df2 = fma(a, deta, R.F - L.F);
-  double inv = 1.0 / (l2 - l1);
+  double inv = 1.0 / (2.0 * cb);
   double b1 = fma(l2, df1, -df2) * inv;
   double b2 = fma(-l1, df1, df2) * inv;
   double z1 = b1 * l1;

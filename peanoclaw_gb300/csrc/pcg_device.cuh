@@ -215,11 +215,12 @@ __device__ __forceinline__ double fmax_nonneg(double a, double b) {
 // f-wave edge solve (same operation sequence as the oracle's fwave_derived).
 // Divides and square roots go through pcg_ieee.cuh (integer pipes, results
 // identical to the IEEE operations).
-// Cell quantities: h, hu (normal momentum, zero for dry cells), b, s = sqrt(h),
-// p = hu / s, F = p*p; wet = h > dry_tol; a dry cell has h = max(h, 0).
+// Cell quantities: h, hu (normal momentum, zero for dry cells), b, surface
+// eta = h + b, s = sqrt(h), p = hu / s, F = p*p; wet = h > dry_tol; a dry cell
+// has h = max(h, 0).
 // ---------------------------------------------------------------------------
 struct CellQ {
-  double h, hu, b, s, p, F;
+  double h, hu, b, eta, s, p, F;
   bool wet;
 };
 
@@ -242,6 +243,17 @@ __device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu
     cx.s = 0.0; cx.p = 0.0; cx.F = 0.0; cx.hu = 0.0;
     cy.s = 0.0; cy.p = 0.0; cy.F = 0.0; cy.hu = 0.0;
   }
+  const double eta = __dadd_rn(cx.h, b);
+  cx.eta = eta; cy.eta = eta;
+}
+
+// 2 x, exact: the exponent field is incremented on the integer pipe when x is
+// normal and 2 x stays finite; other values take the FP64 multiply.
+__device__ __forceinline__ double twice(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(u >> 52) & 0x7FFu;
+  if (e - 1u < 0x7FDu) return __longlong_as_double((long long)(u + (1ull << 52)));
+  return __dmul_rn(2.0, x);
 }
 
 // IEEE negation as a sign-bit flip (a standalone FP64 negation would take an
@@ -253,10 +265,10 @@ __device__ __forceinline__ double neg(double x) {
 // Wet|dry edge: decide whether the dry side is a reflecting wall and, if so,
 // replace it by the mirrored wet state.
 __device__ __forceinline__ void coastline(CellQ &L, CellQ &R, bool &wallL, bool &wallR) {
-  wallR = L.wet && (__dadd_rn(L.h, L.b) <= R.b);
-  wallL = R.wet && (__dadd_rn(R.h, R.b) <= L.b);
-  if (wallR) { R.h = L.h; R.hu = neg(L.hu); R.b = L.b; R.s = L.s; R.p = neg(L.p); R.F = L.F; }
-  if (wallL) { L.h = R.h; L.hu = neg(R.hu); L.b = R.b; L.s = R.s; L.p = neg(R.p); L.F = R.F; }
+  wallR = L.wet && (L.eta <= R.b);
+  wallL = R.wet && (R.eta <= L.b);
+  if (wallR) { R.h = L.h; R.hu = neg(L.hu); R.b = L.b; R.eta = L.eta; R.s = L.s; R.p = neg(L.p); R.F = L.F; }
+  if (wallL) { L.h = R.h; L.hu = neg(R.hu); L.b = R.b; L.eta = R.eta; L.s = R.s; L.p = neg(R.p); L.F = R.F; }
 }
 
 // out: Lh, Lhu, Rh, Rhu (net updates of the left/right cell) and the edge's
@@ -280,9 +292,10 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
   double l1 = __dsub_rn(ub, cb);
   double l2 = __dadd_rn(ub, cb);
   double df1 = __dsub_rn(R.hu, L.hu);
-  double deta = __dadd_rn(__dsub_rn(R.h, L.h), __dsub_rn(R.b, L.b));
+  double deta = __dsub_rn(R.eta, L.eta);
   double df2 = __fma_rn(a, deta, __dsub_rn(R.F, L.F));
-  double inv = ieee::rcp_rn(__dsub_rn(l2, l1));
+  // lambda2 - lambda1 = 2 cbar
+  double inv = ieee::rcp_rn(twice(cb));
   double b1 = __dmul_rn(__fma_rn(l2, df1, -df2), inv);
   double b2 = __dmul_rn(__fma_rn(-l1, df1, df2), inv);
   double z1 = __dmul_rn(b1, l1);

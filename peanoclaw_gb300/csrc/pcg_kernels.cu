@@ -21,6 +21,7 @@ namespace pcg {
 struct SweepSmem {
   double h[kTile + 2][kTile + 2];
   double b[kTile + 2][kTile + 2];
+  double eta[kTile + 2][kTile + 2];
   double hu[kTile + 2][kTile + 2];
   double hv[kTile + 2][kTile + 2];
   double s[kTile + 2][kTile + 2];
@@ -37,13 +38,13 @@ struct SweepSmem {
 
 __device__ __forceinline__ CellQ load_x(const SweepSmem &S, int i, int j) {
   CellQ c;
-  c.h = S.h[i][j]; c.b = S.b[i][j]; c.hu = S.hu[i][j]; c.s = S.s[i][j]; c.p = S.p[i][j];
+  c.h = S.h[i][j]; c.b = S.b[i][j]; c.eta = S.eta[i][j]; c.hu = S.hu[i][j]; c.s = S.s[i][j]; c.p = S.p[i][j];
   c.F = S.F[i][j]; c.wet = S.wet[i][j] != 0;
   return c;
 }
 __device__ __forceinline__ CellQ load_y(const SweepSmem &S, int i, int j) {
   CellQ c;
-  c.h = S.h[i][j]; c.b = S.b[i][j]; c.hu = S.hv[i][j]; c.s = S.s[i][j]; c.p = S.q[i][j];
+  c.h = S.h[i][j]; c.b = S.b[i][j]; c.eta = S.eta[i][j]; c.hu = S.hv[i][j]; c.s = S.s[i][j]; c.p = S.q[i][j];
   c.F = S.G[i][j]; c.wet = S.wet[i][j] != 0;
   return c;
 }
@@ -84,7 +85,7 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
     double b = slab[idx_pw(P, 0, x, y)];
     CellQ qx, qy;
     cell_derived(dry, h, hu, hv, b, qx, qy);
-    S.h[sx][sy] = qx.h; S.b[sx][sy] = b; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
+    S.h[sx][sy] = qx.h; S.b[sx][sy] = b; S.eta[sx][sy] = qx.eta; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
     S.s[sx][sy] = qx.s; S.p[sx][sy] = qx.p; S.q[sx][sy] = qy.p;
     S.F[sx][sy] = qx.F; S.G[sx][sy] = qy.F; S.wet[sx][sy] = qx.wet ? 1 : 0;
   }

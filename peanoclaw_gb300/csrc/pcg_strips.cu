@@ -23,7 +23,7 @@ namespace {
 
 // Per-warp shared memory: one entry per (group, column), G * w <= 32.
 struct StripWarpSmem {
-  double h[32], b[32], hv[32], s[32], q[32], G[32];  // cell below the group's first row
+  double h[32], b[32], eta[32], hv[32], s[32], q[32], G[32];  // cell below the group's first row
   double top_h[32], top_hv[32], top_sp[32];            // edge above the group's last row
   unsigned char wet[32];
 };
@@ -45,17 +45,17 @@ __device__ __forceinline__ void load_state(const double *__restrict__ slab, cons
 
 // Per-lane slot for the x-direction quantities of the previous column's cell.
 struct StripLaneSmem {
-  double h[32], hu[32], b[32], s[32], p[32], F[32];
+  double h[32], hu[32], b[32], eta[32], s[32], p[32], F[32];
   unsigned char wet[32];
 };
 
 __device__ __forceinline__ void store_x(StripLaneSmem &L, int lane, const CellQ &c) {
-  L.h[lane] = c.h; L.hu[lane] = c.hu; L.b[lane] = c.b; L.s[lane] = c.s; L.p[lane] = c.p;
+  L.h[lane] = c.h; L.hu[lane] = c.hu; L.b[lane] = c.b; L.eta[lane] = c.eta; L.s[lane] = c.s; L.p[lane] = c.p;
   L.F[lane] = c.F; L.wet[lane] = c.wet ? 1 : 0;
 }
 __device__ __forceinline__ CellQ load_x(const StripLaneSmem &L, int lane) {
   CellQ c;
-  c.h = L.h[lane]; c.hu = L.hu[lane]; c.b = L.b[lane]; c.s = L.s[lane]; c.p = L.p[lane];
+  c.h = L.h[lane]; c.hu = L.hu[lane]; c.b = L.b[lane]; c.eta = L.eta[lane]; c.s = L.s[lane]; c.p = L.p[lane];
   c.F = L.F[lane]; c.wet = L.wet[lane] != 0;
   return c;
 }
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       CellQ cx, cy, ty, ay;
       load_state(slab, PH, x, HG.y0 - 1, h, hu, hv, b);
       cell_derived(dry, h, hu, hv, b, cx, cy);
-      S.h[lane] = cy.h; S.b[lane] = cy.b; S.hv[lane] = cy.hu; S.s[lane] = cy.s;
+      S.h[lane] = cy.h; S.b[lane] = cy.b; S.eta[lane] = cy.eta; S.hv[lane] = cy.hu; S.s[lane] = cy.s;
       S.q[lane] = cy.p; S.G[lane] = cy.F; S.wet[lane] = cy.wet ? 1 : 0;
       load_state(slab, PH, x, HG.y0 + hs - 1, h, hu, hv, b);
       cell_derived(dry, h, hu, hv, b, cx, ty);
@@ -164,6 +164,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       CellQ dn;
       dn.h = shfl_up_d(cy.h, 1);
       dn.b = shfl_up_d(cy.b, 1);
+      dn.eta = shfl_up_d(cy.eta, 1);
       dn.hu = shfl_up_d(cy.hu, 1);
       dn.s = shfl_up_d(cy.s, 1);
       dn.p = shfl_up_d(cy.p, 1);
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       dn.wet = __shfl_up_sync(0xffffffffu, (int)cy.wet, 1) != 0;
       const int sl = gi * w + c;
       if (j == 0 && act) {
-        dn.h = S.h[sl]; dn.b = S.b[sl]; dn.hu = S.hv[sl]; dn.s = S.s[sl];
+        dn.h = S.h[sl]; dn.b = S.b[sl]; dn.eta = S.eta[sl]; dn.hu = S.hv[sl]; dn.s = S.s[sl];
         dn.p = S.q[sl]; dn.F = S.G[sl]; dn.wet = S.wet[sl] != 0;
       }
       double yLh, yLhv, yRh, yRhv, sp2;
