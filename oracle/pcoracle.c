@@ -124,7 +124,9 @@ double pco_time_unew(const pco_patch *p) {
 /*  - wave strengths (lambda2 df1 - df2) / (2 cbar) and                      */
 /*    (df2 - lambda1 df1) / (2 cbar), lambda2 - lambda1 = 2 cbar, each as a  */
 /*    product with 1 / (2 cbar);                                             */
-/*  - waves with speed < 0 go left, all others go right.                     */
+/*  - waves with speed < 0 go left, all others go right; when both go to    */
+/*    one side that side receives the whole flux jump (df1, df2), which      */
+/*    beta1 r1 + beta2 r2 equals;                                            */
 /* out = {hNetLeft, huNetLeft, hNetRight, huNetRight, maxEdgeSpeed}          */
 /* ------------------------------------------------------------------------ */
 typedef struct {
@@ -184,14 +186,15 @@ static void fwave_derived(const pco_swe_params *prm, cellq L, cellq R, double ou
   double z1 = b1 * l1;
   double z2 = b2 * l2;
   double Lh, Lhu, Rh, Rhu;
+  /* both waves to one side: the whole flux jump (df1, df2) goes there */
   if (l1 < 0.0) {
     if (l2 < 0.0) {
-      Lh = b1 + b2; Lhu = z1 + z2; Rh = 0.0; Rhu = 0.0;
+      Lh = df1; Lhu = df2; Rh = 0.0; Rhu = 0.0;
     } else {
       Lh = b1; Lhu = z1; Rh = b2; Rhu = z2;
     }
   } else {
-    Lh = 0.0; Lhu = 0.0; Rh = b1 + b2; Rhu = z1 + z2;
+    Lh = 0.0; Lhu = 0.0; Rh = df1; Rhu = df2;
   }
   if (wallR) { Rh = 0.0; Rhu = 0.0; }
   if (wallL) { Lh = 0.0; Lhu = 0.0; }

@@ -92,9 +92,24 @@ struct __align__(16) GhostItemStepDev {
   int vn_src, vo_src, vo_dst, nq;
 };
 
+// Bit pattern of a double and back through an opaque register move: the
+// compiler cannot see integer tests on these bits as floating-point
+// operations (it would otherwise turn sign tests, absolute values and
+// maxima into FP64 instructions, which take FP64 pipe slots).
+__device__ __forceinline__ unsigned long long obits(double x) {
+  unsigned long long u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  return u;
+}
+__device__ __forceinline__ double ofrom(unsigned long long u) {
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+  return x;
+}
+
 // |x| < 2^1022 (so that x + y of two such values is finite); NaN fails.
 __device__ __forceinline__ bool small_mag(double x) {
-  return ((unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull) < 0x7FD0000000000000ull;
+  return (obits(x) & 0x7FFFFFFFFFFFFFFFull) < 0x7FD0000000000000ull;
 }
 constexpr int kFinUOld = 1;  // patch finiteness flags (see k_scan_fin)
 constexpr int kFinB = 2;
@@ -165,10 +180,10 @@ __device__ __forceinline__ double iter_pos(const PatchDev &p, int d, int i) {
 // Positive doubles order like their bit patterns; used for exact max/min
 // reductions with integer atomics.
 __device__ __forceinline__ unsigned long long dbits(double v) {
-  return (unsigned long long)__double_as_longlong(v);
+  return obits(v);
 }
 __device__ __forceinline__ double bitsd(unsigned long long b) {
-  return __longlong_as_double((long long)b);
+  return ofrom(b);
 }
 
 // IEEE comparisons evaluated on the bit patterns (integer pipes); each one
@@ -177,13 +192,13 @@ constexpr unsigned long long kAbsMask = 0x7FFFFFFFFFFFFFFFull;
 constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
 // x < 0.0
 __device__ __forceinline__ bool lt_zero(double x) {
-  long long b = __double_as_longlong(x);
+  long long b = (long long)obits(x);
   unsigned long long m = (unsigned long long)b & kAbsMask;
   return b < 0 && m != 0ull && m <= kInfBits;
 }
 // a < b, the IEEE comparison (false if either is NaN; -0 == +0)
 __device__ __forceinline__ bool lt_ieee(double a, double b) {
-  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  const long long ia = (long long)obits(a), ib = (long long)obits(b);
   const unsigned long long ma = (unsigned long long)ia & kAbsMask, mb = (unsigned long long)ib & kAbsMask;
   if (ma > kInfBits || mb > kInfBits || (ma | mb) == 0ull) return false;
   // sign-magnitude -> order-preserving two's complement keys
@@ -193,22 +208,22 @@ __device__ __forceinline__ bool lt_ieee(double a, double b) {
 }
 // x > c for a constant c >= +0.0 (not NaN)
 __device__ __forceinline__ bool gt_nonneg(double x, double c) {
-  long long b = __double_as_longlong(x);
-  return b > __double_as_longlong(c) && ((unsigned long long)b & kAbsMask) <= kInfBits;
+  long long b = (long long)obits(x);
+  return b > (long long)obits(c) && ((unsigned long long)b & kAbsMask) <= kInfBits;
 }
 // fmax(fabs(a), fabs(b)) with fmax's NaN rule (a NaN operand is ignored)
 __device__ __forceinline__ double fmax_abs(double a, double b) {
-  unsigned long long ma = (unsigned long long)__double_as_longlong(a) & kAbsMask;
-  unsigned long long mb = (unsigned long long)__double_as_longlong(b) & kAbsMask;
+  unsigned long long ma = obits(a) & kAbsMask;
+  unsigned long long mb = obits(b) & kAbsMask;
   unsigned long long r = ma > kInfBits ? mb : (mb > kInfBits ? ma : (ma > mb ? ma : mb));
-  return __longlong_as_double((long long)r);
+  return ofrom(r);
 }
 // fmax(a, b) for a, b >= +0.0 or NaN
 __device__ __forceinline__ double fmax_nonneg(double a, double b) {
-  unsigned long long ua = (unsigned long long)__double_as_longlong(a);
-  unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+  unsigned long long ua = obits(a);
+  unsigned long long ub = obits(b);
   unsigned long long r = ua > kInfBits ? ub : (ub > kInfBits ? ua : (ua > ub ? ua : ub));
-  return __longlong_as_double((long long)r);
+  return ofrom(r);
 }
 
 // ---------------------------------------------------------------------------
@@ -247,19 +262,23 @@ __device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu
   cx.eta = eta; cy.eta = eta;
 }
 
-// 2 x, exact: the exponent field is incremented on the integer pipe when x is
-// normal and 2 x stays finite; other values take the FP64 multiply.
+// 2 x, the IEEE product for every x.  A normal x whose double stays finite
+// gets its exponent field incremented on the integer pipe; zeros,
+// subnormals, overflow, infinities and NaNs go to an out-of-line multiply
+// (out of line so that it is not evaluated speculatively beside the fast
+// path, where it would take an FP64 slot on every call).
+static __device__ __noinline__ double twice_slow(double x) { return __dmul_rn(2.0, x); }
 __device__ __forceinline__ double twice(double x) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long u = obits(x);
   const unsigned e = (unsigned)(u >> 52) & 0x7FFu;
-  if (e - 1u < 0x7FDu) return __longlong_as_double((long long)(u + (1ull << 52)));
-  return __dmul_rn(2.0, x);
+  if (e - 1u < 0x7FDu) return ofrom(u + (1ull << 52));
+  return twice_slow(x);
 }
 
 // IEEE negation as a sign-bit flip (a standalone FP64 negation would take an
 // FP64 issue slot).
 __device__ __forceinline__ double neg(double x) {
-  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+  return ofrom(obits(x) ^ 0x8000000000000000ull);
 }
 
 // Wet|dry edge: decide whether the dry side is a reflecting wall and, if so,
@@ -300,16 +319,13 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
   double b2 = __dmul_rn(__fma_rn(-l1, df1, df2), inv);
   double z1 = __dmul_rn(b1, l1);
   double z2 = __dmul_rn(b2, l2);
-  // both waves to one side (supersonic edges): their sums go to that side.
-  // Branch per warp (a vote) so that subsonic warps skip the FP64 additions.
+  // both waves to one side (supersonic edges): the whole flux jump
+  // (df1, df2) = beta1 r1 + beta2 r2 goes to that side (selects only)
   const bool left1 = lt_zero(l1), split = left1 && !lt_zero(l2);
   Lh = b1; Lhu = z1; Rh = b2; Rhu = z2;
-  if (__any_sync(__activemask(), !split)) {
-    if (!split) {
-      const double sh = __dadd_rn(b1, b2), shu = __dadd_rn(z1, z2);
-      if (left1) { Lh = sh; Lhu = shu; Rh = 0.0; Rhu = 0.0; }
-      else { Lh = 0.0; Lhu = 0.0; Rh = sh; Rhu = shu; }
-    }
+  if (!split) {
+    if (left1) { Lh = df1; Lhu = df2; Rh = 0.0; Rhu = 0.0; }
+    else { Lh = 0.0; Lhu = 0.0; Rh = df1; Rhu = df2; }
   }
   if (wallR) { Rh = 0.0; Rhu = 0.0; }
   if (wallL) { Lh = 0.0; Lhu = 0.0; }

@@ -51,9 +51,13 @@ PCG_HD uint64_t mulhi(uint64_t a, uint64_t b) {
 #endif
 }
 
+// On the device the bits move through an opaque register copy, so that the
+// compiler does not turn integer tests on them back into FP64 instructions.
 PCG_HD uint64_t bits(double x) {
 #if defined(__CUDA_ARCH__)
-  return (uint64_t)__double_as_longlong(x);
+  uint64_t u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  return u;
 #else
   uint64_t u;
   std::memcpy(&u, &x, 8);
@@ -63,7 +67,9 @@ PCG_HD uint64_t bits(double x) {
 
 PCG_HD double from_bits(uint64_t u) {
 #if defined(__CUDA_ARCH__)
-  return __longlong_as_double((long long)u);
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+  return x;
 #else
   double x;
   std::memcpy(&x, &u, 8);
