@@ -32,10 +32,12 @@ METRIC = "SWE cell-updates/s batched vs per-patch on 1 GB300; p50/p99 scenario l
 UNIT = "cell-updates/s"
 
 # Algorithmic FP64 work of one cell update (wet cell, subsonic edges), counted
-# from the f-wave operation list of pcg_device.cuh (FMA = 2 flops, divide and
-# square root = 1 flop each): per cell 6 ops (sqrt, 1/s, p, q, p^2, q^2); per
-# edge 19 plain ops + 3 FMA (2 edges per cell); accumulation 8 FMA; update 3 FMA.
-FLOP_PER_CELL = 6 + 2 * (19 + 2 * 3) + 2 * 8 + 2 * 3
+# from the f-wave operation list of pcg_device.cuh (FMA = 2 flops, divide,
+# reciprocal and square root = 1 flop each): per cell 7 ops (sqrt, 1/s, p, q,
+# p^2, q^2, h + b); per edge 17 plain ops (8 adds, 5 multiplies, 2 cbar, sqrt,
+# divide, reciprocal) + 3 FMA (2 edges per cell); accumulation 8 FMA; update
+# 3 FMA.
+FLOP_PER_CELL = 7 + 2 * (17 + 2 * 3) + 2 * 8 + 2 * 3
 # Algorithmic bytes per patch step: read h, hu, hv, b with halo, write h, hu, hv.
 def bytes_per_patch(n):
     return 8 * (4 * (n + 2) ** 2 + 3 * n * n)
@@ -56,7 +58,7 @@ def profile_figure(name, key):
 # FP64 instructions per cell update of the strip sweep (ncu count, see
 # profiles/k_sweep_strips_uneven_patches_4k.md) and the FP64 pipe width of
 # GB300 (FP64 lanes per clock per SM; the DFMA probe reaches it).
-FP64_INST_PER_CELL = 60.2
+FP64_INST_PER_CELL = profile_figure("k_sweep_strips_uneven_patches_4k.md", "fp64_inst_per_cell_update") or 46.2
 FP64_LANES_PER_SM_CLK = 2
 
 
