@@ -223,6 +223,14 @@ int pcg_refinement_indicator(pcg_context *ctx, int32_t n, const int32_t *ids, do
 int pcg_gather_cells(pcg_context *ctx, int32_t n, const int32_t *ids, double *out, int64_t out_len);
 /* Time intervals of the listed patches in one call. */
 int pcg_patches_get_time(pcg_context *ctx, int32_t n, const int32_t *ids, pcg_patch_time *out);
+/* Neighbouring ghost-layer bounds (restr_lower / restr_upper of
+ * pcg_patch_time) of the listed patches in one call: lower[2k], lower[2k+1],
+ * upper[2k], upper[2k+1] for ids[k]; the other time fields are kept.  The
+ * reference accumulates these bounds per virtual patch during the traversal
+ * (GhostLayerCompositor::updateLower/UpperGhostlayerBound,
+ * GhostLayerCompositor.cpp:177-259); ids must be distinct. */
+int pcg_patches_set_restriction_bounds(pcg_context *ctx, int32_t n, const int32_t *ids, const double *lower,
+                                       const double *upper);
 
 /* ------------------------------------------------------ batched grid step */
 

@@ -1,9 +1,9 @@
 """Adaptive grids of n x n patches with Peano-style 3x refinement, and dynamic
 remeshing driven by the device-side refinement criterion.
 
-`AmrGrid` holds the hierarchy as sets of patch slots per level (level l has
-(base * 3^l)^2 slots on [0,1]^2; a refined slot's patch is virtual and its 9
-children exist on level l+1) and derives from it what the Peano traversal
+`AmrGrid` holds the hierarchy as boolean arrays over the patch slots of each
+level (level l has (base * 3^l)^2 slots on [0,1]^2; a refined slot's patch is
+virtual and its 9 children exist on level l+1) and derives from it what the Peano traversal
 derives per grid iteration: the ghost face-pair list (same-level copies,
 coarse-to-fine interpolation; GhostlayerCompositorFunctors.cpp:23-148), the
 flux-correction list (fine leaf faces against a coarser neighbour), the
@@ -37,13 +37,73 @@ DIRECTIONS = ((-1, 0), (1, 0), (0, -1), (0, 1), (-1, -1), (1, -1), (-1, 1), (1, 
 
 
 class AmrGrid:
+    """The hierarchy as one boolean array per level over its slots:
+    `exists` (the slot holds a patch) and `refined` (its patch is virtual and
+    its 9 children exist).  The set views `grid.exists[l]` / `grid.refined[l]`
+    (sets of (i, j)) are derived on demand; assigning them (sets or arrays)
+    replaces the state."""
+
     def __init__(self, base, n, levels, buffers=(1, 2), threshold=0.1):
         self.base, self.n, self.levels = base, n, levels
         self.buffers = tuple(buffers)
         self.threshold = threshold
-        self.exists = [set() for _ in range(levels)]
-        self.refined = [set() for _ in range(levels)]
-        self.exists[0] = {(i, j) for i in range(base) for j in range(base)}
+        self._E = [np.zeros((m, m), dtype=bool) for m in self._sizes()]
+        self._R = [np.zeros((m, m), dtype=bool) for m in self._sizes()]
+        self._E[0][:] = True
+        self._cache = {}
+
+    def _sizes(self):
+        return [self.slots_per_edge(l) for l in range(self.levels)]
+
+    # ----------------------------------------------------------------- state
+    def arrays(self):
+        """(exists, refined): lists of per-level boolean arrays (not copies)."""
+        return self._E, self._R
+
+    def set_arrays(self, E, R):
+        self._E = [np.array(e, dtype=bool) for e in E]
+        self._R = [np.array(r, dtype=bool) for r in R]
+        self._cache = {}
+
+    def _to_arrays(self, sets):
+        out = []
+        for l, m in enumerate(self._sizes()):
+            a = np.zeros((m, m), dtype=bool)
+            v = sets[l]
+            if isinstance(v, np.ndarray):
+                a[:] = v
+            elif len(v):
+                ij = np.array(list(v), dtype=np.int64).reshape(-1, 2)
+                a[ij[:, 0], ij[:, 1]] = True
+            out.append(a)
+        return out
+
+    def _sets(self, key, arrs):
+        if key not in self._cache:
+            out = []
+            for a in arrs:
+                ii, jj = np.nonzero(a)
+                out.append(set(zip(ii.tolist(), jj.tolist())))
+            self._cache[key] = out
+        return self._cache[key]
+
+    @property
+    def exists(self):
+        return self._sets("exists", self._E)
+
+    @exists.setter
+    def exists(self, v):
+        self._E = self._to_arrays(v)
+        self._cache = {}
+
+    @property
+    def refined(self):
+        return self._sets("refined", self._R)
+
+    @refined.setter
+    def refined(self, v):
+        self._R = self._to_arrays(v)
+        self._cache = {}
 
     # -------------------------------------------------------------- geometry
     def slots_per_edge(self, l):
@@ -54,7 +114,10 @@ class AmrGrid:
         return (i * L, j * L), (L, L)
 
     def is_leaf(self, l, i, j):
-        return (i, j) in self.exists[l] and (i, j) not in self.refined[l]
+        m = self.slots_per_edge(l)
+        if not (0 <= l < self.levels and 0 <= i < m and 0 <= j < m):
+            return False
+        return bool(self._E[l][i, j] and not self._R[l][i, j])
 
     def wall(self, l, i, j):
         if not self.is_leaf(l, i, j):
@@ -67,56 +130,127 @@ class AmrGrid:
         if j == m - 1: w |= 8
         return w
 
+    def slot_arrays(self):
+        """Patch order as arrays (level, i, j, refined) (cached)."""
+        if "slots" not in self._cache:
+            lv, si, sj, rf = [], [], [], []
+            for l in range(self.levels):
+                ii, jj = np.nonzero(self._E[l])
+                lv.append(np.full(len(ii), l, dtype=np.int64))
+                si.append(ii)
+                sj.append(jj)
+                rf.append(self._R[l][ii, jj])
+            self._cache["slots"] = tuple(np.concatenate(x) for x in (lv, si, sj, rf))
+        return self._cache["slots"]
+
     def order(self):
         """Slots in patch order: level ascending, then (i, j)."""
-        return [(l, i, j) for l in range(self.levels) for (i, j) in sorted(self.exists[l])]
+        if "order" not in self._cache:
+            lv, si, sj, _ = self.slot_arrays()
+            self._cache["order"] = list(zip(lv.tolist(), si.tolist(), sj.tolist()))
+        return list(self._cache["order"])
 
     def leaves(self):
-        return [s for s in self.order() if self.is_leaf(*s)]
+        if "leaves" not in self._cache:
+            lv, si, sj, rf = self.slot_arrays()
+            k = ~rf
+            self._cache["leaves"] = list(zip(lv[k].tolist(), si[k].tolist(), sj[k].tolist()))
+        return list(self._cache["leaves"])
 
     def buffer(self, l):
         return self.buffers[l] if l < len(self.buffers) else 1
 
     # ------------------------------------------------------------- hierarchy
-    def _grow(self, core, l, exists_l):
-        buf = self.buffer(l)
-        out = set()
-        for (i, j) in core:
-            for di in range(-buf, buf + 1):
-                for dj in range(-buf, buf + 1):
-                    if (i + di, j + dj) in exists_l:
-                        out.add((i + di, j + dj))
+    @staticmethod
+    def _dilate(a, b):
+        """Slots within Chebyshev distance b of a marked slot."""
+        if b <= 0:
+            return a.copy()
+        m0, m1 = a.shape
+        p = np.pad(a, b)
+        out = np.zeros_like(a)
+        for di in range(2 * b + 1):
+            for dj in range(2 * b + 1):
+                out |= p[di:di + m0, dj:dj + m1]
         return out
+
+    @staticmethod
+    def _children(a):
+        return a.repeat(3, axis=0).repeat(3, axis=1)
 
     def refine_from(self, flags):
         """Build the hierarchy top-down from refinement flags: flags(l, i, j)
         is called for every existing slot of levels 0 .. levels-2."""
+        E = [e.copy() for e in self._E]
+        R = [np.zeros_like(e) for e in E]
         for l in range(self.levels - 1):
-            core = {s for s in self.exists[l] if flags(l, *s)}
-            self.refined[l] = self._grow(core, l, self.exists[l])
-            self.exists[l + 1] = {(3 * i + a, 3 * j + c) for (i, j) in self.refined[l]
-                                  for a in range(3) for c in range(3)}
-        self.refined[self.levels - 1] = set()
+            core = np.zeros_like(E[l])
+            for i, j in zip(*np.nonzero(E[l])):
+                core[i, j] = bool(flags(l, int(i), int(j)))
+            R[l] = self._dilate(core, self.buffer(l)) & E[l]
+            E[l + 1] = self._children(R[l])
+        self.set_arrays(E, R)
+
+    def _values(self, g):
+        """Per-level arrays of the criterion g (dict (l, i, j) -> value, or an
+        object with an `arrays` attribute (level, i, j, value)); 0 where absent."""
+        G = [np.zeros((m, m)) for m in self._sizes()]
+        if hasattr(g, "arrays"):
+            lv, ii, jj, vv = g.arrays
+        elif len(g):
+            kk = np.array(list(g.keys()), dtype=np.int64).reshape(-1, 3)
+            lv, ii, jj = kk[:, 0], kk[:, 1], kk[:, 2]
+            vv = np.fromiter(g.values(), dtype=np.float64, count=len(g))
+        else:
+            return G
+        for l in range(self.levels):
+            k = lv == l
+            G[l][ii[k], jj[k]] = vv[k]
+        return G
 
     def decide(self, g):
-        """Next (exists, refined) from the refinement criterion g[(l, i, j)] of
-        every leaf.  Returns new lists of sets; the grid itself is unchanged."""
+        """Next (exists, refined), as per-level boolean arrays, from the
+        refinement criterion g[(l, i, j)] of every leaf; the grid itself is
+        unchanged.  A refined slot stays refined unless all 9 children are
+        leaves below the threshold; a leaf above the threshold refines;
+        refined regions grow by buffers[l] slots within the existing ones."""
         thr = self.threshold
         L = self.levels
-        # a refined slot stays refined unless all 9 children are leaves below
-        # the threshold (a refined child, or a leaf at or above it, keeps it)
+        G = self._values(g)
+        leaf = [self._E[l] & ~self._R[l] for l in range(L)]
+        keep = []
+        for l in range(L - 1):
+            m = self.slots_per_edge(l)
+            ok = (leaf[l + 1] & (G[l + 1] < thr)).reshape(m, 3, m, 3).all(axis=(1, 3))
+            keep.append(self._R[l] & ~ok)
+        E = [self._E[0].copy()] + [None] * (L - 1)
+        R = [None] * L
+        for l in range(L - 1):
+            core = (keep[l] & E[l]) | (E[l] & leaf[l] & (G[l] > thr))
+            R[l] = self._dilate(core, self.buffer(l)) & E[l]
+            E[l + 1] = self._children(R[l])
+        R[L - 1] = np.zeros_like(E[L - 1])
+        return E, R
+
+    def decide_py(self, g):
+        """decide() on the set views, slot by slot (the reference for tests).
+        Returns lists of sets."""
+        thr = self.threshold
+        L = self.levels
         keep = [set() for _ in range(L)]
         for l in range(L - 1):
             for (i, j) in self.refined[l]:
                 kids = [(3 * i + a, 3 * j + c) for a in range(3) for c in range(3)]
-                if any(not (self.is_leaf(l + 1, *ch) and g[(l + 1,) + ch] < thr) for ch in kids):
+                if any(not (self.is_leaf(l + 1, *ch) and g.get((l + 1,) + ch, 0.0) < thr) for ch in kids):
                     keep[l].add((i, j))
         exists = [set(self.exists[0])] + [set() for _ in range(L - 1)]
         refined = [set() for _ in range(L)]
         for l in range(L - 1):
             core = {s for s in keep[l] if s in exists[l]}
             core |= {s for s in exists[l] if self.is_leaf(l, *s) and g.get((l,) + s, 0.0) > thr}
-            refined[l] = self._grow(core, l, exists[l])
+            buf = self.buffer(l)
+            refined[l] = {(i + di, j + dj) for (i, j) in core for di in range(-buf, buf + 1)
+                          for dj in range(-buf, buf + 1) if (i + di, j + dj) in exists[l]}
             exists[l + 1] = {(3 * i + a, 3 * j + c) for (i, j) in refined[l]
                              for a in range(3) for c in range(3)}
         return exists, refined
@@ -129,9 +263,9 @@ class AmrGrid:
         from . import pcg as P
         order = self.order()
         npch = len(order)
-        arr = np.array(order, dtype=np.int32).reshape(-1, 3)
-        lvl, si, sj = (np.ascontiguousarray(arr[:, k]) for k in range(3))
-        ref = np.array([0 if self.is_leaf(*s) else 1 for s in order], dtype=np.uint8)
+        lv, ii, jj, rf = self.slot_arrays()
+        lvl, si, sj = (np.ascontiguousarray(a, dtype=np.int32) for a in (lv, ii, jj))
+        ref = rf.astype(np.uint8)
         items = np.zeros((8 * npch + 1, 9), dtype=np.int32)
         flux = np.zeros((4 * npch + 1, 4), dtype=np.int32)
         restr = np.zeros((self.levels * npch + 1, 2), dtype=np.int32)
@@ -148,14 +282,39 @@ class AmrGrid:
         L = 1.0 / (self.base * np.power(3.0, lvl.astype(np.float64)))
         pos = np.stack([si * L, sj * L], axis=1)
         size = np.stack([L, L], axis=1)
-        index = {s: k for k, s in enumerate(order)}
+        index = dict(zip(order, range(npch)))
         leaf = (ref == 0).tolist()
         return {"order": order, "index": index, "pos": pos, "size": size,
                 "leaf": leaf, "level": lvl.tolist(), "wall": walls[:npch].tolist(),
                 "items": items[:ni.value].copy(), "flux_items": flux[:nf.value].copy(),
                 "restrict_items": restr[:nr.value].copy(),
                 "restr_lower": lower[:npch].copy(), "restr_upper": upper[:npch].copy(),
-                "virtual_time_items": virtual_time_items(order, index, leaf)}
+                "virtual_time_items": self._virtual_time_items(lv, ii, jj, rf)}
+
+    def _virtual_time_items(self, lv, ii, jj, rf):
+        """virtual_time_items() on the slot arrays: every leaf against each
+        refined ancestor, found by binary search of the ancestors' keys in the
+        patch order (which is sorted by (level, i, j))."""
+        M = self.slots_per_edge(self.levels - 1)
+        keys = (lv * M + ii) * M + jj
+        lf = np.nonzero(~rf)[0]
+        vs, ss = [], []
+        for d in range(1, self.levels):
+            s = lf[lv[lf] >= d]
+            f = 3 ** d
+            ak = ((lv[s] - d) * M + ii[s] // f) * M + jj[s] // f
+            pos = np.searchsorted(keys, ak)
+            ok = pos < len(keys)
+            ok[ok] = keys[pos[ok]] == ak[ok]
+            ok[ok] = rf[pos[ok]]
+            vs.append(pos[ok])
+            ss.append(s[ok])
+        if not vs:
+            return np.zeros((0, 2), dtype=np.int32)
+        v = np.concatenate(vs)
+        s = np.concatenate(ss)
+        o = np.lexsort((s, v))
+        return np.stack([s[o], v[o]], axis=1).astype(np.int32).reshape(-1, 2)
 
     def layout_py(self):
         """Patch order and every list the batched step needs, in patch-order
@@ -270,20 +429,21 @@ def remesh(grid, backend, g, b_of):
     switch_to_leaf(handle), install(layout, handles), restrict_all().
     Returns (#refined, #coarsened)."""
     from .scenarios import _centers
-    exists, refined = grid.decide(g)
-    if exists == grid.exists and refined == grid.refined:
+    E1, R1 = grid.decide(g)
+    E0, R0 = grid.arrays()
+    if all(np.array_equal(a, b) for a, b in zip(E1 + R1, E0 + R0)):
         return 0, 0
     n = grid.n
     n_ref = n_crs = 0
     # refinement, coarse to fine: children of newly refined slots
     for l in range(grid.levels - 1):
-        for (i, j) in sorted(refined[l] - grid.refined[l]):
+        for i, j in np.argwhere(R1[l] & ~R0[l]).tolist():
             parent = backend.handle((l, i, j))
             t = backend.times(parent)
             for a in range(3):
                 for c in range(3):
                     ch = (l + 1, 3 * i + a, 3 * j + c)
-                    if (ch[1], ch[2]) in grid.exists[l + 1]:
+                    if E0[l + 1][ch[1], ch[2]]:
                         continue
                     pos, size = grid.geometry(*ch)
                     h = backend.alloc(ch, pos, size, l + 1)
@@ -294,7 +454,7 @@ def remesh(grid, backend, g, b_of):
             n_ref += 1
     # coarsening, fine to coarse: restrict the children into their parent
     for l in range(grid.levels - 2, -1, -1):
-        for (i, j) in sorted(grid.refined[l] - refined[l]):
+        for i, j in np.argwhere(R0[l] & ~R1[l]).tolist():
             parent = backend.handle((l, i, j))
             kids = [(l + 1, 3 * i + a, 3 * j + c) for a in range(3) for c in range(3)]
             hk = [backend.handle(k) for k in kids]
@@ -306,12 +466,14 @@ def remesh(grid, backend, g, b_of):
                 backend.free(h)
                 backend.forget(k)
             n_crs += 1
-    old_state = {s: (grid.is_leaf(*s), grid.wall(*s)) for s in grid.order()}
-    grid.exists, grid.refined = exists, refined
+    # slots that are new or changed between leaf and refined get their flags
+    changed = [E1[l] & (~E0[l] | (R1[l] != R0[l])) for l in range(grid.levels)]
+    grid.set_arrays(E1, R1)
     lay = grid.layout()
-    for s, leaf, w in zip(lay["order"], lay["leaf"], lay["wall"]):
-        if old_state.get(s) != (leaf, w) or s not in old_state:
-            backend.set_leaf(backend.handle(s), leaf, w)
+    for l in range(grid.levels):
+        for i, j in np.argwhere(changed[l]).tolist():
+            k = lay["index"][(l, i, j)]
+            backend.set_leaf(backend.handle((l, i, j)), lay["leaf"][k], lay["wall"][k])
     backend.install(lay, [backend.handle(s) for s in lay["order"]])
     # virtual patches (new ones included) receive the restriction of the
     # current leaves before the next ghost fill reads them
@@ -326,7 +488,7 @@ class DeviceAmr:
         self.ctx, self.grid, self.b_of = ctx, grid, b_of
         self.flux, self.g_flux = flux, g_flux
         self.pid = {}
-        self._bounds = {}   # restriction bounds last written per virtual patch
+        self._bounds = None   # (virtual?, lower, upper) last written, per patch id
         self.timing = {}
 
     # -- remesh protocol
@@ -385,17 +547,27 @@ class DeviceAmr:
 
     def install(self, lay, handles):
         ids = np.asarray(handles, dtype=np.int32)
-        bounds = {}
-        for k, pid in enumerate(ids):
-            if not lay["leaf"][k]:
-                b = (tuple(lay["restr_lower"][k]), tuple(lay["restr_upper"][k]))
-                bounds[int(pid)] = b
-                if self._bounds.get(int(pid)) == b:
-                    continue
-                t = self.ctx.get_time(int(pid))
-                self.ctx.set_time(int(pid), time=t["time"], dt=t["dt"], est_next=t["est_next"],
-                                  restr_lower=b[0], restr_upper=b[1])
-        self._bounds = bounds
+        # restriction bounds of the virtual patches whose bounds are new or
+        # changed since the last install, in one call
+        virt = ~np.asarray(lay["leaf"], dtype=bool)
+        vid = ids[virt]
+        lo = np.asarray(lay["restr_lower"], dtype=np.float64).reshape(-1, 2)[virt]
+        up = np.asarray(lay["restr_upper"], dtype=np.float64).reshape(-1, 2)[virt]
+        m = int(ids.max()) + 1 if len(ids) else 0
+        if self._bounds is None or len(self._bounds[0]) < m:
+            old = self._bounds
+            self._bounds = (np.zeros(m, dtype=bool), np.zeros((m, 2)), np.zeros((m, 2)))
+            if old is not None:
+                k = len(old[0])
+                self._bounds[0][:k], self._bounds[1][:k], self._bounds[2][:k] = old
+        known, plo, pup = self._bounds
+        changed = ~known[vid] | (plo[vid] != lo).any(axis=1) | (pup[vid] != up).any(axis=1)
+        if changed.any():
+            self.ctx.set_restriction_bounds(vid[changed], lo[changed], up[changed])
+        known[:] = False
+        known[vid] = True
+        plo[vid] = lo
+        pup[vid] = up
         from .scenarios import remap_items
         self.ctx.set_ghost_items(remap_items(lay["items"], ids))
         r = lay["restrict_items"]

@@ -66,6 +66,16 @@ __global__ void k_fp64_probe(double *out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// Restriction bounds (lower x, y, upper x, y) of listed patches.
+__global__ void k_scatter_bounds(const long long *__restrict__ ids, const double *__restrict__ b, int n,
+                                 pcg::PatchTimeDev *__restrict__ times) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    pcg::PatchTimeDev &T = times[ids[k]];
+    T.rl[0] = b[4 * k]; T.rl[1] = b[4 * k + 1];
+    T.ru[0] = b[4 * k + 2]; T.ru[1] = b[4 * k + 3];
+  }
+}
+
 // Self-check of the integer-pipe divide / square root against the hardware
 // IEEE operations on pseudo-random operands (splitmix64 of seed and index).
 __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
@@ -1227,6 +1237,35 @@ int pcg_patches_get_time(pcg_context *c, int32_t n, const int32_t *ids, pcg_patc
     out[k].restr_lower[0] = T.rl[0]; out[k].restr_lower[1] = T.rl[1];
     out[k].restr_upper[0] = T.ru[0]; out[k].restr_upper[1] = T.ru[1];
   }
+  return PCG_OK;
+}
+
+int pcg_patches_set_restriction_bounds(pcg_context *c, int32_t n, const int32_t *ids, const double *lower,
+                                       const double *upper) {
+  if (!c || n < 0 || (n > 0 && (!ids || !lower || !upper))) return fail(PCG_E_INVALID, "bad arguments");
+  if (n == 0) return PCG_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  std::vector<char> seen(c->max_patches, 0);
+  std::vector<long long> meta(n);
+  std::vector<double> b(4 * (size_t)n);
+  for (int32_t k = 0; k < n; k++) {
+    if (!valid_id(c, ids[k])) return fail(PCG_E_INVALID, "unknown patch id " + std::to_string(ids[k]));
+    if (seen[ids[k]]) return fail(PCG_E_INVALID, "patch id " + std::to_string(ids[k]) + " listed twice");
+    seen[ids[k]] = 1;
+    meta[k] = ids[k];
+    b[4 * k] = lower[2 * k]; b[4 * k + 1] = lower[2 * k + 1];
+    b[4 * k + 2] = upper[2 * k]; b[4 * k + 3] = upper[2 * k + 1];
+  }
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = ensure_staging(c, b.size(), (size_t)n);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(c->d_copy_meta, meta.data(), sizeof(long long) * meta.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+  PCG_CUDA(cudaMemcpyAsync(c->d_staging, b.data(), sizeof(double) * b.size(), cudaMemcpyHostToDevice, c->stream));
+  k_scatter_bounds<<<std::min(1024, (n + 255) / 256), 256, 0, c->stream>>>(c->d_copy_meta, c->d_staging, n,
+                                                                             c->d_times);
+  PCG_CUDA(cudaGetLastError());
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
   return PCG_OK;
 }
 

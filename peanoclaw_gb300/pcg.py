@@ -116,6 +116,7 @@ SIGNATURES = {
     "pcg_clear_subgrid": (C.c_int, [_CTX, C.c_int32]),
     "pcg_gather_cells": (C.c_int, [_CTX, C.c_int32, _I2, _D, C.c_int64]),
     "pcg_patches_get_time": (C.c_int, [_CTX, C.c_int32, _I2, C.POINTER(PatchTime)]),
+    "pcg_patches_set_restriction_bounds": (C.c_int, [_CTX, C.c_int32, _I2, _D, _D]),
     "pcg_switch_to_leaf": (C.c_int, [_CTX, C.c_int32]),
     "pcg_amr_layout": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _I2, _I2, _I2,
                                  C.POINTER(C.c_uint8), _I2, _I2, _I2, _I2, _I2, _I2, _D, _D, _I2]),
@@ -326,6 +327,17 @@ class Context:
         arr = (PatchTime * max(1, len(ids)))()
         check(lib().pcg_patches_get_time(self.h, len(ids), ids.ctypes.data_as(_I2), arr))
         return np.array([[arr[k].time, arr[k].dt] for k in range(len(ids))]).reshape(-1, 2)
+
+    def set_restriction_bounds(self, ids, lower, upper):
+        """Restriction bounds of many patches (pcg_patches_set_restriction_bounds);
+        lower and upper are (n, 2) arrays."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        lo = np.ascontiguousarray(lower, dtype=np.float64).reshape(-1, 2)
+        up = np.ascontiguousarray(upper, dtype=np.float64).reshape(-1, 2)
+        if len(lo) != len(ids) or len(up) != len(ids):
+            raise ValueError("ids, lower and upper differ in length")
+        check(lib().pcg_patches_set_restriction_bounds(self.h, len(ids), ids.ctypes.data_as(_I2), dptr(lo),
+                                                       dptr(up)))
 
     def switch_to_leaf(self, pid):
         check(lib().pcg_switch_to_leaf(self.h, int(pid)))

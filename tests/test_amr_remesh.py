@@ -97,5 +97,26 @@ def test_native_layout_equals_the_python_builder():
         a, b = g.layout(), g.layout_py()
         assert a["order"] == b["order"]
         for k in ("items", "flux_items", "restrict_items", "restr_lower", "restr_upper", "wall",
-                  "leaf", "level", "pos", "size"):
+                  "leaf", "level", "pos", "size", "virtual_time_items"):
             assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+
+
+def test_array_decision_equals_the_slot_by_slot_decision():
+    """AmrGrid.decide (per-level arrays) and AmrGrid.decide_py (sets, slot by
+    slot) give the same next hierarchy for random criterion values around
+    the threshold, on grids with and without refined regions."""
+    rng = np.random.default_rng(7)
+    grids = [S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0).grid,
+             S.breaking_dam_amr(base=4, n=6, levels=3, buffers=(2, 1)).grid,
+             S.adaptive_tsunami(base=5, n=8, levels=3).grid,
+             AmrGrid(3, 4, 2)]
+    for grid in grids:
+        leaves = grid.leaves()
+        for scale in (0.5, 1.0, 2.0):
+            vals = rng.uniform(0.0, 2.0 * scale * grid.threshold, len(leaves))
+            g = dict(zip(leaves, vals.tolist()))
+            E, R = grid.decide(g)
+            e2, r2 = grid.decide_py(g)
+            for l in range(grid.levels):
+                assert set(map(tuple, np.argwhere(E[l]).tolist())) == e2[l]
+                assert set(map(tuple, np.argwhere(R[l]).tolist())) == r2[l]

@@ -65,3 +65,35 @@ def test_remesh_matches_the_oracle(mode):
             assert (t["time"], t["dt"]) == (p.s.time, p.s.dt)
     finally:
         ctx.close()
+
+
+def test_batched_restriction_bounds():
+    """pcg_patches_set_restriction_bounds writes the bounds of every listed
+    patch, keeps their other time fields and rejects repeated ids."""
+    import ctypes as C
+    ctx = P.Context(slab_doubles=1_000_000, max_patches=16, max_groups=1, params=PRM)
+    try:
+        ids = [ctx.alloc(8, pos=(0.1 * k, 0.0), size=(0.1, 0.1)) for k in range(6)]
+        for k, pid in enumerate(ids):
+            ctx.set_time(pid, time=0.5 + k, dt=0.25, est_next=0.125)
+        sel = np.array(ids[1:5], dtype=np.int32)
+        lo = np.arange(8, dtype=np.float64).reshape(4, 2) * 0.01
+        up = 1.0 + lo
+        ctx.set_restriction_bounds(sel, lo, up)
+        arr = (P.PatchTime * len(ids))()
+        P.check(P.lib().pcg_patches_get_time(ctx.h, len(ids), np.asarray(ids, dtype=np.int32).ctypes.data_as(
+            C.POINTER(C.c_int32)), arr))
+        big = np.finfo(np.float64).max
+        for k, pid in enumerate(ids):
+            t = arr[k]
+            assert (t.time, t.dt, t.est_next) == (0.5 + k, 0.25, 0.125)
+            if 1 <= k <= 4:
+                assert tuple(t.restr_lower) == tuple(lo[k - 1]) and tuple(t.restr_upper) == tuple(up[k - 1])
+            else:
+                assert tuple(t.restr_lower) == (big, big) and tuple(t.restr_upper) == (-big, -big)
+        with pytest.raises(P.PcgError):
+            ctx.set_restriction_bounds([ids[0], ids[0]], np.zeros((2, 2)), np.zeros((2, 2)))
+        with pytest.raises(P.PcgError):
+            ctx.set_restriction_bounds([99], np.zeros((1, 2)), np.zeros((1, 2)))
+    finally:
+        ctx.close()
