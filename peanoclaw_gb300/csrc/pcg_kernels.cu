@@ -1005,13 +1005,134 @@ __global__ void k_restrict(double *slab, const PatchDev *patches, const PatchTim
 }
 
 // Batched restriction: block b handles the items [begin[b], begin[b+1]) that
-// all share one destination, in list order.
-__global__ void k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                                 const int4 *items, const int *begin, const int *group_active) {
+// all share one destination, in list order, and within an item its regions
+// in order (the same sequence as restrict_block).  One warp per destination
+// cell: the lanes evaluate the contributions of up to 32 source cells at a
+// time, lane 0 adds them to the cell's uOld / uNew values in source-cell
+// order, so every sum is formed in the reference's order.
+constexpr int kRestrWarps = 8;
+__global__ void __launch_bounds__(kRestrWarps * 32)
+    k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                     const int4 *items, const int *begin, const int *group_active) {
+  __shared__ double W[kRestrWarps][32][6];
   if (group_active && !group_active[patches[items[begin[blockIdx.x]].y].group]) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
-    int4 it = items[k];  // src, dst, only_overlapped, swe
-    restrict_block(slab, patches[it.x], times[it.x], patches[it.y], times[it.y], it.z != 0, it.w != 0);
+    const int4 it = items[k];  // src, dst, only_overlapped, swe
+    const PatchDev S = patches[it.x], D = patches[it.y];
+    const PatchTimeDev ST = times[it.x], DT = times[it.y];
+    const bool only_overlapped = it.z != 0, swe = it.w != 0;
+    if (D.nq > 3) {
+      restrict_block(slab, S, ST, D, DT, only_overlapped, swe);
+      __syncthreads();
+      continue;
+    }
+    int roff[8], rsz[8], nr;
+    int n[2] = {S.nx, S.ny};
+    if (only_overlapped) {
+      double sp[2] = {S.pos[0], S.pos[1]}, ss[2] = {S.size[0], S.size[1]};
+      double sub[2] = {subcell(S, 0), subcell(S, 1)};
+      nr = regions_overlapped(DT.rl, DT.ru, sp, ss, sub, n, roff, rsz);
+    } else {
+      nr = 1;
+      roff[0] = 0; roff[1] = 0; rsz[0] = n[0]; rsz[1] = n[1];
+    }
+    const double eps = 1e-12;
+    const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
+    const double dsub[2] = {iter_sub(D, 0), iter_sub(D, 1)};
+    const double dvol = __dmul_rn(dsub[0], dsub[1]);
+    double tfo = 1.0, tfn = 1.0;
+    if (tl_greater(ST.dt, 0.0)) {
+      double so = time_uold(S, ST), su = time_unew(S, ST);
+      tfo = __ddiv_rn(__dsub_rn(0.0, so), __dsub_rn(su, so));
+      tfn = __ddiv_rn(__dsub_rn(1.0, so), __dsub_rn(su, so));
+    }
+    const double itfo = __dsub_rn(1.0, tfo), itfn = __dsub_rn(1.0, tfn);
+    for (int r = 0; r < nr; r++) {
+      const int *ro = &roff[2 * r], *rs = &rsz[2 * r];
+      if (only_overlapped && !(rs[0] > 0 && rs[1] > 0)) continue;
+      int doff[2], dsz[2];
+      map_to_patch(ro, rs, S, D, eps, doff, dsz);
+      const int ncell = dsz[0] > 0 && dsz[1] > 0 ? dsz[0] * dsz[1] : 0;
+      for (int c = wid; c < ncell; c += kRestrWarps) {
+        const int x = doff[0] + c / dsz[1], y = doff[1] + c % dsz[1];
+        const double dpos[2] = {iter_pos(D, 0, x), iter_pos(D, 1, y)};
+        int coff[2], csz[2];
+        for (int d = 0; d < 2; d++) {
+          double ot = __ddiv_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
+          int o = (int)ot;
+          double st = __ddiv_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
+          st = __dsub_rn(st, ot);
+          st = __dadd_rn(st, 1.0);
+          int up = o + (int)st;
+          int rup = ro[d] + rs[d];
+          int oo = o > ro[d] ? o : ro[d];
+          int uu = up < rup ? up : rup;
+          coff[d] = oo;
+          csz[d] = uu - oo;
+        }
+        const int nsrc = csz[0] > 0 && csz[1] > 0 ? csz[0] * csz[1] : 0;
+        if (nsrc == 0) continue;
+        double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (lane == 0) {
+#pragma unroll
+          for (int q = 0; q < 3; q++)
+            if (q < D.nq) {
+              acc[q] = slab[idx_uold(D, q, x, y)];
+              acc[3 + q] = slab[idx_unew(D, q, x, y)];
+            }
+        }
+        for (int base = 0; base < nsrc; base += 32) {
+          const int kk = base + lane;
+          if (kk < nsrc) {
+            const int sx = coff[0] + kk / csz[1], sy = coff[1] + kk % csz[1];
+            const double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
+            double region = 1.0;
+            for (int d = 0; d < 2; d++) {
+              double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
+              double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
+              region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
+              region = fmax(region, 0.0);
+            }
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+              if (q >= D.nq) break;
+              double vo = slab[idx_uold(S, q, sx, sy)];
+              double vn = slab[idx_unew(S, q, sx, sy)];
+              if (swe && q == 0) {
+                double bb = slab[idx_pw(S, 0, sx, sy)];
+                vo = __dadd_rn(vo, bb);
+                vn = __dadd_rn(vn, bb);
+              }
+              W[wid][lane][q] = __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfo), __dmul_rn(vn, tfo)), region), dvol);
+              W[wid][lane][3 + q] = __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfn), __dmul_rn(vn, tfn)), region), dvol);
+            }
+          }
+          __syncwarp();
+          if (lane == 0) {
+            const int m = nsrc - base < 32 ? nsrc - base : 32;
+            for (int j = 0; j < m; j++) {
+#pragma unroll
+              for (int q = 0; q < 3; q++)
+                if (q < D.nq) {
+                  acc[q] = __dadd_rn(acc[q], W[wid][j][q]);
+                  acc[3 + q] = __dadd_rn(acc[3 + q], W[wid][j][3 + q]);
+                }
+            }
+          }
+          __syncwarp();
+        }
+        if (lane == 0) {
+#pragma unroll
+          for (int q = 0; q < 3; q++)
+            if (q < D.nq) {
+              slab[idx_uold(D, q, x, y)] = acc[q];
+              slab[idx_unew(D, q, x, y)] = acc[3 + q];
+            }
+        }
+      }
+      __syncthreads();
+    }
     __syncthreads();
   }
 }
@@ -1127,14 +1248,76 @@ __global__ void k_flux_correction(double *slab, const PatchDev *patches, const P
 }
 
 // Batched flux correction: block b applies the items [begin[b], begin[b+1])
-// (all with the same destination) in list order.
-__global__ void k_flux_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                             const int4 *items, const int *begin, const int *group_active) {
-  if (threadIdx.x != 0) return;
+// (all with the same destination) in list order.  Within an item one thread
+// owns each destination face cell and adds the corrections of the source
+// face cells that overlap it in source order (the order of
+// flux_correction_one); the source cells' destination ranges are computed
+// once per item into shared memory.
+constexpr int kFluxThreads = 32;
+constexpr int kFluxMaxCells = 1024;
+__global__ void __launch_bounds__(kFluxThreads)
+    k_flux_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                 const int4 *items, const int *begin, const int *group_active) {
+  __shared__ int s_lb[kFluxMaxCells], s_ub[kFluxMaxCells];
   for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
-    int4 it = items[k];  // src, dst, dim, dir
+    const int4 it = items[k];  // src, dst, dim, dir
     if (group_active && !group_active[patches[it.y].group]) continue;
-    flux_correction_one(slab, patches, times, it.x, it.y, it.z, it.w);
+    const PatchDev S = patches[it.x], D = patches[it.y];
+    const int dim = it.z, dir = it.w, other = 1 - dim;
+    const int sno = other == 0 ? S.nx : S.ny, dno = other == 0 ? D.nx : D.ny, dnd = dim == 0 ? D.nx : D.ny;
+    if (sno > kFluxMaxCells) {
+      if (threadIdx.x == 0) flux_correction_one(slab, patches, times, it.x, it.y, dim, dir);
+      __syncthreads();
+      continue;
+    }
+    const PatchTimeDev ST = times[it.x], DT = times[it.y];
+    const double lo = fmax(ST.time, DT.time);
+    const double hi = fmin(__dadd_rn(ST.time, ST.dt), __dadd_rn(DT.time, DT.dt));
+    const double tov = __dsub_rn(hi, lo);
+    int rdim = 0;
+    for (int d = 0; d < 2; d++) {
+      if (tl_greater(D.pos[d], S.pos[d])) rdim = d;
+      else if (tl_greater(S.pos[d], D.pos[d])) rdim = d;
+    }
+    const double ssub0 = subcell(S, 0), ssub1 = subcell(S, 1), dsub0 = subcell(D, 0), dsub1 = subcell(D, 1);
+    const double dvol = __dmul_rn(dsub0, dsub1);
+    const double heps = 1e-10;
+    const int po = 1 - rdim;
+    const double ssp = po == 0 ? ssub0 : ssub1, dsp = po == 0 ? dsub0 : dsub1;
+    const double spp = po == 0 ? S.pos[0] : S.pos[1], dpp = po == 0 ? D.pos[0] : D.pos[1];
+    const double sso = other == 0 ? ssub0 : ssub1, dso = other == 0 ? dsub0 : dsub1;
+    const double spo = other == 0 ? S.pos[0] : S.pos[1], dpo = other == 0 ? D.pos[0] : D.pos[1];
+    for (int cs = threadIdx.x; cs < sno; cs += kFluxThreads) {
+      double npos = __dadd_rn(spp, __dmul_rn(ssp, (double)cs));
+      double lb = fmax(dpp, npos);
+      double ub = fmin(__dadd_rn(dpp, dsp), __dadd_rn(npos, ssp));
+      s_lb[cs] = (int)__ddiv_rn(__dadd_rn(__dsub_rn(lb, dpp), heps), dsp);
+      s_ub[cs] = (int)ceil(__ddiv_rn(__dsub_rn(__dsub_rn(ub, dpp), heps), dsp));
+    }
+    __syncthreads();
+    const int dinner = (-dir == -1) ? 0 : dnd - 1;
+    for (int cd = threadIdx.x; cd < dno; cd += kFluxThreads) {
+      const int ux = dim == 0 ? dinner : cd, uy = dim == 0 ? cd : dinner;
+      if (ux < 0 || uy < 0 || ux >= D.nx || uy >= D.ny) continue;
+      double dF[3];
+      for (int q = 0; q < 3; q++) dF[q] = slab[idx_flux(D, q, cd, dim, -dir)];
+      const double a2 = __dadd_rn(dpo, __dmul_rn(__dadd_rn((double)cd, 1.0), dso));
+      const double b2 = __dadd_rn(dpo, __dmul_rn((double)cd, dso));
+      for (int cs = 0; cs < sno; cs++) {
+        if (cd < s_lb[cs] || cd >= s_ub[cs]) continue;
+        double a1 = __dadd_rn(spo, __dmul_rn(__dadd_rn((double)cs, 1.0), sso));
+        double b1 = __dadd_rn(spo, __dmul_rn((double)cs, sso));
+        double area = __dmul_rn(1.0, __dsub_rn(a1 < a2 ? a1 : a2, b1 > b2 ? b1 : b2));
+        if (area < 0.0) area = 0.0;
+        for (int q = 0; q < 3; q++) {
+          double sF = slab[idx_flux(S, q, cs, dim, dir)];
+          double corr = __ddiv_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF, dF[q]), tov), area), dvol);
+          long long id = idx_unew(D, q, ux, uy);
+          slab[id] = __dadd_rn(slab[id], corr);
+        }
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -1468,7 +1651,7 @@ cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev 
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
                                   int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
-  k_restrict_items<<<n_dst, 256, 0, st>>>(slab, patches, times, items, begin, group_active);
+  k_restrict_items<<<n_dst, kRestrWarps * 32, 0, st>>>(slab, patches, times, items, begin, group_active);
   return cudaGetLastError();
 }
 
@@ -1490,7 +1673,7 @@ cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *pat
                               const PatchTimeDev *times, const int4 *items, const int *begin,
                               int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
-  k_flux_items<<<n_dst, 32, 0, st>>>(slab, patches, times, items, begin, group_active);
+  k_flux_items<<<n_dst, kFluxThreads, 0, st>>>(slab, patches, times, items, begin, group_active);
   return cudaGetLastError();
 }
 
