@@ -1004,20 +1004,17 @@ __global__ void k_restrict(double *slab, const PatchDev *patches, const PatchTim
   restrict_block(slab, patches[src], times[src], patches[dst], times[dst], only_overlapped != 0, swe != 0);
 }
 
-// Batched restriction: block b handles the items [begin[b], begin[b+1]) that
-// all share one destination, in list order, and within an item its regions
-// in order (the same sequence as restrict_block).  One warp per destination
-// cell: the lanes evaluate the contributions of up to 32 source cells at a
-// time, lane 0 adds them to the cell's uOld / uNew values in source-cell
-// order, so every sum is formed in the reference's order.
-constexpr int kRestrWarps = 8;
-__global__ void __launch_bounds__(kRestrWarps * 32)
-    k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                     const int4 *items, const int *begin, const int *group_active) {
-  __shared__ double W[kRestrWarps][32][6];
-  if (group_active && !group_active[patches[items[begin[blockIdx.x]].y].group]) return;
+// Restriction of the items [b0, b1) (one destination) in list order, and
+// within an item its regions in order (the same sequence as restrict_block).
+// One warp per destination cell of a region: the lanes evaluate the
+// contributions of up to 32 source cells at a time, lane 0 adds them to the
+// cell's uOld / uNew values in source-cell order.
+constexpr int kRestrWarps = 8;   // warps per CTA of the batched restriction
+constexpr int kRestrSplit = 1;   // CTAs per destination (interleaved cells)
+__device__ void restrict_items_in_order(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                        const int4 *items, int b0, int b1, double (*W)[32][6]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
+  for (int k = b0; k < b1; k++) {
     const int4 it = items[k];  // src, dst, only_overlapped, swe
     const PatchDev S = patches[it.x], D = patches[it.y];
     const PatchTimeDev ST = times[it.x], DT = times[it.y];
@@ -1054,7 +1051,7 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
       int doff[2], dsz[2];
       map_to_patch(ro, rs, S, D, eps, doff, dsz);
       const int ncell = dsz[0] > 0 && dsz[1] > 0 ? dsz[0] * dsz[1] : 0;
-      for (int c = wid; c < ncell; c += kRestrWarps) {
+      for (int c = wid; c < ncell; c += (int)(blockDim.x >> 5)) {
         const int x = doff[0] + c / dsz[1], y = doff[1] + c % dsz[1];
         const double dpos[2] = {iter_pos(D, 0, x), iter_pos(D, 1, y)};
         int coff[2], csz[2];
@@ -1134,6 +1131,170 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
       __syncthreads();
     }
     __syncthreads();
+  }
+}
+
+
+// Batched restriction: block b handles the items [begin[b], begin[b+1]) that
+// share one destination.  A table of the items' regions (item order, then
+// region order) and time factors is built once per block; then each
+// destination cell walks the table in order and adds the terms of every
+// source cell of every matching region, one thread per destination cell.
+// Each cell's sum is therefore formed in exactly the order of the
+// item-by-item restriction, and the cells of one destination need no
+// barrier between items (kRestrSplit CTAs may share the cells of one
+// destination, interleaved; more than one measured slower on the adaptive
+// tsunami, where every CTA rebuilds the table).  Destinations with more than
+// kRestrMaxItems items, more than 3 unknowns or a region leaving the
+// destination take restrict_items_in_order in their first CTA.
+constexpr int kRestrMaxItems = 128;
+struct RestrItemTab {
+  double tfo, tfn;
+  int src, nr, swe, pad_;
+  int doff[4][2], dsz[4][2], ro[4][2], rs[4][2];
+};
+__global__ void __launch_bounds__(kRestrWarps * 32)
+    k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                     const int4 *items, const int *begin, const int *group_active) {
+  __shared__ double W[kRestrWarps][32][6];
+  __shared__ RestrItemTab T[kRestrMaxItems];
+  __shared__ int s_bad;
+  const int dst_block = blockIdx.x / kRestrSplit, part = blockIdx.x % kRestrSplit;
+  const int b0 = begin[dst_block], b1 = begin[dst_block + 1];
+  const PatchDev D = patches[items[b0].y];
+  if (group_active && !group_active[D.group]) return;
+  const int ni = b1 - b0;
+  if (ni > kRestrMaxItems || D.nq > 3) {
+    if (part == 0) restrict_items_in_order(slab, patches, times, items, b0, b1, W);
+    return;
+  }
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+  const double eps = 1e-12;
+  for (int t = threadIdx.x; t < ni; t += blockDim.x) {
+    const int4 it = items[b0 + t];
+    const PatchDev S = patches[it.x];
+    const PatchTimeDev ST = times[it.x], DT = times[it.y];
+    RestrItemTab &E = T[t];
+    int roff[8], rsz[8], nr;
+    int n[2] = {S.nx, S.ny};
+    if (it.z != 0) {
+      double sp[2] = {S.pos[0], S.pos[1]}, ss[2] = {S.size[0], S.size[1]};
+      double sub[2] = {subcell(S, 0), subcell(S, 1)};
+      nr = regions_overlapped(DT.rl, DT.ru, sp, ss, sub, n, roff, rsz);
+    } else {
+      nr = 1;
+      roff[0] = 0; roff[1] = 0; rsz[0] = n[0]; rsz[1] = n[1];
+    }
+    double tfo = 1.0, tfn = 1.0;
+    if (tl_greater(ST.dt, 0.0)) {
+      double so = time_uold(S, ST), su = time_unew(S, ST);
+      tfo = __ddiv_rn(__dsub_rn(0.0, so), __dsub_rn(su, so));
+      tfn = __ddiv_rn(__dsub_rn(1.0, so), __dsub_rn(su, so));
+    }
+    E.tfo = tfo; E.tfn = tfn; E.src = it.x; E.nr = nr; E.swe = it.w;
+    for (int r = 0; r < 4; r++) {
+      int doff[2] = {0, 0}, dsz[2] = {0, 0};
+      if (r < nr && !(it.z != 0 && !(rsz[2 * r] > 0 && rsz[2 * r + 1] > 0))) {
+        map_to_patch(&roff[2 * r], &rsz[2 * r], S, D, eps, doff, dsz);
+        if (dsz[0] > 0 && dsz[1] > 0 &&
+            (doff[0] < 0 || doff[1] < 0 || doff[0] + dsz[0] > D.nx || doff[1] + dsz[1] > D.ny))
+          atomicOr(&s_bad, 1);
+      }
+      for (int d = 0; d < 2; d++) {
+        E.doff[r][d] = doff[d];
+        E.dsz[r][d] = dsz[d] > 0 ? dsz[d] : 0;
+        E.ro[r][d] = r < nr ? roff[2 * r + d] : 0;
+        E.rs[r][d] = r < nr ? rsz[2 * r + d] : 0;
+      }
+    }
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (part == 0) restrict_items_in_order(slab, patches, times, items, b0, b1, W);
+    return;
+  }
+  const double dsub[2] = {iter_sub(D, 0), iter_sub(D, 1)};
+  const double dvol = __dmul_rn(dsub[0], dsub[1]);
+  const int ncell = D.nx * D.ny;
+  for (int c = part + kRestrSplit * (int)threadIdx.x; c < ncell; c += kRestrSplit * (int)blockDim.x) {
+    const int x = c / D.ny, y = c % D.ny;
+    double dpos[2] = {0.0, 0.0};
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    bool any = false;
+    for (int t = 0; t < ni; t++) {
+      const int nr = T[t].nr < 4 ? T[t].nr : 4;
+      for (int r = 0; r < nr; r++) {
+        if (!(x >= T[t].doff[r][0] && x < T[t].doff[r][0] + T[t].dsz[r][0] && y >= T[t].doff[r][1] &&
+              y < T[t].doff[r][1] + T[t].dsz[r][1]))
+          continue;
+        if (!any) {
+          dpos[0] = iter_pos(D, 0, x);
+          dpos[1] = iter_pos(D, 1, y);
+        }
+        const PatchDev S = patches[T[t].src];
+        const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
+        int coff[2], csz[2];
+        for (int d = 0; d < 2; d++) {
+          double ot = __ddiv_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
+          int o = (int)ot;
+          double st = __ddiv_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
+          st = __dsub_rn(st, ot);
+          st = __dadd_rn(st, 1.0);
+          int up = o + (int)st;
+          int rup = T[t].ro[r][d] + T[t].rs[r][d];
+          int oo = o > T[t].ro[r][d] ? o : T[t].ro[r][d];
+          int uu = up < rup ? up : rup;
+          coff[d] = oo;
+          csz[d] = uu - oo;
+        }
+        if (!(csz[0] > 0 && csz[1] > 0)) continue;
+        if (!any) {
+          any = true;
+#pragma unroll
+          for (int q = 0; q < 3; q++)
+            if (q < D.nq) {
+              acc[q] = slab[idx_uold(D, q, x, y)];
+              acc[3 + q] = slab[idx_unew(D, q, x, y)];
+            }
+        }
+        const double tfo = T[t].tfo, tfn = T[t].tfn;
+        const double itfo = __dsub_rn(1.0, tfo), itfn = __dsub_rn(1.0, tfn);
+        const bool swe = T[t].swe != 0;
+        for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++)
+          for (int sy = coff[1]; sy < coff[1] + csz[1]; sy++) {
+            const double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
+            double region = 1.0;
+            for (int d = 0; d < 2; d++) {
+              double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
+              double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
+              region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
+              region = fmax(region, 0.0);
+            }
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+              if (q >= D.nq) break;
+              double vo = slab[idx_uold(S, q, sx, sy)];
+              double vn = slab[idx_unew(S, q, sx, sy)];
+              if (swe && q == 0) {
+                double bb = slab[idx_pw(S, 0, sx, sy)];
+                vo = __dadd_rn(vo, bb);
+                vn = __dadd_rn(vn, bb);
+              }
+              acc[q] = __dadd_rn(acc[q], __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfo), __dmul_rn(vn, tfo)), region), dvol));
+              acc[3 + q] = __dadd_rn(acc[3 + q], __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfn), __dmul_rn(vn, tfn)), region), dvol));
+            }
+          }
+      }
+    }
+    if (any) {
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+        if (q < D.nq) {
+          slab[idx_uold(D, q, x, y)] = acc[q];
+          slab[idx_unew(D, q, x, y)] = acc[3 + q];
+        }
+    }
   }
 }
 
@@ -1651,7 +1812,8 @@ cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev 
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
                                   int n_dst, const int *group_active) {
   if (n_dst <= 0) return cudaSuccess;
-  k_restrict_items<<<n_dst, kRestrWarps * 32, 0, st>>>(slab, patches, times, items, begin, group_active);
+  k_restrict_items<<<n_dst * kRestrSplit, kRestrWarps * 32, 0, st>>>(slab, patches, times, items, begin,
+                                                                     group_active);
   return cudaGetLastError();
 }
 
