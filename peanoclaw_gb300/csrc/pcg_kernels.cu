@@ -1236,9 +1236,9 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
         const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
         int coff[2], csz[2];
         for (int d = 0; d < 2; d++) {
-          double ot = __ddiv_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
+          double ot = ieee::div_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
           int o = (int)ot;
-          double st = __ddiv_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
+          double st = ieee::div_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
           st = __dsub_rn(st, ot);
           st = __dadd_rn(st, 1.0);
           int up = o + (int)st;
@@ -1281,8 +1281,8 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
                 vo = __dadd_rn(vo, bb);
                 vn = __dadd_rn(vn, bb);
               }
-              acc[q] = __dadd_rn(acc[q], __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfo), __dmul_rn(vn, tfo)), region), dvol));
-              acc[3 + q] = __dadd_rn(acc[3 + q], __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfn), __dmul_rn(vn, tfn)), region), dvol));
+              acc[q] = __dadd_rn(acc[q], ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfo), __dmul_rn(vn, tfo)), region), dvol));
+              acc[3 + q] = __dadd_rn(acc[3 + q], ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfn), __dmul_rn(vn, tfn)), region), dvol));
             }
           }
       }
@@ -1452,8 +1452,8 @@ __global__ void __launch_bounds__(kFluxThreads)
       double npos = __dadd_rn(spp, __dmul_rn(ssp, (double)cs));
       double lb = fmax(dpp, npos);
       double ub = fmin(__dadd_rn(dpp, dsp), __dadd_rn(npos, ssp));
-      s_lb[cs] = (int)__ddiv_rn(__dadd_rn(__dsub_rn(lb, dpp), heps), dsp);
-      s_ub[cs] = (int)ceil(__ddiv_rn(__dsub_rn(__dsub_rn(ub, dpp), heps), dsp));
+      s_lb[cs] = (int)ieee::div_rn(__dadd_rn(__dsub_rn(lb, dpp), heps), dsp);
+      s_ub[cs] = (int)ceil(ieee::div_rn(__dsub_rn(__dsub_rn(ub, dpp), heps), dsp));
     }
     __syncthreads();
     const int dinner = (-dir == -1) ? 0 : dnd - 1;
@@ -1472,7 +1472,7 @@ __global__ void __launch_bounds__(kFluxThreads)
         if (area < 0.0) area = 0.0;
         for (int q = 0; q < 3; q++) {
           double sF = slab[idx_flux(S, q, cs, dim, dir)];
-          double corr = __ddiv_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF, dF[q]), tov), area), dvol);
+          double corr = ieee::div_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF, dF[q]), tov), area), dvol);
           long long id = idx_unew(D, q, ux, uy);
           slab[id] = __dadd_rn(slab[id], corr);
         }
