@@ -82,6 +82,7 @@ def parse():
     ap.add_argument("--amr-steps", type=int, default=100)
     ap.add_argument("--remesh-steps", type=int, default=100)
     ap.add_argument("--remesh-every", type=int, default=10)
+    ap.add_argument("--lts-t-end", type=float, default=0.02)
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=8.0)
     ap.add_argument("--serve-batch", type=int, default=8,
@@ -274,6 +275,47 @@ def bench_amr(prm, steps):
         ctx.close()
         res[name] = ps.meta["leaf_cells"] * k / ((m1 - m0) / 1e3)
         res[name + "_ms_per_step"] = (m1 - m0) / k
+    return res
+
+
+def bench_lts(prm, t_end):
+    """Local time stepping against the synchronous step on the adaptive
+    breaking dam (3 levels of 3x refinement, 27 x 27 cells per patch, ghost
+    interpolation and restriction, no flux correction in either run): both
+    advance every leaf to the same end time; reported are the cell updates
+    spent, the device time to solution and the iterations / steps."""
+    from peanoclaw_gb300 import pcg as P
+    from peanoclaw_gb300 import scenarios as S
+    ps = S.breaking_dam_amr(base=9, n=27, levels=3)
+    slab = int(sum(P.vector_size(n) + 32 for n in ps.n)) + 4096
+    res = {"patches": len(ps), "leaves": int(sum(ps.leaf)), "leaf_cells": ps.meta["leaf_cells"], "t_end": t_end}
+    for ts, name in ((P.TS_LOCAL, "local"), (P.TS_GLOBAL, "global")):
+        ctx = P.Context(slab_doubles=slab, max_patches=len(ps) + 16, max_groups=1, params=prm)
+        try:
+            S.install_amr(ctx, ps, flux=False)
+            ctx.restrict_all()
+            ctx.set_group_max_dt(0, np.inf)
+            ctx.set_group_end_time(0, 0.0, t_end)
+            ctx.set_time_stepping(ts)
+            if ts == P.TS_LOCAL:
+                # one iteration advances few leaves: 16x16 tiles (many short
+                # work items) beat the warp strips' long column marches here
+                ctx.set_schedule(P.SCHED_TILES)
+            ctx.synchronize()
+            c0, m0 = ctx.stats()
+            t0 = time.perf_counter()
+            iters = 0
+            while float(ctx.group_times()[0]) < t_end and iters < 100000:
+                hist = ctx.run(64, P.PCG_MODE_BATCHED)
+                iters += int(np.count_nonzero(hist[:, 0] > 0.0))
+            ctx.synchronize()
+            wall = time.perf_counter() - t0
+            c1, m1 = ctx.stats()
+            res[name] = {"iterations": iters, "cell_updates": int(c1 - c0), "device_ms": m1 - m0,
+                         "wall_ms": wall * 1e3, "cell_updates_per_s": (c1 - c0) / ((m1 - m0) / 1e3),
+                         "reached": float(ctx.group_times()[0])}
+        finally:
+            ctx.close()
     return res
 
 
@@ -485,7 +527,8 @@ def main():
         legs = {"radial_dam_break_9x9x16": lambda: bench_radial(prm),
                 "adaptive_breaking_dam_3_levels": lambda: bench_amr(prm, args.amr_steps),
                 "adaptive_tsunami_remesh": lambda: bench_remesh(prm, args.remesh_steps, args.remesh_every),
-                "serving_stream": lambda: bench_serving(args, prm)}
+                "serving_stream": lambda: bench_serving(args, prm),
+                "local_time_stepping_breaking_dam": lambda: bench_lts(prm, args.lts_t_end)}
         only = set(args.config_legs.split(",")) if args.config_legs else set(legs)
         configs = {k: f() for k, f in legs.items() if k in only}
 

@@ -276,7 +276,8 @@ int pcg_step(pcg_context *ctx, int32_t mode, double *dt_out);
 /* `steps` synchronous steps; BATCHED mode replays a captured CUDA graph.  The
  * dt of every step and group is written to dt_hist[steps * max_groups] (may be NULL). */
 int pcg_run(pcg_context *ctx, int32_t steps, int32_t mode, double *dt_hist);
-/* Cumulative interior cell updates and device time of pcg_step / pcg_run. */
+/* Cumulative interior cell updates and device time of pcg_step / pcg_run;
+ * under local time stepping the cells of the leaves that advanced. */
 int pcg_stats(pcg_context *ctx, int64_t *cell_updates, double *device_ms);
 /* Block until all work issued on the context has finished. */
 int pcg_synchronize(pcg_context *ctx);

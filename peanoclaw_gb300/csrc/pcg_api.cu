@@ -172,6 +172,8 @@ struct pcg_context {
   int *d_vt_virtuals = nullptr;
   size_t d_vt_cap = 0, d_vtv_cap = 0;
   unsigned long long *d_vstart = nullptr, *d_vend = nullptr;
+  // cells of the leaves advanced by local-time-stepping iterations
+  unsigned long long *d_lts_cells = nullptr;
   double *d_dt_out = nullptr;
   double *h_pinned = nullptr;  // pinned scratch for small D2H/H2D
   std::vector<double> h_group_max_dt;
@@ -224,6 +226,8 @@ struct pcg_context {
   std::vector<int> restr_begin, flux_begin, restr_dsts;
   int4 *d_restr = nullptr, *d_flux = nullptr;
   int *d_restr_begin = nullptr, *d_flux_begin = nullptr, *d_restr_dsts = nullptr, *d_leaf_ids = nullptr;
+  int *d_restr_dirty = nullptr;
+  size_t d_rdirty_cap = 0;
   size_t d_restr_cap = 0, d_flux_cap = 0, d_rb_cap = 0, d_fb_cap = 0, d_rd_cap = 0, d_leaf_cap = 0;
   double g_flux = 1.0;
 
@@ -518,6 +522,7 @@ int rebuild_topology(pcg_context *c) {
   if ((rc = ensure_device(c, &c->d_restr_begin, &c->d_rb_cap, c->restr_begin.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_flux_begin, &c->d_fb_cap, c->flux_begin.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_restr_dsts, &c->d_rd_cap, c->restr_dsts.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_restr_dirty, &c->d_rdirty_cap, c->restr_dsts.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_leaf_ids, &c->d_leaf_cap, c->leaf_ids.size())) != PCG_OK) return rc;
   auto up = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) : cudaSuccess;
@@ -593,10 +598,17 @@ int enqueue_post_update(pcg_context *c) {
   }
   if (!c->h_restr.empty()) {
     int nd = (int)c->restr_dsts.size();
-    PCG_CUDA(launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga));
+    // under local time stepping only destinations with an advancing source
+    const int *dirty = nullptr;
+    if (c->ts_local) {
+      PCG_CUDA(launch_restr_dirty(c->stream, c->d_restr, c->d_restr_begin, nd, c->d_pact, c->d_restr_dirty));
+      dirty = c->d_restr_dirty;
+    }
+    PCG_CUDA(launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga, dirty));
     PCG_CUDA(launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
-                                   c->d_restr_begin, nd, ga));
-    PCG_CUDA(launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga));
+                                   c->d_restr_begin, nd, ga, dirty));
+    PCG_CUDA(launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga,
+                                             dirty));
   }
   return PCG_OK;
 }
@@ -652,7 +664,8 @@ int enqueue_lts(pcg_context *c, int phase) {
   PCG_CUDA(pcg::launch_lts(c->stream, phase, c->max_patches, c->max_groups, c->d_patches, c->d_times,
                            c->d_items, (int)c->h_items.size(), vt, c->d_nbmin, c->d_patch_smax,
                            c->d_group_tmin, c->d_group_dt, c->d_group_max_dt, c->d_group_t_end,
-                           c->d_group_active, c->d_pact, c->d_pmaxdt, c->d_pdt, c->d_group_time, c->prm));
+                           c->d_group_active, c->d_pact, c->d_pmaxdt, c->d_pdt, c->d_group_time, c->prm,
+                           c->d_lts_cells));
   return PCG_OK;
 }
 
@@ -825,6 +838,8 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->d_pdt, sizeof(unsigned long long) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_nbmin, sizeof(unsigned long long) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_group_tmin, sizeof(unsigned long long) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_lts_cells, sizeof(unsigned long long)));
+  CREATE_CK(cudaMemset(c->d_lts_cells, 0, sizeof(unsigned long long)));
   CREATE_CK(cudaMalloc(&c->d_vstart, sizeof(unsigned long long) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_vend, sizeof(unsigned long long) * c->max_patches));
   {
@@ -863,6 +878,7 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_nbmin);
   cudaFree(c->d_group_tmin);
   cudaFree(c->d_vstart);
+  cudaFree(c->d_lts_cells);
   cudaFree(c->d_vend);
   cudaFree(c->d_vt);
   cudaFree(c->d_vt_virtuals);
@@ -874,6 +890,7 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_restr_begin);
   cudaFree(c->d_flux_begin);
   cudaFree(c->d_restr_dsts);
+  cudaFree(c->d_restr_dirty);
   cudaFree(c->d_leaf_ids);
   cudaFree(c->d_plan);
   cudaFree(c->d_copy_plan);
@@ -1522,7 +1539,7 @@ int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
   float ms = 0.f;
   PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->device_ms += ms;
-  c->cell_updates += c->cells_per_step;
+  if (!c->ts_local) c->cell_updates += c->cells_per_step;
   if (dt_out) std::memcpy(dt_out, c->h_pinned, sizeof(double) * c->max_groups);
   return PCG_OK;
 }
@@ -1585,7 +1602,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   float ms = 0.f;
   PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->device_ms += ms;
-  c->cell_updates += c->cells_per_step * steps;
+  if (!c->ts_local || mode != PCG_MODE_BATCHED) c->cell_updates += c->cells_per_step * steps;
   return PCG_OK;
 }
 
@@ -1656,7 +1673,7 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
       PCG_CUDA(cudaEventElapsedTime(&e, c->ev0, c->ev1));
       t[k] += e;
       c->device_ms += e;
-      c->cell_updates += c->cells_per_step;
+      if (!c->ts_local) c->cell_updates += c->cells_per_step;
     }
     t[k] /= reps;
   }
@@ -1681,7 +1698,14 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
 
 int pcg_stats(pcg_context *c, int64_t *cell_updates, double *device_ms) {
   if (!c) return fail(PCG_E_INVALID, "null context");
-  if (cell_updates) *cell_updates = c->cell_updates;
+  if (cell_updates) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    PCG_CUDA(cudaSetDevice(c->device));
+    unsigned long long lts = 0;
+    PCG_CUDA(cudaMemcpyAsync(&lts, c->d_lts_cells, sizeof(lts), cudaMemcpyDeviceToHost, c->stream));
+    PCG_CUDA(cudaStreamSynchronize(c->stream));
+    *cell_updates = c->cell_updates + (int64_t)lts;
+  }
   if (device_ms) *device_ms = c->device_ms;
   return PCG_OK;
 }

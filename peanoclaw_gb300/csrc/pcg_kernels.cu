@@ -352,12 +352,13 @@ __global__ void k_lts_activity(const PatchDev *__restrict__ patches, const Patch
 }
 
 // dt of every advancing leaf (min of its block CFL dt and its max_dt), the
-// group's minimal dt taken and minimal uNew time after the step.
+// group's minimal dt taken and minimal uNew time after the step; the cells
+// of the leaves that advance are added to *cells.
 __global__ void k_lts_dt(const PatchDev *__restrict__ patches, const PatchTimeDev *__restrict__ times,
                          int n_patches, const int *__restrict__ pact, const double *__restrict__ pmaxdt,
                          const unsigned long long *__restrict__ patch_smax, SweParamsDev prm,
                          unsigned long long *__restrict__ pdt, unsigned long long *__restrict__ group_dt,
-                         unsigned long long *__restrict__ group_tmin) {
+                         unsigned long long *__restrict__ group_tmin, unsigned long long *__restrict__ cells) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_patches; p += gridDim.x * blockDim.x) {
     const PatchDev P = patches[p];
     if (P.nx <= 0 || !is_leaf(P)) continue;
@@ -368,7 +369,10 @@ __global__ void k_lts_dt(const PatchDev *__restrict__ patches, const PatchTimeDe
       const double dt = fmin(own, pmaxdt[p]);
       pdt[p] = dbits(dt);
       atomicMin(&group_dt[P.group], dbits(dt));
-      if (tl_greater(dt, 0.0)) tnext = __dadd_rn(__dadd_rn(T.time, T.dt), dt);
+      if (tl_greater(dt, 0.0)) {
+        tnext = __dadd_rn(__dadd_rn(T.time, T.dt), dt);
+        if (cells) atomicAdd(cells, (unsigned long long)P.nx * (unsigned long long)P.ny);
+      }
     }
     atomicMin(&group_tmin[P.group], okey(tnext));
   }
@@ -1155,11 +1159,12 @@ struct RestrItemTab {
 };
 __global__ void __launch_bounds__(kRestrWarps * 32)
     k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                     const int4 *items, const int *begin, const int *group_active) {
+                     const int4 *items, const int *begin, const int *group_active, const int *dirty) {
   __shared__ double W[kRestrWarps][32][6];
   __shared__ RestrItemTab T[kRestrMaxItems];
   __shared__ int s_bad;
   const int dst_block = blockIdx.x / kRestrSplit, part = blockIdx.x % kRestrSplit;
+  if (dirty && !dirty[dst_block]) return;
   const int b0 = begin[dst_block], b1 = begin[dst_block + 1];
   const PatchDev D = patches[items[b0].y];
   if (group_active && !group_active[D.group]) return;
@@ -1299,9 +1304,10 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
 }
 
 __global__ void k_post_process_restriction(double *slab, const PatchDev *patches, const int *ids, int count,
-                                           const int *group_active) {
+                                           const int *group_active, const int *dirty) {
   PatchDev P = patches[ids[blockIdx.x % count]];
   if ((int)blockIdx.x >= count) return;
+  if (dirty && !dirty[blockIdx.x]) return;
   if (group_active && !group_active[P.group]) return;
   for (int c = threadIdx.x; c < P.nx * P.ny; c += blockDim.x) {
     int x = c / P.ny, y = c % P.ny;
@@ -1486,8 +1492,9 @@ __global__ void __launch_bounds__(kFluxThreads)
 // the restriction accumulates into them (Patch accessor clearRegion, called
 // from GridLevelTransfer::switchToAndAddVirtualSubgrid).
 __global__ void k_clear_interior(double *slab, const PatchDev *patches, const int *ids, int count,
-                                 const int *group_active) {
+                                 const int *group_active, const int *dirty) {
   if ((int)blockIdx.x >= count) return;
+  if (dirty && !dirty[blockIdx.x]) return;
   PatchDev P = patches[ids[blockIdx.x]];
   if (group_active && !group_active[P.group]) return;
   int n = P.nx * P.ny;
@@ -1643,7 +1650,7 @@ cudaError_t launch_lts(cudaStream_t st, int phase, int n_patches, int n_groups, 
                        unsigned long long *group_tmin, unsigned long long *group_dt,
                        const double *group_max_dt, const double *group_t_end, const int *group_active,
                        int *pact, double *pmaxdt, unsigned long long *pdt, double *group_time,
-                       const SweParamsDev &prm) {
+                       const SweParamsDev &prm, unsigned long long *cells) {
   const int np = n_patches > 0 ? n_patches : 1;
   const int gp = (np + 255) / 256 < 1024 ? (np + 255) / 256 : 1024;
   auto grid_for = [](int n) { return (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096; };
@@ -1663,7 +1670,7 @@ cudaError_t launch_lts(cudaStream_t st, int phase, int n_patches, int n_groups, 
       break;
     case 1:
       k_lts_dt<<<gp, 256, 0, st>>>(patches, times, n_patches, pact, pmaxdt, patch_smax, prm, pdt, group_dt,
-                                   group_tmin);
+                                   group_tmin, cells);
       break;
     default:
       k_lts_end<<<(n_groups + 127) / 128, 128, 0, st>>>(n_groups, group_tmin, group_time, group_dt);
@@ -1808,19 +1815,38 @@ cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patch
   return cudaGetLastError();
 }
 
+// Destinations of the restriction list with at least one advancing source
+// (local time stepping): the others' restricted values would not change.
+__global__ void k_restr_dirty(const int4 *__restrict__ items, const int *__restrict__ begin,
+                              const int *__restrict__ pact, int *__restrict__ dirty) {
+  int any = 0;
+  for (int k = begin[blockIdx.x] + threadIdx.x; k < begin[blockIdx.x + 1]; k += blockDim.x)
+    any |= pact[items[k].x] ? 1 : 0;
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) dirty[blockIdx.x] = any;
+}
+
+cudaError_t launch_restr_dirty(cudaStream_t st, const int4 *items, const int *begin, int n_dst, const int *pact,
+                               int *dirty) {
+  if (n_dst <= 0) return cudaSuccess;
+  k_restr_dirty<<<n_dst, 128, 0, st>>>(items, begin, pact, dirty);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst, const int *group_active) {
+                                  int n_dst, const int *group_active, const int *dirty) {
   if (n_dst <= 0) return cudaSuccess;
   k_restrict_items<<<n_dst * kRestrSplit, kRestrWarps * 32, 0, st>>>(slab, patches, times, items, begin,
-                                                                     group_active);
+                                                                     group_active, dirty);
   return cudaGetLastError();
 }
 
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
-                                            const int *ids, int count, const int *group_active) {
+                                            const int *ids, int count, const int *group_active,
+                                            const int *dirty) {
   if (count <= 0) return cudaSuccess;
-  k_post_process_restriction<<<count, 256, 0, st>>>(slab, patches, ids, count, group_active);
+  k_post_process_restriction<<<count, 256, 0, st>>>(slab, patches, ids, count, group_active, dirty);
   return cudaGetLastError();
 }
 
@@ -1867,9 +1893,9 @@ cudaError_t launch_refinement_indicator(cudaStream_t st, const double *slab, con
 }
 
 cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const int *ids, int count, const int *group_active) {
+                                  const int *ids, int count, const int *group_active, const int *dirty) {
   if (count <= 0) return cudaSuccess;
-  k_clear_interior<<<count, 256, 0, st>>>(slab, patches, ids, count, group_active);
+  k_clear_interior<<<count, 256, 0, st>>>(slab, patches, ids, count, group_active, dirty);
   return cudaGetLastError();
 }
 

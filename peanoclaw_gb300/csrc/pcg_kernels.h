@@ -46,7 +46,7 @@ cudaError_t launch_lts(cudaStream_t st, int phase, int n_patches, int n_groups, 
                        unsigned long long *group_tmin, unsigned long long *group_dt,
                        const double *group_max_dt, const double *group_t_end, const int *group_active,
                        int *pact, double *pmaxdt, unsigned long long *pdt, double *group_time,
-                       const SweParamsDev &prm);
+                       const SweParamsDev &prm, unsigned long long *cells = nullptr);
 cudaError_t launch_group_advance(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
                                  const int *group_active, double *group_time);
 cudaError_t launch_record_dt(cudaStream_t st, int n_groups, const unsigned long long *group_dt,
@@ -93,10 +93,12 @@ cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patch
                             const PatchTimeDev *times, int src, int dst, int only_overlapped, int swe);
 cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst, const int *group_active = nullptr);
+                                  int n_dst, const int *group_active = nullptr, const int *dirty = nullptr);
+cudaError_t launch_restr_dirty(cudaStream_t st, const int4 *items, const int *begin, int n_dst, const int *pact,
+                               int *dirty);
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
                                             const int *ids, int count,
-                                            const int *group_active = nullptr);
+                                            const int *group_active = nullptr, const int *dirty = nullptr);
 cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const int *ids, int count, double gf,
                                   const int *group_active = nullptr);
@@ -110,7 +112,8 @@ cudaError_t launch_switch_to_leaf(cudaStream_t st, double *slab, const PatchDev 
 cudaError_t launch_refinement_indicator(cudaStream_t st, const double *slab, const PatchDev *patches,
                                         const int *ids, int count, double *out);
 cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const int *ids, int count, const int *group_active = nullptr);
+                                  const int *ids, int count, const int *group_active = nullptr,
+                                  const int *dirty = nullptr);
 cudaError_t launch_flux_correction(cudaStream_t st, double *slab, const PatchDev *patches,
                                    const PatchTimeDev *times, int src, int dst, int dim, int dir);
 

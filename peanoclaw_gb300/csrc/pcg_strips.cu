@@ -96,6 +96,9 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     const StripGroup SG = groups[I.g0 + (in_group ? gi : 0)];
     const PatchDev P = patches[SG.pid];
     const bool act = in_group && (!group_active || group_active[P.group]) && (!pact || pact[SG.pid]);
+    // an item without an advancing lane group writes nothing: skip it whole
+    // (finished groups, leaves that wait under local time stepping)
+    if (!__any_sync(0xffffffffu, act)) continue;
     const int y = SG.y0 + j;
 
     // ---- boundary rows: lane l < G*w takes (group l / w, column l % w)

@@ -32,6 +32,8 @@ def test_local_time_stepping_matches_the_oracle(sched):
         prm = oracle_params(PRM)
         seen = set()
         iterations = 0
+        advanced_cells = 0
+        cu0, _ = c.stats()
         done = False
         while not done:
             # four iterations per replay of the captured graph
@@ -41,6 +43,7 @@ def test_local_time_stepping_matches_the_oracle(sched):
                 taken = dto[dto > 0.0]
                 assert hist[k] == (taken.min() if n else 0.0), (iterations, k)
                 seen.update(taken.tolist())
+                advanced_cells += sum(ps.n[p] ** 2 for p in np.flatnonzero(dto > 0.0))
                 if n == 0:
                     done = True
                 else:
@@ -54,6 +57,9 @@ def test_local_time_stepping_matches_the_oracle(sched):
             assert (t["time"], t["dt"]) == (pats[p].s.time, pats[p].s.dt)
             assert t["time"] + t["dt"] == t_end
         assert c.group_times()[0] == t_end
+        # the statistics count the cells of the leaves that advanced
+        cu1, _ = c.stats()
+        assert cu1 - cu0 == advanced_cells
         # more dts than one per step of a synchronous scheme
         assert len(seen) > 3 * iterations // 4
         # nothing changes once every leaf is at the end time
