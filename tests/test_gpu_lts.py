@@ -167,3 +167,29 @@ def test_local_time_stepping_refuses_flux_correction_lists():
             c.run(1)
     finally:
         c.close()
+
+
+def test_virtual_interval_known_answer_on_the_device():
+    """PatchTest::testCoarsePatchTimeInterval (PatchTest.cpp:140-215) through
+    pcg_set_virtual_time_items: nine leaves with the test's intervals under one
+    virtual patch; an iteration that advances nothing sets its interval to
+    time 2.5, timestep 0.2, bit-identical to the oracle."""
+    from test_oracle_lts import _patch_test_intervals
+    c = P.Context(slab_doubles=200_000, max_patches=16, max_groups=1, params=PRM)
+    try:
+        leaves = []
+        for k, (t, dt) in enumerate(_patch_test_intervals()):
+            pid = c.alloc(3, pos=((k // 3) / 3.0, (k % 3) / 3.0), size=(1.0 / 3.0, 1.0 / 3.0), level=1)
+            c.set_time(pid, time=t, dt=dt)
+            leaves.append(pid)
+        virt = c.alloc(3, pos=(0.0, 0.0), size=(1.0, 1.0), level=0, leaf=False, virtual=True)
+        c.set_virtual_time_items(leaves, [virt] * 9)
+        c.set_group_max_dt(0, np.inf)
+        c.set_group_end_time(0, 0.0, 0.0)
+        c.set_time_stepping(P.TS_LOCAL)
+        assert np.all(c.run(1) == 0.0)
+        t = c.get_time(virt)
+        assert t["time"] == 2.5
+        assert t["dt"] == 1.0 + 1.7 - 2.5
+    finally:
+        c.close()

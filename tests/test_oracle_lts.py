@@ -85,3 +85,32 @@ def test_virtual_patches_take_the_intersection_of_their_leaves_intervals():
     for p, lf in zip(pats, ps.leaf):
         if lf:
             assert _tu(p) == t_end
+
+
+def _patch_test_intervals():
+    # the nine fine intervals of PatchTest::testCoarsePatchTimeInterval
+    # (src/peanoclaw/tests/PatchTest.cpp:140-215): (time, dt)
+    return [(1.0, 2.0), (1.0, 2.0), (1.0, 3.0), (0.0, 3.0), (1.0, 1.7), (0.0, 4.0), (0.0, 3.0),
+            (1.0, 2.0), (2.5, 1.5)]
+
+
+def test_virtual_interval_known_answer():
+    """PatchTest::testCoarsePatchTimeInterval: the coarse patch over nine fine
+    patches takes time 2.5 and timestep 0.2 (the intersection of the fine
+    intervals).  Here the fine patches are leaves under one virtual patch and
+    an iteration that advances nothing (end time 0) sets the interval."""
+    from helpers import oracle_patch_from
+    leaves = []
+    for k, (t, dt) in enumerate(_patch_test_intervals()):
+        p = oracle_patch_from(np.zeros(P.vector_size(3)), 3, pos=((k // 3) / 3.0, (k % 3) / 3.0),
+                              size=(1.0 / 3.0, 1.0 / 3.0), level=1, time=t, dt=dt)
+        leaves.append(p)
+    virt = oracle_patch_from(np.zeros(P.vector_size(3)), 3, pos=(0.0, 0.0), size=(1.0, 1.0), level=0,
+                             leaf=False, virtual=True)
+    pats = leaves + [virt]
+    vt = np.array([[k, 9] for k in range(9)], dtype=np.int32)
+    n, dto = O.grid_step_lts(pats, np.zeros((0, 9), dtype=np.int32), np.zeros(10, dtype=np.uint8),
+                             oracle_params(PRM), np.inf, 0.0, vt)
+    assert n == 0 and np.all(dto == 0.0)
+    assert virt.s.time == 2.5
+    assert abs(virt.s.dt - 0.2) <= 1e-12
