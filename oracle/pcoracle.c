@@ -121,9 +121,9 @@ double pco_time_unew(const pco_patch *p) {
 /*  - momentum flux jump through the free-surface difference                 */
 /*    df2 = (F_R - F_L) + g/2 (h_L+h_R) (eta_R - eta_L), so a lake at rest   */
 /*    (equal eta) gives exactly zero;                                        */
-/*  - wave strengths (lambda2 df1 - df2) / (2 cbar) and                      */
-/*    (df2 - lambda1 df1) / (2 cbar), lambda2 - lambda1 = 2 cbar, each as a  */
-/*    product with 1 / (2 cbar);                                             */
+/*  - wave strengths beta1 = (lambda2 df1 - df2) * (1 / (2 cbar)), with     */
+/*    lambda2 - lambda1 = 2 cbar, and beta2 = df1 - beta1 (the first         */
+/*    component of beta1 r1 + beta2 r2 = (df1, df2));                        */
 /*  - waves with speed < 0 go left, all others go right; when both go to    */
 /*    one side that side receives the whole flux jump (df1, df2), which      */
 /*    beta1 r1 + beta2 r2 equals;                                            */
@@ -182,7 +182,7 @@ static void fwave_derived(const pco_swe_params *prm, cellq L, cellq R, double ou
   double df2 = fma(a, deta, R.F - L.F);
   double inv = 1.0 / (2.0 * cb);
   double b1 = fma(l2, df1, -df2) * inv;
-  double b2 = fma(-l1, df1, df2) * inv;
+  double b2 = df1 - b1;
   double z1 = b1 * l1;
   double z2 = b2 * l2;
   double Lh, Lhu, Rh, Rhu;

@@ -316,7 +316,8 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
   // lambda2 - lambda1 = 2 cbar
   double inv = ieee::rcp_rn(twice(cb));
   double b1 = __dmul_rn(__fma_rn(l2, df1, -df2), inv);
-  double b2 = __dmul_rn(__fma_rn(-l1, df1, df2), inv);
+  // beta1 + beta2 = df1 (first component of the flux jump)
+  double b2 = __dsub_rn(df1, b1);
   double z1 = __dmul_rn(b1, l1);
   double z2 = __dmul_rn(b2, l2);
   // both waves to one side (supersonic edges): the whole flux jump
