@@ -33,11 +33,11 @@ UNIT = "cell-updates/s"
 
 # Algorithmic FP64 work of one cell update (wet cell, subsonic edges), counted
 # from the f-wave operation list of pcg_device.cuh (FMA = 2 flops, divide,
-# reciprocal and square root = 1 flop each): per cell 7 ops (sqrt, 1/s, p, q,
-# p^2, q^2, h + b); per edge 17 plain ops (9 adds, 4 multiplies, 2 cbar, sqrt,
-# divide, reciprocal) + 2 FMA (2 edges per cell); accumulation 8 FMA; update
-# 3 FMA.
-FLOP_PER_CELL = 7 + 2 * (17 + 2 * 2) + 2 * 8 + 2 * 3
+# reciprocal and square root = 1 flop each): per cell 8 ops (sqrt, 1/s, p, q,
+# p^2, q^2, h + b, g/2 h); per edge 16 plain ops (9 adds, 3 multiplies,
+# 2 cbar, sqrt, divide, reciprocal) + 2 FMA (2 edges per cell); accumulation
+# 8 FMA; update 3 FMA.
+FLOP_PER_CELL = 8 + 2 * (16 + 2 * 2) + 2 * 8 + 2 * 3
 # Algorithmic bytes per patch step: read h, hu, hv, b with halo, write h, hu, hv.
 def bytes_per_patch(n):
     return 8 * (4 * (n + 2) ** 2 + 3 * n * n)

@@ -117,7 +117,8 @@ double pco_time_unew(const pco_patch *p) {
 /*    bathymetry: reflecting wall (dry side replaced by the mirrored wet     */
 /*    state), and the update of the dry cell is dropped;                     */
 /*  - otherwise (inundation) the dry side enters as (h, 0, b);               */
-/*  - per cell: s = sqrt(h), p = hu * (1/s), F = p*p, surface eta = h + b;  */
+/*  - per cell: s = sqrt(h), p = hu * (1/s), F = p*p, surface eta = h + b,  */
+/*    gh = g/2 h; per edge cbar^2 = gh_L + gh_R;                             */
 /*  - momentum flux jump through the free-surface difference                 */
 /*    df2 = (F_R - F_L) + g/2 (h_L+h_R) (eta_R - eta_L), so a lake at rest   */
 /*    (equal eta) gives exactly zero;                                        */
@@ -130,12 +131,11 @@ double pco_time_unew(const pco_patch *p) {
 /* out = {hNetLeft, huNetLeft, hNetRight, huNetRight, maxEdgeSpeed}          */
 /* ------------------------------------------------------------------------ */
 typedef struct {
-  double h, hu, b, eta, s, p, F;
+  double gh, hu, b, eta, s, p, F; /* gh = g/2 h */
   int wet;
 } cellq;
 
 static void cell_derived(const pco_swe_params *prm, double h, double hu, double b, cellq *c) {
-  c->h = h;
   c->b = b;
   c->wet = h > prm->dry_tol;
   if (c->wet) {
@@ -149,13 +149,14 @@ static void cell_derived(const pco_swe_params *prm, double h, double hu, double 
   } else {
     /* a dry cell enters with zero velocity and a non-negative depth (a ghost
      * value interpolated across a coastline can be negative) */
-    c->h = h > 0.0 ? h : 0.0;
+    h = h > 0.0 ? h : 0.0;
     c->s = 0.0;
     c->p = 0.0;
     c->F = 0.0;
     c->hu = 0.0;
   }
-  c->eta = c->h + b;
+  c->eta = h + b;
+  c->gh = (0.5 * prm->g) * h;
 }
 
 static void fwave_derived(const pco_swe_params *prm, cellq L, cellq R, double out[5]) {
@@ -166,13 +167,12 @@ static void fwave_derived(const pco_swe_params *prm, cellq L, cellq R, double ou
   int wallR = L.wet && !R.wet && (L.eta <= R.b);
   int wallL = R.wet && !L.wet && (R.eta <= L.b);
   if (wallR) {
-    R.h = L.h; R.hu = -L.hu; R.b = L.b; R.eta = L.eta; R.s = L.s; R.p = -L.p; R.F = L.F;
+    R.gh = L.gh; R.hu = -L.hu; R.b = L.b; R.eta = L.eta; R.s = L.s; R.p = -L.p; R.F = L.F;
   }
   if (wallL) {
-    L.h = R.h; L.hu = -R.hu; L.b = R.b; L.eta = R.eta; L.s = R.s; L.p = -R.p; L.F = R.F;
+    L.gh = R.gh; L.hu = -R.hu; L.b = R.b; L.eta = R.eta; L.s = R.s; L.p = -R.p; L.F = R.F;
   }
-  double halfg = 0.5 * prm->g;
-  double a = halfg * (L.h + R.h);
+  double a = L.gh + R.gh; /* g/2 (hL + hR) as g/2 hL + g/2 hR */
   double cb = sqrt(a);
   double ub = (L.p + R.p) / (L.s + R.s);
   double l1 = ub - cb;

@@ -230,20 +230,20 @@ __device__ __forceinline__ double fmax_nonneg(double a, double b) {
 // f-wave edge solve (same operation sequence as the oracle's fwave_derived).
 // Divides and square roots go through pcg_ieee.cuh (integer pipes, results
 // identical to the IEEE operations).
-// Cell quantities: h, hu (normal momentum, zero for dry cells), b, surface
-// eta = h + b, s = sqrt(h), p = hu / s, F = p*p; wet = h > dry_tol; a dry cell
-// has h = max(h, 0).
+// Cell quantities: gh = g/2 h, hu (normal momentum, zero for dry cells), b,
+// surface eta = h + b, s = sqrt(h), p = hu / s, F = p*p; wet = h > dry_tol; a
+// dry cell has h = max(h, 0).
 // ---------------------------------------------------------------------------
 struct CellQ {
-  double h, hu, b, eta, s, p, F;
+  double gh, hu, b, eta, s, p, F;
   bool wet;
 };
 
-__device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu, double hv,
+__device__ __forceinline__ void cell_derived(double dry_tol, double halfg, double h, double hu, double hv,
                                              double b, CellQ &cx, CellQ &cy) {
   bool wet = gt_nonneg(h, dry_tol);
-  cx.h = h; cx.b = b; cx.wet = wet;
-  cy.h = h; cy.b = b; cy.wet = wet;
+  cx.b = b; cx.wet = wet;
+  cy.b = b; cy.wet = wet;
   if (wet) {
     double s = ieee::sqrt_rn(h);
     double rs = ieee::rcp_rn(s);
@@ -254,12 +254,14 @@ __device__ __forceinline__ void cell_derived(double dry_tol, double h, double hu
   } else {
     // dry: zero velocity, depth clamped to >= 0 (interpolated ghosts can be negative)
     double hd = gt_nonneg(h, 0.0) ? h : 0.0;
-    cx.h = hd; cy.h = hd;
+    h = hd;
     cx.s = 0.0; cx.p = 0.0; cx.F = 0.0; cx.hu = 0.0;
     cy.s = 0.0; cy.p = 0.0; cy.F = 0.0; cy.hu = 0.0;
   }
-  const double eta = __dadd_rn(cx.h, b);
+  const double eta = __dadd_rn(h, b);
   cx.eta = eta; cy.eta = eta;
+  const double gh = __dmul_rn(halfg, h);
+  cx.gh = gh; cy.gh = gh;
 }
 
 // 2 x, the IEEE product for every x.  A normal x whose double stays finite
@@ -286,13 +288,13 @@ __device__ __forceinline__ double neg(double x) {
 __device__ __forceinline__ void coastline(CellQ &L, CellQ &R, bool &wallL, bool &wallR) {
   wallR = L.wet && (L.eta <= R.b);
   wallL = R.wet && (R.eta <= L.b);
-  if (wallR) { R.h = L.h; R.hu = neg(L.hu); R.b = L.b; R.eta = L.eta; R.s = L.s; R.p = neg(L.p); R.F = L.F; }
-  if (wallL) { L.h = R.h; L.hu = neg(R.hu); L.b = R.b; L.eta = R.eta; L.s = R.s; L.p = neg(R.p); L.F = R.F; }
+  if (wallR) { R.gh = L.gh; R.hu = neg(L.hu); R.b = L.b; R.eta = L.eta; R.s = L.s; R.p = neg(L.p); R.F = L.F; }
+  if (wallL) { L.gh = R.gh; L.hu = neg(R.hu); L.b = R.b; L.eta = R.eta; L.s = R.s; L.p = neg(R.p); L.F = R.F; }
 }
 
 // out: Lh, Lhu, Rh, Rhu (net updates of the left/right cell) and the edge's
 // max wave speed.
-__device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, double &Lh,
+__device__ __forceinline__ void fwave_edge(CellQ L, CellQ R, double &Lh,
                                            double &Lhu, double &Rh, double &Rhu, double &speed) {
   if (!L.wet && !R.wet) {
     Lh = Lhu = Rh = Rhu = speed = 0.0;
@@ -305,7 +307,8 @@ __device__ __forceinline__ void fwave_edge(double halfg, CellQ L, CellQ R, doubl
   if (__any_sync(__activemask(), coast)) {
     if (coast) coastline(L, R, wallL, wallR);
   }
-  double a = __dmul_rn(halfg, __dadd_rn(L.h, R.h));
+  // a = g/2 (hL + hR), as g/2 hL + g/2 hR from the cells
+  double a = __dadd_rn(L.gh, R.gh);
   double cb = ieee::sqrt_rn(a);
   double ub = ieee::div_rn(__dadd_rn(L.p, R.p), __dadd_rn(L.s, R.s));
   double l1 = __dsub_rn(ub, cb);

@@ -19,7 +19,7 @@ namespace pcg {
 // Sweep: one 16x16 (or smaller) tile per CTA iteration.
 // ===========================================================================
 struct SweepSmem {
-  double h[kTile + 2][kTile + 2];
+  double gh[kTile + 2][kTile + 2];
   double b[kTile + 2][kTile + 2];
   double eta[kTile + 2][kTile + 2];
   double hu[kTile + 2][kTile + 2];
@@ -38,13 +38,13 @@ struct SweepSmem {
 
 __device__ __forceinline__ CellQ load_x(const SweepSmem &S, int i, int j) {
   CellQ c;
-  c.h = S.h[i][j]; c.b = S.b[i][j]; c.eta = S.eta[i][j]; c.hu = S.hu[i][j]; c.s = S.s[i][j]; c.p = S.p[i][j];
+  c.gh = S.gh[i][j]; c.b = S.b[i][j]; c.eta = S.eta[i][j]; c.hu = S.hu[i][j]; c.s = S.s[i][j]; c.p = S.p[i][j];
   c.F = S.F[i][j]; c.wet = S.wet[i][j] != 0;
   return c;
 }
 __device__ __forceinline__ CellQ load_y(const SweepSmem &S, int i, int j) {
   CellQ c;
-  c.h = S.h[i][j]; c.b = S.b[i][j]; c.eta = S.eta[i][j]; c.hu = S.hv[i][j]; c.s = S.s[i][j]; c.p = S.q[i][j];
+  c.gh = S.gh[i][j]; c.b = S.b[i][j]; c.eta = S.eta[i][j]; c.hu = S.hv[i][j]; c.s = S.s[i][j]; c.p = S.q[i][j];
   c.F = S.G[i][j]; c.wet = S.wet[i][j] != 0;
   return c;
 }
@@ -60,6 +60,7 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
                                              double &nh, double &nhu, double &nhv) {
   const int t = threadIdx.x;
   const double dry = prm.dry_tol;
+  const double halfg = __dmul_rn(0.5, prm.g);
   if (t == 0) {
     S.dxi = __ddiv_rn(1.0, subcell(P, 0));
     S.dyi = __ddiv_rn(1.0, subcell(P, 1));
@@ -84,13 +85,12 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
     }
     double b = slab[idx_pw(P, 0, x, y)];
     CellQ qx, qy;
-    cell_derived(dry, h, hu, hv, b, qx, qy);
-    S.h[sx][sy] = qx.h; S.b[sx][sy] = b; S.eta[sx][sy] = qx.eta; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
+    cell_derived(dry, halfg, h, hu, hv, b, qx, qy);
+    S.gh[sx][sy] = qx.gh; S.b[sx][sy] = b; S.eta[sx][sy] = qx.eta; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
     S.s[sx][sy] = qx.s; S.p[sx][sy] = qx.p; S.q[sx][sy] = qy.p;
     S.F[sx][sy] = qx.F; S.G[sx][sy] = qy.F; S.wet[sx][sy] = qx.wet ? 1 : 0;
   }
   __syncthreads();
-  const double halfg = __dmul_rn(0.5, prm.g);
   double smax = 0.0;
   double xr_h = 0.0, xr_hu = 0.0, yr_h = 0.0, yr_hv = 0.0;
   const bool active = t < tw * th;
@@ -98,12 +98,12 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
   if (active) {
     double Lh, Lhu, Rh, Rhu, sp;
     // x-edge between (lx-1, ly) and (lx, ly)
-    fwave_edge(halfg, load_x(S, lx, ly + 1), load_x(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
+    fwave_edge(load_x(S, lx, ly + 1), load_x(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
     smax = fmax_nonneg(smax, sp);
     xr_h = Rh; xr_hu = Rhu;
     if (lx >= 1) { S.xl_h[lx - 1][ly] = Lh; S.xl_hu[lx - 1][ly] = Lhu; }
     // y-edge between (lx, ly-1) and (lx, ly)
-    fwave_edge(halfg, load_y(S, lx + 1, ly), load_y(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
+    fwave_edge(load_y(S, lx + 1, ly), load_y(S, lx + 1, ly + 1), Lh, Lhu, Rh, Rhu, sp);
     smax = fmax_nonneg(smax, sp);
     yr_h = Rh; yr_hv = Rhu;
     if (ly >= 1) { S.yl_h[lx][ly - 1] = Lh; S.yl_hv[lx][ly - 1] = Lhu; }
@@ -115,11 +115,11 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
     double Lh, Lhu, Rh, Rhu, sp;
     if (ce < th) {
       int j = ce;
-      fwave_edge(halfg, load_x(S, tw, j + 1), load_x(S, tw + 1, j + 1), Lh, Lhu, Rh, Rhu, sp);
+      fwave_edge(load_x(S, tw, j + 1), load_x(S, tw + 1, j + 1), Lh, Lhu, Rh, Rhu, sp);
       S.xl_h[tw - 1][j] = Lh; S.xl_hu[tw - 1][j] = Lhu;
     } else {
       int i = ce - th;
-      fwave_edge(halfg, load_y(S, i + 1, th), load_y(S, i + 1, th + 1), Lh, Lhu, Rh, Rhu, sp);
+      fwave_edge(load_y(S, i + 1, th), load_y(S, i + 1, th + 1), Lh, Lhu, Rh, Rhu, sp);
       S.yl_h[i][th - 1] = Lh; S.yl_hv[i][th - 1] = Lhu;
     }
     smax = fmax_nonneg(smax, sp);

@@ -23,7 +23,7 @@ namespace {
 
 // Per-warp shared memory: one entry per (group, column), G * w <= 32.
 struct StripWarpSmem {
-  double h[32], b[32], eta[32], hv[32], s[32], q[32], G[32];  // cell below the group's first row
+  double gh[32], b[32], eta[32], hv[32], s[32], q[32], G[32];  // cell below the group's first row
   double top_h[32], top_hv[32], top_sp[32];            // edge above the group's last row
   unsigned char wet[32];
 };
@@ -45,17 +45,17 @@ __device__ __forceinline__ void load_state(const double *__restrict__ slab, cons
 
 // Per-lane slot for the x-direction quantities of the previous column's cell.
 struct StripLaneSmem {
-  double h[32], hu[32], b[32], eta[32], s[32], p[32], F[32];
+  double gh[32], hu[32], b[32], eta[32], s[32], p[32], F[32];
   unsigned char wet[32];
 };
 
 __device__ __forceinline__ void store_x(StripLaneSmem &L, int lane, const CellQ &c) {
-  L.h[lane] = c.h; L.hu[lane] = c.hu; L.b[lane] = c.b; L.eta[lane] = c.eta; L.s[lane] = c.s; L.p[lane] = c.p;
+  L.gh[lane] = c.gh; L.hu[lane] = c.hu; L.b[lane] = c.b; L.eta[lane] = c.eta; L.s[lane] = c.s; L.p[lane] = c.p;
   L.F[lane] = c.F; L.wet[lane] = c.wet ? 1 : 0;
 }
 __device__ __forceinline__ CellQ load_x(const StripLaneSmem &L, int lane) {
   CellQ c;
-  c.h = L.h[lane]; c.hu = L.hu[lane]; c.b = L.b[lane]; c.eta = L.eta[lane]; c.s = L.s[lane]; c.p = L.p[lane];
+  c.gh = L.gh[lane]; c.hu = L.hu[lane]; c.b = L.b[lane]; c.eta = L.eta[lane]; c.s = L.s[lane]; c.p = L.p[lane];
   c.F = L.F[lane]; c.wet = L.wet[lane] != 0;
   return c;
 }
@@ -110,15 +110,15 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       double h, hu, hv, b;
       CellQ cx, cy, ty, ay;
       load_state(slab, PH, x, HG.y0 - 1, h, hu, hv, b);
-      cell_derived(dry, h, hu, hv, b, cx, cy);
-      S.h[lane] = cy.h; S.b[lane] = cy.b; S.eta[lane] = cy.eta; S.hv[lane] = cy.hu; S.s[lane] = cy.s;
+      cell_derived(dry, halfg, h, hu, hv, b, cx, cy);
+      S.gh[lane] = cy.gh; S.b[lane] = cy.b; S.eta[lane] = cy.eta; S.hv[lane] = cy.hu; S.s[lane] = cy.s;
       S.q[lane] = cy.p; S.G[lane] = cy.F; S.wet[lane] = cy.wet ? 1 : 0;
       load_state(slab, PH, x, HG.y0 + hs - 1, h, hu, hv, b);
-      cell_derived(dry, h, hu, hv, b, cx, ty);
+      cell_derived(dry, halfg, h, hu, hv, b, cx, ty);
       load_state(slab, PH, x, HG.y0 + hs, h, hu, hv, b);
-      cell_derived(dry, h, hu, hv, b, cx, ay);
+      cell_derived(dry, halfg, h, hu, hv, b, cx, ay);
       double Lh, Lhv, Rh, Rhv, sp;
-      fwave_edge(halfg, ty, ay, Lh, Lhv, Rh, Rhv, sp);
+      fwave_edge(ty, ay, Lh, Lhv, Rh, Rhv, sp);
       S.top_h[lane] = Lh; S.top_hv[lane] = Lhv; S.top_sp[lane] = sp;
     }
     __syncwarp();
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
     {
       CellQ cx, cy;
       if (act) load_state(slab, P, SG.x0 - 1, y, h, hu, hv, b);
-      cell_derived(dry, h, hu, hv, b, cx, cy);
+      cell_derived(dry, halfg, h, hu, hv, b, cx, cy);
       store_x(L, lane, cx);
     }
     // partial sums of the previous column's cell, in the accumulation order
@@ -148,9 +148,9 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       h = fh; hu = fhu; hv = fhv; b = fb;
       if (act && c < w) load_state(slab, P, x + 1, y, fh, fhu, fhv, fb);
       CellQ cx, cy;
-      cell_derived(dry, h, hu, hv, b, cx, cy);
+      cell_derived(dry, halfg, h, hu, hv, b, cx, cy);
       double Lh, Lhu, Rh, Rhu, sp;
-      fwave_edge(halfg, load_x(L, lane), cx, Lh, Lhu, Rh, Rhu, sp);
+      fwave_edge(load_x(L, lane), cx, Lh, Lhu, Rh, Rhu, sp);
       smax = fmax_nonneg(smax, sp);
       if (c > 0 && act) {
         double a = __fma_rn(dxi, Lh, a1);
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       // y-edge below this lane's cell; the lower cell comes from the next
       // lane down, or from shared memory for a group's first row
       CellQ dn;
-      dn.h = shfl_up_d(cy.h, 1);
+      dn.gh = shfl_up_d(cy.gh, 1);
       dn.b = shfl_up_d(cy.b, 1);
       dn.eta = shfl_up_d(cy.eta, 1);
       dn.hu = shfl_up_d(cy.hu, 1);
@@ -175,11 +175,11 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks)
       dn.wet = __shfl_up_sync(0xffffffffu, (int)cy.wet, 1) != 0;
       const int sl = gi * w + c;
       if (j == 0 && act) {
-        dn.h = S.h[sl]; dn.b = S.b[sl]; dn.eta = S.eta[sl]; dn.hu = S.hv[sl]; dn.s = S.s[sl];
+        dn.gh = S.gh[sl]; dn.b = S.b[sl]; dn.eta = S.eta[sl]; dn.hu = S.hv[sl]; dn.s = S.s[sl];
         dn.p = S.q[sl]; dn.F = S.G[sl]; dn.wet = S.wet[sl] != 0;
       }
       double yLh, yLhv, yRh, yRhv, sp2;
-      fwave_edge(halfg, dn, cy, yLh, yLhv, yRh, yRhv, sp2);
+      fwave_edge(dn, cy, yLh, yLhv, yRh, yRhv, sp2);
       smax = fmax_nonneg(smax, sp2);
       double uh = shfl_down_d(yLh, 1), uhv = shfl_down_d(yLhv, 1);
       if (j == hs - 1 && act) {
