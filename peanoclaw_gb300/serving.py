@@ -126,8 +126,9 @@ class Server:
         need = sum(P.vector_size(n) + 32 for n in ps.n)
         return need <= free
 
-    def admit(self, req, now):
-        ps = scenario_patchset(req)
+    def admit(self, req, now, ps=None):
+        if ps is None:
+            ps = scenario_patchset(req)
         if not self.free_groups or not self._fits(ps):
             return False
         g = self.free_groups.pop(0)
@@ -184,28 +185,45 @@ class Server:
         return done
 
     def serve(self, requests, clock=time.perf_counter, max_wall=600.0):
-        """Run the continuous-batching loop over `requests` (sorted by arrival)."""
+        """Run the continuous-batching loop over `requests` (sorted by arrival).
+
+        A request's patch set is built on a worker thread as soon as it
+        arrives, while the device advances the resident scenarios (the
+        library calls release the interpreter lock while they wait for the
+        GPU); admission then only allocates and uploads."""
+        from concurrent.futures import ThreadPoolExecutor
         pending = sorted(requests, key=lambda r: r.arrival)
         waiting = []
         finished = []
+        built = {}
+        pool = ThreadPoolExecutor(max_workers=1)
         t0 = clock()
-        while pending or waiting or self.resident:
-            now = clock() - t0
-            if now > max_wall:
-                break
-            while pending and pending[0].arrival <= now:
-                waiting.append(pending.pop(0))
-            still = []
-            for r in waiting:
-                if not self.admit(r, now):
+        try:
+            while pending or waiting or self.resident:
+                now = clock() - t0
+                if now > max_wall:
+                    break
+                while pending and pending[0].arrival <= now:
+                    r = pending.pop(0)
+                    waiting.append(r)
+                    built[id(r)] = pool.submit(scenario_patchset, r)
+                still = []
+                for r in waiting:
+                    f = built[id(r)]
+                    if not self.resident or f.done():
+                        if self.admit(r, now, f.result()):
+                            del built[id(r)]
+                            continue
                     still.append(r)
-            waiting = still
-            if not self.resident:
-                if pending:
-                    time.sleep(max(0.0, min(0.01, pending[0].arrival - now)))
-                continue
-            for g in self.step():
-                finished.append(self.retire(g, clock() - t0))
+                waiting = still
+                if not self.resident:
+                    if pending:
+                        time.sleep(max(0.0, min(0.01, pending[0].arrival - now)))
+                    continue
+                for g in self.step():
+                    finished.append(self.retire(g, clock() - t0))
+        finally:
+            pool.shutdown(wait=True, cancel_futures=True)
         return finished, clock() - t0
 
 
