@@ -161,6 +161,14 @@ int pcg_transfer_ghostlayer(pcg_context *ctx, const int32_t size[2], const int32
 int pcg_interpolate_solution(pcg_context *ctx, const int32_t size[2], const int32_t dst_offset[2],
                              int32_t src, int32_t dst, int32_t to_uold, int32_t to_current_time,
                              int32_t use_time_unew_or_uold, int32_t swe);
+/* n interpolations with the same flags in one launch: size[2k], dst_offset[2k]
+ * and src[k] -> dst[k] as in pcg_interpolate_solution.  The destinations
+ * must be distinct and none may be a source (the items run concurrently);
+ * Remesh::createCell initialises every new fine patch this way
+ * (Remesh.cpp:399-420). */
+int pcg_interpolate_solution_many(pcg_context *ctx, int32_t n, const int32_t *src, const int32_t *dst,
+                                  const int32_t *size, const int32_t *dst_offset, int32_t to_uold,
+                                  int32_t to_current_time, int32_t use_time_unew_or_uold, int32_t swe);
 /* SWEKernel::restrictSolution (SWEKernel.cpp:288-307) over DefaultRestriction
  * (DefaultRestriction.cpph:17-150); swe = 0 gives Numerics::restrictSolution. */
 int pcg_restrict_solution(pcg_context *ctx, int32_t src, int32_t dst, int32_t only_overlapped,
@@ -223,6 +231,9 @@ int pcg_refinement_indicator(pcg_context *ctx, int32_t n, const int32_t *ids, do
 int pcg_gather_cells(pcg_context *ctx, int32_t n, const int32_t *ids, double *out, int64_t out_len);
 /* Time intervals of the listed patches in one call. */
 int pcg_patches_get_time(pcg_context *ctx, int32_t n, const int32_t *ids, pcg_patch_time *out);
+/* Time records of the listed patches in one call (pcg_patch_set_time for
+ * each); ids must be distinct. */
+int pcg_patches_set_time(pcg_context *ctx, int32_t n, const int32_t *ids, const pcg_patch_time *in);
 /* Neighbouring ghost-layer bounds (restr_lower / restr_upper of
  * pcg_patch_time) of the listed patches in one call: lower[2k], lower[2k+1],
  * upper[2k], upper[2k+1] for ids[k]; the other time fields are kept.  The

@@ -435,8 +435,10 @@ def remesh(grid, backend, g, b_of):
         return 0, 0
     n = grid.n
     n_ref = n_crs = 0
-    # refinement, coarse to fine: children of newly refined slots
+    # refinement, coarse to fine: children of newly refined slots, created one
+    # level at a time (a new child can be refined in the same remesh)
     for l in range(grid.levels - 1):
+        kids = []
         for i, j in np.argwhere(R1[l] & ~R0[l]).tolist():
             parent = backend.handle((l, i, j))
             t = backend.times(parent)
@@ -446,12 +448,17 @@ def remesh(grid, backend, g, b_of):
                     if E0[l + 1][ch[1], ch[2]]:
                         continue
                     pos, size = grid.geometry(*ch)
-                    h = backend.alloc(ch, pos, size, l + 1)
-                    backend.set_times(h, *t)
                     X, Y = _centers(pos, size, n, ghost=True)
-                    backend.set_b(h, b_of(X, Y))
-                    backend.interpolate_child(parent, h)
+                    kids.append((parent, ch, pos, size, l + 1, t, b_of(X, Y)))
             n_ref += 1
+        if hasattr(backend, "create_children"):
+            backend.create_children(kids)
+        else:
+            for parent, ch, pos, size, lvl, t, b in kids:
+                h = backend.alloc(ch, pos, size, lvl)
+                backend.set_times(h, *t)
+                backend.set_b(h, b)
+                backend.interpolate_child(parent, h)
     # coarsening, fine to coarse: restrict the children into their parent
     for l in range(grid.levels - 2, -1, -1):
         for i, j in np.argwhere(R0[l] & ~R1[l]).tolist():
@@ -524,6 +531,29 @@ class DeviceAmr:
         off = 3 * n * n + 3 * (n + 2) * (n + 2)
         vec[off:off + (n + 2) * (n + 2)] = np.ascontiguousarray(b).ravel()
         self.ctx.upload(pid, vec)
+
+    def create_children(self, kids):
+        """The per-child sequence of remesh (alloc, time interval of the coarse
+        patch, bathymetry, interpolation into uNew, then into uOld at the
+        current time) for all new children of one level, in batched calls."""
+        if not kids:
+            return
+        from .pcg import vector_size
+        n = self.grid.n
+        pids = [self.alloc(ch, pos, size, lvl) for _, ch, pos, size, lvl, _, _ in kids]
+        ts = np.array([t for _, _, _, _, _, t, _ in kids], dtype=np.float64).reshape(-1, 3)
+        self.ctx.set_times_many(pids, ts[:, 0], ts[:, 1], ts[:, 2])
+        ln = vector_size(n)
+        off = 3 * n * n + 3 * (n + 2) * (n + 2)
+        packed = np.zeros(ln * len(kids))
+        for k, kid in enumerate(kids):
+            packed[k * ln + off:k * ln + off + (n + 2) * (n + 2)] = np.ascontiguousarray(kid[6]).ravel()
+        self.ctx.upload_many(pids, packed)
+        parents = [kid[0] for kid in kids]
+        sz = np.tile(np.array([n, n], dtype=np.int32), (len(kids), 1))
+        of = np.zeros((len(kids), 2), dtype=np.int32)
+        for to_uold, current in ((0, 0), (1, 1)):
+            self.ctx.interpolate_many(parents, pids, sz, of, to_uold, current, 0, True)
 
     def interpolate_child(self, parent, child):
         from . import pcg as P

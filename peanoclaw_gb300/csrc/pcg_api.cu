@@ -1150,6 +1150,77 @@ int pcg_interpolate_solution(pcg_context *c, const int32_t size[2], const int32_
   return PCG_OK;
 }
 
+int pcg_interpolate_solution_many(pcg_context *c, int32_t n, const int32_t *src, const int32_t *dst,
+                                  const int32_t *size, const int32_t *dof, int32_t to_uold, int32_t to_current_time,
+                                  int32_t use_time_unew_or_uold, int32_t swe) {
+  if (!c || n < 0 || (n > 0 && (!src || !dst || !size || !dof))) return fail(PCG_E_INVALID, "bad arguments");
+  if (n == 0) return PCG_OK;
+  std::vector<pcg::GhostItemDev> items(n);
+  std::vector<char> seen(c->max_patches, 0);
+  for (int32_t k = 0; k < n; k++) {
+    if (!valid_id(c, src[k]) || !valid_id(c, dst[k]))
+      return fail(PCG_E_INVALID, "interpolation " + std::to_string(k) + ": unknown patch id");
+    if (seen[dst[k]]) return fail(PCG_E_INVALID, "interpolation " + std::to_string(k) + ": destination listed twice");
+    seen[dst[k]] = 1;
+    const pcg::PatchDev &S = c->h_patches[src[k]], &D = c->h_patches[dst[k]];
+    if (S.nq != D.nq) return fail(PCG_E_INVALID, "interpolation " + std::to_string(k) + ": unknowns differ");
+    if (S.nx < 2 || S.ny < 2) return fail(PCG_E_INVALID, "interpolation " + std::to_string(k) + ": source below 2x2");
+    if (!region_inside(D, &dof[2 * k], &size[2 * k], to_uold != 0))
+      return fail(PCG_E_INVALID, "interpolation " + std::to_string(k) + ": region outside the destination");
+    if (swe && (S.np_w < 1 || D.np_w < 1))
+      return fail(PCG_E_INVALID, "interpolation " + std::to_string(k) + ": needs the bathymetry parameter");
+    items[k] = make_item(1, &size[2 * k], nullptr, &dof[2 * k], src[k], dst[k]);
+  }
+  for (int32_t k = 0; k < n; k++)
+    if (seen[src[k]]) return fail(PCG_E_INVALID, "a destination is also a source");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->fin_dirty = true;
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  rc = ensure_staging(c, (sizeof(pcg::GhostItemDev) * (size_t)n + 7) / 8, 0);
+  if (rc != PCG_OK) return rc;
+  pcg::GhostItemDev *d_items = reinterpret_cast<pcg::GhostItemDev *>(c->d_staging);
+  PCG_CUDA(cudaMemcpyAsync(d_items, items.data(), sizeof(pcg::GhostItemDev) * (size_t)n, cudaMemcpyHostToDevice,
+                           c->stream));
+  PCG_CUDA(pcg::launch_interpolate_many(c->stream, c->slab, c->d_patches, c->d_times, d_items, n, to_uold,
+                                        to_current_time, use_time_unew_or_uold, swe));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
+int pcg_patches_set_time(pcg_context *c, int32_t n, const int32_t *ids, const pcg_patch_time *in) {
+  if (!c || n < 0 || (n > 0 && (!ids || !in))) return fail(PCG_E_INVALID, "bad arguments");
+  if (n == 0) return PCG_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  std::vector<char> seen(c->max_patches, 0);
+  std::vector<long long> meta(n);
+  std::vector<pcg::PatchTimeDev> rec(n);
+  for (int32_t k = 0; k < n; k++) {
+    if (!valid_id(c, ids[k])) return fail(PCG_E_INVALID, "unknown patch id " + std::to_string(ids[k]));
+    if (seen[ids[k]]) return fail(PCG_E_INVALID, "patch id " + std::to_string(ids[k]) + " listed twice");
+    seen[ids[k]] = 1;
+    meta[k] = ids[k];
+    pcg::PatchTimeDev d{};
+    d.time = in[k].time; d.dt = in[k].dt; d.est_next = in[k].est_next;
+    d.min_nb_time = in[k].min_neighbor_time; d.max_nb_dt = in[k].max_neighbor_dt;
+    d.rl[0] = in[k].restr_lower[0]; d.rl[1] = in[k].restr_lower[1];
+    d.ru[0] = in[k].restr_upper[0]; d.ru[1] = in[k].restr_upper[1];
+    rec[k] = d;
+  }
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = ensure_staging(c, (sizeof(pcg::PatchTimeDev) * (size_t)n + 7) / 8, (size_t)n);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(c->d_copy_meta, meta.data(), sizeof(long long) * (size_t)n, cudaMemcpyHostToDevice,
+                           c->stream));
+  PCG_CUDA(cudaMemcpyAsync(c->d_staging, rec.data(), sizeof(pcg::PatchTimeDev) * (size_t)n,
+                           cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(pcg::launch_scatter_times(c->stream, c->d_copy_meta,
+                                     reinterpret_cast<const pcg::PatchTimeDev *>(c->d_staging), n, c->d_times));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  return PCG_OK;
+}
+
 int pcg_restrict_solution(pcg_context *c, int32_t src, int32_t dst, int32_t only_overlapped, int32_t swe) {
   if (!valid_id(c, src) || !valid_id(c, dst)) return fail(PCG_E_INVALID, "unknown patch id");
   const pcg::PatchDev &S = c->h_patches[src], &D = c->h_patches[dst];

@@ -1800,6 +1800,40 @@ cudaError_t launch_transfer(cudaStream_t st, double *slab, const PatchDev *patch
   return cudaGetLastError();
 }
 
+// Interpolations of several (source, destination) items with distinct
+// destinations: one CTA per item, the cells of k_interpolate.
+__global__ void k_interpolate_many(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                   const GhostItemDev *items, int to_uold, int to_current, int use_unew_uold,
+                                   int swe) {
+  const GhostItemDev it = items[blockIdx.x];
+  const PatchDev S = patches[it.src], D = patches[it.dst];
+  const double tf = interp_tf(S, times[it.src], D, times[it.dst], to_current != 0, use_unew_uold != 0);
+  const int ncell = it.size[0] * it.size[1];
+  for (int k = threadIdx.x; k < ncell; k += blockDim.x)
+    interp_cell(slab, S, D, it.size, it.dst_off, tf, to_uold != 0, swe != 0, k);
+}
+
+cudaError_t launch_interpolate_many(cudaStream_t st, double *slab, const PatchDev *patches,
+                                    const PatchTimeDev *times, const GhostItemDev *items, int n, int to_uold,
+                                    int to_current, int use_unew_uold, int swe) {
+  if (n <= 0) return cudaSuccess;
+  k_interpolate_many<<<n, 256, 0, st>>>(slab, patches, times, items, to_uold, to_current, use_unew_uold, swe);
+  return cudaGetLastError();
+}
+
+// Time records of listed patches.
+__global__ void k_scatter_times(const long long *__restrict__ ids, const PatchTimeDev *__restrict__ in, int n,
+                                PatchTimeDev *__restrict__ times) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) times[ids[k]] = in[k];
+}
+
+cudaError_t launch_scatter_times(cudaStream_t st, const long long *ids, const PatchTimeDev *in, int n,
+                                 PatchTimeDev *times) {
+  if (n <= 0) return cudaSuccess;
+  k_scatter_times<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, st>>>(ids, in, n, times);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_interpolate(cudaStream_t st, double *slab, const PatchDev *patches,
                                const PatchTimeDev *times, const GhostItemDev &it, int to_uold,
                                int to_current, int use_unew_uold, int swe) {

@@ -86,6 +86,11 @@ cudaError_t launch_fill_boundary_layer(cudaStream_t st, double *slab, const Patc
                                        int pid, int dim, int up);
 cudaError_t launch_transfer(cudaStream_t st, double *slab, const PatchDev *patches,
                             const PatchTimeDev *times, const GhostItemDev &it);
+cudaError_t launch_interpolate_many(cudaStream_t st, double *slab, const PatchDev *patches,
+                                    const PatchTimeDev *times, const GhostItemDev *items, int n, int to_uold,
+                                    int to_current, int use_unew_uold, int swe);
+cudaError_t launch_scatter_times(cudaStream_t st, const long long *ids, const PatchTimeDev *in, int n,
+                                 PatchTimeDev *times);
 cudaError_t launch_interpolate(cudaStream_t st, double *slab, const PatchDev *patches,
                                const PatchTimeDev *times, const GhostItemDev &it, int to_uold,
                                int to_current, int use_unew_uold, int swe);

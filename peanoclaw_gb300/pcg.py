@@ -117,6 +117,9 @@ SIGNATURES = {
     "pcg_gather_cells": (C.c_int, [_CTX, C.c_int32, _I2, _D, C.c_int64]),
     "pcg_patches_get_time": (C.c_int, [_CTX, C.c_int32, _I2, C.POINTER(PatchTime)]),
     "pcg_patches_set_restriction_bounds": (C.c_int, [_CTX, C.c_int32, _I2, _D, _D]),
+    "pcg_patches_set_time": (C.c_int, [_CTX, C.c_int32, _I2, C.POINTER(PatchTime)]),
+    "pcg_interpolate_solution_many": (C.c_int, [_CTX, C.c_int32, _I2, _I2, _I2, _I2, C.c_int32, C.c_int32,
+                                                C.c_int32, C.c_int32]),
     "pcg_switch_to_leaf": (C.c_int, [_CTX, C.c_int32]),
     "pcg_amr_layout": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _I2, _I2, _I2,
                                  C.POINTER(C.c_uint8), _I2, _I2, _I2, _I2, _I2, _I2, _D, _D, _I2]),
@@ -327,6 +330,27 @@ class Context:
         arr = (PatchTime * max(1, len(ids)))()
         check(lib().pcg_patches_get_time(self.h, len(ids), ids.ctypes.data_as(_I2), arr))
         return np.array([[arr[k].time, arr[k].dt] for k in range(len(ids))]).reshape(-1, 2)
+
+    def set_times_many(self, ids, time, dt, est_next):
+        """Time, dt and estimated next dt of many patches in one call
+        (pcg_patches_set_time; restriction bounds reset to empty)."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        big = np.finfo(np.float64).max
+        arr = (PatchTime * max(1, len(ids)))()
+        for k in range(len(ids)):
+            arr[k] = PatchTime(float(time[k]), float(dt[k]), float(est_next[k]), 0.0, 0.0,
+                               (C.c_double * 2)(big, big), (C.c_double * 2)(-big, -big))
+        check(lib().pcg_patches_set_time(self.h, len(ids), ids.ctypes.data_as(_I2), arr))
+
+    def interpolate_many(self, src, dst, size, dst_offset, to_uold, to_current, use_unew_uold, swe=True):
+        """pcg_interpolate_solution_many: size and dst_offset are (n, 2)."""
+        src = np.ascontiguousarray(src, dtype=np.int32)
+        dst = np.ascontiguousarray(dst, dtype=np.int32)
+        sz = np.ascontiguousarray(size, dtype=np.int32).reshape(-1, 2)
+        of = np.ascontiguousarray(dst_offset, dtype=np.int32).reshape(-1, 2)
+        check(lib().pcg_interpolate_solution_many(self.h, len(src), src.ctypes.data_as(_I2), dst.ctypes.data_as(_I2),
+                                                  sz.ctypes.data_as(_I2), of.ctypes.data_as(_I2), int(to_uold),
+                                                  int(to_current), int(use_unew_uold), int(swe)))
 
     def set_restriction_bounds(self, ids, lower, upper):
         """Restriction bounds of many patches (pcg_patches_set_restriction_bounds);

@@ -97,3 +97,41 @@ def test_batched_restriction_bounds():
             ctx.set_restriction_bounds([99], np.zeros((1, 2)), np.zeros((1, 2)))
     finally:
         ctx.close()
+
+
+def test_batched_times_and_interpolations():
+    """pcg_patches_set_time writes every listed record; pcg_interpolate_solution_many
+    equals one pcg_interpolate_solution per item; both reject repeated or
+    conflicting ids."""
+    import ctypes as C
+    rng = np.random.default_rng(3)
+    ctx = P.Context(slab_doubles=2_000_000, max_patches=32, max_groups=1, params=PRM)
+    try:
+        coarse = [ctx.alloc(9, pos=(0.3 * k, 0.0), size=(0.3, 0.3)) for k in range(2)]
+        for k, pid in enumerate(coarse):
+            v = np.zeros(P.vector_size(9))
+            v[:] = rng.uniform(0.5, 1.5, v.size)
+            ctx.upload(pid, v)
+        fine_a = [ctx.alloc(9, pos=(0.3 * (k // 3) + 0.1 * (k % 3), 0.0), size=(0.1, 0.1), level=1) for k in range(6)]
+        fine_b = [ctx.alloc(9, pos=(0.3 * (k // 3) + 0.1 * (k % 3), 0.0), size=(0.1, 0.1), level=1) for k in range(6)]
+        ctx.set_times_many(coarse + fine_a + fine_b, np.full(14, 0.5), np.full(14, 0.25), np.full(14, 0.125))
+        for pid in coarse + fine_a:
+            t = ctx.get_time(pid)
+            assert (t["time"], t["dt"], t["est_next"]) == (0.5, 0.25, 0.125)
+        src = [coarse[k // 3] for k in range(6)]
+        for to_uold, cur in ((0, 0), (1, 1)):
+            ctx.interpolate_many(src, fine_a, np.full((6, 2), 9), np.zeros((6, 2)), to_uold, cur, 0, True)
+            for s, d in zip(src, fine_b):
+                P.check(P.lib().pcg_interpolate_solution(ctx.h, P.i2((9, 9)), P.i2((0, 0)), s, d, to_uold, cur, 0, 1))
+        a = ctx.download_many(fine_a, 6 * P.vector_size(9))
+        b = ctx.download_many(fine_b, 6 * P.vector_size(9))
+        assert np.array_equal(a.view(np.int64), b.view(np.int64))
+        with pytest.raises(P.PcgError):
+            ctx.interpolate_many(src[:2], [fine_a[0], fine_a[0]], np.full((2, 2), 9), np.zeros((2, 2)), 0, 0, 0)
+        with pytest.raises(P.PcgError):
+            ctx.interpolate_many([fine_a[0], coarse[0]], [fine_a[1], fine_a[0]], np.full((2, 2), 9),
+                                 np.zeros((2, 2)), 0, 0, 0)
+        with pytest.raises(P.PcgError):
+            ctx.set_times_many([coarse[0], coarse[0]], [0, 0], [0, 0], [0, 0])
+    finally:
+        ctx.close()
