@@ -43,14 +43,20 @@ __global__ void k_scatter(double *slab, const double *staging, const long long *
   }
 }
 
+// Records every group's dt of a step; with `advance` it also ends the step
+// (t += dt for the active groups, as k_group_advance) in the same launch.
 __global__ void k_record_hist(int n_groups, const unsigned long long *group_dt, double *hist,
-                              int *counter, int capacity) {
+                              int *counter, int capacity, int advance, const int *group_active,
+                              double *group_time) {
   __shared__ int idx;
   if (threadIdx.x == 0) idx = *counter;
   __syncthreads();
   if (idx < capacity)
     for (int g = threadIdx.x; g < n_groups; g += blockDim.x)
       hist[(long long)idx * n_groups + g] = __longlong_as_double((long long)group_dt[g]);
+  if (advance)
+    for (int g = threadIdx.x; g < n_groups; g += blockDim.x)
+      if (group_active[g]) group_time[g] = __dadd_rn(group_time[g], __longlong_as_double((long long)group_dt[g]));
   __syncthreads();
   if (threadIdx.x == 0) *counter = idx + 1;
 }
@@ -672,17 +678,18 @@ int enqueue_lts(pcg_context *c, int phase) {
 // Enqueue one synchronous step (no synchronisation, capturable in BATCHED
 // mode); with local time stepping one iteration in which only the leaves
 // that may advance are filled and solved, each with its own dt.
-int enqueue_step(pcg_context *c, int mode) {
+int enqueue_step(pcg_context *c, int mode, bool advance = true) {
   using namespace pcg;
-  PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_t_end, c->d_group_time,
-                        c->d_group_dt, c->d_group_active, c->max_patches,
-                        c->d_patch_smax));
   int rc;
   if (mode == PCG_MODE_BATCHED) {
+    // reset and per-item time factors in one launch (the time factors read
+    // the times before the step, which neither the reset nor the first
+    // local-time-stepping phase changes)
+    PCG_CUDA(launch_reset_items(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_t_end, c->d_group_time,
+                                c->d_group_dt, c->d_group_active, c->max_patches, c->d_patch_smax, c->d_patches,
+                                c->d_times, c->d_items, (int)c->h_items.size(), c->d_item_step));
     const int *pact = c->ts_local ? c->d_pact : nullptr;
     if (c->ts_local && (rc = enqueue_lts(c, 0)) != PCG_OK) return rc;
-    PCG_CUDA(launch_item_step(c->stream, c->d_patches, c->d_times, c->d_items, (int)c->h_items.size(),
-                              c->d_item_step));
     PCG_CUDA(launch_ghost_cells(c->stream, c->slab, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
                                 c->n_interp_cells, c->d_copy_plan, c->d_plan, c->d_item_step,
                                 c->d_group_active, c->d_fin, pact));
@@ -696,6 +703,8 @@ int enqueue_step(pcg_context *c, int mode) {
       return enqueue_post_update(c);
     }
   } else {
+    PCG_CUDA(launch_reset(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_t_end, c->d_group_time,
+                          c->d_group_dt, c->d_group_active, c->max_patches, c->d_patch_smax));
     for (int p : c->leaf_ids)
       PCG_CUDA(launch_fill_patch(c->stream, c->slab, c->d_patches, c->d_times, c->d_items,
                                  c->item_first[p], c->item_count[p], p, c->d_group_active));
@@ -715,8 +724,9 @@ int enqueue_step(pcg_context *c, int mode) {
   }
   rc = enqueue_post_update(c);
   if (rc != PCG_OK) return rc;
-  PCG_CUDA(launch_group_advance(c->stream, c->max_groups, c->d_group_dt, c->d_group_active,
-                                c->d_group_time));
+  if (advance)
+    PCG_CUDA(launch_group_advance(c->stream, c->max_groups, c->d_group_dt, c->d_group_active,
+                                  c->d_group_time));
   return PCG_OK;
 }
 
@@ -1640,9 +1650,12 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
       if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
       cudaGraph_t g;
       PCG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      int erc = enqueue_step(c, PCG_MODE_BATCHED);
+      // the history kernel also advances the group times (one launch less);
+      // local time stepping sets them in its own last phase
+      int erc = enqueue_step(c, PCG_MODE_BATCHED, false);
       k_record_hist<<<1, threads, 0, c->stream>>>(c->max_groups, c->d_group_dt, c->d_hist, c->d_counter,
-                                                 c->hist_cap);
+                                                 c->hist_cap, c->ts_local ? 0 : 1, c->d_group_active,
+                                                 c->d_group_time);
       cudaError_t le = cudaGetLastError();
       cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
       if (erc != PCG_OK) return erc;
@@ -1659,9 +1672,9 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   } else {
     PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < steps; s++) {
-      if ((rc = enqueue_step(c, PCG_MODE_PLAIN)) != PCG_OK) return rc;
+      if ((rc = enqueue_step(c, PCG_MODE_PLAIN, false)) != PCG_OK) return rc;
       k_record_hist<<<1, threads, 0, c->stream>>>(c->max_groups, c->d_group_dt, c->d_hist, c->d_counter,
-                                                 c->hist_cap);
+                                                 c->hist_cap, 1, c->d_group_active, c->d_group_time);
       PCG_CUDA(cudaGetLastError());
     }
     PCG_CUDA(cudaEventRecord(c->ev1, c->stream));

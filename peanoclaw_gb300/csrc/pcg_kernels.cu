@@ -615,11 +615,48 @@ __global__ void k_build_copy_plan(const PatchDev *__restrict__ patches,
 
 // Start of a batched fill: the time factor of every item (it is the same for
 // all cells of the item) and its unknown strides.
+__device__ __forceinline__ void item_step_one(const PatchDev *__restrict__ patches,
+                                              const PatchTimeDev *__restrict__ times,
+                                              const GhostItemDev *__restrict__ items, int i,
+                                              GhostItemStepDev *__restrict__ out);
+
 __global__ void k_item_step(const PatchDev *__restrict__ patches,
                             const PatchTimeDev *__restrict__ times,
                             const GhostItemDev *__restrict__ items, int count,
                             GhostItemStepDev *__restrict__ out) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    item_step_one(patches, times, items, i, out);
+}
+
+// Step start of the batched form in one launch: k_reset_step's per-group dt
+// caps and activity and the per-item time factors of k_item_step (neither
+// reads what the other writes).
+__global__ void k_reset_items(int n_groups, const double *__restrict__ group_max_dt,
+                              const double *__restrict__ group_t_end, const double *__restrict__ group_time,
+                              unsigned long long *__restrict__ group_dt, int *__restrict__ group_active,
+                              int n_patches, unsigned long long *__restrict__ patch_smax,
+                              const PatchDev *__restrict__ patches, const PatchTimeDev *__restrict__ times,
+                              const GhostItemDev *__restrict__ items, int count,
+                              GhostItemStepDev *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  if (i < n_groups) {
+    const double rem = __dsub_rn(group_t_end[i], group_time[i]);
+    const bool active = gt_nonneg(rem, 0.0);
+    const double cap = active ? rem : 0.0;
+    const double mx = group_max_dt[i];
+    group_dt[i] = dbits(lt_ieee(cap, mx) ? cap : mx);
+    group_active[i] = active ? 1 : 0;
+  }
+  for (int k = i; k < n_patches; k += stride) patch_smax[k] = 0ull;
+  for (int k = i; k < count; k += stride) item_step_one(patches, times, items, k, out);
+}
+
+__device__ __forceinline__ void item_step_one(const PatchDev *__restrict__ patches,
+                                              const PatchTimeDev *__restrict__ times,
+                                              const GhostItemDev *__restrict__ items, int i,
+                                              GhostItemStepDev *__restrict__ out) {
+  {
     const GhostItemDev it = items[i];
     const PatchDev &S = patches[it.src], &D = patches[it.dst];
     const PatchTimeDev &ST = times[it.src], &DT = times[it.dst];
@@ -1733,6 +1770,21 @@ cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, con
   int grid = (count + 255) / 256;
   if (grid > 152 * 32) grid = 152 * 32;
   k_build_copy_plan<<<grid, 256, 0, st>>>(patches, items, cells, count, plan);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reset_items(cudaStream_t st, int n_groups, const double *group_max_dt, const double *group_t_end,
+                               const double *group_time, unsigned long long *group_dt, int *group_active,
+                               int n_patches, unsigned long long *patch_smax, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev *items, int count,
+                               GhostItemStepDev *out) {
+  int n = n_groups > n_patches ? n_groups : n_patches;
+  if (count > n) n = count;
+  int grid = (n + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  if (grid < 1) grid = 1;
+  k_reset_items<<<grid, 256, 0, st>>>(n_groups, group_max_dt, group_t_end, group_time, group_dt, group_active,
+                                      n_patches, patch_smax, patches, times, items, count, out);
   return cudaGetLastError();
 }
 

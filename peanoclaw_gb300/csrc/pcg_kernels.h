@@ -66,6 +66,11 @@ cudaError_t launch_scan_fin(cudaStream_t st, const double *slab, const PatchDev 
                             int *fin);
 cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
                                    const GhostCellDev *cells, int count, CopyPlanDev *plan);
+cudaError_t launch_reset_items(cudaStream_t st, int n_groups, const double *group_max_dt, const double *group_t_end,
+                               const double *group_time, unsigned long long *group_dt, int *group_active,
+                               int n_patches, unsigned long long *patch_smax, const PatchDev *patches,
+                               const PatchTimeDev *times, const GhostItemDev *items, int count,
+                               GhostItemStepDev *out);
 cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
                              const GhostItemDev *items, int count, GhostItemStepDev *out);
 cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
