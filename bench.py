@@ -191,36 +191,48 @@ def build_context(ps, prm):
     return ctx, ids
 
 
-def cpu_baseline(args, prm, seconds_target=15.0):
+def cpu_baseline(args, prm, seconds_target=15.0, fp32_seconds=6.0):
     """The oracle (CPU restatement, OpenMP over patches, all host threads) on a
-    bounded sample of the same generator: a G x G slot mosaic."""
+    bounded sample of the same generator: a G x G slot mosaic.  Timed twice:
+    the FP64 restatement (the arithmetic of the GPU path) and its FP32 twin
+    (the reference's float storage and arithmetic), each with all threads and
+    with one."""
     from oracle import oracle as O
     from peanoclaw_gb300 import scenarios as S
     ps = S.uneven_patches(grid=args.cpu_sample_grid)
-    pats = []
-    for p in range(len(ps)):
-        op = O.Patch(ps.n[p], pos=ps.pos[p], size=ps.size[p])
-        op.u[:] = ps.vector(p)
-        pats.append(op)
+
+    def patches():
+        out = []
+        for p in range(len(ps)):
+            op = O.Patch(ps.n[p], pos=ps.pos[p], size=ps.size[p])
+            op.u[:] = ps.vector(p)
+            out.append(op)
+        return out
+
     oprm = O.swe_params(prm.g, prm.cfl, prm.dry_tol, prm.dry_tol_update, prm.s_min, prm.dt_inf)
     threads = os.cpu_count() or 1
-    O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=threads)  # warm-up
-    steps = 0
-    t0 = time.perf_counter()
-    while True:
-        O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=threads)
-        steps += 1
-        el = time.perf_counter() - t0
-        if el > seconds_target or steps >= 200:
-            break
     cells = ps.cells()
-    # one core on the same sample, a few steps
-    s1 = 0
-    t1 = time.perf_counter()
-    while s1 < 3 and time.perf_counter() - t1 < max(2.0, seconds_target / 5):
-        O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=1)
-        s1 += 1
-    el1 = time.perf_counter() - t1
+
+    def timed(step, target, n_threads, max_steps):
+        step(n_threads)  # warm-up
+        steps = 0
+        t0 = time.perf_counter()
+        while True:
+            step(n_threads)
+            steps += 1
+            el = time.perf_counter() - t0
+            if el > target or steps >= max_steps:
+                return steps, el
+
+    pats = patches()
+    f64 = lambda n: O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=n)
+    steps, el = timed(f64, seconds_target, threads, 200)
+    s1, el1 = timed(f64, max(2.0, seconds_target / 5), 1, 3)
+    pats32 = patches()
+    u32 = [np.ascontiguousarray(p.u.astype(np.float32)) for p in pats32]
+    f32 = lambda n: O.grid_step_f32(pats32, u32, ps.items, ps.wall, oprm, 1e9, n_threads=n)
+    steps32, el32 = timed(f32, fp32_seconds, threads, 400)
+    s132, el132 = timed(f32, max(1.0, fp32_seconds / 4), 1, 3)
     cpu_model = ""
     try:
         for line in open("/proc/cpuinfo"):
@@ -230,9 +242,13 @@ def cpu_baseline(args, prm, seconds_target=15.0):
     except OSError:
         pass
     return {"value": cells * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "single_core_value": cells * s1 / el1, "cpu": cpu_model,
-            "sample": "%dx%d-slot mosaic of the same generator (%d patches, %d cells), %d steps, %.1f s"
-                      % (args.cpu_sample_grid, args.cpu_sample_grid, len(ps), cells, steps, el)}
+            "dtype": "f64", "single_core_value": cells * s1 / el1,
+            "fp32_value": cells * steps32 / el32, "fp32_single_core_value": cells * s132 / el132,
+            "cpu": cpu_model,
+            "sample": "%dx%d-slot mosaic of the same generator (%d patches, %d cells), "
+                      "FP64 %d steps in %.1f s, FP32 twin %d steps in %.1f s"
+                      % (args.cpu_sample_grid, args.cpu_sample_grid, len(ps), cells, steps, el,
+                         steps32, el32)}
 
 
 def bench_radial(prm):
@@ -396,10 +412,18 @@ def run_reference(args):
         return 0
     from peanoclaw_gb300 import pcg as P
     prm = P.swe_params(g=9.81, cfl=0.5)
-    cb = cpu_baseline(args, prm, seconds_target=max(5.0, min(60.0, 2.0 * args.steps)))
+    t = max(5.0, min(60.0, 2.0 * args.steps))
+    cb = cpu_baseline(args, prm, seconds_target=t / 2, fp32_seconds=t)
+    # the reference stores and computes the SWE block in float: its arm is
+    # the FP32 twin; the FP64 restatement's figure rides along
+    ref = dict(cb, value=cb["fp32_value"], single_core_value=cb["fp32_single_core_value"],
+               dtype="f32", fp64_value=cb["value"], fp64_single_core_value=cb["single_core_value"])
+    for k in ("fp32_value", "fp32_single_core_value"):
+        ref.pop(k)
+    cb = ref
     line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "uneven patches, sample of the 224x224-slot mosaic",
                        "sample_grid": args.cpu_sample_grid},

@@ -86,6 +86,9 @@ def lib():
         L.pco_grid_step.argtypes = [C.POINTER(P), C.c_int, C.POINTER(PcoGhostItem), C.c_int,
                                     C.POINTER(C.c_uint8), C.POINTER(C.c_int32), C.c_int,
                                     C.POINTER(PcoSweParams), D, D, C.c_int]
+        L.pco32_grid_step.argtypes = [C.POINTER(P), C.POINTER(C.POINTER(C.c_float)), C.c_int,
+                                      C.POINTER(PcoGhostItem), C.c_int, C.POINTER(C.c_uint8),
+                                      C.POINTER(PcoSweParams), C.c_double, D, C.c_int]
         L.pco_grid_step_lts.restype = C.c_int
         L.pco_grid_step_lts.argtypes = [C.POINTER(P), C.c_int, C.POINTER(PcoGhostItem), C.c_int,
                                         C.POINTER(C.c_uint8), C.POINTER(PcoSweParams), C.c_double,
@@ -273,3 +276,23 @@ def grid_step_lts(patches, items, wall_mask, prm, max_dt, t_end, virtual_time_it
                                 dto.ctypes.data_as(C.POINTER(C.c_double)), n_threads)
     return n, dto
 
+
+
+def grid_step_f32(patches, u32, items, wall_mask, prm, max_dt, n_threads=0):
+    """FP32 twin of grid_step for one group (a timing baseline at the
+    reference's float precision): u32[p] is patch p's data vector as float32
+    in the layout of patches[p]; the patches' time intervals advance.
+    Returns the dt taken."""
+    P = C.POINTER(PcoPatch)
+    F = C.POINTER(C.c_float)
+    parr = (P * len(patches))(*[C.pointer(p.s) for p in patches])
+    for a, p in zip(u32, patches):
+        assert a.dtype == np.float32 and a.flags.c_contiguous and a.size == p.u.size
+    uarr = (F * len(u32))(*[a.ctypes.data_as(F) for a in u32])
+    it, keep = ghost_items(items)
+    wm = np.ascontiguousarray(wall_mask, dtype=np.uint8)
+    dto = C.c_double(0.0)
+    lib().pco32_grid_step(parr, uarr, len(patches), it, len(keep) if len(items) else 0,
+                          wm.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(prm), float(max_dt),
+                          C.byref(dto), n_threads)
+    return dto.value

@@ -151,6 +151,14 @@ void pco_grid_fill(pco_patch **patches, int n_patches,
                    const pco_ghost_item *items, int n_items,
                    const uint8_t *wall_mask);
 
+/* ---- FP32 twin (pcoracle_f32.c): timing baseline at the reference's storage
+ * precision, not a parity reference.  pco_grid_step for one group with float
+ * patch vectors u[p] in the layout of patches[p] (whose own u is not used);
+ * the time intervals in patches[p] are advanced; *dt_out = the dt taken. */
+void pco32_grid_step(pco_patch **patches, float **u, int n_patches,
+                     const pco_ghost_item *items, int n_items, const uint8_t *wall_mask,
+                     const pco_swe_params *prm, double max_dt, double *dt_out, int n_threads);
+
 #ifdef __cplusplus
 }
 #endif
