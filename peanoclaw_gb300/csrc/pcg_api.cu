@@ -234,6 +234,10 @@ struct pcg_context {
   int *d_restr_begin = nullptr, *d_flux_begin = nullptr, *d_restr_dsts = nullptr, *d_leaf_ids = nullptr;
   int *d_restr_dirty = nullptr;
   size_t d_rdirty_cap = 0;
+  pcg::RestrItemTab *d_restr_tab = nullptr;  // per restriction item, rewritten every step
+  size_t d_rtab_cap = 0;
+  int *d_restr_bad = nullptr;                // per destination: item-by-item form
+  size_t d_rbad_cap = 0;
   size_t d_restr_cap = 0, d_flux_cap = 0, d_rb_cap = 0, d_fb_cap = 0, d_rd_cap = 0, d_leaf_cap = 0;
   double g_flux = 1.0;
 
@@ -529,6 +533,8 @@ int rebuild_topology(pcg_context *c) {
   if ((rc = ensure_device(c, &c->d_flux_begin, &c->d_fb_cap, c->flux_begin.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_restr_dsts, &c->d_rd_cap, c->restr_dsts.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_restr_dirty, &c->d_rdirty_cap, c->restr_dsts.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_restr_tab, &c->d_rtab_cap, c->h_restr.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_restr_bad, &c->d_rbad_cap, c->restr_dsts.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_leaf_ids, &c->d_leaf_cap, c->leaf_ids.size())) != PCG_OK) return rc;
   auto up = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) : cudaSuccess;
@@ -610,9 +616,11 @@ int enqueue_post_update(pcg_context *c) {
       PCG_CUDA(launch_restr_dirty(c->stream, c->d_restr, c->d_restr_begin, nd, c->d_pact, c->d_restr_dirty));
       dirty = c->d_restr_dirty;
     }
-    PCG_CUDA(launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga, dirty));
+    PCG_CUDA(launch_restr_prepare(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr, c->d_restr_begin,
+                                  c->d_restr_dsts, nd, c->d_restr_tab, c->d_restr_bad, ga, dirty));
     PCG_CUDA(launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
-                                   c->d_restr_begin, nd, ga, dirty));
+                                   c->d_restr_begin, nd, restr_split(nd, c->num_sms), c->d_restr_tab,
+                                   c->d_restr_bad, ga, dirty));
     PCG_CUDA(launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga,
                                              dirty));
   }
@@ -901,6 +909,8 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_flux_begin);
   cudaFree(c->d_restr_dsts);
   cudaFree(c->d_restr_dirty);
+  cudaFree(c->d_restr_tab);
+  cudaFree(c->d_restr_bad);
   cudaFree(c->d_leaf_ids);
   cudaFree(c->d_plan);
   cudaFree(c->d_copy_plan);
@@ -1508,9 +1518,12 @@ int pcg_restrict_all(pcg_context *c) {
   if (rc != PCG_OK) return rc;
   if (!c->h_restr.empty()) {
     int nd = (int)c->restr_dsts.size();
-    PCG_CUDA(pcg::launch_clear_interior(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
+    PCG_CUDA(pcg::launch_restr_prepare(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
+                                       c->d_restr_begin, c->d_restr_dsts, nd, c->d_restr_tab,
+                                       c->d_restr_bad));
     PCG_CUDA(pcg::launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
-                                        c->d_restr_begin, nd));
+                                        c->d_restr_begin, nd, pcg::restr_split(nd, c->num_sms),
+                                        c->d_restr_tab, c->d_restr_bad));
     PCG_CUDA(pcg::launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
   }
   PCG_CUDA(cudaStreamSynchronize(c->stream));

@@ -13,6 +13,9 @@
 #include "pcg_device.cuh"
 #include "pcg_kernels.h"
 
+#include <algorithm>
+#include <cstdint>
+
 namespace pcg {
 
 // ===========================================================================
@@ -1050,8 +1053,7 @@ __global__ void k_restrict(double *slab, const PatchDev *patches, const PatchTim
 // One warp per destination cell of a region: the lanes evaluate the
 // contributions of up to 32 source cells at a time, lane 0 adds them to the
 // cell's uOld / uNew values in source-cell order.
-constexpr int kRestrWarps = 8;   // warps per CTA of the batched restriction
-constexpr int kRestrSplit = 1;   // CTAs per destination (interleaved cells)
+constexpr int kRestrWarps = 6;   // warps per CTA of the batched restriction (32 cells x 6 sums)
 __device__ void restrict_items_in_order(double *slab, const PatchDev *patches, const PatchTimeDev *times,
                                         const int4 *items, int b0, int b1, double (*W)[32][6]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1176,57 +1178,67 @@ __device__ void restrict_items_in_order(double *slab, const PatchDev *patches, c
 }
 
 
-// Batched restriction: block b handles the items [begin[b], begin[b+1]) that
-// share one destination.  A table of the items' regions (item order, then
-// region order) and time factors is built once per block; then each
-// destination cell walks the table in order and adds the terms of every
-// source cell of every matching region, one thread per destination cell.
-// Each cell's sum is therefore formed in exactly the order of the
-// item-by-item restriction, and the cells of one destination need no
-// barrier between items (kRestrSplit CTAs may share the cells of one
-// destination, interleaved; more than one measured slower on the adaptive
-// tsunami, where every CTA rebuilds the table).  Destinations with more than
-// kRestrMaxItems items, more than 3 unknowns or a region leaving the
-// destination take restrict_items_in_order in their first CTA.
-constexpr int kRestrMaxItems = 128;
-struct RestrItemTab {
-  double tfo, tfn;
-  int src, nr, swe, pad_;
-  int doff[4][2], dsz[4][2], ro[4][2], rs[4][2];
-};
-__global__ void __launch_bounds__(kRestrWarps * 32)
-    k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                     const int4 *items, const int *begin, const int *group_active, const int *dirty) {
-  __shared__ double W[kRestrWarps][32][6];
-  __shared__ RestrItemTab T[kRestrMaxItems];
+// Batched restriction, in two kernels per step.
+//
+// k_restr_prepare (one CTA per destination): clears the destination's
+// interior (uOld and uNew, as k_clear_interior) and writes the table of its
+// items [begin[b], begin[b+1]): per item the source, the time factors of its
+// uOld / uNew values at the virtual times 0 and 1, and its regions (item
+// order, then region order) mapped into the destination.  bad[b] is set when
+// the destination needs the item-by-item form instead (more than
+// kRestrMaxItems items, more than 3 unknowns, or a region leaving the
+// destination).
+//
+// k_restrict_items (`split` CTAs per destination): each CTA copies the table
+// into shared memory; then one thread per (destination cell, unknown, time
+// level) walks the table in order and adds the terms of every source cell of
+// every matching region.  Each of a cell's six sums is therefore formed in
+// exactly the order of the item-by-item restriction (the six are independent
+// of each other), and the cells of one destination need no barrier between
+// items.  Only the cells of the regions' destination rectangles are visited
+// (with overlapped-only restriction these are the few cells under the
+// neighbours' ghost layers), rectangle by rectangle, each cell from the first
+// rectangle that holds it; a rectangle's tasks are dealt to the
+// destination's CTAs in blocks of one CTA's threads (dealing them
+// round-robin over the CTAs measured 2x slower on the adaptive breaking
+// dam, whose rims are 54 tasks per rectangle).  Destinations flagged bad take
+// restrict_items_in_order in their first CTA.
+constexpr int kRestrPerCell = 6;                       // 3 unknowns x (uOld, uNew)
+constexpr int kRestrSlots = kRestrWarps * 32 / kRestrPerCell;
+
+__global__ void __launch_bounds__(256)
+    k_restr_prepare(double *slab, const PatchDev *patches, const PatchTimeDev *times, const int4 *items,
+                    const int *begin, const int *ids, int count, RestrItemTab *tab, int *bad,
+                    const int *group_active, const int *dirty) {
   __shared__ int s_bad;
-  const int dst_block = blockIdx.x / kRestrSplit, part = blockIdx.x % kRestrSplit;
-  if (dirty && !dirty[dst_block]) return;
-  const int b0 = begin[dst_block], b1 = begin[dst_block + 1];
-  const PatchDev D = patches[items[b0].y];
+  if ((int)blockIdx.x >= count) return;
+  if (dirty && !dirty[blockIdx.x]) return;
+  const PatchDev D = patches[ids[blockIdx.x]];
   if (group_active && !group_active[D.group]) return;
-  const int ni = b1 - b0;
-  if (ni > kRestrMaxItems || D.nq > 3) {
-    if (part == 0) restrict_items_in_order(slab, patches, times, items, b0, b1, W);
-    return;
+  const int n = D.nx * D.ny;
+  for (int k = threadIdx.x; k < D.nq * n; k += blockDim.x) {
+    int q = k / n, c = k - q * n, x = c / D.ny, y = c - x * D.ny;
+    slab[idx_unew(D, q, x, y)] = 0.0;
+    slab[idx_uold(D, q, x, y)] = 0.0;
   }
-  if (threadIdx.x == 0) s_bad = 0;
+  const int b0 = begin[blockIdx.x], ni = begin[blockIdx.x + 1] - b0;
+  if (threadIdx.x == 0) s_bad = (ni > kRestrMaxItems || D.nq > 3) ? 1 : 0;
   __syncthreads();
   const double eps = 1e-12;
-  for (int t = threadIdx.x; t < ni; t += blockDim.x) {
+  for (int t = threadIdx.x; t < ni && !s_bad; t += blockDim.x) {
     const int4 it = items[b0 + t];
     const PatchDev S = patches[it.x];
     const PatchTimeDev ST = times[it.x], DT = times[it.y];
-    RestrItemTab &E = T[t];
+    RestrItemTab E;
     int roff[8], rsz[8], nr;
-    int n[2] = {S.nx, S.ny};
+    int nn[2] = {S.nx, S.ny};
     if (it.z != 0) {
       double sp[2] = {S.pos[0], S.pos[1]}, ss[2] = {S.size[0], S.size[1]};
       double sub[2] = {subcell(S, 0), subcell(S, 1)};
-      nr = regions_overlapped(DT.rl, DT.ru, sp, ss, sub, n, roff, rsz);
+      nr = regions_overlapped(DT.rl, DT.ru, sp, ss, sub, nn, roff, rsz);
     } else {
       nr = 1;
-      roff[0] = 0; roff[1] = 0; rsz[0] = n[0]; rsz[1] = n[1];
+      roff[0] = 0; roff[1] = 0; rsz[0] = nn[0]; rsz[1] = nn[1];
     }
     double tfo = 1.0, tfn = 1.0;
     if (tl_greater(ST.dt, 0.0)) {
@@ -1234,7 +1246,7 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
       tfo = __ddiv_rn(__dsub_rn(0.0, so), __dsub_rn(su, so));
       tfn = __ddiv_rn(__dsub_rn(1.0, so), __dsub_rn(su, so));
     }
-    E.tfo = tfo; E.tfn = tfn; E.src = it.x; E.nr = nr; E.swe = it.w;
+    E.tfo = tfo; E.tfn = tfn; E.src = it.x; E.nr = nr; E.swe = it.w; E.pad_ = 0;
     for (int r = 0; r < 4; r++) {
       int doff[2] = {0, 0}, dsz[2] = {0, 0};
       if (r < nr && !(it.z != 0 && !(rsz[2 * r] > 0 && rsz[2 * r + 1] > 0))) {
@@ -1250,92 +1262,119 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
         E.rs[r][d] = r < nr ? rsz[2 * r + d] : 0;
       }
     }
+    tab[b0 + t] = E;
   }
   __syncthreads();
-  if (s_bad) {
+  if (threadIdx.x == 0) bad[blockIdx.x] = s_bad;
+}
+
+__global__ void __launch_bounds__(kRestrWarps * 32)
+    k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                     const int4 *items, const int *begin, int split, const RestrItemTab *tab,
+                     const int *bad, const int *group_active, const int *dirty) {
+  __shared__ double W[kRestrWarps][32][6];
+  __shared__ RestrItemTab T[kRestrMaxItems];
+  const int dst_block = blockIdx.x / split, part = blockIdx.x % split;
+  if (dirty && !dirty[dst_block]) return;
+  const int b0 = begin[dst_block], b1 = begin[dst_block + 1];
+  const PatchDev D = patches[items[b0].y];
+  if (group_active && !group_active[D.group]) return;
+  if (bad[dst_block]) {
     if (part == 0) restrict_items_in_order(slab, patches, times, items, b0, b1, W);
     return;
   }
+  const int ni = b1 - b0;
+  for (int t = threadIdx.x; t < ni; t += blockDim.x) T[t] = tab[b0 + t];
+  __syncthreads();
+  const double eps = 1e-12;
   const double dsub[2] = {iter_sub(D, 0), iter_sub(D, 1)};
   const double dvol = __dmul_rn(dsub[0], dsub[1]);
-  const int ncell = D.nx * D.ny;
-  for (int c = part + kRestrSplit * (int)threadIdx.x; c < ncell; c += kRestrSplit * (int)blockDim.x) {
-    const int x = c / D.ny, y = c % D.ny;
-    double dpos[2] = {0.0, 0.0};
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    bool any = false;
-    for (int t = 0; t < ni; t++) {
-      const int nr = T[t].nr < 4 ? T[t].nr : 4;
-      for (int r = 0; r < nr; r++) {
-        if (!(x >= T[t].doff[r][0] && x < T[t].doff[r][0] + T[t].dsz[r][0] && y >= T[t].doff[r][1] &&
-              y < T[t].doff[r][1] + T[t].dsz[r][1]))
-          continue;
-        if (!any) {
-          dpos[0] = iter_pos(D, 0, x);
-          dpos[1] = iter_pos(D, 1, y);
-        }
-        const PatchDev S = patches[T[t].src];
-        const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
-        int coff[2], csz[2];
-        for (int d = 0; d < 2; d++) {
-          double ot = ieee::div_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
-          int o = (int)ot;
-          double st = ieee::div_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
-          st = __dsub_rn(st, ot);
-          st = __dadd_rn(st, 1.0);
-          int up = o + (int)st;
-          int rup = T[t].ro[r][d] + T[t].rs[r][d];
-          int oo = o > T[t].ro[r][d] ? o : T[t].ro[r][d];
-          int uu = up < rup ? up : rup;
-          coff[d] = oo;
-          csz[d] = uu - oo;
-        }
-        if (!(csz[0] > 0 && csz[1] > 0)) continue;
-        if (!any) {
-          any = true;
-#pragma unroll
-          for (int q = 0; q < 3; q++)
-            if (q < D.nq) {
-              acc[q] = slab[idx_uold(D, q, x, y)];
-              acc[3 + q] = slab[idx_unew(D, q, x, y)];
-            }
-        }
-        const double tfo = T[t].tfo, tfn = T[t].tfn;
-        const double itfo = __dsub_rn(1.0, tfo), itfn = __dsub_rn(1.0, tfn);
-        const bool swe = T[t].swe != 0;
-        for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++)
-          for (int sy = coff[1]; sy < coff[1] + csz[1]; sy++) {
-            const double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
-            double region = 1.0;
-            for (int d = 0; d < 2; d++) {
-              double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
-              double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
-              region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
-              region = fmax(region, 0.0);
-            }
-#pragma unroll
-            for (int q = 0; q < 3; q++) {
-              if (q >= D.nq) break;
+  // the cells of the regions' destination rectangles, rectangle by
+  // rectangle in table order; a cell inside an earlier rectangle as well is
+  // left to that one
+  const int stride = split * (int)blockDim.x;
+  for (int e = 0; e < 4 * ni; e++) {
+    const int te = e >> 2, re = e & 3;
+    if (re >= (T[te].nr < 4 ? T[te].nr : 4)) continue;
+    const int w1 = T[te].dsz[re][1];
+    const int ntask = T[te].dsz[re][0] * w1 * kRestrPerCell;
+    for (int k = part * (int)blockDim.x + (int)threadIdx.x; k < ntask; k += stride) {
+      const int cell = k / kRestrPerCell, comp = k - cell * kRestrPerCell;
+      const int q = comp % 3, level = comp / 3;  // level 0: uOld (time 0), 1: uNew (time 1)
+      if (q >= D.nq) continue;
+      const int x = T[te].doff[re][0] + cell / w1, y = T[te].doff[re][1] + cell % w1;
+      bool earlier = false;
+      for (int f = 0; f < e && !earlier; f++) {
+        const int tq = f >> 2, rq = f & 3;
+        if (rq >= (T[tq].nr < 4 ? T[tq].nr : 4)) continue;
+        earlier = x >= T[tq].doff[rq][0] && x < T[tq].doff[rq][0] + T[tq].dsz[rq][0] &&
+                  y >= T[tq].doff[rq][1] && y < T[tq].doff[rq][1] + T[tq].dsz[rq][1];
+      }
+      if (earlier) continue;
+      // the cell's sum over every matching region of every item, in order
+      double dpos[2] = {0.0, 0.0};
+      double acc = 0.0;
+      bool any = false;
+      for (int t = 0; t < ni; t++) {
+        const int nr = T[t].nr < 4 ? T[t].nr : 4;
+        for (int r = 0; r < nr; r++) {
+          if (!(x >= T[t].doff[r][0] && x < T[t].doff[r][0] + T[t].dsz[r][0] && y >= T[t].doff[r][1] &&
+                y < T[t].doff[r][1] + T[t].dsz[r][1]))
+            continue;
+          if (!any) {
+            dpos[0] = iter_pos(D, 0, x);
+            dpos[1] = iter_pos(D, 1, y);
+          }
+          const PatchDev S = patches[T[t].src];
+          const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
+          int coff[2], csz[2];
+          for (int d = 0; d < 2; d++) {
+            double ot = ieee::div_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
+            int o = (int)ot;
+            double st = ieee::div_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
+            st = __dsub_rn(st, ot);
+            st = __dadd_rn(st, 1.0);
+            int up = o + (int)st;
+            int rup = T[t].ro[r][d] + T[t].rs[r][d];
+            int oo = o > T[t].ro[r][d] ? o : T[t].ro[r][d];
+            int uu = up < rup ? up : rup;
+            coff[d] = oo;
+            csz[d] = uu - oo;
+          }
+          if (!(csz[0] > 0 && csz[1] > 0)) continue;
+          if (!any) {
+            any = true;
+            acc = level ? slab[idx_unew(D, q, x, y)] : slab[idx_uold(D, q, x, y)];
+          }
+          const double tf = level ? T[t].tfn : T[t].tfo;
+          const double itf = __dsub_rn(1.0, tf);
+          const bool addb = T[t].swe != 0 && q == 0;
+          for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++)
+            for (int sy = coff[1]; sy < coff[1] + csz[1]; sy++) {
+              const double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
+              double region = 1.0;
+              for (int d = 0; d < 2; d++) {
+                double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
+                double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
+                region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
+                region = fmax(region, 0.0);
+              }
               double vo = slab[idx_uold(S, q, sx, sy)];
               double vn = slab[idx_unew(S, q, sx, sy)];
-              if (swe && q == 0) {
+              if (addb) {
                 double bb = slab[idx_pw(S, 0, sx, sy)];
                 vo = __dadd_rn(vo, bb);
                 vn = __dadd_rn(vn, bb);
               }
-              acc[q] = __dadd_rn(acc[q], ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfo), __dmul_rn(vn, tfo)), region), dvol));
-              acc[3 + q] = __dadd_rn(acc[3 + q], ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfn), __dmul_rn(vn, tfn)), region), dvol));
+              acc = __dadd_rn(acc, ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itf), __dmul_rn(vn, tf)), region),
+                                                dvol));
             }
-          }
-      }
-    }
-    if (any) {
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-        if (q < D.nq) {
-          slab[idx_uold(D, q, x, y)] = acc[q];
-          slab[idx_unew(D, q, x, y)] = acc[3 + q];
         }
+      }
+      if (any) {
+        if (level) slab[idx_unew(D, q, x, y)] = acc;
+        else slab[idx_uold(D, q, x, y)] = acc;
+      }
     }
   }
 }
@@ -1453,11 +1492,12 @@ __global__ void k_flux_correction(double *slab, const PatchDev *patches, const P
 
 // Batched flux correction: block b applies the items [begin[b], begin[b+1])
 // (all with the same destination) in list order.  Within an item one thread
-// owns each destination face cell and adds the corrections of the source
-// face cells that overlap it in source order (the order of
-// flux_correction_one); the source cells' destination ranges are computed
-// once per item into shared memory.
-constexpr int kFluxThreads = 32;
+// owns each (destination face cell, unknown) and adds the corrections of the
+// source face cells that overlap it in source order (the order of
+// flux_correction_one; the three unknowns are separate sums); the source
+// cells' destination ranges are computed once per item into shared memory.
+constexpr int kFluxLanes = 32;                 // face cells per round
+constexpr int kFluxThreads = 3 * kFluxLanes;   // x 3 unknowns
 constexpr int kFluxMaxCells = 1024;
 __global__ void __launch_bounds__(kFluxThreads)
     k_flux_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
@@ -1500,11 +1540,11 @@ __global__ void __launch_bounds__(kFluxThreads)
     }
     __syncthreads();
     const int dinner = (-dir == -1) ? 0 : dnd - 1;
-    for (int cd = threadIdx.x; cd < dno; cd += kFluxThreads) {
+    const int q = (int)threadIdx.x / kFluxLanes;
+    for (int cd = (int)threadIdx.x - q * kFluxLanes; cd < dno; cd += kFluxLanes) {
       const int ux = dim == 0 ? dinner : cd, uy = dim == 0 ? cd : dinner;
       if (ux < 0 || uy < 0 || ux >= D.nx || uy >= D.ny) continue;
-      double dF[3];
-      for (int q = 0; q < 3; q++) dF[q] = slab[idx_flux(D, q, cd, dim, -dir)];
+      const double dF = slab[idx_flux(D, q, cd, dim, -dir)];
       const double a2 = __dadd_rn(dpo, __dmul_rn(__dadd_rn((double)cd, 1.0), dso));
       const double b2 = __dadd_rn(dpo, __dmul_rn((double)cd, dso));
       for (int cs = 0; cs < sno; cs++) {
@@ -1513,12 +1553,10 @@ __global__ void __launch_bounds__(kFluxThreads)
         double b1 = __dadd_rn(spo, __dmul_rn((double)cs, sso));
         double area = __dmul_rn(1.0, __dsub_rn(a1 < a2 ? a1 : a2, b1 > b2 ? b1 : b2));
         if (area < 0.0) area = 0.0;
-        for (int q = 0; q < 3; q++) {
-          double sF = slab[idx_flux(S, q, cs, dim, dir)];
-          double corr = ieee::div_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF, dF[q]), tov), area), dvol);
-          long long id = idx_unew(D, q, ux, uy);
-          slab[id] = __dadd_rn(slab[id], corr);
-        }
+        double sF = slab[idx_flux(S, q, cs, dim, dir)];
+        double corr = ieee::div_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF, dF), tov), area), dvol);
+        long long id = idx_unew(D, q, ux, uy);
+        slab[id] = __dadd_rn(slab[id], corr);
       }
     }
     __syncthreads();
@@ -1919,12 +1957,32 @@ cudaError_t launch_restr_dirty(cudaStream_t st, const int4 *items, const int *be
   return cudaGetLastError();
 }
 
+// CTAs per destination of the batched restriction: about four CTAs per SM
+// over all destinations, at most 16.
+int restr_split(int n_dst, int num_sms) {
+  if (n_dst <= 0) return 1;
+  const int target = 4 * (num_sms > 0 ? num_sms : 1);
+  return std::max(1, std::min(16, (target + n_dst - 1) / n_dst));
+}
+
+cudaError_t launch_restr_prepare(cudaStream_t st, double *slab, const PatchDev *patches,
+                                 const PatchTimeDev *times, const int4 *items, const int *begin,
+                                 const int *ids, int n_dst, RestrItemTab *tab, int *bad,
+                                 const int *group_active, const int *dirty) {
+  if (n_dst <= 0) return cudaSuccess;
+  k_restr_prepare<<<n_dst, 256, 0, st>>>(slab, patches, times, items, begin, ids, n_dst, tab, bad,
+                                         group_active, dirty);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst, const int *group_active, const int *dirty) {
+                                  int n_dst, int split, const RestrItemTab *tab, const int *bad,
+                                  const int *group_active, const int *dirty) {
   if (n_dst <= 0) return cudaSuccess;
-  k_restrict_items<<<n_dst * kRestrSplit, kRestrWarps * 32, 0, st>>>(slab, patches, times, items, begin,
-                                                                     group_active, dirty);
+  if (split < 1 || (int64_t)n_dst * split > 0x7fffffff) return cudaErrorInvalidValue;
+  k_restrict_items<<<n_dst * split, kRestrWarps * 32, 0, st>>>(slab, patches, times, items, begin, split, tab,
+                                                               bad, group_active, dirty);
   return cudaGetLastError();
 }
 

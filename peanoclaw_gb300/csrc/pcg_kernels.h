@@ -101,9 +101,25 @@ cudaError_t launch_interpolate(cudaStream_t st, double *slab, const PatchDev *pa
                                int to_current, int use_unew_uold, int swe);
 cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patches,
                             const PatchTimeDev *times, int src, int dst, int only_overlapped, int swe);
+// Per-item table of the batched restriction (regions mapped into the
+// destination, time factors), written by k_restr_prepare each step.
+constexpr int kRestrMaxItems = 128;
+struct RestrItemTab {
+  double tfo, tfn;
+  int src, nr, swe, pad_;
+  int doff[4][2], dsz[4][2], ro[4][2], rs[4][2];
+};
+int restr_split(int n_dst, int num_sms);
+// Clears the interior of every destination ids[b] and writes the tables of
+// its items into tab (indexed like items) and bad[b].
+cudaError_t launch_restr_prepare(cudaStream_t st, double *slab, const PatchDev *patches,
+                                 const PatchTimeDev *times, const int4 *items, const int *begin,
+                                 const int *ids, int n_dst, RestrItemTab *tab, int *bad,
+                                 const int *group_active = nullptr, const int *dirty = nullptr);
 cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst, const int *group_active = nullptr, const int *dirty = nullptr);
+                                  int n_dst, int split, const RestrItemTab *tab, const int *bad,
+                                  const int *group_active = nullptr, const int *dirty = nullptr);
 cudaError_t launch_restr_dirty(cudaStream_t st, const int4 *items, const int *begin, int n_dst, const int *pact,
                                int *dirty);
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
