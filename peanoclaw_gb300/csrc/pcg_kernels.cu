@@ -1198,10 +1198,12 @@ __device__ void restrict_items_in_order(double *slab, const PatchDev *patches, c
 // items.  Only the cells of the regions' destination rectangles are visited
 // (with overlapped-only restriction these are the few cells under the
 // neighbours' ghost layers), rectangle by rectangle, each cell from the first
-// rectangle that holds it; a rectangle's tasks are dealt to the
-// destination's CTAs in blocks of one CTA's threads (dealing them
-// round-robin over the CTAs measured 2x slower on the adaptive breaking
-// dam, whose rims are 54 tasks per rectangle).  Destinations flagged bad take
+// rectangle that holds it.  All rectangles of a destination form one task
+// space, dealt to its CTAs in blocks of one CTA's threads, so that a
+// destination with a few small rectangles (the rims of the adaptive
+// breaking dam: three of 54 tasks) runs them side by side in one CTA rather
+// than one after another; dealing tasks round-robin over the CTAs measured
+// 2x slower there.  Destinations flagged bad take
 // restrict_items_in_order in their first CTA.
 constexpr int kRestrPerCell = 6;                       // 3 unknowns x (uOld, uNew)
 constexpr int kRestrSlots = kRestrWarps * 32 / kRestrPerCell;
@@ -1274,6 +1276,7 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
                      const int *bad, const int *group_active, const int *dirty) {
   __shared__ double W[kRestrWarps][32][6];
   __shared__ RestrItemTab T[kRestrMaxItems];
+  __shared__ int P[4 * kRestrMaxItems + 1];
   const int dst_block = blockIdx.x / split, part = blockIdx.x % split;
   if (dirty && !dirty[dst_block]) return;
   const int b0 = begin[dst_block], b1 = begin[dst_block + 1];
@@ -1286,6 +1289,19 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
   const int ni = b1 - b0;
   for (int t = threadIdx.x; t < ni; t += blockDim.x) T[t] = tab[b0 + t];
   __syncthreads();
+  // task prefix over the rectangles (item order, region order): all of a
+  // destination's rectangles form one task space, dealt to its CTAs in
+  // blocks of one CTA's threads
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int e = 0; e < 4 * ni; e++) {
+      const int te = e >> 2, re = e & 3;
+      P[e] = acc;
+      if (re < (T[te].nr < 4 ? T[te].nr : 4)) acc += T[te].dsz[re][0] * T[te].dsz[re][1] * kRestrPerCell;
+    }
+    P[4 * ni] = acc;
+  }
+  __syncthreads();
   const double eps = 1e-12;
   const double dsub[2] = {iter_sub(D, 0), iter_sub(D, 1)};
   const double dvol = __dmul_rn(dsub[0], dsub[1]);
@@ -1293,88 +1309,95 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
   // rectangle in table order; a cell inside an earlier rectangle as well is
   // left to that one
   const int stride = split * (int)blockDim.x;
-  for (int e = 0; e < 4 * ni; e++) {
+  const int ntask = P[4 * ni];
+  for (int k = part * (int)blockDim.x + (int)threadIdx.x; k < ntask; k += stride) {
+    // rectangle e holding task k: the last e with P[e] <= k and a
+    // non-empty task range (binary search over the prefix)
+    int lo = 0, hi = 4 * ni - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (P[mid] <= k) lo = mid;
+      else hi = mid - 1;
+    }
+    const int e = lo;
     const int te = e >> 2, re = e & 3;
-    if (re >= (T[te].nr < 4 ? T[te].nr : 4)) continue;
     const int w1 = T[te].dsz[re][1];
-    const int ntask = T[te].dsz[re][0] * w1 * kRestrPerCell;
-    for (int k = part * (int)blockDim.x + (int)threadIdx.x; k < ntask; k += stride) {
-      const int cell = k / kRestrPerCell, comp = k - cell * kRestrPerCell;
-      const int q = comp % 3, level = comp / 3;  // level 0: uOld (time 0), 1: uNew (time 1)
-      if (q >= D.nq) continue;
-      const int x = T[te].doff[re][0] + cell / w1, y = T[te].doff[re][1] + cell % w1;
-      bool earlier = false;
-      for (int f = 0; f < e && !earlier; f++) {
-        const int tq = f >> 2, rq = f & 3;
-        if (rq >= (T[tq].nr < 4 ? T[tq].nr : 4)) continue;
-        earlier = x >= T[tq].doff[rq][0] && x < T[tq].doff[rq][0] + T[tq].dsz[rq][0] &&
-                  y >= T[tq].doff[rq][1] && y < T[tq].doff[rq][1] + T[tq].dsz[rq][1];
-      }
-      if (earlier) continue;
-      // the cell's sum over every matching region of every item, in order
-      double dpos[2] = {0.0, 0.0};
-      double acc = 0.0;
-      bool any = false;
-      for (int t = 0; t < ni; t++) {
-        const int nr = T[t].nr < 4 ? T[t].nr : 4;
-        for (int r = 0; r < nr; r++) {
-          if (!(x >= T[t].doff[r][0] && x < T[t].doff[r][0] + T[t].dsz[r][0] && y >= T[t].doff[r][1] &&
-                y < T[t].doff[r][1] + T[t].dsz[r][1]))
-            continue;
-          if (!any) {
-            dpos[0] = iter_pos(D, 0, x);
-            dpos[1] = iter_pos(D, 1, y);
-          }
-          const PatchDev S = patches[T[t].src];
-          const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
-          int coff[2], csz[2];
-          for (int d = 0; d < 2; d++) {
-            double ot = ieee::div_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
-            int o = (int)ot;
-            double st = ieee::div_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
-            st = __dsub_rn(st, ot);
-            st = __dadd_rn(st, 1.0);
-            int up = o + (int)st;
-            int rup = T[t].ro[r][d] + T[t].rs[r][d];
-            int oo = o > T[t].ro[r][d] ? o : T[t].ro[r][d];
-            int uu = up < rup ? up : rup;
-            coff[d] = oo;
-            csz[d] = uu - oo;
-          }
-          if (!(csz[0] > 0 && csz[1] > 0)) continue;
-          if (!any) {
-            any = true;
-            acc = level ? slab[idx_unew(D, q, x, y)] : slab[idx_uold(D, q, x, y)];
-          }
-          const double tf = level ? T[t].tfn : T[t].tfo;
-          const double itf = __dsub_rn(1.0, tf);
-          const bool addb = T[t].swe != 0 && q == 0;
-          for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++)
-            for (int sy = coff[1]; sy < coff[1] + csz[1]; sy++) {
-              const double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
-              double region = 1.0;
-              for (int d = 0; d < 2; d++) {
-                double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
-                double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
-                region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
-                region = fmax(region, 0.0);
-              }
-              double vo = slab[idx_uold(S, q, sx, sy)];
-              double vn = slab[idx_unew(S, q, sx, sy)];
-              if (addb) {
-                double bb = slab[idx_pw(S, 0, sx, sy)];
-                vo = __dadd_rn(vo, bb);
-                vn = __dadd_rn(vn, bb);
-              }
-              acc = __dadd_rn(acc, ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itf), __dmul_rn(vn, tf)), region),
-                                                dvol));
-            }
+    const int kk = k - P[e];
+    const int cell = kk / kRestrPerCell, comp = kk - cell * kRestrPerCell;
+    const int q = comp % 3, level = comp / 3;  // level 0: uOld (time 0), 1: uNew (time 1)
+    if (q >= D.nq) continue;
+    const int x = T[te].doff[re][0] + cell / w1, y = T[te].doff[re][1] + cell % w1;
+    bool earlier = false;
+    for (int f = 0; f < e && !earlier; f++) {
+      const int tq = f >> 2, rq = f & 3;
+      if (rq >= (T[tq].nr < 4 ? T[tq].nr : 4)) continue;
+      earlier = x >= T[tq].doff[rq][0] && x < T[tq].doff[rq][0] + T[tq].dsz[rq][0] &&
+                y >= T[tq].doff[rq][1] && y < T[tq].doff[rq][1] + T[tq].dsz[rq][1];
+    }
+    if (earlier) continue;
+    // the cell's sum over every matching region of every item, in order
+    double dpos[2] = {0.0, 0.0};
+    double acc = 0.0;
+    bool any = false;
+    for (int t = 0; t < ni; t++) {
+      const int nr = T[t].nr < 4 ? T[t].nr : 4;
+      for (int r = 0; r < nr; r++) {
+        if (!(x >= T[t].doff[r][0] && x < T[t].doff[r][0] + T[t].dsz[r][0] && y >= T[t].doff[r][1] &&
+              y < T[t].doff[r][1] + T[t].dsz[r][1]))
+          continue;
+        if (!any) {
+          dpos[0] = iter_pos(D, 0, x);
+          dpos[1] = iter_pos(D, 1, y);
         }
+        const PatchDev S = patches[T[t].src];
+        const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
+        int coff[2], csz[2];
+        for (int d = 0; d < 2; d++) {
+          double ot = ieee::div_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
+          int o = (int)ot;
+          double st = ieee::div_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
+          st = __dsub_rn(st, ot);
+          st = __dadd_rn(st, 1.0);
+          int up = o + (int)st;
+          int rup = T[t].ro[r][d] + T[t].rs[r][d];
+          int oo = o > T[t].ro[r][d] ? o : T[t].ro[r][d];
+          int uu = up < rup ? up : rup;
+          coff[d] = oo;
+          csz[d] = uu - oo;
+        }
+        if (!(csz[0] > 0 && csz[1] > 0)) continue;
+        if (!any) {
+          any = true;
+          acc = level ? slab[idx_unew(D, q, x, y)] : slab[idx_uold(D, q, x, y)];
+        }
+        const double tf = level ? T[t].tfn : T[t].tfo;
+        const double itf = __dsub_rn(1.0, tf);
+        const bool addb = T[t].swe != 0 && q == 0;
+        for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++)
+          for (int sy = coff[1]; sy < coff[1] + csz[1]; sy++) {
+            const double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
+            double region = 1.0;
+            for (int d = 0; d < 2; d++) {
+              double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
+              double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
+              region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
+              region = fmax(region, 0.0);
+            }
+            double vo = slab[idx_uold(S, q, sx, sy)];
+            double vn = slab[idx_unew(S, q, sx, sy)];
+            if (addb) {
+              double bb = slab[idx_pw(S, 0, sx, sy)];
+              vo = __dadd_rn(vo, bb);
+              vn = __dadd_rn(vn, bb);
+            }
+            acc = __dadd_rn(acc, ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itf), __dmul_rn(vn, tf)), region),
+                                              dvol));
+          }
       }
-      if (any) {
-        if (level) slab[idx_unew(D, q, x, y)] = acc;
-        else slab[idx_uold(D, q, x, y)] = acc;
-      }
+    }
+    if (any) {
+      if (level) slab[idx_unew(D, q, x, y)] = acc;
+      else slab[idx_uold(D, q, x, y)] = acc;
     }
   }
 }
