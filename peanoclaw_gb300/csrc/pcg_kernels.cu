@@ -1053,7 +1053,7 @@ __global__ void k_restrict(double *slab, const PatchDev *patches, const PatchTim
 // One warp per destination cell of a region: the lanes evaluate the
 // contributions of up to 32 source cells at a time, lane 0 adds them to the
 // cell's uOld / uNew values in source-cell order.
-constexpr int kRestrWarps = 6;   // warps per CTA of the batched restriction (32 cells x 6 sums)
+constexpr int kRestrWarps = 6;   // warps per CTA of the batched restriction (one sum per thread)
 __device__ void restrict_items_in_order(double *slab, const PatchDev *patches, const PatchTimeDev *times,
                                         const int4 *items, int b0, int b1, double (*W)[32][6]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1206,7 +1206,6 @@ __device__ void restrict_items_in_order(double *slab, const PatchDev *patches, c
 // 2x slower there.  Destinations flagged bad take
 // restrict_items_in_order in their first CTA.
 constexpr int kRestrPerCell = 6;                       // 3 unknowns x (uOld, uNew)
-constexpr int kRestrSlots = kRestrWarps * 32 / kRestrPerCell;
 
 __global__ void __launch_bounds__(256)
     k_restr_prepare(double *slab, const PatchDev *patches, const PatchTimeDev *times, const int4 *items,
@@ -1981,7 +1980,9 @@ cudaError_t launch_restr_dirty(cudaStream_t st, const int4 *items, const int *be
 }
 
 // CTAs per destination of the batched restriction: about four CTAs per SM
-// over all destinations, at most 16.
+// over all destinations, at most 16.  A destination's task space is dealt in
+// blocks of one CTA's threads, so CTAs beyond its task count only read the
+// table and return.
 int restr_split(int n_dst, int num_sms) {
   if (n_dst <= 0) return 1;
   const int target = 4 * (num_sms > 0 ? num_sms : 1);
