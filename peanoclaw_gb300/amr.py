@@ -36,6 +36,19 @@ from .pcg import PCG_GHOST_COPY, PCG_GHOST_INTERP
 DIRECTIONS = ((-1, 0), (1, 0), (0, -1), (0, 1), (-1, -1), (1, -1), (-1, 1), (1, 1))
 
 
+class _Layout(dict):
+    """The lists of AmrGrid.layout; "index" (slot -> position in the patch
+    order) is built on first use."""
+
+    def __missing__(self, key):
+        if key != "index":
+            raise KeyError(key)
+        order = self["order"]
+        v = dict(zip(order, range(len(order))))
+        self["index"] = v
+        return v
+
+
 class AmrGrid:
     """The hierarchy as one boolean array per level over its slots:
     `exists` (the slot holds a patch) and `refined` (its patch is virtual and
@@ -156,6 +169,14 @@ class AmrGrid:
             k = ~rf
             self._cache["leaves"] = list(zip(lv[k].tolist(), si[k].tolist(), sj[k].tolist()))
         return list(self._cache["leaves"])
+
+    def leaf_arrays(self):
+        """Leaves as arrays (level, i, j), in the order of leaves() (cached)."""
+        if "leaf_arrays" not in self._cache:
+            lv, si, sj, rf = self.slot_arrays()
+            k = ~rf
+            self._cache["leaf_arrays"] = (lv[k], si[k], sj[k])
+        return self._cache["leaf_arrays"]
 
     def buffer(self, l):
         return self.buffers[l] if l < len(self.buffers) else 1
@@ -282,14 +303,13 @@ class AmrGrid:
         L = 1.0 / (self.base * np.power(3.0, lvl.astype(np.float64)))
         pos = np.stack([si * L, sj * L], axis=1)
         size = np.stack([L, L], axis=1)
-        index = dict(zip(order, range(npch)))
         leaf = (ref == 0).tolist()
-        return {"order": order, "index": index, "pos": pos, "size": size,
+        return _Layout({"order": order, "pos": pos, "size": size,
                 "leaf": leaf, "level": lvl.tolist(), "wall": walls[:npch].tolist(),
                 "items": items[:ni.value].copy(), "flux_items": flux[:nf.value].copy(),
                 "restrict_items": restr[:nr.value].copy(),
                 "restr_lower": lower[:npch].copy(), "restr_upper": upper[:npch].copy(),
-                "virtual_time_items": self._virtual_time_items(lv, ii, jj, rf)}
+                "virtual_time_items": self._virtual_time_items(lv, ii, jj, rf)})
 
     def _virtual_time_items(self, lv, ii, jj, rf):
         """virtual_time_items() on the slot arrays: every leaf against each
@@ -477,15 +497,30 @@ def remesh(grid, backend, g, b_of):
     changed = [E1[l] & (~E0[l] | (R1[l] != R0[l])) for l in range(grid.levels)]
     grid.set_arrays(E1, R1)
     lay = grid.layout()
+    # positions in the patch order (sorted by level, i, j) by binary search
+    lv, si, sj, _ = grid.slot_arrays()
+    M = grid.slots_per_edge(grid.levels - 1)
+    keys = (lv * M + si) * M + sj
     for l in range(grid.levels):
-        for i, j in np.argwhere(changed[l]).tolist():
-            k = lay["index"][(l, i, j)]
+        ch = np.argwhere(changed[l])
+        if not len(ch):
+            continue
+        at = np.searchsorted(keys, (l * M + ch[:, 0]) * M + ch[:, 1])
+        for (i, j), k in zip(ch.tolist(), at.tolist()):
             backend.set_leaf(backend.handle((l, i, j)), lay["leaf"][k], lay["wall"][k])
     backend.install(lay, [backend.handle(s) for s in lay["order"]])
     # virtual patches (new ones included) receive the restriction of the
     # current leaves before the next ghost fill reads them
     backend.restrict_all()
     return n_ref, n_crs
+
+
+class LeafValues:
+    """Refinement criterion of the leaves as arrays (level, i, j, value): the
+    form AmrGrid.decide reads without going through a dict."""
+
+    def __init__(self, lv, ii, jj, vv):
+        self.arrays = (lv, ii, jj, vv)
 
 
 class DeviceAmr:
@@ -496,6 +531,7 @@ class DeviceAmr:
         self.flux, self.g_flux = flux, g_flux
         self.pid = {}
         self._bounds = None   # (virtual?, lower, upper) last written, per patch id
+        self._order_ids = None  # (grid slot arrays, patch ids in that order) at the last install
         self.timing = {}
 
     # -- remesh protocol
@@ -577,6 +613,7 @@ class DeviceAmr:
 
     def install(self, lay, handles):
         ids = np.asarray(handles, dtype=np.int32)
+        self._order_ids = (self.grid.slot_arrays(), ids.copy())
         # restriction bounds of the virtual patches whose bounds are new or
         # changed since the last install, in one call
         virt = ~np.asarray(lay["leaf"], dtype=bool)
@@ -612,14 +649,27 @@ class DeviceAmr:
 
     # -- driver
     def indicators(self):
+        """The refinement criterion of every leaf, as a dict slot -> value."""
         leaves = self.grid.leaves()
         vals = self.ctx.refinement_indicator([self.pid[s] for s in leaves])
         return dict(zip(leaves, vals))
 
+    def indicator_arrays(self):
+        """The same values as LeafValues (what remesh() passes to decide)."""
+        lv, ii, jj = self.grid.leaf_arrays()
+        slots = self.grid.slot_arrays()
+        # the ids of the last install are in the patch order while the grid
+        # is unchanged since (its cached slot arrays are the same object)
+        if self._order_ids is not None and self._order_ids[0] is slots:
+            ids = self._order_ids[1][~slots[3]]
+        else:
+            ids = [self.pid[s] for s in self.grid.leaves()]
+        return LeafValues(lv, ii, jj, self.ctx.refinement_indicator(ids))
+
     def remesh(self):
         import time
         t0 = time.perf_counter()
-        g = self.indicators()
+        g = self.indicator_arrays()
         t1 = time.perf_counter()
         r = remesh(self.grid, self, g, self.b_of)
         self.ctx.synchronize()

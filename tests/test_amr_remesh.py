@@ -11,7 +11,7 @@ import numpy as np
 from helpers import OracleAmr, oracle_params
 from peanoclaw_gb300 import pcg as P
 from peanoclaw_gb300 import scenarios as S
-from peanoclaw_gb300.amr import AmrGrid
+from peanoclaw_gb300.amr import AmrGrid, LeafValues
 
 PRM = P.swe_params(g=9.81, cfl=0.5)
 
@@ -120,3 +120,9 @@ def test_array_decision_equals_the_slot_by_slot_decision():
             for l in range(grid.levels):
                 assert set(map(tuple, np.argwhere(E[l]).tolist())) == e2[l]
                 assert set(map(tuple, np.argwhere(R[l]).tolist())) == r2[l]
+            # the same values as leaf arrays (what the device driver passes)
+            lv, ii, jj = grid.leaf_arrays()
+            assert list(zip(lv.tolist(), ii.tolist(), jj.tolist())) == leaves
+            E3, R3 = grid.decide(LeafValues(lv, ii, jj, vals))
+            for l in range(grid.levels):
+                assert np.array_equal(E3[l], E[l]) and np.array_equal(R3[l], R[l])
