@@ -126,3 +126,59 @@ def test_array_decision_equals_the_slot_by_slot_decision():
             E3, R3 = grid.decide(LeafValues(lv, ii, jj, vals))
             for l in range(grid.levels):
                 assert np.array_equal(E3[l], E[l]) and np.array_equal(R3[l], R[l])
+
+
+class _FakeCtx:
+    """The calls DeviceAmr.install and indicator_arrays make, recorded; the
+    criterion of patch id k is k / 1000."""
+
+    def __init__(self):
+        self.calls = []
+
+    def refinement_indicator(self, ids):
+        ids = np.asarray(ids, dtype=np.int64)
+        self.calls.append(("indicator", ids.copy()))
+        return ids.astype(np.float64) / 1000.0
+
+    def __getattr__(self, name):
+        def record(*a, **k):
+            self.calls.append((name, a))
+        return record
+
+
+def test_device_indicator_arrays_follow_the_leaf_order():
+    """DeviceAmr.indicator_arrays (what DeviceAmr.remesh passes to decide)
+    carries, per leaf in leaves() order, the value of that leaf's patch id:
+    through the ids of the last install while the grid is unchanged, through
+    the slot -> id map once it changed; decide reads it like the dict form."""
+    from peanoclaw_gb300.amr import DeviceAmr
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3, h_left=1.0, h_right=0.2, threshold=1.0)
+    grid = ps.grid
+    ctx = _FakeCtx()
+    dev = DeviceAmr(ctx, grid, ps.b_of)
+    order = grid.order()
+    ids = np.arange(100, 100 + len(order))[::-1].copy()   # ids unrelated to positions
+    dev.pid = dict(zip(order, ids.tolist()))
+    leaves = grid.leaves()
+    want = np.array([dev.pid[s] for s in leaves], dtype=np.float64) / 1000.0
+    # before any install: the slot -> id map
+    lv, ii, jj, vv = dev.indicator_arrays().arrays
+    assert list(zip(lv.tolist(), ii.tolist(), jj.tolist())) == leaves
+    assert np.array_equal(vv, want)
+    # after an install: the install's ids, same values
+    dev.install(grid.layout(), ids.tolist())
+    assert dev._order_ids[0] is grid.slot_arrays()
+    assert np.array_equal(dev.indicator_arrays().arrays[3], want)
+    # the decision equals the one from the dict of the same values
+    g = dict(zip(leaves, want.tolist()))
+    for a, b in zip(grid.decide(dev.indicator_arrays()), grid.decide(g)):
+        assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    # a changed grid invalidates the install's ids (its slot arrays are new)
+    E, R = grid.decide({s: 1e9 for s in leaves})
+    grid.set_arrays(E, R)
+    assert dev._order_ids[0] is not grid.slot_arrays()
+    new_leaves = grid.leaves()
+    for k, s in enumerate(grid.order()):
+        dev.pid.setdefault(s, 10_000 + k)
+    got = dev.indicator_arrays().arrays[3]
+    assert np.array_equal(got, np.array([dev.pid[s] for s in new_leaves], dtype=np.float64) / 1000.0)
