@@ -787,20 +787,64 @@ void pco_apply_flux_correction(const pco_patch *src, pco_patch *dst, int dim, in
 /* ------------------------------------------------------------------------ */
 /* Synchronous grid step: the semantics of the batched GPU form.             */
 /* ------------------------------------------------------------------------ */
+/* Ghost items grouped by destination (declared in pcoracle.h). */
+int *pco_items_by_dst(pco_patch **patches, int n_patches, const pco_ghost_item *items, int n_items,
+                      int **start_out) {
+  for (int k = 0; k < n_items; k++) {
+    const pco_ghost_item *it = &items[k];
+    if (it->kind != PCO_GHOST_COPY) continue; /* interpolation reads cells [0, n-1] */
+    const pco_patch *src = patches[it->src];
+    const int n[2] = {src->nx, src->ny};
+    for (int d = 0; d < 2; d++)
+      if (it->src_offset[d] < 0 || it->src_offset[d] + it->size[d] > n[d]) return NULL;
+  }
+  int *start = (int *)calloc((size_t)n_patches + 1, sizeof(int));
+  int *cur = (int *)malloc(sizeof(int) * ((size_t)n_patches + 1));
+  int *ord = (int *)malloc(sizeof(int) * (size_t)(n_items > 0 ? n_items : 1));
+  for (int k = 0; k < n_items; k++) start[items[k].dst + 1]++;
+  for (int p = 0; p < n_patches; p++) start[p + 1] += start[p];
+  memcpy(cur, start, sizeof(int) * ((size_t)n_patches + 1));
+  for (int k = 0; k < n_items; k++) ord[cur[items[k].dst]++] = k;
+  free(cur);
+  *start_out = start;
+  return ord;
+}
+
+static void fill_item(pco_patch **patches, const pco_ghost_item *it) {
+  pco_patch *src = patches[it->src], *dst = patches[it->dst];
+  if (it->kind == PCO_GHOST_COPY)
+    pco_transfer_ghostlayer(it->size, it->src_offset, it->dst_offset, src, dst);
+  else
+    pco_interpolate(it->size, it->dst_offset, src, dst, 1, 0, 1, 1);
+}
+
 void pco_grid_fill(pco_patch **patches, int n_patches,
                    const pco_ghost_item *items, int n_items, const uint8_t *wall_mask) {
   /* SolveTimestep::enterCell copies uNew into uOld before filling the domain
    * boundary (src/peanoclaw/mappings/SolveTimestep.cpp:637-643); ghost layers
    * transferred by the compositor live in uOld's ghost region and survive the
-   * copy.  The copy is done first here, which gives the same uOld. */
-  for (int k = 0; k < n_items; k++) {
-    const pco_ghost_item *it = &items[k];
-    pco_patch *src = patches[it->src], *dst = patches[it->dst];
-    if (it->kind == PCO_GHOST_COPY)
-      pco_transfer_ghostlayer(it->size, it->src_offset, it->dst_offset, src, dst);
-    else
-      pco_interpolate(it->size, it->dst_offset, src, dst, 1, 0, 1, 1);
+   * copy.  The copy is done first here, which gives the same uOld.
+   * An item writes only its destination's ghost layer and reads source
+   * interiors, so the destinations are filled in parallel, each with its
+   * items in list order: the same writes in the same order as one pass over
+   * the list.  The interior copies, which overwrite the uOld interiors the
+   * items read, come after every item. */
+  int *start = NULL;
+  int *ord = pco_items_by_dst(patches, n_patches, items, n_items, &start);
+  if (ord) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int p = 0; p < n_patches; p++)
+      for (int q = start[p]; q < start[p + 1]; q++) fill_item(patches, &items[ord[q]]);
+    free(ord);
+    free(start);
+  } else {
+    for (int k = 0; k < n_items; k++) fill_item(patches, &items[k]);
   }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
   for (int p = 0; p < n_patches; p++) {
     if (!patches[p]->is_leaf) continue;
     pco_copy_unew_to_uold(patches[p]);
@@ -813,11 +857,13 @@ void pco_grid_step(pco_patch **patches, int n_patches,
                    const uint8_t *wall_mask, const int32_t *group, int n_groups,
                    const pco_swe_params *prm, const double *max_dt,
                    double *dt_out, int n_threads) {
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
   pco_grid_fill(patches, n_patches, items, n_items, wall_mask);
   double *own = (double *)malloc(sizeof(double) * (size_t)n_patches);
   double **nets = (double **)calloc((size_t)n_patches, sizeof(double *));
 #ifdef _OPENMP
-  if (n_threads > 0) omp_set_num_threads(n_threads);
 #pragma omp parallel for schedule(dynamic, 16)
 #endif
   for (int p = 0; p < n_patches; p++) {

@@ -151,6 +151,14 @@ void pco_grid_fill(pco_patch **patches, int n_patches,
                    const pco_ghost_item *items, int n_items,
                    const uint8_t *wall_mask);
 
+/* Ghost items grouped by destination, in list order within each (counting
+ * sort): *start_out receives n_patches + 1 offsets into the returned array of
+ * item indices (both malloc'ed; the caller frees them).  NULL when some copy
+ * item reads outside its source's interior: then an item may read cells that
+ * another item writes, and only the list order is exact. */
+int *pco_items_by_dst(pco_patch **patches, int n_patches, const pco_ghost_item *items, int n_items,
+                      int **start_out);
+
 /* ---- FP32 twin (pcoracle_f32.c): timing baseline at the reference's storage
  * precision, not a parity reference.  pco_grid_step for one group with float
  * patch vectors u[p] in the layout of patches[p] (whose own u is not used);

@@ -284,22 +284,39 @@ static void update_swap32(const pco_patch *p, float *u, const prm32 *P, const fl
     }
 }
 
+static void fill32(pco_patch **patches, float **u, const pco_ghost_item *it) {
+  if (it->kind == PCO_GHOST_COPY)
+    transfer32(it, patches[it->src], u[it->src], patches[it->dst], u[it->dst]);
+  else
+    interpolate32(it, patches[it->src], u[it->src], patches[it->dst], u[it->dst]);
+}
+
 void pco32_grid_step(pco_patch **patches, float **u, int n_patches,
                      const pco_ghost_item *items, int n_items, const uint8_t *wall_mask,
                      const pco_swe_params *prm, double max_dt, double *dt_out, int n_threads) {
   prm32 P = {(float)(0.5 * prm->g), (float)prm->dry_tol, (float)prm->dry_tol_update,
              (float)prm->s_min, (float)prm->cfl, (float)prm->dt_inf};
-  for (int k = 0; k < n_items; k++) {
-    const pco_ghost_item *it = &items[k];
-    if (it->kind == PCO_GHOST_COPY)
-      transfer32(it, patches[it->src], u[it->src], patches[it->dst], u[it->dst]);
-    else
-      interpolate32(it, patches[it->src], u[it->src], patches[it->dst], u[it->dst]);
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  /* destinations in parallel, each with its items in list order (as
+   * pco_grid_fill); the interior copies follow in the solve loop */
+  int *start = NULL;
+  int *ord = pco_items_by_dst(patches, n_patches, items, n_items, &start);
+  if (ord) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int p = 0; p < n_patches; p++)
+      for (int q = start[p]; q < start[p + 1]; q++) fill32(patches, u, &items[ord[q]]);
+    free(ord);
+    free(start);
+  } else {
+    for (int k = 0; k < n_items; k++) fill32(patches, u, &items[k]);
   }
   float *own = (float *)malloc(sizeof(float) * (size_t)(n_patches > 0 ? n_patches : 1));
   float **nets = (float **)calloc((size_t)(n_patches > 0 ? n_patches : 1), sizeof(float *));
 #ifdef _OPENMP
-  if (n_threads > 0) omp_set_num_threads(n_threads);
 #pragma omp parallel for schedule(dynamic, 16)
 #endif
   for (int p = 0; p < n_patches; p++) {
