@@ -72,12 +72,43 @@ def _centers(pos, size, n, ghost=True):
     return np.meshgrid(xs, ys, indexing="ij")
 
 
+def face_adjacent_traversal():
+    """The face transfers GhostLayerCompositor issues around one vertex in 2D
+    (FaceAdjacentPatchTraversal.cpph), as (source, destination, direction)
+    over the vertex's 4 adjacent patches.  Peano numbers them with bit d set
+    for the patch on the negative side of the vertex in dimension d; the
+    direction points from the source to the destination, i.e. bits(source) -
+    bits(destination).  Sources in descending index, for each its face
+    neighbours in dimension order."""
+    calls = []
+    for src in (3, 2, 1, 0):
+        for d in (0, 1):
+            dst = src ^ (1 << d)
+            calls.append((src, dst, tuple(((src >> e) & 1) - ((dst >> e) & 1) for e in (0, 1))))
+    return calls
+
+
+def edge_adjacent_traversal():
+    """The corner transfers around one vertex in 2D
+    (EdgeAdjacentPatchTraversal.cpph): each patch to the diagonally opposite
+    one, sources in descending index; numbering and direction as in
+    face_adjacent_traversal."""
+    calls = []
+    for src in (3, 2, 1, 0):
+        dst = 3 - src
+        calls.append((src, dst, tuple(((src >> e) & 1) - ((dst >> e) & 1) for e in (0, 1))))
+    return calls
+
+
 def _build_grid_items(ps, grid_index, nslots_x, nslots_y):
     """Face and corner items for a regular grid of equally sized slots holding
     patches of different subdivision.  Same subdivision: copy; otherwise
     interpolation from the neighbour (its subcells are larger or smaller).
     Returns an (N, 9) int32 array: kind, src, dst, size[2], src_offset[2],
-    dst_offset[2] (the pcg_ghost_item layout)."""
+    dst_offset[2] (the pcg_ghost_item layout).  The items are the calls of
+    face_adjacent_traversal and edge_adjacent_traversal over every interior
+    vertex (each face once), ordered by destination; every ghost cell is
+    written by one item, so the order does not change the result."""
     rows = []
     for sx in range(nslots_x):
         for sy in range(nslots_y):
