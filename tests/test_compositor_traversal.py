@@ -80,3 +80,19 @@ def test_mosaic_lists_are_the_vertex_traversals():
 
 def test_regular_grid_lists_are_the_vertex_traversals():
     _check(S.radial_dam_break(npx=5, n=8))
+
+
+def test_adaptive_lists_write_each_ghost_cell_once():
+    """The same for the lists of the adaptive hierarchies (copies between
+    leaves of one level, interpolation from coarser leaves and virtual
+    patches, corners included): no ghost cell of a destination is written
+    twice and no interior cell at all."""
+    for ps in (S.breaking_dam_amr(base=3, n=9, levels=3), S.adaptive_tsunami(base=5, n=8, levels=3)):
+        items = np.asarray(ps.items)
+        for d in np.unique(items[:, 2]):
+            n = ps.n[int(d)]
+            hits = np.zeros((n + 2, n + 2), dtype=np.int64)
+            for it in items[items[:, 2] == d]:
+                ox, oy = it[7] + 1, it[8] + 1
+                hits[ox:ox + it[3], oy:oy + it[4]] += 1
+            assert hits.max() <= 1 and hits[1:-1, 1:-1].sum() == 0, int(d)
