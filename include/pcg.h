@@ -220,6 +220,20 @@ int pcg_switch_to_leaf(pcg_context *ctx, int32_t id);
  * forward differences of |grad h| on uNew.  The scenario refines where it
  * exceeds 0.1 and coarsens where it is below. */
 int pcg_refinement_indicator(pcg_context *ctx, int32_t n, const int32_t *ids, double *out);
+/* The refinement criterion `kind` of every listed patch, one double per
+ * patch (the scenario compares it with its threshold):
+ *   PCG_CRIT_DEPTH_GRADIENT: as pcg_refinement_indicator (BreakingDam);
+ *   PCG_CRIT_SURFACE_DIFFERENCE: max over interior forward differences of
+ *     the surface h + b, not divided by the mesh width (BowlOcean's wave-front
+ *     criterion, native/scenarios/BowlOcean.cpp:91-123, threshold 0.05);
+ *   PCG_CRIT_SURFACE_GRADIENT: the BreakingDam stencil on the surface h + b
+ *     (forward differences divided by the subcell size): a still lake over
+ *     any bathymetry gives 0, a wave or a wet/dry coastline does not.
+ * The surface criteria read b (the first parameter with ghost layer). */
+#define PCG_CRIT_DEPTH_GRADIENT 0
+#define PCG_CRIT_SURFACE_DIFFERENCE 1
+#define PCG_CRIT_SURFACE_GRADIENT 2
+int pcg_refinement_criterion(pcg_context *ctx, int32_t n, const int32_t *ids, int32_t kind, double *out);
 
 /* ----------------------------------------------------------------- output */
 
@@ -392,8 +406,12 @@ int pcg_check_ieee_emulation(pcg_context *ctx, int64_t samples, uint64_t seed, i
  * time intervals.  stream: a cudaStream_t (NULL = default stream).
  * Scratch is a fixed 393 KB array inside the library, held by every GPU that
  * loads it until exit and shared by all calls: calls that overlap on the GPU
- * race.  The first call on a device resolves that array's device address (a
- * one-time set-up); make that first call before any stream capture. */
+ * race.  The first call in a device's context resolves that array's device
+ * address (a set-up done again after the context was destroyed and created
+ * anew, e.g. by cudaDeviceReset); make that first call before any stream
+ * capture (PCG_E_STATE otherwise).  Calls made while `stream` is being
+ * captured must pass NULL for dt_used and est_next, whose read-back copies
+ * and synchronises the stream (PCG_E_INVALID otherwise). */
 int pcg_solve_timestep_noalloc(double *d_vector, int32_t nx, int32_t ny, const double size[2],
                                const pcg_swe_params *params, double max_dt, double *dt_used,
                                double *est_next, void *stream);

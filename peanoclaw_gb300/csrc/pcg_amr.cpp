@@ -40,6 +40,9 @@ extern "C" int pcg_amr_layout(int32_t base, int32_t n, int32_t levels, int32_t n
   std::vector<int64_t> m(levels);
   int64_t e = base;
   for (int l = 0; l < levels; l++, e *= 3) m[l] = e;
+  // slot keys pack i and j into 26 bits each
+  if (m[levels - 1] > ((int64_t)1 << 26))
+    return pcg_report_error(PCG_E_INVALID, "pcg_amr_layout: more than 2^26 slots per side on the finest level");
   std::unordered_map<int64_t, int32_t> index;
   index.reserve((size_t)np * 2);
   std::vector<double> px(np), py(np), sx(np), sy(np);

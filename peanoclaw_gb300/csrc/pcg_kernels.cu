@@ -1678,17 +1678,30 @@ __global__ void k_gather_cells(const double *__restrict__ slab, const PatchDev *
 // gy = (h[xi][yi+1] - h[xi][yi]) / dy on uNew; fmax keeps the non-NaN operand.
 // One CTA per listed patch.
 __global__ void k_refinement_indicator(const double *__restrict__ slab, const PatchDev *__restrict__ patches,
-                                       const int *__restrict__ ids, int count, double *__restrict__ out) {
+                                       const int *__restrict__ ids, int count, int kind,
+                                       double *__restrict__ out) {
   if ((int)blockIdx.x >= count) return;
   const PatchDev P = patches[ids[blockIdx.x]];
   const double dx = subcell(P, 0), dy = subcell(P, 1);
   const int mx = P.nx - 1, my = P.ny - 1;
+  // kind 0: depth h, differences / subcell size (BreakingDam.cpp:100-116);
+  // kind 1: surface h + b, plain differences (BowlOcean.cpp:106-122);
+  // kind 2: surface h + b, differences / subcell size
+  const bool surface = kind != 0, divide = kind != 1;
+  auto value = [&](int x, int y) {
+    const double h = slab[idx_unew(P, 0, x, y)];
+    return surface ? __dadd_rn(h, slab[idx_pw(P, 0, x, y)]) : h;
+  };
   double m = 0.0;
   for (int k = threadIdx.x; k < mx * my; k += blockDim.x) {
     const int xi = k / my, yi = k - xi * my;
-    const double q0 = slab[idx_unew(P, 0, xi, yi)];
-    const double gx = ieee::div_rn(__dsub_rn(slab[idx_unew(P, 0, xi + 1, yi)], q0), dx);
-    const double gy = ieee::div_rn(__dsub_rn(slab[idx_unew(P, 0, xi, yi + 1)], q0), dy);
+    const double q0 = value(xi, yi);
+    double gx = __dsub_rn(value(xi + 1, yi), q0);
+    double gy = __dsub_rn(value(xi, yi + 1), q0);
+    if (divide) {
+      gx = ieee::div_rn(gx, dx);
+      gy = ieee::div_rn(gy, dy);
+    }
     const double ax = fabs(gx), ay = fabs(gy);
     m = fmax_nonneg(m, ieee::sqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay))));
   }
@@ -2054,9 +2067,9 @@ cudaError_t launch_switch_to_leaf(cudaStream_t st, double *slab, const PatchDev 
 }
 
 cudaError_t launch_refinement_indicator(cudaStream_t st, const double *slab, const PatchDev *patches,
-                                        const int *ids, int count, double *out) {
+                                        const int *ids, int count, int kind, double *out) {
   if (count <= 0) return cudaSuccess;
-  k_refinement_indicator<<<count, 256, 0, st>>>(slab, patches, ids, count, out);
+  k_refinement_indicator<<<count, 256, 0, st>>>(slab, patches, ids, count, kind, out);
   return cudaGetLastError();
 }
 
@@ -2147,6 +2160,8 @@ __global__ void __launch_bounds__(kSweepThreads)
 
 }  // namespace pcg
 
+#include <cuda.h>
+
 #include <mutex>
 
 #include "../../include/pcg.h"
@@ -2154,7 +2169,44 @@ __global__ void __launch_bounds__(kSweepThreads)
 namespace {
 std::mutex g_noalloc_mu;
 constexpr int kNoAllocMaxDevices = 64;
-double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+// Device address of the scratch array per device ordinal, valid for the
+// context whose id is stored beside it: a context that was destroyed and
+// created again (cudaDeviceReset, or a framework that resets the device)
+// loads the library's module again, possibly at another address.
+struct NoAllocScratchAddr {
+  unsigned long long ctx_id;
+  double *ptr;
+};
+NoAllocScratchAddr g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (the
+// library does not link the driver library itself, so that it still loads on
+// machines without a GPU driver).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// Id of the calling thread's current context, 0 if there is none yet.
+cudaError_t current_context_id(unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    if (e == cudaSuccess)
+      e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess) return e;
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return cudaErrorSymbolNotFound;
+    get_current = (CtxGetCurrentFn)f1;
+    get_id = (CtxGetIdFn)f2;
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return cudaErrorContextIsDestroyed;
+  *id = 0;
+  if (ctx && get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorContextIsDestroyed;
+  return cudaSuccess;
+}
 }  // namespace
 
 extern "C" int pcg_solve_timestep_noalloc(double *d_vector, int32_t nx, int32_t ny,
@@ -2176,20 +2228,45 @@ extern "C" int pcg_solve_timestep_noalloc(double *d_vector, int32_t nx, int32_t 
   if (e != cudaSuccess) return pcg_report_error(PCG_E_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return pcg_report_error(PCG_E_INVALID, "pcg_solve_timestep_noalloc: device ordinal too large");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return pcg_report_error(PCG_E_CUDA, cudaGetErrorString(e));
+  const bool capturing = cap != cudaStreamCaptureStatusNone;
+  // dt_used / est_next are read back with a copy and a stream synchronisation,
+  // neither of which a stream under capture allows
+  if (capturing && (dt_used || est_next))
+    return pcg_report_error(PCG_E_INVALID,
+                            "pcg_solve_timestep_noalloc: dt_used and est_next must be NULL while the "
+                            "stream is being captured");
   double *scratch;
   {
-    // First call on a device: resolve the device address of the scratch
-    // array with that device current (the host-side name is not a device
-    // address).
+    // First call on a device (or in a new context of it): resolve the device
+    // address of the scratch array with that device current (the host-side
+    // name is not a device address).
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    unsigned long long id = 0;
+    e = current_context_id(&id);
+    if (e != cudaSuccess)
+      return pcg_report_error(PCG_E_CUDA, std::string("current context: ") + cudaGetErrorString(e));
+    NoAllocScratchAddr &A = g_noalloc_addr[dev];
+    if (id == 0 || !A.ptr || A.ctx_id != id) {
+      if (capturing)
+        return pcg_report_error(PCG_E_STATE,
+                                "pcg_solve_timestep_noalloc: the first call in a device context must "
+                                "come before any stream capture");
       double *p = nullptr;
       e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p)
         return pcg_report_error(PCG_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      g_noalloc_ptr[dev] = p;
+      // the context exists now (the call above initialises it if needed)
+      e = current_context_id(&id);
+      if (e != cudaSuccess || id == 0)
+        return pcg_report_error(PCG_E_CUDA, std::string("current context: ") + cudaGetErrorString(e));
+      A.ptr = p;
+      A.ctx_id = id;
     }
-    scratch = g_noalloc_ptr[dev];
+    scratch = A.ptr;
   }
   PatchDev P{};
   P.off = 0;
@@ -2198,7 +2275,6 @@ extern "C" int pcg_solve_timestep_noalloc(double *d_vector, int32_t nx, int32_t 
   P.size[0] = size[0]; P.size[1] = size[1];
   SweParamsDev prm{params->g, params->cfl, params->dry_tol, params->dry_tol_update, params->s_min,
                    params->dt_inf};
-  cudaStream_t st = (cudaStream_t)stream;
   k_solve_patch_noalloc<<<1, kSweepThreads, 0, st>>>(d_vector, P, prm, max_dt, scratch);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pcg_report_error(PCG_E_CUDA, cudaGetErrorString(e));

@@ -11,15 +11,18 @@ def oracle_params(prm):
 
 def random_swe_vector(rng, n, dry_fraction=0.2, lake=False, ghost_b=True):
     """Patch vector (reference layout, ghost 1, 3 unknowns, b with ghost) with a
-    random wet/dry state in uNew and uOld (incl. ghost ring)."""
-    ln = P.vector_size(n)
+    random wet/dry state in uNew and uOld (incl. ghost ring); n is the side or
+    the (nx, ny) pair."""
+    nx, ny = (n, n) if np.isscalar(n) else n
+    ln = P.vector_size((nx, ny))
     v = np.zeros(ln)
-    a = 3 * n * n
-    o = 3 * (n + 2) ** 2
-    unew = v[:a].reshape(3, n, n)
-    uold = v[a:a + o].reshape(3, n + 2, n + 2)
-    b = v[a + o:a + o + (n + 2) ** 2].reshape(n + 2, n + 2)
-    b[:] = rng.uniform(-0.3, 0.6, (n + 2, n + 2))
+    a = 3 * nx * ny
+    vo = (nx + 2) * (ny + 2)
+    o = 3 * vo
+    unew = v[:a].reshape(3, nx, ny)
+    uold = v[a:a + o].reshape(3, nx + 2, ny + 2)
+    b = v[a + o:a + o + vo].reshape(nx + 2, ny + 2)
+    b[:] = rng.uniform(-0.3, 0.6, (nx + 2, ny + 2))
     if lake:
         # dyadic values so that h + b is exact: a lake at rest with dry cells
         b[:] = np.round(b * 64.0) / 64.0
@@ -28,16 +31,16 @@ def random_swe_vector(rng, n, dry_fraction=0.2, lake=False, ghost_b=True):
         uold[0] = h
         unew[0] = h[1:-1, 1:-1]
         return v
-    h = rng.uniform(0.0, 2.0, (n + 2, n + 2))
-    dry = rng.uniform(0, 1, (n + 2, n + 2)) < dry_fraction
+    h = rng.uniform(0.0, 2.0, (nx + 2, ny + 2))
+    dry = rng.uniform(0, 1, (nx + 2, ny + 2)) < dry_fraction
     h[dry] = rng.uniform(0.0, 0.02, dry.sum())
-    hu = rng.normal(0.0, 0.5, (n + 2, n + 2))
-    hv = rng.normal(0.0, 0.5, (n + 2, n + 2))
+    hu = rng.normal(0.0, 0.5, (nx + 2, ny + 2))
+    hv = rng.normal(0.0, 0.5, (nx + 2, ny + 2))
     uold[0], uold[1], uold[2] = h, hu, hv
-    unew[0] = rng.uniform(0.0, 2.0, (n, n))
-    unew[1] = rng.normal(0.0, 0.5, (n, n))
-    unew[2] = rng.normal(0.0, 0.5, (n, n))
-    v[a + o + (n + 2) ** 2:] = rng.normal(0.0, 1.0, v.size - (a + o + (n + 2) ** 2))
+    unew[0] = rng.uniform(0.0, 2.0, (nx, ny))
+    unew[1] = rng.normal(0.0, 0.5, (nx, ny))
+    unew[2] = rng.normal(0.0, 0.5, (nx, ny))
+    v[a + o + vo:] = rng.normal(0.0, 1.0, v.size - (a + o + vo))
     return v
 
 
@@ -121,12 +124,32 @@ def gpu_amr_patchset(ctx, ps, flux=True, g_flux=1.0):
     return install_amr(ctx, ps, flux=flux, g_flux=g_flux)
 
 
+def oracle_criterion(p, kind=0):
+    """Refinement criterion of an oracle patch (pcg_refinement_criterion kinds):
+    0 the BreakingDam depth gradient (BreakingDam.cpp:100-116), 1 BowlOcean's
+    surface differences (BowlOcean.cpp:106-122), 2 the BreakingDam stencil on
+    the surface h + b."""
+    h = p.unew()[0]
+    if kind != 0:
+        g = p.s.ghost
+        h = h + p.param_w()[0][g:-g, g:-g]
+    dx, dy = p.s.size[0] / p.s.nx, p.s.size[1] / p.s.ny
+    gx = h[1:, :-1] - h[:-1, :-1]
+    gy = h[:-1, 1:] - h[:-1, :-1]
+    if kind != 1:
+        gx = gx / dx
+        gy = gy / dy
+    g = np.sqrt(np.abs(gx) * np.abs(gx) + np.abs(gy) * np.abs(gy))
+    return float(np.fmax.reduce(g.ravel(), initial=0.0))
+
+
 class OracleAmr:
     """Backend of peanoclaw_gb300.amr.remesh on oracle patches (the CPU side of
     the remesh parity tests); mirrors DeviceAmr call for call."""
 
-    def __init__(self, grid, ps, b_of, flux=True, g_flux=1.0):
+    def __init__(self, grid, ps, b_of, flux=True, g_flux=1.0, criterion=0):
         self.grid, self.b_of, self.flux, self.g_flux = grid, b_of, flux, g_flux
+        self.criterion = criterion  # pcg_refinement_criterion kind
         pats = oracle_amr_patchset(ps)
         self.pat = dict(zip(grid.order(), pats))
         self.lay = grid.layout()
@@ -210,16 +233,7 @@ class OracleAmr:
         return [self.pat[s] for s in self.lay["order"]]
 
     def indicators(self):
-        out = {}
-        for s in self.grid.leaves():
-            p = self.pat[s]
-            h = p.unew()[0]
-            dx, dy = p.s.size[0] / p.s.nx, p.s.size[1] / p.s.ny
-            gx = (h[1:, :-1] - h[:-1, :-1]) / dx
-            gy = (h[:-1, 1:] - h[:-1, :-1]) / dy
-            g = np.sqrt(np.abs(gx) * np.abs(gx) + np.abs(gy) * np.abs(gy))
-            out[s] = float(np.fmax.reduce(g.ravel(), initial=0.0))
-        return out
+        return {s: oracle_criterion(self.pat[s], self.criterion) for s in self.grid.leaves()}
 
     def step(self, prm, max_dt):
         from types import SimpleNamespace
