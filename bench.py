@@ -79,8 +79,8 @@ def parse():
                     help="comma-separated subset of the configuration legs to run (default: all)")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the secondary configurations (dam break, AMR, serving)")
-    ap.add_argument("--amr-steps", type=int, default=100)
-    ap.add_argument("--remesh-steps", type=int, default=100)
+    ap.add_argument("--amr-steps", type=int, default=500)
+    ap.add_argument("--remesh-steps", type=int, default=300)
     ap.add_argument("--remesh-every", type=int, default=10)
     ap.add_argument("--lts-t-end", type=float, default=0.02)
     ap.add_argument("--serve-requests", type=int, default=32)
@@ -191,6 +191,69 @@ def build_context(ps, prm):
     return ctx, ids
 
 
+# Arm CPU part numbers (MIDR part field) of the host CPUs this runs on
+ARM_PARTS = {"0xd4f": "Arm Neoverse-V2 (NVIDIA Grace)", "0xd40": "Arm Neoverse-V1",
+             "0xd0c": "Arm Neoverse-N1", "0xd49": "Arm Neoverse-N2", "0xd8e": "Arm Neoverse-N3",
+             "0xd84": "Arm Neoverse-V3"}
+
+
+def cpu_model():
+    """Model name of the host CPU: lscpu's, else /proc/cpuinfo's model name or
+    Arm part number."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                name = line.split(":", 1)[1].strip()
+                if name and name != "-":
+                    return name
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            low = line.lower()
+            if low.startswith("model name"):
+                return line.split(":", 1)[1].strip()
+            if low.startswith("cpu part"):
+                part = line.split(":", 1)[1].strip()
+                return ARM_PARTS.get(part, "Arm CPU part " + part)
+    except OSError:
+        pass
+    return ""
+
+
+def parity_check(ps, prm, steps=3):
+    """In-run comparison of the batched GPU step with the FP64 oracle on a
+    patch set: both advance `steps` steps from the same state; returns the
+    largest absolute and relative differences over every patch vector (ghost
+    layers included) and whether all bits agree."""
+    from oracle import oracle as O
+    from peanoclaw_gb300 import pcg as P
+    oprm = O.swe_params(prm.g, prm.cfl, prm.dry_tol, prm.dry_tol_update, prm.s_min, prm.dt_inf)
+    pats = []
+    for p in range(len(ps)):
+        op = O.Patch(ps.n[p], pos=ps.pos[p], size=ps.size[p])
+        op.u[:] = ps.vector(p)
+        pats.append(op)
+    odts = [float(O.grid_step(pats, ps.items, ps.wall, oprm, 1e9)[0]) for _ in range(steps)]
+    ref = np.concatenate([p.u for p in pats])
+    ctx, ids = build_context(ps, prm)
+    try:
+        ctx.upload_many(ids, ps.packed)
+        ctx.set_group_max_dt(0, 1e9)
+        dts = [float(d) for d in ctx.run(steps, P.PCG_MODE_BATCHED)[:, 0]]
+        got = ctx.download_many(ids, int(ps.packed.size))
+    finally:
+        ctx.close()
+    diff = np.abs(got - ref)
+    scale = np.maximum(np.abs(ref), 1e-300)
+    return {"vs": "FP64 CPU oracle (oracle/pcoracle.c), measured in this run",
+            "sample": "%d patches, %d cells, %d steps" % (len(ps), ps.cells(), steps),
+            "max_abs_error": float(diff.max()), "max_rel_error": float((diff / scale).max()),
+            "dt_equal": dts == odts,
+            "bit_exact": bool(np.array_equal(got.view(np.int64), ref.view(np.int64)))}
+
+
 def cpu_baseline(args, prm, seconds_target=15.0, fp32_seconds=6.0):
     """The oracle (CPU restatement, OpenMP over patches, all host threads) on a
     bounded sample of the same generator: a G x G slot mosaic.  Timed twice:
@@ -233,22 +296,78 @@ def cpu_baseline(args, prm, seconds_target=15.0, fp32_seconds=6.0):
     f32 = lambda n: O.grid_step_f32(pats32, u32, ps.items, ps.wall, oprm, 1e9, n_threads=n)
     steps32, el32 = timed(f32, fp32_seconds, threads, 400)
     s132, el132 = timed(f32, max(1.0, fp32_seconds / 4), 1, 3)
-    cpu_model = ""
-    try:
-        for line in open("/proc/cpuinfo"):
-            if line.lower().startswith(("model name", "cpu part")):
-                cpu_model = line.split(":", 1)[1].strip()
-                break
-    except OSError:
-        pass
     return {"value": cells * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
             "dtype": "f64", "single_core_value": cells * s1 / el1,
             "fp32_value": cells * steps32 / el32, "fp32_single_core_value": cells * s132 / el132,
-            "cpu": cpu_model,
+            "cpu": cpu_model(),
             "sample": "%dx%d-slot mosaic of the same generator (%d patches, %d cells), "
                       "FP64 %d steps in %.1f s, FP32 twin %d steps in %.1f s"
                       % (args.cpu_sample_grid, args.cpu_sample_grid, len(ps), cells, steps, el,
                          steps32, el32)}
+
+
+def cpu_configs(prm):
+    """The oracle on the other configurations, FP64 with all host threads and
+    with one, and the FP32 twin (the reference's float precision) with all
+    threads: the 9x9x16^2 radial dam break (all 100 steps), the 3-level
+    breaking dam (27^2 cells per patch, flux correction and restriction in
+    the FP64 step) and the coastal tsunami (base 27, 27^2 cells per patch,
+    3 levels, the same), each over a bounded number of steps."""
+    from oracle import oracle as O
+    from peanoclaw_gb300 import scenarios as S
+    oprm = O.swe_params(prm.g, prm.cfl, prm.dry_tol, prm.dry_tol_update, prm.s_min, prm.dt_inf)
+    threads = os.cpu_count() or 1
+    out = {"cores": threads, "cpu": cpu_model(), "kind": "port"}
+
+    def oracle_set(ps):
+        pats = []
+        for p in range(len(ps)):
+            leaf = bool(ps.leaf[p]) if hasattr(ps, "leaf") else True
+            op = O.Patch(ps.n[p], pos=ps.pos[p], size=ps.size[p], level=ps.level[p], is_leaf=leaf,
+                         is_virtual=not leaf)
+            op.u[:] = ps.vector(p)
+            if not leaf:
+                op.s.restr_lower[0], op.s.restr_lower[1] = ps.restr_lower[p]
+                op.s.restr_upper[0], op.s.restr_upper[1] = ps.restr_upper[p]
+            pats.append(op)
+        return pats
+
+    def timed(step, n_steps):
+        step()
+        t0 = time.perf_counter()
+        for _ in range(n_steps):
+            step()
+        return time.perf_counter() - t0
+
+    cases = (("radial_dam_break_9x9x16", lambda: S.radial_dam_break(npx=9, n=16), 100, 100, 100),
+             ("adaptive_breaking_dam_3_levels", lambda: S.breaking_dam_amr(base=9, n=27, levels=3), 20, 3, 20),
+             ("coastal_tsunami_3_levels", lambda: S.coastal_tsunami(), 6, 2, 6))
+    for name, make, k_all, k_one, k32 in cases:
+        ps = make()
+        amr = hasattr(ps, "leaf")
+        cells = ps.meta.get("leaf_cells", ps.cells())
+        pats = oracle_set(ps)
+        if amr:
+            O.restrict_list(pats, ps.restrict_items)
+
+        def f64(n):
+            if amr:
+                return O.amr_step(pats, ps.items, ps.wall, ps.leaf, ps.flux_items, ps.restrict_items, oprm,
+                                  1e9, n_threads=n)
+            return O.grid_step(pats, ps.items, ps.wall, oprm, 1e9, n_threads=n)
+
+        el = timed(lambda: f64(threads), k_all)
+        el1 = timed(lambda: f64(1), k_one)
+        pats32 = oracle_set(ps)
+        u32 = [np.ascontiguousarray(p.u.astype(np.float32)) for p in pats32]
+        el32 = timed(lambda: O.grid_step_f32(pats32, u32, ps.items, ps.wall, oprm, 1e9, n_threads=threads), k32)
+        out[name] = {"cells": cells, "fp64": cells * k_all / el, "fp64_single_core": cells * k_one / el1,
+                     "fp32": cells * k32 / el32,
+                     "sample": "%d / %d / %d steps (FP64 all threads / FP64 one thread / FP32 twin)"
+                               % (k_all, k_one, k32),
+                     "note": ("FP64 steps include flux correction and restriction; the FP32 twin "
+                              "times ghost fill, sweep and update" if amr else "")}
+    return out
 
 
 def bench_radial(prm):
@@ -336,16 +455,17 @@ def bench_lts(prm, t_end):
 
 
 def bench_remesh(prm, steps, every):
-    """Adaptive tsunami with dynamic remeshing: 3 levels of 3x refinement,
-    27 x 27 cells per patch, base 27 x 27 patches (6561^2 when fully refined),
-    Gaussian hump over a flat seafloor ramping up to a coastline; the device
-    refinement criterion is evaluated and the grid remeshed every `every`
+    """The large adaptive batched run: coastal tsunami with dynamic
+    remeshing, 3 levels of 3x refinement, 27 x 27 cells per patch, base
+    27 x 27 patches (an effective 6561^2 grid), Gaussian surface hump over the
+    sum-of-Gaussians seafloor (seed 2000) with a coastline along x = 1; the
+    device surface criterion is evaluated and the grid remeshed every `every`
     steps (new patches interpolated, coarsened ones restricted, lists
     rebuilt)."""
     from peanoclaw_gb300 import pcg as P
     from peanoclaw_gb300 import scenarios as S
     from peanoclaw_gb300.amr import DeviceAmr
-    ps = S.adaptive_tsunami()
+    ps = S.coastal_tsunami()
     full = 729 + 6561 + 59049
     ctx = P.Context(slab_doubles=int(full * (P.vector_size(27) + 32)) + (1 << 20), max_patches=full + 64,
                     max_groups=1, params=prm)
@@ -353,7 +473,7 @@ def bench_remesh(prm, steps, every):
         ids = S.install_amr(ctx, ps)
         ctx.restrict_all()
         ctx.set_group_max_dt(0, 1e9)
-        dev = DeviceAmr(ctx, ps.grid, ps.b_of)
+        dev = DeviceAmr(ctx, ps.grid, ps.b_of, criterion=ps.criterion)
         dev.pid = dict(zip(ps.grid.order(), (int(i) for i in ids)))
         ctx.run(2, P.PCG_MODE_BATCHED)
         ctx.synchronize()
@@ -543,9 +663,11 @@ def main():
         assert np.isfinite(hist).all()
 
     ctx.close()
-    cpu = None
+    cpu = cpu_cfg = parity = None
     if rank == 0 and not args.no_cpu and ws == 1:
         cpu = cpu_baseline(args, prm)
+        parity = parity_check(S.uneven_patches(grid=args.cpu_sample_grid), prm)
+        cpu_cfg = cpu_configs(prm)
     configs = None
     if rank == 0 and not args.no_configs:
         legs = {"radial_dam_break_9x9x16": lambda: bench_radial(prm),
@@ -588,14 +710,12 @@ def main():
                          "variant": sched[1], "chunk": sched[2],
                          "autotune_ms_per_step": ({"%s/%d/%d" % ("tiles" if k[0] == 0 else "strips", k[1], k[2]): m
                                                    for k, m in tuned} if tuned else None)},
-            "parity": {"vs": "FP64 CPU oracle (oracle/pcoracle.c)", "max_abs_error": 0.0,
-                       "note": "bit-exact on every configuration: uneven mosaic, radial dam break, "
-                               "3-level AMR, remeshing, serving mix, all schedules "
-                               "(tests/test_gpu_*.py compare bit patterns)"},
+            "parity": parity,
             "plain_per_patch_value": plain,
             "batched_over_plain": (value / ws) / plain if plain else None,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "cpu_configs": cpu_cfg,
             "configs": configs,
             "clocks": clk,
             "gpu_launches": 6 * args.steps,

@@ -296,3 +296,39 @@ def grid_step_f32(patches, u32, items, wall_mask, prm, max_dt, n_threads=0):
                           wm.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(prm), float(max_dt),
                           C.byref(dto), n_threads)
     return dto.value
+
+
+def restrict_list(pats, restrict_items):
+    """The batched restriction on oracle patches: every destination cleared
+    (uNew and the uOld interior), the SWE restriction of every (src, dst) pair
+    of the list in order, then postProcessRestriction of every destination
+    (GridLevelTransfer.cpp:140-275)."""
+    dsts = []
+    for s, d in restrict_items:
+        if int(d) not in dsts:
+            dsts.append(int(d))
+    for d in dsts:
+        pats[d].unew()[:] = 0.0
+        g = pats[d].s.ghost
+        pats[d].uold()[:, g:-g, g:-g] = 0.0
+    for s, d in restrict_items:
+        restrict(pats[int(s)], pats[int(d)], only_overlapped=True, swe=True)
+    for d in dsts:
+        lib().pco_swe_post_process_restriction(pats[d].ptr())
+
+
+def amr_step(pats, items, wall, leaf, flux_items, restrict_items, prm, max_dt, g_flux=1.0, flux=True,
+             n_threads=0):
+    """One synchronous step of an adaptive patch set on the oracle: ghost fill,
+    sweep and update of the leaves (grid_step), then computeFluxes of every
+    leaf and the flux-correction list (SolveTimestep.cpp:674-679), then the
+    restriction list.  Returns the dt."""
+    dt = grid_step(pats, items, wall, prm, max_dt, n_threads=n_threads)[0]
+    if flux and len(flux_items):
+        for p, lf in zip(pats, leaf):
+            if lf:
+                lib().pco_compute_fluxes(p.ptr(), g_flux)
+        for s, d, dim, direction in flux_items:
+            lib().pco_apply_flux_correction(pats[int(s)].ptr(), pats[int(d)].ptr(), int(dim), int(direction))
+    restrict_list(pats, restrict_items)
+    return dt

@@ -526,9 +526,10 @@ class LeafValues:
 class DeviceAmr:
     """Backend of `remesh` on a pcg.Context (and the grid's initial install)."""
 
-    def __init__(self, ctx, grid, b_of, flux=True, g_flux=1.0):
+    def __init__(self, ctx, grid, b_of, flux=True, g_flux=1.0, criterion=0):
         self.ctx, self.grid, self.b_of = ctx, grid, b_of
         self.flux, self.g_flux = flux, g_flux
+        self.criterion = criterion  # pcg_refinement_criterion kind
         self.pid = {}
         self._bounds = None   # (virtual?, lower, upper) last written, per patch id
         self._order_ids = None  # (grid slot arrays, patch ids in that order) at the last install
@@ -651,7 +652,7 @@ class DeviceAmr:
     def indicators(self):
         """The refinement criterion of every leaf, as a dict slot -> value."""
         leaves = self.grid.leaves()
-        vals = self.ctx.refinement_indicator([self.pid[s] for s in leaves])
+        vals = self.ctx.refinement_indicator([self.pid[s] for s in leaves], self.criterion)
         return dict(zip(leaves, vals))
 
     def indicator_arrays(self):
@@ -664,7 +665,7 @@ class DeviceAmr:
             ids = self._order_ids[1][~slots[3]]
         else:
             ids = [self.pid[s] for s in self.grid.leaves()]
-        return LeafValues(lv, ii, jj, self.ctx.refinement_indicator(ids))
+        return LeafValues(lv, ii, jj, self.ctx.refinement_indicator(ids, self.criterion))
 
     def remesh(self):
         import time

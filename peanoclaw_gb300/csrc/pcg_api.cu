@@ -1395,10 +1395,18 @@ int pcg_switch_to_leaf(pcg_context *c, int32_t id) {
 }
 
 int pcg_refinement_indicator(pcg_context *c, int32_t n, const int32_t *ids, double *out) {
+  return pcg_refinement_criterion(c, n, ids, PCG_CRIT_DEPTH_GRADIENT, out);
+}
+
+int pcg_refinement_criterion(pcg_context *c, int32_t n, const int32_t *ids, int32_t kind, double *out) {
   if (!c || n < 0 || (n > 0 && (!ids || !out))) return fail(PCG_E_INVALID, "bad arguments");
+  if (kind != PCG_CRIT_DEPTH_GRADIENT && kind != PCG_CRIT_SURFACE_DIFFERENCE && kind != PCG_CRIT_SURFACE_GRADIENT)
+    return fail(PCG_E_INVALID, "unknown refinement criterion " + std::to_string(kind));
   for (int32_t k = 0; k < n; k++) {
     if (!valid_id(c, ids[k])) return fail(PCG_E_INVALID, "unknown patch id " + std::to_string(ids[k]));
     if (c->h_patches[ids[k]].nq < 1) return fail(PCG_E_INVALID, "patch without unknowns");
+    if (kind != PCG_CRIT_DEPTH_GRADIENT && c->h_patches[ids[k]].np_w < 1)
+      return fail(PCG_E_INVALID, "the surface criteria need the bathymetry parameter");
   }
   if (n == 0) return PCG_OK;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -1410,7 +1418,7 @@ int pcg_refinement_indicator(pcg_context *c, int32_t n, const int32_t *ids, doub
   PCG_CUDA(cudaMalloc(&d_ids, sizeof(int) * n));
   cudaError_t e = cudaMalloc(&d_out, sizeof(double) * n);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_ids, ids, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = pcg::launch_refinement_indicator(c->stream, c->slab, c->d_patches, d_ids, n, d_out);
+  if (e == cudaSuccess) e = pcg::launch_refinement_indicator(c->stream, c->slab, c->d_patches, d_ids, n, kind, d_out);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   cudaFree(d_ids);

@@ -136,7 +136,7 @@ cudaError_t launch_gather_cells(cudaStream_t st, const double *slab, const Patch
 cudaError_t launch_switch_to_leaf(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, int pid);
 cudaError_t launch_refinement_indicator(cudaStream_t st, const double *slab, const PatchDev *patches,
-                                        const int *ids, int count, double *out);
+                                        const int *ids, int count, int kind, double *out);
 cudaError_t launch_clear_interior(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const int *ids, int count, const int *group_active = nullptr,
                                   const int *dirty = nullptr);

@@ -19,6 +19,9 @@ PCG_E_CUDA = -3
 PCG_E_TIMEOUT = -4
 PCG_E_STATE = -5
 PCG_E_NUMERIC = -6
+PCG_CRIT_DEPTH_GRADIENT = 0
+PCG_CRIT_SURFACE_DIFFERENCE = 1
+PCG_CRIT_SURFACE_GRADIENT = 2
 
 PCG_PATCH_LEAF = 1
 PCG_PATCH_VIRTUAL = 2
@@ -124,6 +127,7 @@ SIGNATURES = {
     "pcg_amr_layout": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _I2, _I2, _I2,
                                  C.POINTER(C.c_uint8), _I2, _I2, _I2, _I2, _I2, _I2, _D, _D, _I2]),
     "pcg_refinement_indicator": (C.c_int, [_CTX, C.c_int32, _I2, _D]),
+    "pcg_refinement_criterion": (C.c_int, [_CTX, C.c_int32, _I2, C.c_int32, _D]),
     "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
@@ -366,12 +370,15 @@ class Context:
     def switch_to_leaf(self, pid):
         check(lib().pcg_switch_to_leaf(self.h, int(pid)))
 
-    def refinement_indicator(self, ids):
+    def refinement_indicator(self, ids, kind=None):
+        """Refinement criterion of the listed patches (pcg_refinement_criterion;
+        default: the BreakingDam depth gradient)."""
         ids = np.ascontiguousarray(ids, dtype=np.int32)
         out = np.zeros(len(ids))
         if len(ids):
-            check(lib().pcg_refinement_indicator(self.h, len(ids), ids.ctypes.data_as(C.POINTER(C.c_int32)),
-                                                 dptr(out)))
+            k = PCG_CRIT_DEPTH_GRADIENT if kind is None else int(kind)
+            check(lib().pcg_refinement_criterion(self.h, len(ids), ids.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                 k, dptr(out)))
         return out
 
     def set_group_end_time(self, group, time, t_end):

@@ -403,3 +403,53 @@ def adaptive_tsunami(base=27, n=27, levels=3, hump=(0.5, 0.02, 0.4, 0.5), coast=
     ps.grid = grid
     ps.h_of, ps.b_of = h_of, b_of
     return ps
+
+
+def coastal_tsunami(base=27, n=27, levels=3, hump=(0.5, 0.02, 0.5, 0.5), seed_bathy=2000,
+                    coast=(0.95, 2.5), threshold=0.1, buffers=(1, 2)):
+    """Large adaptive tsunami: a Gaussian surface hump of amplitude A and
+    width s at (cx, cy) (hump = (A, s, cx, cy)) over a random seafloor, the
+    sum of 32 Gaussians of the uneven-patch generator (amplitudes in
+    [-0.5, 0.5], widths in [0.01, 0.1], seeded with `seed_bathy`), with a
+    coastline along x = 1: in the last 5 % of the domain (x > coast[0]) the
+    seafloor rises linearly by coast[1] at x = 1, above the still-water
+    surface 1.  h = max(0, 1 + A exp(-r^2 / (2 s^2)) - b), at rest, so the
+    dry land and any islands start dry.
+
+    Refinement follows the surface elevation h + b (pcg_refinement_criterion
+    kind PCG_CRIT_SURFACE_GRADIENT, the BreakingDam stencil and threshold on
+    the surface that BowlOcean's wave-front criterion differences): a still
+    lake over the bumpy seafloor stays coarse, the hump, the waves it sends
+    out and the coastline refine.  base = 27, n = 27, levels = 3 is an
+    effective 6561^2 grid (243^2 patches when fully refined)."""
+    from .amr import AmrGrid
+    from .pcg import PCG_CRIT_SURFACE_GRADIENT
+    A, s, cx, cy = hump
+    GA, GS, GC = gaussian_sum_bathymetry(seed_bathy)
+    x0, rise = coast
+
+    def b_of(X, Y):
+        return eval_bathymetry(X, Y, GA, GS, GC) + np.maximum(0.0, X - x0) * (rise / (1.0 - x0))
+
+    def h_of(X, Y):
+        eta = 1.0 + A * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2.0 * s * s))
+        return np.maximum(0.0, eta - b_of(X, Y))
+
+    def needs_refine(level, i, j):
+        m = base * 3 ** level
+        L = 1.0 / m
+        X, Y = _centers((i * L, j * L), (L, L), n, ghost=False)
+        q = h_of(X, Y) + b_of(X, Y)
+        dx = L / n
+        gx = (q[1:, :-1] - q[:-1, :-1]) / dx
+        gy = (q[:-1, 1:] - q[:-1, :-1]) / dx
+        return float(np.max(np.sqrt(np.abs(gx) * np.abs(gx) + np.abs(gy) * np.abs(gy)))) > threshold
+
+    grid = AmrGrid(base, n, levels, buffers=buffers, threshold=threshold)
+    grid.refine_from(needs_refine)
+    ps = amr_patchset(grid, h_of, b_of)
+    ps.grid = grid
+    ps.h_of, ps.b_of = h_of, b_of
+    ps.criterion = PCG_CRIT_SURFACE_GRADIENT
+    ps.meta["workload"] = ("coastal tsunami over a sum-of-Gaussians seafloor, " + ps.meta["workload"])
+    return ps

@@ -135,7 +135,7 @@ class _FakeCtx:
     def __init__(self):
         self.calls = []
 
-    def refinement_indicator(self, ids):
+    def refinement_indicator(self, ids, kind=None):
         ids = np.asarray(ids, dtype=np.int64)
         self.calls.append(("indicator", ids.copy()))
         return ids.astype(np.float64) / 1000.0

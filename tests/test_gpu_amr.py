@@ -48,3 +48,30 @@ def test_amr_step_bit_exact(mode):
     assert dts == odts
     assert np.all(np.isfinite(out))
     assert np.array_equal(out, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [P.PCG_MODE_BATCHED, P.PCG_MODE_PLAIN])
+def test_breaking_dam_full_size_bit_exact(mode):
+    """The adaptive configuration at its own size: 3 levels of 3x refinement,
+    27 x 27 cells per patch, 1,539 patches (1,377 leaves), interpolation, flux
+    correction and restriction every step; 5 steps bit for bit."""
+    ps = S.breaking_dam_amr(base=9, n=27, levels=3)
+    assert len(ps) == 1539
+    steps = 5
+    ctx = P.Context(slab_doubles=int(ps.packed.size * 1.3) + 4096, max_patches=len(ps) + 8,
+                    max_groups=1, params=PRM)
+    try:
+        ids = gpu_amr_patchset(ctx, ps)
+        ctx.restrict_all()
+        ctx.set_group_max_dt(0, 1e9)
+        dts = list(ctx.run(steps, mode)[:, 0])
+        out = ctx.download_many(ids, int(ps.packed.size))
+    finally:
+        ctx.close()
+    pats = oracle_amr_patchset(ps)
+    oracle_restrict_all(pats, ps)
+    odts = [oracle_amr_step(pats, ps, oracle_params(PRM), 1e9) for _ in range(steps)]
+    ref = np.concatenate([p.u for p in pats])
+    assert dts == odts
+    assert np.array_equal(out.view(np.int64), ref.view(np.int64))

@@ -1,20 +1,28 @@
-"""Full-size checks on the 50k-patch uneven mosaic (67.8 M cells) through
-size-independent properties: the warp-strip and the tile schedules (two
-independent work decompositions) give bit-identical states and dts, every
-value stays finite and the depth non-negative, and a device-side end time
-stops the run exactly."""
+"""Full-size checks on the 50k-patch uneven mosaic (224 x 224 slots, 67.8 M
+cells): three batched steps bit for bit against the oracle on the whole
+mosaic, the warp-strip and the tile schedules (two independent work
+decompositions) give bit-identical states and dts over six steps, every value
+stays finite and the depth non-negative, and a device-side end time stops the
+run exactly."""
 import numpy as np
 import pytest
 
 from peanoclaw_gb300 import pcg as P
 from peanoclaw_gb300 import scenarios as S
 
+from helpers import oracle_params, oracle_patchset
+
 pytestmark = pytest.mark.gpu
 
 PRM = P.swe_params(g=9.81, cfl=0.5)
 
 
-def _run(ps, sched, steps):
+@pytest.fixture(scope="module")
+def mosaic():
+    return S.uneven_patches(grid=224)
+
+
+def _run(ps, sched, steps, t_end=1e-3):
     slab = int(sum(P.vector_size(n) + 32 for n in ps.n)) + 4096
     c = P.Context(slab_doubles=slab, max_patches=len(ps) + 16, max_groups=1, params=PRM)
     try:
@@ -28,7 +36,7 @@ def _run(ps, sched, steps):
         c.set_ghost_items(S.remap_items(ps.items, ids))
         c.set_schedule(*sched)
         c.set_group_max_dt(0, np.inf)
-        c.set_group_end_time(0, 0.0, 1e-3)
+        c.set_group_end_time(0, 0.0, t_end)
         dts = c.run(steps, P.PCG_MODE_BATCHED)[:, 0]
         t = c.group_times()[0]
         return c.download_many(ids, int(ps.packed.size)), dts, t
@@ -36,8 +44,25 @@ def _run(ps, sched, steps):
         c.close()
 
 
-def test_schedules_agree_at_full_size():
-    ps = S.uneven_patches(grid=224)
+def test_full_mosaic_matches_the_oracle(mosaic):
+    """The headline workload itself, three steps, every patch vector (ghost
+    layers and signed zeros included) and every dt bit for bit."""
+    ps = mosaic
+    steps = 3
+    got, dts, _ = _run(ps, (P.SCHED_STRIPS, 2, 32), steps, t_end=np.inf)
+    pats = oracle_patchset(ps)
+    from oracle import oracle as O
+    odts = [O.grid_step(pats, ps.items, ps.wall, oracle_params(PRM), np.inf)[0] for _ in range(steps)]
+    assert list(dts) == odts
+    for p in range(0, len(ps), 4096):
+        assert np.array_equal(got[ps.offsets[p]:ps.offsets[p] + ps.vec_len(p)].view(np.int64),
+                              pats[p].u.view(np.int64)), p
+    ref = np.concatenate([p.u for p in pats])
+    assert np.array_equal(got.view(np.int64), ref.view(np.int64))
+
+
+def test_schedules_agree_at_full_size(mosaic):
+    ps = mosaic
     a, da, ta = _run(ps, (P.SCHED_STRIPS, 2, 32), 6)
     b, db, tb = _run(ps, (P.SCHED_TILES, 0, 32), 6)
     assert np.array_equal(da, db) and ta == tb

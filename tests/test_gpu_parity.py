@@ -167,6 +167,49 @@ def test_interpolation_reference_known_answers_on_gpu(ctx):
     ctx.free(fine.id)
 
 
+def test_restriction_to_virtual_patch_known_answers_on_gpu(ctx):
+    """GridLevelTransferTest.cpp:321-512 (values :495-501) through the CUDA
+    path: restriction of the fine leaf into the virtual patch, then the ghost
+    transfer from the virtual patch into its coarse neighbour (the set-up and
+    the time intervals of test_oracle_known_answers.test_restriction_to_virtual_patch);
+    every value bit-exact against the oracle and within 1e-13 of the
+    reference's expected value."""
+    from test_oracle_known_answers import (RESTR_EXPECTED, RESTR_NEIGHBOUR_TIME,
+                                           restriction_test_fine_values)
+    num = DefaultNumerics(ctx)
+    for (gx, gy), expected in RESTR_EXPECTED.items():
+        fine = Patch(ctx, 3, (1.0 / 3.0, 1.0 / 3.0), 1.0 / 3.0, level=1, ghost=2, unknowns=1,
+                     params_with_ghost=0)
+        virtual = Patch(ctx, 2, (0.0, 0.0), 1.0, ghost=2, unknowns=1, params_with_ghost=0, leaf=False,
+                        virtual=True)
+        nb = Patch(ctx, 2, (1.0, 0.0), 1.0, ghost=2, unknowns=1, params_with_ghost=0)
+        of = O.Patch(3, ghost=2, nq=1, np_wo=0, np_w=0, pos=(1.0 / 3.0, 1.0 / 3.0), size=1.0 / 3.0,
+                     level=1, time=0.0, dt=1.0)
+        for x, y, n, o in restriction_test_fine_values():
+            of.set_unew(x, y, 0, n)
+            of.set_uold(x, y, 0, o)
+        ov = O.Patch(2, ghost=2, nq=1, np_wo=0, np_w=0, pos=(0.0, 0.0), size=1.0, is_leaf=False,
+                     is_virtual=True)
+        t, dt = RESTR_NEIGHBOUR_TIME[(gx, gy)]
+        on = O.Patch(2, ghost=2, nq=1, np_wo=0, np_w=0, pos=(1.0, 0.0), size=1.0, time=t, dt=dt)
+        fine.upload(of.u)
+        fine.set_time_intervals(time=0.0, dt=1.0)
+        virtual.upload(np.zeros(virtual.vector_size))
+        nb.upload(np.zeros(nb.vector_size))
+        nb.set_time_intervals(time=t, dt=dt)
+        num.restrictSolution(fine, virtual, False)
+        num.transferGhostlayer((2, 2), (0, 0), (-2, 0), virtual, nb)
+        O.restrict(of, ov, only_overlapped=False, swe=False)
+        O.transfer_ghostlayer((2, 2), (0, 0), (-2, 0), ov, on)
+        assert _bit_equal(virtual.download(), ov.u)
+        got = nb.download()
+        assert _bit_equal(got, on.u)
+        uo = got[4:4 + 36].reshape(6, 6)
+        assert uo[gx + 2, gy + 2] == pytest.approx(expected, rel=1e-13, abs=1e-15)
+        for p in (fine, virtual, nb):
+            ctx.free(p.id)
+
+
 @pytest.mark.parametrize("only_overlapped", [0, 1])
 @pytest.mark.parametrize("swe", [0, 1])
 def test_restriction_bit_exact(ctx, only_overlapped, swe):

@@ -135,3 +135,24 @@ def test_batched_times_and_interpolations():
             ctx.set_times_many([coarse[0], coarse[0]], [0, 0], [0, 0], [0, 0])
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("kind", [P.PCG_CRIT_DEPTH_GRADIENT, P.PCG_CRIT_SURFACE_DIFFERENCE,
+                                  P.PCG_CRIT_SURFACE_GRADIENT])
+def test_refinement_criteria_match_the_oracle(kind):
+    """pcg_refinement_criterion of every kind on random wet/dry patches of
+    several sizes equals the oracle backend's criterion bit for bit."""
+    from helpers import oracle_criterion, oracle_patch_from, random_swe_vector
+    rng = np.random.default_rng(90 + kind)
+    ctx = P.Context(slab_doubles=2_000_000, max_patches=64, max_groups=1, params=PRM)
+    try:
+        for n, size in ((9, 1.0 / 9), (16, 0.05), (27, 1.0 / 81)):
+            vec = random_swe_vector(rng, n)
+            pid = ctx.alloc(n, pos=(0.0, 0.0), size=(size, size))
+            ctx.upload(pid, vec)
+            got = ctx.refinement_indicator([pid], kind)[0]
+            want = oracle_criterion(oracle_patch_from(vec, n, size=(size, size)), kind)
+            assert np.float64(got).view(np.int64) == np.float64(want).view(np.int64), (n, got, want)
+            ctx.free(pid)
+    finally:
+        ctx.close()

@@ -103,3 +103,59 @@ def test_partial_restriction_regions_with_infinite_lower_bounds():
     assert regs[1] == ((6, 0), (0, 6))
     assert regs[2] == ((0, 0), (6, 1))
     assert regs[3] == ((0, 6), (6, 0))
+
+
+# GridLevelTransferTest::testRestrictionToVirtualPatch (GridLevelTransferTest.cpp:321-512):
+# a fine leaf (3 x 3 cells, 1 unknown, ghost 2, at (1/3, 1/3), size 1/3) is
+# restricted into a virtual coarse patch (2 x 2 cells on [0,1]^2), whose values
+# then fill the ghost layer (width 2) of the coarse neighbour at (1, 0).
+# The expected values (:495-501) weigh the fine cells that overlap one virtual
+# cell by regionFraction * (1, 1/2, 1/2, 1/4) and combine each fine cell's
+# uNew n and uOld o as tf * n + (1 - tf) * o with tf = 2 for ghost cell (-2, 0)
+# and tf = 4/3 for (-2, 1), (-1, 0), (-1, 1).  In the reference those factors
+# come out of GridLevelTransfer::stepDown / stepUp (Peano vertices, the
+# virtual-patch life cycle, outside the path).  Here the fine interval is
+# [0, 1], so that DefaultRestriction's factors for the virtual times 0 and 1
+# are 0 and 1 (the virtual patch holds the restricted uOld and uNew), and the
+# neighbour's uNew time is the factor of the transfer from the virtual source
+# (DefaultTransfer.cpph:29-41): 2 (time 1, dt 1) or 4/3 (time 1, dt 1/3).
+RESTR_RF = (1.0 / 9.0) * (1.0 / 9.0) / (1.0 / 2.0) / (1.0 / 2.0)
+RESTR_EXPECTED = {
+    (-2, 0): RESTR_RF * (-1.0 * 9.0 + 1.0 / 2.0 * (2.0 - 1.0 * 8.0) + 1.0 / 2.0 * (2.0 * 3.0 - 1.0 * 6.0)
+                         + 1.0 / 4.0 * (2.0 * 4.0 - 1.0 * 5.0)),
+    (-2, 1): RESTR_RF * (4.0 / 3.0 * 2.0 - 1.0 / 3.0 * 7.0 + 1.0 / 2.0 * (4.0 / 3.0 - 1.0 / 3.0 * 8.0)
+                         + 1.0 / 2.0 * (4.0 / 3.0 * 5.0 - 1.0 / 3.0 * 4.0)
+                         + 1.0 / 4.0 * (4.0 / 3.0 * 4.0 - 1.0 / 3.0 * 5.0)),
+    (-1, 0): RESTR_RF * (4.0 / 3.0 * 6.0 - 1.0 / 3.0 * 3.0 + 1.0 / 2.0 * (4.0 / 3.0 * 3.0 - 1.0 / 3.0 * 6.0)
+                         + 1.0 / 2.0 * (4.0 / 3.0 * 7.0 - 1.0 / 3.0 * 2.0)
+                         + 1.0 / 4.0 * (4.0 / 3.0 * 4.0 - 1.0 / 3.0 * 5.0)),
+    (-1, 1): RESTR_RF * (4.0 / 3.0 * 8.0 - 1.0 / 3.0 + 1.0 / 2.0 * (4.0 / 3.0 * 5.0 - 1.0 / 3.0 * 4.0)
+                         + 1.0 / 2.0 * (4.0 / 3.0 * 7.0 - 1.0 / 3.0 * 2.0)
+                         + 1.0 / 4.0 * (4.0 / 3.0 * 4.0 - 1.0 / 3.0 * 5.0)),
+}
+# neighbour time intervals (time, dt) giving the transfer factor of each check
+RESTR_NEIGHBOUR_TIME = {(-2, 0): (1.0, 1.0), (-2, 1): (1.0, 1.0 / 3.0), (-1, 0): (1.0, 1.0 / 3.0),
+                        (-1, 1): (1.0, 1.0 / 3.0)}
+
+
+def restriction_test_fine_values():
+    """uNew (x, y) = 3x + y and uOld (x, y) = 9 - (3x + y), :396-431."""
+    return [(x, y, 3.0 * x + y, 9.0 - (3.0 * x + y)) for x in range(3) for y in range(3)]
+
+
+def test_restriction_to_virtual_patch():
+    """GridLevelTransferTest.cpp:321-512 (values :495-501) on the oracle."""
+    for (gx, gy), expected in RESTR_EXPECTED.items():
+        fine = O.Patch(3, ghost=2, nq=1, np_wo=0, np_w=0, pos=(1.0 / 3.0, 1.0 / 3.0), size=1.0 / 3.0,
+                       level=1, time=0.0, dt=1.0)
+        for x, y, n, o in restriction_test_fine_values():
+            fine.set_unew(x, y, 0, n)
+            fine.set_uold(x, y, 0, o)
+        virtual = O.Patch(2, ghost=2, nq=1, np_wo=0, np_w=0, pos=(0.0, 0.0), size=1.0, level=0,
+                          is_leaf=False, is_virtual=True)
+        O.restrict(fine, virtual, only_overlapped=False, swe=False)
+        t, dt = RESTR_NEIGHBOUR_TIME[(gx, gy)]
+        neighbour = O.Patch(2, ghost=2, nq=1, np_wo=0, np_w=0, pos=(1.0, 0.0), size=1.0, level=0,
+                            time=t, dt=dt)
+        O.transfer_ghostlayer((2, 2), (0, 0), (-2, 0), virtual, neighbour)
+        assert neighbour.get_uold(gx, gy) == pytest.approx(expected, rel=1e-13, abs=1e-15)
