@@ -577,6 +577,7 @@ def main():
         tuned = ctx.autotune(reps=2)
         ctx.run(2, P.PCG_MODE_BATCHED)
     sched = ctx.get_schedule()
+    fused = ctx.step_is_fused(P.PCG_MODE_BATCHED)
     dist_barrier(dist)
     ctx.synchronize()
     clocks = ClockSampler(local)
@@ -708,7 +709,9 @@ def main():
                          "update": ph[4]},
             "schedule": {"kind": "tiles" if sched[0] == P.SCHED_TILES else "strips",
                          "variant": sched[1], "chunk": sched[2],
-                         "autotune_ms_per_step": ({"%s/%d/%d" % ("tiles" if k[0] == 0 else "strips", k[1], k[2]): m
+                         "form": "unfused" if sched[3] or not fused else "fused",
+                         "autotune_ms_per_step": ({"%s/%d/%d%s" % ("tiles" if k[0] == 0 else "strips", k[1], k[2],
+                                                                 "/unfused" if k[3] else ""): m
                                                    for k, m in tuned} if tuned else None)},
             "parity": parity,
             "plain_per_patch_value": plain,

@@ -102,8 +102,8 @@ typedef struct pcg_ghost_item {
 #define PCG_GHOST_INTERP 1
 
 /* Execution forms of a synchronous grid step. */
-#define PCG_MODE_PLAIN 0    /* one launch per patch for fill, sweep and update */
-#define PCG_MODE_BATCHED 1  /* batched fill + persistent sweep + update, one set per step */
+#define PCG_MODE_PLAIN 0    /* one launch per patch (per phase in the unfused step form) */
+#define PCG_MODE_BATCHED 1  /* all patches in shared launches, replayed from a CUDA graph */
 
 /* ---------------------------------------------------------------- context */
 
@@ -301,6 +301,26 @@ int pcg_step(pcg_context *ctx, int32_t mode, double *dt_out);
 /* `steps` synchronous steps; BATCHED mode replays a captured CUDA graph.  The
  * dt of every step and group is written to dt_hist[steps * max_groups] (may be NULL). */
 int pcg_run(pcg_context *ctx, int32_t steps, int32_t mode, double *dt_hist);
+/* No counterpart in the reference (its block applies the update right after
+ * the sweep).  Step forms of pcg_step / pcg_run:
+ *   PCG_FORM_AUTO (default): the fused form wherever it applies -- the
+ *     synchronous step without restriction or flux-correction lists, every
+ *     ghost item between leaves with one ghost layer, and (BATCHED) the
+ *     warp-strip schedule.  One kernel per step fills each strip's ghost
+ *     cells from its neighbours, applies the previous step's update to every
+ *     cell it reads, sweeps and reduces the CFL dt; two small launches
+ *     advance the time intervals and prepare the next step (the PLAIN form:
+ *     the fused kernel once per patch).  The update of the last step stays
+ *     pending in device memory until a call that reads or changes patch data,
+ *     lists or parameters applies it, so the reference layout a download
+ *     returns is the same as after unfused steps, bit for bit.
+ *   PCG_FORM_UNFUSED: separate launches for ghost fill, walls, sweep and update.
+ * The form never changes results. */
+#define PCG_FORM_AUTO 0
+#define PCG_FORM_UNFUSED 1
+int pcg_set_step_form(pcg_context *ctx, int32_t form);
+/* *fused = 1 if a step of `mode` takes the fused form with the current lists. */
+int pcg_get_step_form(pcg_context *ctx, int32_t mode, int32_t *fused);
 /* Cumulative interior cell updates and device time of pcg_step / pcg_run;
  * under local time stepping the cells of the leaves that advanced. */
 int pcg_stats(pcg_context *ctx, int64_t *cell_updates, double *device_ms);
@@ -359,7 +379,7 @@ typedef struct pcg_schedule {
   int32_t kind;
   int32_t variant;
   int32_t chunk;
-  int32_t reserved_;
+  int32_t unfused;   /* strips: 1 = the unfused step form even where the fused one applies */
 } pcg_schedule;
 #define PCG_SCHED_TILES 0
 #define PCG_SCHED_STRIPS 1
@@ -367,7 +387,8 @@ typedef struct pcg_schedule {
 int pcg_set_schedule(pcg_context *ctx, const pcg_schedule *s);
 int pcg_get_schedule(pcg_context *ctx, pcg_schedule *s);
 /* Autotuner: runs `reps` BATCHED steps with each candidate schedule (tiles;
- * strips x 5 variants x chunk 32 / 16), times each candidate's steps with
+ * strips x 5 variants x chunk 32 / 16, in the fused step form where it
+ * applies; then the fastest strip schedule in the unfused form), times each candidate's steps with
  * CUDA events, keeps the fastest for this context and caches it for the
  * process under the key (SM count, histogram of leaf patch shapes), so later
  * contexts with the same patch mix start with it.  The simulation advances by
@@ -381,7 +402,10 @@ int pcg_autotune(pcg_context *ctx, int32_t reps, pcg_schedule *tried, double *ms
 
 /* No counterpart in the reference.  One BATCHED step with CUDA events between
  * its phases on the context stream; ms[5] receives the device time of
- * reset, ghost items, walls, sweep and update. */
+ * reset, ghost items, walls, sweep and update.  In the fused form the ghost
+ * fill, walls and update are inside the sweep launch: ms[1] = ms[2] = 0,
+ * ms[3] is the fused kernel, ms[4] the time advance, ms[0] the reset and
+ * item factors of the next step. */
 int pcg_profile_step(pcg_context *ctx, double *ms);
 /* No counterpart in the reference.  Measures the FP64 FMA throughput of the
  * context's device (dependent-chain loop on every SM); returns TFLOP/s with an

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libpcg.so")
-SOURCES = ["pcg_kernels.cu", "pcg_strips.cu", "pcg_api.cu", "pcg_amr.cpp"]
+SOURCES = ["pcg_kernels.cu", "pcg_strips.cu", "pcg_fused.cu", "pcg_api.cu", "pcg_amr.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
          "-Xptxas", "-warn-spills"]

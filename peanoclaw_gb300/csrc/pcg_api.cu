@@ -254,6 +254,40 @@ struct pcg_context {
   long long *d_copy_meta = nullptr;
   size_t copy_meta_cap = 0;
 
+  // fused batched step (pcg_fused.cu): the step form (pcg_set_step_form);
+  // whether the ghost list suits it (leaf sources, ring destinations, copies
+  // from interiors); a group may hold a pending update (the reference layout
+  // is stale until settle()); the next step's reset and item factors are
+  // done; the form of the captured step graph
+  int form = PCG_FORM_AUTO;
+  bool fused_lists_ok = false;
+  bool fused_pending = false;
+  bool fused_ready = false;
+  bool graph_fused = false;
+  // second state set of every leaf (6 nx ny doubles at PatchDev::sh_off)
+  double *d_shadow = nullptr;
+  size_t shadow_cap = 0;
+  int64_t shadow_need = 0;
+  // per group: update pending, set written last, dt of the pending update
+  int *d_pend = nullptr, *d_par = nullptr;
+  unsigned long long *d_dt_prev = nullptr;
+  // face / corner ghost tables and their evaluation plans
+  std::vector<int> h_face_begin;
+  int *d_face_begin = nullptr, *d_face = nullptr, *d_corner = nullptr;
+  size_t d_face_cap = 0;
+  pcg::FusedCopyDev *d_fcopies = nullptr;
+  size_t d_fcopies_cap = 0;
+  pcg::FusedInterpDev *d_finterps = nullptr;
+  size_t d_finterps_cap = 0;
+  int fused_grid = 0;
+  // plain form of the fused step: strips of one patch per item, ranges per patch
+  std::vector<pcg::StripItem> h_pitems;
+  std::vector<pcg::StripGroup> h_pgroups;
+  std::vector<int> pitem_first, pitem_count;
+  pcg::StripItem *d_pitems = nullptr;
+  pcg::StripGroup *d_pgroups = nullptr;
+  size_t d_pitems_cap = 0, d_pgroups_cap = 0;
+
   int64_t cell_updates = 0;
   double device_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -421,7 +455,106 @@ int apply_schedule(pcg_context *c) {
   if (upd_sm < 1) upd_sm = 1;
   c->update_grid = (int)std::min<int64_t>((int64_t)c->num_sms * upd_sm,
                                           std::max<int64_t>(1, ((int64_t)c->h_sitems.size() + 7) / 8));
+  int fused_sm = 0;
+  PCG_CUDA(pcg::fused_occupancy(v, &fused_sm));
+  if (fused_sm < 1) fused_sm = 1;
+  c->fused_grid = (int)std::min<int64_t>((int64_t)c->num_sms * fused_sm, need);
   c->graph_valid = false;
+  return PCG_OK;
+}
+
+// Strips of one patch per item (the plain form of the fused step: one launch
+// per patch), the strip cut of build_strips with 32-column chunks.
+void build_patch_strips(pcg_context *c) {
+  c->h_pitems.clear();
+  c->h_pgroups.clear();
+  c->pitem_first.assign(c->max_patches, 0);
+  c->pitem_count.assign(c->max_patches, 0);
+  for (int p : c->leaf_ids) {
+    const pcg::PatchDev &P = c->h_patches[p];
+    c->pitem_first[p] = (int)c->h_pitems.size();
+    const int nsy = (P.ny + 31) / 32;
+    for (int ky = 0; ky < nsy; ky++) {
+      const int y0 = (int)((int64_t)ky * P.ny / nsy), y1 = (int)((int64_t)(ky + 1) * P.ny / nsy);
+      const int nsx = (P.nx + 31) / 32;
+      for (int kx = 0; kx < nsx; kx++) {
+        const int x0 = (int)((int64_t)kx * P.nx / nsx), x1 = (int)((int64_t)(kx + 1) * P.nx / nsx);
+        pcg::StripItem it;
+        it.g0 = (int)c->h_pgroups.size();
+        it.ngroups = 1;
+        it.hs = (unsigned char)(y1 - y0);
+        it.w = (unsigned char)(x1 - x0);
+        it.pad_ = 0;
+        c->h_pgroups.push_back(pcg::StripGroup{p, (short)x0, (short)y0});
+        c->h_pitems.push_back(it);
+      }
+    }
+    c->pitem_count[p] = (int)c->h_pitems.size() - c->pitem_first[p];
+  }
+}
+
+// Whether the ghost list suits the fused step: every item joins two leaves
+// with one ghost layer and three unknowns, writes only ghost-layer cells of
+// its destination, and a copy reads only interior cells of its source.
+bool fused_lists_fit(pcg_context *c) {
+  for (const pcg::GhostItemDev &it : c->h_items) {
+    const pcg::PatchDev &S = c->h_patches[it.src], &D = c->h_patches[it.dst];
+    if (!(S.flags & pcg::kFlagLeaf) || (S.flags & pcg::kFlagVirtual) || !(D.flags & pcg::kFlagLeaf)) return false;
+    if (S.group != D.group) return false;
+    if (S.g != 1 || D.g != 1 || S.nq != 3 || D.nq != 3 || S.np_w < 1 || D.np_w < 1) return false;
+    if (it.size[0] < 1 || it.size[1] < 1) return false;
+    const int x0 = it.dst_off[0], x1 = it.dst_off[0] + it.size[0];
+    const int y0 = it.dst_off[1], y1 = it.dst_off[1] + it.size[1];
+    if (x0 < -1 || x1 > D.nx + 1 || y0 < -1 || y1 > D.ny + 1) return false;
+    const bool x_in = x0 < D.nx && x1 > 0, y_in = y0 < D.ny && y1 > 0;
+    if (x_in && y_in) return false;
+    if (it.kind == PCG_GHOST_COPY) {
+      if (it.src_off[0] < 0 || it.src_off[1] < 0 || it.src_off[0] + it.size[0] > S.nx ||
+          it.src_off[1] + it.size[1] > S.ny)
+        return false;
+    }
+  }
+  return true;
+}
+
+// Face / corner tables of the fused step, the shadow offsets of the leaves
+// and the per-patch strip lists (after the ghost-cell list and the
+// interpolation plan are on the device).
+int build_fused_tables(pcg_context *c) {
+  c->fused_lists_ok = fused_lists_fit(c);
+  c->h_face_begin.assign(c->max_patches, 0);
+  int64_t nf = 0, sh = 0;
+  for (int p : c->leaf_ids) {
+    pcg::PatchDev &P = c->h_patches[p];
+    c->h_face_begin[p] = (int)nf;
+    P.face_begin = (int)std::min<int64_t>(nf, INT32_MAX);
+    nf += 2LL * (P.nx + P.ny);
+    P.sh_off = sh;
+    sh += (6LL * P.nx * P.ny + kAlign - 1) / kAlign * kAlign;
+  }
+  if (nf > INT32_MAX) return fail(PCG_E_INVALID, "too many ghost-layer face cells for the fused step");
+  c->shadow_need = sh;
+  int rc;
+  if ((rc = ensure_device(c, &c->d_face, &c->d_face_cap, (size_t)nf)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_fcopies, &c->d_fcopies_cap, (size_t)c->n_copy_cells)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_finterps, &c->d_finterps_cap, (size_t)c->n_interp_cells)) != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(c->d_face_begin, c->h_face_begin.data(), sizeof(int) * c->max_patches,
+                           cudaMemcpyHostToDevice, c->stream));
+  if (nf) PCG_CUDA(cudaMemsetAsync(c->d_face, 0xFF, sizeof(int) * (size_t)nf, c->stream));
+  PCG_CUDA(cudaMemsetAsync(c->d_corner, 0xFF, sizeof(int) * 4 * (size_t)c->max_patches, c->stream));
+  if (c->fused_lists_ok)
+    PCG_CUDA(pcg::launch_build_fused_ghosts(c->stream, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
+                                            c->n_interp_cells, c->d_plan, c->d_face_begin, c->d_face, c->d_corner,
+                                            c->d_fcopies, c->d_finterps));
+  build_patch_strips(c);
+  if ((rc = ensure_device(c, &c->d_pitems, &c->d_pitems_cap, c->h_pitems.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_pgroups, &c->d_pgroups_cap, c->h_pgroups.size())) != PCG_OK) return rc;
+  if (!c->h_pitems.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_pitems, c->h_pitems.data(), sizeof(pcg::StripItem) * c->h_pitems.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+  if (!c->h_pgroups.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_pgroups, c->h_pgroups.data(), sizeof(pcg::StripGroup) * c->h_pgroups.size(),
+                             cudaMemcpyHostToDevice, c->stream));
   return PCG_OK;
 }
 
@@ -572,6 +705,7 @@ int rebuild_topology(pcg_context *c) {
                                          c->n_interp_cells, c->d_plan));
   PCG_CUDA(pcg::launch_build_copy_plan(c->stream, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
                                        c->d_copy_plan));
+  if ((rc = build_fused_tables(c)) != PCG_OK) return rc;
   int per_sm = 0;
   PCG_CUDA(pcg::sweep_occupancy(&per_sm));
   if (per_sm < 1) per_sm = 1;
@@ -738,6 +872,125 @@ int enqueue_step(pcg_context *c, int mode, bool advance = true) {
   return PCG_OK;
 }
 
+// ---- fused step
+
+pcg::FusedDev fused_dev(pcg_context *c) {
+  pcg::FusedDev F;
+  F.slab = c->slab;
+  F.shadow = c->d_shadow;
+  F.patches = c->d_patches;
+  F.pend = c->d_pend;
+  F.par = c->d_par;
+  F.active = c->d_group_active;
+  F.dt_prev = c->d_dt_prev;
+  F.face_begin = c->d_face_begin;
+  F.face = c->d_face;
+  F.corner = c->d_corner;
+  F.copies = c->d_fcopies;
+  F.interps = c->d_finterps;
+  F.item_step = c->d_item_step;
+  F.prm = c->prm;
+  return F;
+}
+
+// Whether a step of `mode` takes the fused form (after rebuild_topology).
+bool use_fused(pcg_context *c, int mode) {
+  if (c->form == PCG_FORM_UNFUSED || (mode == PCG_MODE_BATCHED && c->sched.unfused)) return false;
+  return c->fused_lists_ok && !c->ts_local && c->h_restr.empty() && c->h_flux.empty() && !c->leaf_ids.empty() &&
+         (mode == PCG_MODE_PLAIN || c->sched.kind == PCG_SCHED_STRIPS);
+}
+
+// Back to the reference layout: every group with a pending update gets it
+// applied (uNew, uOld interior) and its walls filled from the previous state;
+// called by every entry point that reads or changes patch data, lists or
+// parameters.  The next fused step then starts with its own reset.
+int settle(pcg_context *c) {
+  c->fused_ready = false;
+  if (!c->fused_pending) return PCG_OK;
+  PCG_CUDA(cudaSetDevice(c->device));
+  const pcg::FusedDev F = fused_dev(c);
+  PCG_CUDA(pcg::launch_fused_flush(c->stream, F, c->d_leaf_ids, (int)c->leaf_ids.size()));
+  PCG_CUDA(pcg::launch_walls(c->stream, c->slab, c->d_patches, c->d_wall, (int)c->h_wall.size(), c->d_pend,
+                             nullptr, 0));
+  PCG_CUDA(cudaMemsetAsync(c->d_pend, 0, sizeof(int) * c->max_groups, c->stream));
+  c->fused_pending = false;
+  c->fin_dirty = true;
+  return PCG_OK;
+}
+
+#define PCG_SETTLE(c)                          \
+  do {                                         \
+    int src_ = settle(c);                      \
+    if (src_ != PCG_OK) return src_;           \
+  } while (0)
+
+int ensure_shadow(pcg_context *c) {
+  if (c->d_shadow && (int64_t)c->shadow_cap >= c->shadow_need) return PCG_OK;
+  if (c->d_shadow) PCG_CUDA(cudaFree(c->d_shadow));
+  c->d_shadow = nullptr;
+  c->shadow_cap = 0;
+  const size_t n = (size_t)std::max<int64_t>(c->shadow_need, kAlign);
+  cudaError_t e = cudaMalloc(&c->d_shadow, sizeof(double) * n);
+  if (e != cudaSuccess) {
+    c->d_shadow = nullptr;
+    return fail(e == cudaErrorMemoryAllocation ? PCG_E_NOMEM : PCG_E_CUDA,
+                std::string("fused step state buffer: ") + cudaGetErrorString(e));
+  }
+  c->shadow_cap = n;
+  return PCG_OK;
+}
+
+// The reset and per-item time factors that start a step.
+int enqueue_reset_items(pcg_context *c) {
+  PCG_CUDA(pcg::launch_reset_items(c->stream, c->max_groups, c->d_group_max_dt, c->d_group_t_end, c->d_group_time,
+                                   c->d_group_dt, c->d_group_active, c->max_patches, c->d_patch_smax, c->d_patches,
+                                   c->d_times, c->d_items, (int)c->h_items.size(), c->d_item_step));
+  return PCG_OK;
+}
+
+// One fused step: the fused sweep (one launch, or one per patch in the plain
+// form), the time advance with the dt record, and the reset and item factors
+// of the next step (three launches in the batched form; capturable).
+int enqueue_fused_step(pcg_context *c, int mode) {
+  const pcg::FusedDev F = fused_dev(c);
+  if (mode == PCG_MODE_BATCHED) {
+    PCG_CUDA(pcg::launch_fused_strips(c->stream, c->sched.variant, c->fused_grid, F, c->d_sitems, c->d_sgroups,
+                                      (int)c->h_sitems.size(), c->d_patch_smax, c->d_group_dt));
+  } else {
+    for (int p : c->leaf_ids) {
+      const int n = c->pitem_count[p];
+      PCG_CUDA(pcg::launch_fused_strips(c->stream, 2, (n + 7) / 8, F, c->d_pitems + c->pitem_first[p],
+                                        c->d_pgroups, n, c->d_patch_smax, c->d_group_dt));
+    }
+  }
+  PCG_CUDA(pcg::launch_fused_advance(c->stream, F, c->d_leaf_ids, (int)c->leaf_ids.size(), c->d_times,
+                                     c->d_patch_smax, c->max_groups, c->d_group_dt, c->d_group_time, c->d_pend,
+                                     c->d_par, c->d_dt_prev, c->d_hist, c->d_counter, c->hist_cap));
+  return enqueue_reset_items(c);
+}
+
+// Before fused steps: the state buffer and, unless the previous fused step
+// left it done, the reset of the first step.
+int fused_prologue(pcg_context *c) {
+  int rc = ensure_shadow(c);
+  if (rc != PCG_OK) return rc;
+  if (!c->fused_ready) {
+    if ((rc = enqueue_reset_items(c)) != PCG_OK) return rc;
+    c->fused_ready = true;
+  }
+  return PCG_OK;
+}
+
+int ensure_hist(pcg_context *c, int steps) {
+  if (steps <= c->hist_cap) return PCG_OK;
+  if (c->d_hist) PCG_CUDA(cudaFree(c->d_hist));
+  c->d_hist = nullptr;
+  PCG_CUDA(cudaMalloc(&c->d_hist, sizeof(double) * (size_t)steps * c->max_groups));
+  c->hist_cap = steps;
+  c->graph_valid = false;
+  return PCG_OK;
+}
+
 int ensure_staging(pcg_context *c, size_t doubles, size_t metas) {
   int rc;
   if ((rc = ensure_device(c, &c->d_staging, &c->staging_cap, doubles)) != PCG_OK) return rc;
@@ -866,6 +1119,14 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
     CREATE_CK(cudaMemcpy(c->d_group_time, zero.data(), sizeof(double) * c->max_groups, cudaMemcpyHostToDevice));
     CREATE_CK(cudaMemset(c->d_group_active, 0, sizeof(int) * c->max_groups));
   }
+  CREATE_CK(cudaMalloc(&c->d_pend, sizeof(int) * c->max_groups));
+  CREATE_CK(cudaMemset(c->d_pend, 0, sizeof(int) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_par, sizeof(int) * c->max_groups));
+  CREATE_CK(cudaMemset(c->d_par, 0, sizeof(int) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_dt_prev, sizeof(unsigned long long) * c->max_groups));
+  CREATE_CK(cudaMemset(c->d_dt_prev, 0, sizeof(unsigned long long) * c->max_groups));
+  CREATE_CK(cudaMalloc(&c->d_face_begin, sizeof(int) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_corner, sizeof(int) * 4 * (size_t)c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_dt_out, sizeof(double) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_solve_out, sizeof(double) * 2));
   CREATE_CK(cudaMalloc(&c->d_counter, sizeof(int)));
@@ -924,6 +1185,17 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_counter);
   cudaFree(c->d_staging);
   cudaFree(c->d_copy_meta);
+  cudaFree(c->d_shadow);
+  cudaFree(c->d_pend);
+  cudaFree(c->d_par);
+  cudaFree(c->d_dt_prev);
+  cudaFree(c->d_face_begin);
+  cudaFree(c->d_face);
+  cudaFree(c->d_corner);
+  cudaFree(c->d_fcopies);
+  cudaFree(c->d_finterps);
+  cudaFree(c->d_pitems);
+  cudaFree(c->d_pgroups);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -944,6 +1216,7 @@ int pcg_slab_info(pcg_context *c, int64_t *free_doubles, int64_t *total_doubles)
 int pcg_set_params(pcg_context *c, const pcg_swe_params *p) {
   if (!c || !p) return fail(PCG_E_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->prm = {p->g, p->cfl, p->dry_tol, p->dry_tol_update, p->s_min, p->dt_inf};
   c->graph_valid = false;
   return PCG_OK;
@@ -955,6 +1228,7 @@ int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
     return fail(PCG_E_INVALID, "invalid patch shape");
   if (!(d->size[0] > 0.0) || !(d->size[1] > 0.0)) return fail(PCG_E_INVALID, "patch size must be positive");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int slot = -1;
   for (int k = 0; k < c->max_patches; k++) {
@@ -992,6 +1266,7 @@ int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
 int pcg_patch_free(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   slab_free(c, c->h_patches[id].off, c->h_len[id]);
@@ -1005,6 +1280,8 @@ int pcg_patch_free(pcg_context *c, int32_t id) {
 int pcg_patch_upload(pcg_context *c, int32_t id, const double *vec, int64_t n) {
   if (!valid_id(c, id) || !vec) return fail(PCG_E_INVALID, "unknown patch id or null vector");
   if (n != c->h_len[id]) return fail(PCG_E_INVALID, "vector length does not match the patch layout");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   PCG_CUDA(cudaMemcpyAsync(c->slab + c->h_patches[id].off, vec, sizeof(double) * n,
                            cudaMemcpyHostToDevice, c->stream));
@@ -1015,6 +1292,8 @@ int pcg_patch_upload(pcg_context *c, int32_t id, const double *vec, int64_t n) {
 int pcg_patch_download(pcg_context *c, int32_t id, double *vec, int64_t n) {
   if (!valid_id(c, id) || !vec) return fail(PCG_E_INVALID, "unknown patch id or null vector");
   if (n != c->h_len[id]) return fail(PCG_E_INVALID, "vector length does not match the patch layout");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   PCG_CUDA(cudaMemcpyAsync(vec, c->slab + c->h_patches[id].off, sizeof(double) * n,
                            cudaMemcpyDeviceToHost, c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
@@ -1024,6 +1303,7 @@ int pcg_patch_download(pcg_context *c, int32_t id, double *vec, int64_t n) {
 int pcg_patches_upload(pcg_context *c, int32_t n, const int32_t *ids, const double *vecs) {
   if (!c || (n > 0 && (!ids || !vecs))) return fail(PCG_E_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   return multi_copy(c, n, ids, const_cast<double *>(vecs), true);
 }
@@ -1031,12 +1311,14 @@ int pcg_patches_upload(pcg_context *c, int32_t n, const int32_t *ids, const doub
 int pcg_patches_download(pcg_context *c, int32_t n, const int32_t *ids, double *vecs) {
   if (!c || (n > 0 && (!ids || !vecs))) return fail(PCG_E_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   return multi_copy(c, n, ids, vecs, false);
 }
 
 int pcg_patch_set_desc_flags(pcg_context *c, int32_t id, int32_t flags) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   c->h_patches[id].flags = flags;
   c->patches_dirty = c->topo_dirty = true;
@@ -1045,6 +1327,8 @@ int pcg_patch_set_desc_flags(pcg_context *c, int32_t id, int32_t flags) {
 
 int pcg_patch_set_time(pcg_context *c, int32_t id, const pcg_patch_time *t) {
   if (!valid_id(c, id) || !t) return fail(PCG_E_INVALID, "unknown patch id or null time");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   pcg::PatchTimeDev d{};
   d.time = t->time; d.dt = t->dt; d.est_next = t->est_next;
   d.min_nb_time = t->min_neighbor_time; d.max_nb_dt = t->max_neighbor_dt;
@@ -1071,6 +1355,7 @@ int pcg_patch_set_boundary(pcg_context *c, int32_t id, uint32_t wall_mask) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   if (wall_mask > 15u) return fail(PCG_E_INVALID, "wall mask has 4 bits in 2D");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->h_patches[id].wall = (int)wall_mask;
   c->patches_dirty = c->topo_dirty = true;
   return PCG_OK;
@@ -1080,8 +1365,9 @@ int pcg_patch_set_group(pcg_context *c, int32_t id, int32_t group) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   if (group < 0 || group >= c->max_groups) return fail(PCG_E_INVALID, "group out of range");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->h_patches[id].group = group;
-  c->patches_dirty = true;
+  c->patches_dirty = c->topo_dirty = true;
   c->graph_valid = false;
   return PCG_OK;
 }
@@ -1091,6 +1377,7 @@ int pcg_patch_set_group(pcg_context *c, int32_t id, int32_t group) {
 int pcg_copy_unew_to_uold(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1104,6 +1391,7 @@ int pcg_fill_boundary_layer(pcg_context *c, int32_t id, int32_t dimension, int32
   if (c->h_patches[id].g != 1 || c->h_patches[id].nq < 3)
     return fail(PCG_E_INVALID, "SWE wall boundary needs ghost width 1 and 3 unknowns");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1119,6 +1407,7 @@ int pcg_solve_timestep(pcg_context *c, int32_t id, double max_dt, double *dt_use
   size_t smem = pcg::solve_patch_smem(P.nx, P.ny);
   if (smem > 190 * 1024) return fail(PCG_E_INVALID, "patch too large for the fused per-patch solve");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1143,6 +1432,7 @@ int pcg_transfer_ghostlayer(pcg_context *c, const int32_t size[2], const int32_t
   if (!region_inside(S, so, size, false) || !region_inside(D, dof, size, true))
     return fail(PCG_E_INVALID, "transfer region outside the patches");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1161,6 +1451,7 @@ int pcg_interpolate_solution(pcg_context *c, const int32_t size[2], const int32_
   if (!region_inside(D, dof, size, to_uold != 0)) return fail(PCG_E_INVALID, "region outside the destination");
   if (swe && (S.np_w < 1 || D.np_w < 1)) return fail(PCG_E_INVALID, "SWE interpolation needs the bathymetry parameter");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1194,6 +1485,7 @@ int pcg_interpolate_solution_many(pcg_context *c, int32_t n, const int32_t *src,
   for (int32_t k = 0; k < n; k++)
     if (seen[src[k]]) return fail(PCG_E_INVALID, "a destination is also a source");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = upload_patches(c);
@@ -1213,6 +1505,7 @@ int pcg_patches_set_time(pcg_context *c, int32_t n, const int32_t *ids, const pc
   if (!c || n < 0 || (n > 0 && (!ids || !in))) return fail(PCG_E_INVALID, "bad arguments");
   if (n == 0) return PCG_OK;
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   std::vector<char> seen(c->max_patches, 0);
   std::vector<long long> meta(n);
   std::vector<pcg::PatchTimeDev> rec(n);
@@ -1247,6 +1540,7 @@ int pcg_restrict_solution(pcg_context *c, int32_t src, int32_t dst, int32_t only
   if (S.nq != D.nq) return fail(PCG_E_INVALID, "unknowns per subcell differ");
   if (swe && S.np_w < 1) return fail(PCG_E_INVALID, "SWE restriction needs the bathymetry parameter");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1258,6 +1552,7 @@ int pcg_post_process_restriction(pcg_context *c, int32_t dst) {
   if (!valid_id(c, dst)) return fail(PCG_E_INVALID, "unknown patch id");
   if (c->h_patches[dst].np_w < 1) return fail(PCG_E_INVALID, "needs the bathymetry parameter");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1276,6 +1571,7 @@ int pcg_post_process_restriction(pcg_context *c, int32_t dst) {
 int pcg_clear_subgrid(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1303,6 +1599,7 @@ int pcg_gather_cells(pcg_context *c, int32_t n, const int32_t *ids, double *out,
   if (total != out_len) return fail(PCG_E_INVALID, "out_len must be " + std::to_string(total));
   if (n == 0) return PCG_OK;
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1353,6 +1650,7 @@ int pcg_patches_set_restriction_bounds(pcg_context *c, int32_t n, const int32_t 
   if (!c || n < 0 || (n > 0 && (!ids || !lower || !upper))) return fail(PCG_E_INVALID, "bad arguments");
   if (n == 0) return PCG_OK;
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   std::vector<char> seen(c->max_patches, 0);
   std::vector<long long> meta(n);
   std::vector<double> b(4 * (size_t)n);
@@ -1380,6 +1678,7 @@ int pcg_patches_set_restriction_bounds(pcg_context *c, int32_t n, const int32_t 
 int pcg_switch_to_leaf(pcg_context *c, int32_t id) {
   if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   PCG_CUDA(cudaSetDevice(c->device));
   pcg::PatchDev &P = c->h_patches[id];
@@ -1410,6 +1709,7 @@ int pcg_refinement_criterion(pcg_context *c, int32_t n, const int32_t *ids, int3
   }
   if (n == 0) return PCG_OK;
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1432,6 +1732,7 @@ int pcg_compute_fluxes(pcg_context *c, int32_t id, double g_flux) {
   if (c->h_patches[id].nq != 3 || c->h_patches[id].g < 1)
     return fail(PCG_E_INVALID, "flux computation needs 3 unknowns and a ghost layer");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1452,6 +1753,7 @@ int pcg_apply_flux_correction(pcg_context *c, int32_t src, int32_t dst, int32_t 
     return fail(PCG_E_INVALID, "bad dimension/direction");
   if (c->h_patches[src].nq != 3 || c->h_patches[dst].nq != 3) return fail(PCG_E_INVALID, "needs 3 unknowns");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   int rc = upload_patches(c);
   if (rc != PCG_OK) return rc;
@@ -1464,6 +1766,7 @@ int pcg_apply_flux_correction(pcg_context *c, int32_t src, int32_t dst, int32_t 
 int pcg_set_ghost_items(pcg_context *c, const pcg_ghost_item *items, int32_t n) {
   if (!c || n < 0 || (n > 0 && !items)) return fail(PCG_E_INVALID, "bad item list");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   for (int k = 0; k < n; k++) {
     const pcg_ghost_item &it = items[k];
     if (!valid_id(c, it.src) || !valid_id(c, it.dst) || (it.kind != 0 && it.kind != 1))
@@ -1485,6 +1788,7 @@ int pcg_set_restriction_items(pcg_context *c, int32_t n, const int32_t *src, con
                               int32_t only_overlapped) {
   if (!c || n < 0 || (n > 0 && (!src || !dst))) return fail(PCG_E_INVALID, "bad restriction list");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   std::vector<int4> v;
   for (int k = 0; k < n; k++) {
     if (!valid_id(c, src[k]) || !valid_id(c, dst[k]) || src[k] == dst[k])
@@ -1503,6 +1807,7 @@ int pcg_set_flux_correction_items(pcg_context *c, int32_t n, const int32_t *src,
                                   const int32_t *dim, const int32_t *dir, double g_flux) {
   if (!c || n < 0 || (n > 0 && (!src || !dst || !dim || !dir))) return fail(PCG_E_INVALID, "bad flux list");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   std::vector<int4> v;
   for (int k = 0; k < n; k++) {
     if (!valid_id(c, src[k]) || !valid_id(c, dst[k]) || dim[k] < 0 || dim[k] > 1 || (dir[k] != 1 && dir[k] != -1))
@@ -1520,6 +1825,7 @@ int pcg_set_flux_correction_items(pcg_context *c, int32_t n, const int32_t *src,
 int pcg_restrict_all(pcg_context *c) {
   if (!c) return fail(PCG_E_INVALID, "null context");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   c->fin_dirty = true;
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);
@@ -1541,6 +1847,7 @@ int pcg_restrict_all(pcg_context *c) {
 int pcg_set_group_end_time(pcg_context *c, int32_t group, double time, double t_end) {
   if (!c || group < 0 || group >= c->max_groups) return fail(PCG_E_INVALID, "group out of range");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   PCG_CUDA(cudaSetDevice(c->device));
   c->h_pinned[0] = time;
   c->h_pinned[1] = t_end;
@@ -1565,6 +1872,7 @@ int pcg_get_group_times(pcg_context *c, double *times) {
 int pcg_set_group_max_dt(pcg_context *c, int32_t group, double max_dt) {
   if (!c || group < 0 || group >= c->max_groups) return fail(PCG_E_INVALID, "group out of range");
   std::lock_guard<std::mutex> lk(c->mu);
+  c->fused_ready = false;
   c->h_group_max_dt[group] = max_dt;
   return PCG_OK;
 }
@@ -1598,6 +1906,7 @@ static int check_mode(pcg_context *c, int mode) {
 int pcg_set_virtual_time_items(pcg_context *c, int32_t n, const int32_t *leaf, const int32_t *virt) {
   if (!c || n < 0 || (n > 0 && (!leaf || !virt))) return fail(PCG_E_INVALID, "bad virtual-time list");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   std::vector<int2> v;
   v.reserve(n);
   for (int k = 0; k < n; k++) {
@@ -1613,6 +1922,7 @@ int pcg_set_virtual_time_items(pcg_context *c, int32_t n, const int32_t *leaf, c
 int pcg_set_time_stepping(pcg_context *c, int32_t mode) {
   if (!c || (mode != PCG_TS_GLOBAL && mode != PCG_TS_LOCAL)) return fail(PCG_E_INVALID, "bad time-stepping mode");
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   const bool local = mode == PCG_TS_LOCAL;
   if (local != c->ts_local) {
     c->ts_local = local;
@@ -1630,13 +1940,28 @@ int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = check_mode(c, mode)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
-  if ((rc = refresh_fin(c)) != PCG_OK) return rc;
-  PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
-  if ((rc = enqueue_step(c, mode)) != PCG_OK) return rc;
-  PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
-  PCG_CUDA(pcg::launch_record_dt(c->stream, c->max_groups, c->d_group_dt, c->d_dt_out));
-  PCG_CUDA(cudaMemcpyAsync(c->h_pinned, c->d_dt_out, sizeof(double) * c->max_groups, cudaMemcpyDeviceToHost,
-                           c->stream));
+  const bool fused = use_fused(c, mode);
+  if (fused) {
+    if ((rc = ensure_hist(c, 1)) != PCG_OK) return rc;
+    PCG_CUDA(cudaMemsetAsync(c->d_counter, 0, sizeof(int), c->stream));
+    PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+    if ((rc = fused_prologue(c)) != PCG_OK) return rc;
+    rc = enqueue_fused_step(c, mode);
+    c->fused_pending = true;
+    if (rc != PCG_OK) return rc;
+    PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+    PCG_CUDA(cudaMemcpyAsync(c->h_pinned, c->d_hist, sizeof(double) * c->max_groups, cudaMemcpyDeviceToHost,
+                             c->stream));
+  } else {
+    PCG_SETTLE(c);
+    if ((rc = refresh_fin(c)) != PCG_OK) return rc;
+    PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+    if ((rc = enqueue_step(c, mode)) != PCG_OK) return rc;
+    PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+    PCG_CUDA(pcg::launch_record_dt(c->stream, c->max_groups, c->d_group_dt, c->d_dt_out));
+    PCG_CUDA(cudaMemcpyAsync(c->h_pinned, c->d_dt_out, sizeof(double) * c->max_groups, cudaMemcpyDeviceToHost,
+                             c->stream));
+  }
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   float ms = 0.f;
   PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -1657,18 +1982,47 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = check_mode(c, mode)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
-  if ((rc = refresh_fin(c)) != PCG_OK) return rc;
-  if (steps > c->hist_cap) {
-    if (c->d_hist) PCG_CUDA(cudaFree(c->d_hist));
-    PCG_CUDA(cudaMalloc(&c->d_hist, sizeof(double) * (size_t)steps * c->max_groups));
-    c->hist_cap = steps;
-    c->graph_valid = false;
+  const bool fused = use_fused(c, mode);
+  if (!fused) {
+    PCG_SETTLE(c);
+    if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   }
+  if ((rc = ensure_hist(c, steps)) != PCG_OK) return rc;
   PCG_CUDA(cudaMemsetAsync(c->d_counter, 0, sizeof(int), c->stream));
   int threads = std::min(1024, std::max(32, (c->max_groups + 31) / 32 * 32));
-  if (mode == PCG_MODE_BATCHED) {
-    if (!c->graph_valid) {
+  if (fused) {
+    PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+    if ((rc = fused_prologue(c)) != PCG_OK) return rc;
+    if (mode == PCG_MODE_BATCHED) {
+      if (!c->graph_valid || !c->graph_fused) {
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        c->graph_valid = false;
+        cudaGraph_t g;
+        PCG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int erc = enqueue_fused_step(c, PCG_MODE_BATCHED);
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+        if (erc != PCG_OK) return erc;
+        if (ce != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        c->graph_valid = true;
+        c->graph_fused = true;
+      }
+      for (int s = 0; s < steps; s++) PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    } else {
+      for (int s = 0; s < steps; s++) {
+        rc = enqueue_fused_step(c, PCG_MODE_PLAIN);
+        c->fused_pending = true;
+        if (rc != PCG_OK) return rc;
+      }
+    }
+    c->fused_pending = true;
+    PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+  } else if (mode == PCG_MODE_BATCHED) {
+    if (!c->graph_valid || c->graph_fused) {
       if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+      c->graph_valid = false;
       cudaGraph_t g;
       PCG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
       // the history kernel also advances the group times (one launch less);
@@ -1686,6 +2040,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
       cudaGraphDestroy(g);
       if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
       c->graph_valid = true;
+      c->graph_fused = false;
     }
     PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < steps; s++) PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
@@ -1711,6 +2066,27 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   return PCG_OK;
 }
 
+int pcg_set_step_form(pcg_context *c, int32_t form) {
+  if (!c || (form != PCG_FORM_AUTO && form != PCG_FORM_UNFUSED)) return fail(PCG_E_INVALID, "bad step form");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
+  if (c->form != form) {
+    c->form = form;
+    c->graph_valid = false;
+  }
+  return PCG_OK;
+}
+
+int pcg_get_step_form(pcg_context *c, int32_t mode, int32_t *fused) {
+  if (!c || !fused || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED)) return fail(PCG_E_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  *fused = use_fused(c, mode) ? 1 : 0;
+  return PCG_OK;
+}
+
 namespace {
 
 int check_schedule(const pcg_schedule *s) {
@@ -1720,6 +2096,7 @@ int check_schedule(const pcg_schedule *s) {
   if (s->variant < 0 || s->variant >= pcg::kNumStripVariants)
     return fail(PCG_E_INVALID, "strip variant out of range");
   if (s->chunk < 1 || s->chunk > 32) return fail(PCG_E_INVALID, "strip chunk must be in 1..32");
+  if (s->unfused != 0 && s->unfused != 1) return fail(PCG_E_INVALID, "schedule field unfused must be 0 or 1");
   return PCG_OK;
 }
 
@@ -1730,10 +2107,10 @@ int pcg_set_schedule(pcg_context *c, const pcg_schedule *s) {
   int rc = check_schedule(s);
   if (rc != PCG_OK) return rc;
   std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
   PCG_CUDA(cudaSetDevice(c->device));
   c->sched = *s;
-  c->sched.reserved_ = 0;
-  if (c->sched.kind == PCG_SCHED_TILES) { c->sched.variant = 0; c->sched.chunk = 32; }
+  if (c->sched.kind == PCG_SCHED_TILES) { c->sched.variant = 0; c->sched.chunk = 32; c->sched.unfused = 0; }
   c->sched_fixed = true;
   c->graph_valid = false;
   if (!c->topo_dirty) return apply_schedule(c);
@@ -1760,7 +2137,6 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = check_mode(c, PCG_MODE_BATCHED)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
-  if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   std::vector<pcg_schedule> cand;
   cand.push_back(pcg_schedule{PCG_SCHED_TILES, 0, 32, 0});
   for (int chunk : {32, 16})
@@ -1769,9 +2145,23 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
   for (size_t k = 0; k < cand.size(); k++) {
     c->sched = cand[k];
     if ((rc = apply_schedule(c)) != PCG_OK) return rc;
+    // strip candidates run the fused step where it applies, tiles the unfused one
+    const bool fused = use_fused(c, PCG_MODE_BATCHED);
+    if (fused) {
+      if ((rc = fused_prologue(c)) != PCG_OK) return rc;
+    } else {
+      PCG_SETTLE(c);
+      if ((rc = refresh_fin(c)) != PCG_OK) return rc;
+    }
     for (int r = 0; r < reps; r++) {
       PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
-      if ((rc = enqueue_step(c, PCG_MODE_BATCHED)) != PCG_OK) return rc;
+      if (fused) {
+        rc = enqueue_fused_step(c, PCG_MODE_BATCHED);
+        c->fused_pending = true;
+      } else {
+        rc = enqueue_step(c, PCG_MODE_BATCHED);
+      }
+      if (rc != PCG_OK) return rc;
       PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
       PCG_CUDA(cudaStreamSynchronize(c->stream));
       float e = 0.f;
@@ -1785,6 +2175,30 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
   size_t best = 0;
   for (size_t k = 1; k < cand.size(); k++)
     if (t[k] < t[best]) best = k;
+  // the fastest strip schedule in the unfused form too, where the fused one applied
+  if (cand[best].kind == PCG_SCHED_STRIPS && use_fused(c, PCG_MODE_BATCHED)) {
+    pcg_schedule u = cand[best];
+    u.unfused = 1;
+    cand.push_back(u);
+    t.push_back(0.0);
+    c->sched = u;
+    if ((rc = apply_schedule(c)) != PCG_OK) return rc;
+    PCG_SETTLE(c);
+    if ((rc = refresh_fin(c)) != PCG_OK) return rc;
+    for (int r = 0; r < reps; r++) {
+      PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+      if ((rc = enqueue_step(c, PCG_MODE_BATCHED)) != PCG_OK) return rc;
+      PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+      PCG_CUDA(cudaStreamSynchronize(c->stream));
+      float e = 0.f;
+      PCG_CUDA(cudaEventElapsedTime(&e, c->ev0, c->ev1));
+      t.back() += e;
+      c->device_ms += e;
+      c->cell_updates += c->cells_per_step;
+    }
+    t.back() /= reps;
+    if (t.back() < t[best]) best = cand.size() - 1;
+  }
   c->sched = cand[best];
   c->sched_fixed = true;
   if ((rc = apply_schedule(c)) != PCG_OK) return rc;
@@ -1824,6 +2238,37 @@ int pcg_profile_step(pcg_context *c, double *ms) {
   if (rc != PCG_OK) return rc;
   if ((rc = check_solvable(c)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
+  if (use_fused(c, PCG_MODE_BATCHED)) {
+    // the fused step's three launches: fused sweep, time advance, next reset
+    if ((rc = fused_prologue(c)) != PCG_OK) return rc;
+    cudaEvent_t ev[4];
+    for (int i = 0; i < 4; i++) PCG_CUDA(cudaEventCreate(&ev[i]));
+    const pcg::FusedDev F = fused_dev(c);
+    PCG_CUDA(cudaEventRecord(ev[0], c->stream));
+    PCG_CUDA(pcg::launch_fused_strips(c->stream, c->sched.variant, c->fused_grid, F, c->d_sitems, c->d_sgroups,
+                                      (int)c->h_sitems.size(), c->d_patch_smax, c->d_group_dt));
+    PCG_CUDA(cudaEventRecord(ev[1], c->stream));
+    PCG_CUDA(pcg::launch_fused_advance(c->stream, F, c->d_leaf_ids, (int)c->leaf_ids.size(), c->d_times,
+                                       c->d_patch_smax, c->max_groups, c->d_group_dt, c->d_group_time, c->d_pend,
+                                       c->d_par, c->d_dt_prev, c->d_hist, c->d_counter, 0));
+    PCG_CUDA(cudaEventRecord(ev[2], c->stream));
+    rc = enqueue_reset_items(c);
+    c->fused_pending = true;
+    if (rc != PCG_OK) return rc;
+    PCG_CUDA(cudaEventRecord(ev[3], c->stream));
+    PCG_CUDA(cudaStreamSynchronize(c->stream));
+    float t[3];
+    for (int i = 0; i < 3; i++) PCG_CUDA(cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]));
+    ms[0] = t[2];
+    ms[1] = 0.0;
+    ms[2] = 0.0;
+    ms[3] = t[0];
+    ms[4] = t[1];
+    for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
+    c->cell_updates += c->cells_per_step;
+    return PCG_OK;
+  }
+  PCG_SETTLE(c);
   if ((rc = refresh_fin(c)) != PCG_OK) return rc;
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; i++) PCG_CUDA(cudaEventCreate(&ev[i]));

@@ -24,6 +24,11 @@ struct __align__(16) PatchDev {
   int group, wall, tile_begin, tile_count;
   double pos[2];
   double size[2];
+  // offset (in doubles) of the patch's second state copy in the context's
+  // shadow buffer (fused batched step: state and net updates, 6 nx ny doubles)
+  long long sh_off;
+  // first entry of the patch's 2 (nx + ny) face-ghost codes (fused step)
+  int face_begin, pad_;
 };
 
 struct __align__(16) PatchTimeDev {
@@ -90,6 +95,21 @@ struct __align__(16) CopyPlanDev {
 struct __align__(16) GhostItemStepDev {
   double tf, itf;
   int vn_src, vo_src, vo_dst, nq;
+};
+
+// Face-ghost evaluation plans of the fused batched step (built once per grid
+// change from the ghost-cell list): a COPY ghost cell reads source cell
+// (sx, sy) of patch src, an INTERP ghost cell the d-linear stencil at base
+// cell (bx, by) of patch src with weights sf; `item` indexes the per-step
+// item data (time factor).
+struct __align__(16) FusedCopyDev {
+  int item, src;
+  short sx, sy;
+  int pad_;
+};
+struct __align__(16) FusedInterpDev {
+  int item, src, bx, by;
+  double sf[4];
 };
 
 // Bit pattern of a double and back through an opaque register move: the

@@ -816,7 +816,7 @@ __device__ __forceinline__ void wall_face(double *slab, const PatchDev &P, int d
 // (0,lower), (1,upper), (0,upper), (1,lower).  One warp per patch.
 __global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                         const int *__restrict__ wall_patches, int count,
-                        const int *__restrict__ group_active, const int *__restrict__ pact) {
+                        const int *__restrict__ group_active, const int *__restrict__ pact, int from_unew) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -827,7 +827,7 @@ __global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ 
     if (pact && !pact[wall_patches[w]]) continue;
     for (int f = 0; f < 4; f++) {
       int d = order[f][0], up = order[f][1];
-      if (P.wall & (1 << (2 * d + up))) wall_face(slab, P, d, up, true, lane, 32);
+      if (P.wall & (1 << (2 * d + up))) wall_face(slab, P, d, up, from_unew != 0, lane, 32);
       __syncwarp();
     }
   }
@@ -1872,11 +1872,11 @@ cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const Pat
 
 cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
                          const int *wall_patches, int count, const int *group_active,
-                         const int *pact) {
+                         const int *pact, int from_unew) {
   if (count <= 0) return cudaSuccess;
   int grid = (count + 7) / 8;
   if (grid > 152 * 16) grid = 152 * 16;
-  k_walls<<<grid, 256, 0, st>>>(slab, patches, wall_patches, count, group_active, pact);
+  k_walls<<<grid, 256, 0, st>>>(slab, patches, wall_patches, count, group_active, pact, from_unew);
   return cudaGetLastError();
 }
 

@@ -73,9 +73,11 @@ cudaError_t launch_reset_items(cudaStream_t st, int n_groups, const double *grou
                                GhostItemStepDev *out);
 cudaError_t launch_item_step(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
                              const GhostItemDev *items, int count, GhostItemStepDev *out);
+// from_unew: interior cells read from uNew (the batched step, whose copy
+// uNew -> uOld is implicit) or from uOld (the reference layout after a step).
 cudaError_t launch_walls(cudaStream_t st, double *slab, const PatchDev *patches,
                          const int *wall_patches, int count, const int *group_active,
-                         const int *pact = nullptr);
+                         const int *pact = nullptr, int from_unew = 1);
 cudaError_t launch_fill_patch(cudaStream_t st, double *slab, const PatchDev *patches,
                               const PatchTimeDev *times, const GhostItemDev *items, int first,
                               int count, int pid, const int *group_active = nullptr);
@@ -164,5 +166,38 @@ cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const 
                                  const unsigned long long *group_dt, const int *group_active,
                                  int *fin, const int *pact = nullptr,
                                  const unsigned long long *pdt = nullptr);
+
+// ---- fused batched step (pcg_fused.cu)
+// Everything the fused kernels read besides the work list: the slab and the
+// shadow buffer, the patch table, per group the pending-update state (pend:
+// the group's last step left an update pending; par: the set it wrote, 0 = A
+// in the slab, 1 = B in the shadow; dt_prev: the dt of that update) and
+// activity, the face / corner tables (per patch 2 (nx + ny) face codes from
+// face_begin[pid], 4 corner codes: >= 0 copy plan, <= -2 interpolation plan
+// -code - 2, -1 none) with their plans and the per-item step data.
+struct FusedDev {
+  double *slab, *shadow;
+  const PatchDev *patches;
+  const int *pend, *par, *active;
+  const unsigned long long *dt_prev;
+  const int *face_begin, *face, *corner;
+  const FusedCopyDev *copies;
+  const FusedInterpDev *interps;
+  const GhostItemStepDev *item_step;
+  SweParamsDev prm;
+};
+cudaError_t launch_fused_strips(cudaStream_t st, int variant, int grid, const FusedDev &F, const StripItem *items,
+                                const StripGroup *groups, int count, unsigned long long *patch_smax,
+                                unsigned long long *group_dt);
+cudaError_t fused_occupancy(int variant, int *blocks_per_sm);
+cudaError_t launch_fused_advance(cudaStream_t st, const FusedDev &F, const int *leaf_ids, int n_leaves,
+                                 PatchTimeDev *times, const unsigned long long *patch_smax, int n_groups,
+                                 const unsigned long long *group_dt, double *group_time, int *pend, int *par,
+                                 unsigned long long *dt_prev, double *hist, int *counter, int capacity);
+cudaError_t launch_fused_flush(cudaStream_t st, const FusedDev &F, const int *leaf_ids, int n_leaves);
+cudaError_t launch_build_fused_ghosts(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
+                                      const GhostCellDev *cells, int ncopy, int ninterp, const InterpPlanDev *plan,
+                                      const int *face_begin, int *face, int *corner, FusedCopyDev *copies,
+                                      FusedInterpDev *interps);
 
 }  // namespace pcg

@@ -19,6 +19,8 @@ PCG_E_CUDA = -3
 PCG_E_TIMEOUT = -4
 PCG_E_STATE = -5
 PCG_E_NUMERIC = -6
+FORM_AUTO = 0
+FORM_UNFUSED = 1
 PCG_CRIT_DEPTH_GRADIENT = 0
 PCG_CRIT_SURFACE_DIFFERENCE = 1
 PCG_CRIT_SURFACE_GRADIENT = 2
@@ -63,10 +65,10 @@ class GhostItem(C.Structure):
 
 class Schedule(C.Structure):
     _fields_ = [("kind", C.c_int32), ("variant", C.c_int32), ("chunk", C.c_int32),
-                ("reserved_", C.c_int32)]
+                ("unfused", C.c_int32)]
 
     def as_tuple(self):
-        return (self.kind, self.variant, self.chunk)
+        return (self.kind, self.variant, self.chunk, self.unfused)
 
 
 SCHED_TILES = 0
@@ -129,6 +131,8 @@ SIGNATURES = {
     "pcg_refinement_indicator": (C.c_int, [_CTX, C.c_int32, _I2, _D]),
     "pcg_refinement_criterion": (C.c_int, [_CTX, C.c_int32, _I2, C.c_int32, _D]),
     "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
+    "pcg_set_step_form": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_get_step_form": (C.c_int, [_CTX, C.c_int32, C.POINTER(C.c_int32)]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "pcg_synchronize": (C.c_int, [_CTX]),
@@ -410,6 +414,15 @@ class Context:
         check(lib().pcg_step(self.h, mode, dptr(out)))
         return out
 
+    def set_step_form(self, form):
+        """pcg_set_step_form: FORM_AUTO (fused where it applies) or FORM_UNFUSED."""
+        check(lib().pcg_set_step_form(self.h, int(form)))
+
+    def step_is_fused(self, mode=PCG_MODE_BATCHED):
+        v = C.c_int32()
+        check(lib().pcg_get_step_form(self.h, int(mode), C.byref(v)))
+        return bool(v.value)
+
     def run(self, steps, mode=PCG_MODE_BATCHED):
         hist = np.zeros(steps * self.max_groups)
         check(lib().pcg_run(self.h, steps, mode, dptr(hist)))
@@ -423,9 +436,10 @@ class Context:
     def synchronize(self):
         check(lib().pcg_synchronize(self.h))
 
-    def set_schedule(self, kind, variant=0, chunk=32):
-        """Fix the batched sweep/update schedule (SCHED_TILES or SCHED_STRIPS)."""
-        s = Schedule(kind, variant, chunk, 0)
+    def set_schedule(self, kind, variant=0, chunk=32, unfused=0):
+        """Fix the batched sweep/update schedule (SCHED_TILES or SCHED_STRIPS;
+        unfused = 1 keeps strips in the unfused step form)."""
+        s = Schedule(kind, variant, chunk, unfused)
         check(lib().pcg_set_schedule(self.h, C.byref(s)))
 
     def get_schedule(self):
@@ -436,7 +450,7 @@ class Context:
     def autotune(self, reps=2):
         """Time every candidate schedule over `reps` batched steps each (the
         simulation advances by those steps) and keep the fastest.  Returns
-        [((kind, variant, chunk), mean ms per step), ...]."""
+        [((kind, variant, chunk, unfused), mean ms per step), ...]."""
         cap = 64
         tried = (Schedule * cap)()
         ms = np.zeros(cap)

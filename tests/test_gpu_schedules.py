@@ -39,6 +39,7 @@ def _gpu_run(ps, steps, sched=None, autotune_reps=0):
 
 SCHEDULES = [
     (P.SCHED_TILES, 0, 32),
+    (P.SCHED_STRIPS, 2, 32, 1),
     (P.SCHED_STRIPS, 0, 32),
     (P.SCHED_STRIPS, 1, 16),
     (P.SCHED_STRIPS, 2, 32),
@@ -55,7 +56,7 @@ def test_schedule_bit_exact_on_ragged_sizes(sched):
     ps = S.uneven_patches(grid=5, sizes=(5, 12, 33, 40))
     assert ps.meta["dry_fraction"] > 0.05
     out, dts, _, got = _gpu_run(ps, 12, sched=sched)
-    assert got == sched
+    assert got[:3] == sched[:3]
     oout, odts = _oracle_run(ps, 12)
     assert dts == odts
     assert np.all(np.isfinite(out))
@@ -65,7 +66,9 @@ def test_schedule_bit_exact_on_ragged_sizes(sched):
 def test_autotuner_picks_a_candidate_and_keeps_results_exact():
     ps = S.uneven_patches(grid=4, sizes=(8, 16, 32, 64))
     out, dts, tuned, got = _gpu_run(ps, 3, autotune_reps=1)
-    assert len(tuned) == 11
+    # 11 candidates, and the best strip schedule in the unfused form when a
+    # strip schedule won
+    assert len(tuned) in (11, 12)
     assert all(ms > 0.0 for _, ms in tuned)
     best = min(tuned, key=lambda t: t[1])[0]
     assert got == best
