@@ -145,6 +145,9 @@ int pcg_patch_set_group(pcg_context *ctx, int32_t id, int32_t group);
 
 /* DefaultTransfer::copyUNewToUOld (DefaultTransfer.cpph:103-113). */
 int pcg_copy_unew_to_uold(pcg_context *ctx, int32_t id);
+/* DefaultTransfer::swapUNewAndUOld (DefaultTransfer.cpph:115-127): the
+ * interior values of uNew and uOld trade places. */
+int pcg_swap_unew_and_uold(pcg_context *ctx, int32_t id);
 /* SWEKernel::fillBoundaryLayer (src/peanoclaw/native/SWEKernel.cpp:176-237). */
 int pcg_fill_boundary_layer(pcg_context *ctx, int32_t id, int32_t dimension, int32_t set_upper);
 /* SWEKernel::solveTimestep (src/peanoclaw/native/SWEKernel.cpp:125-167):

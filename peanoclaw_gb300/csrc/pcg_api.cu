@@ -1386,6 +1386,18 @@ int pcg_copy_unew_to_uold(pcg_context *c, int32_t id) {
   return PCG_OK;
 }
 
+int pcg_swap_unew_and_uold(pcg_context *c, int32_t id) {
+  if (!valid_id(c, id)) return fail(PCG_E_INVALID, "unknown patch id");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
+  c->fin_dirty = true;
+  int rc = upload_patches(c);
+  if (rc != PCG_OK) return rc;
+  const pcg::PatchDev &P = c->h_patches[id];
+  PCG_CUDA(pcg::launch_swap_unew_uold(c->stream, c->slab, c->d_patches, id, P.nq * P.nx * P.ny));
+  return PCG_OK;
+}
+
 int pcg_fill_boundary_layer(pcg_context *c, int32_t id, int32_t dimension, int32_t set_upper) {
   if (!valid_id(c, id) || dimension < 0 || dimension > 1) return fail(PCG_E_INVALID, "bad patch or dimension");
   if (c->h_patches[id].g != 1 || c->h_patches[id].nq < 3)

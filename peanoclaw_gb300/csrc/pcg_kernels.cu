@@ -876,6 +876,20 @@ __global__ void k_copy_unew_to_uold(double *slab, const PatchDev *patches, int p
   }
 }
 
+// DefaultTransfer::swapUNewAndUOld (DefaultTransfer.cpph:115-127): the
+// interior values of uNew and uOld trade places.
+__global__ void k_swap_unew_uold(double *slab, const PatchDev *patches, int pid) {
+  PatchDev P = patches[pid];
+  int n = P.nq * P.nx * P.ny;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int q = k / (P.nx * P.ny), r = k - q * P.nx * P.ny, x = r / P.ny, y = r - x * P.ny;
+    const long long in = idx_unew(P, q, x, y), io = idx_uold(P, q, x, y);
+    const double vn = slab[in], vo = slab[io];
+    slab[in] = vo;
+    slab[io] = vn;
+  }
+}
+
 __global__ void k_fill_boundary_layer(double *slab, const PatchDev *patches, int pid, int dim, int up) {
   PatchDev P = patches[pid];
   wall_face(slab, P, dim, up, false, threadIdx.x, blockDim.x);
@@ -1909,6 +1923,11 @@ cudaError_t launch_solve_patch(cudaStream_t st, double *slab, const PatchDev *pa
 cudaError_t launch_copy_unew_to_uold(cudaStream_t st, double *slab, const PatchDev *patches, int pid,
                                      int n) {
   k_copy_unew_to_uold<<<(n + 255) / 256, 256, 0, st>>>(slab, patches, pid);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_swap_unew_uold(cudaStream_t st, double *slab, const PatchDev *patches, int pid, int n) {
+  k_swap_unew_uold<<<(n + 255) / 256, 256, 0, st>>>(slab, patches, pid);
   return cudaGetLastError();
 }
 

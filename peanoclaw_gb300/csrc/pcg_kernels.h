@@ -89,6 +89,7 @@ cudaError_t launch_solve_patch(cudaStream_t st, double *slab, const PatchDev *pa
                                const SweParamsDev &prm, double max_dt, double *out);
 cudaError_t launch_copy_unew_to_uold(cudaStream_t st, double *slab, const PatchDev *patches, int pid,
                                      int n);
+cudaError_t launch_swap_unew_uold(cudaStream_t st, double *slab, const PatchDev *patches, int pid, int n);
 cudaError_t launch_fill_boundary_layer(cudaStream_t st, double *slab, const PatchDev *patches,
                                        int pid, int dim, int up);
 cudaError_t launch_transfer(cudaStream_t st, double *slab, const PatchDev *patches,

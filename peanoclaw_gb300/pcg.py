@@ -100,6 +100,7 @@ SIGNATURES = {
     "pcg_patch_set_boundary": (C.c_int, [_CTX, C.c_int32, C.c_uint32]),
     "pcg_patch_set_group": (C.c_int, [_CTX, C.c_int32, C.c_int32]),
     "pcg_copy_unew_to_uold": (C.c_int, [_CTX, C.c_int32]),
+    "pcg_swap_unew_and_uold": (C.c_int, [_CTX, C.c_int32]),
     "pcg_fill_boundary_layer": (C.c_int, [_CTX, C.c_int32, C.c_int32, C.c_int32]),
     "pcg_solve_timestep": (C.c_int, [_CTX, C.c_int32, C.c_double, _D, _D]),
     "pcg_transfer_ghostlayer": (C.c_int, [_CTX, _I2, _I2, _I2, C.c_int32, C.c_int32]),
