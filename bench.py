@@ -38,6 +38,8 @@ UNIT = "cell-updates/s"
 # 2 cbar, sqrt, divide, reciprocal) + 2 FMA (2 edges per cell); accumulation
 # 8 FMA; update 3 FMA.
 FLOP_PER_CELL = 8 + 2 * (16 + 2 * 2) + 2 * 8 + 2 * 3
+# the sweep's share (everything but the update's 3 FMA)
+FLOP_PER_CELL_SWEEP = FLOP_PER_CELL - 2 * 3
 # Algorithmic bytes per patch step: read h, hu, hv, b with halo, write h, hu, hv.
 def bytes_per_patch(n):
     return 8 * (4 * (n + 2) ** 2 + 3 * n * n)
@@ -75,6 +77,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default batched schedule instead of autotuning it")
+    ap.add_argument("--form", default="auto", choices=["auto", "fused", "unfused"],
+                    help="step form: the autotuner's pick, or the fused / unfused form on the default "
+                         "strip schedule (no autotuning)")
     ap.add_argument("--config-legs", default="",
                     help="comma-separated subset of the configuration legs to run (default: all)")
     ap.add_argument("--no-configs", action="store_true",
@@ -571,13 +576,16 @@ def main():
 
     # warm-up, the schedule autotuner (untimed; it advances the simulation by
     # one or two steps per candidate) and the graph instantiation
+    if args.form != "auto":
+        ctx.set_step_form(P.FORM_UNFUSED if args.form == "unfused" else P.FORM_AUTO)
     ctx.run(max(1, args.warmup), P.PCG_MODE_BATCHED)
     tuned = None
-    if not args.no_autotune:
+    if not args.no_autotune and args.form == "auto":
         tuned = ctx.autotune(reps=2)
         ctx.run(2, P.PCG_MODE_BATCHED)
     sched = ctx.get_schedule()
     fused = ctx.step_is_fused(P.PCG_MODE_BATCHED)
+    step_launches = ctx.step_launches()
     dist_barrier(dist)
     ctx.synchronize()
     clocks = ClockSampler(local)
@@ -603,9 +611,17 @@ def main():
     fp64_peak = ctx.fp64_peak_tflops()
     import torch
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-    flops = FLOP_PER_CELL * cells
-    # the FP64 work sits in the sweep (and 3 FMA/cell in the update)
-    achieved = (flops / 1e12) / ((sweep_ms + update_ms) / 1e3)
+    # dominant kernel: the sweep (unfused form: k_sweep_strips / k_sweep_tiles,
+    # the sweep's flops) or the fused sweep (k_fused_strips: ghost fill,
+    # deferred update and sweep, all flops of a cell update); its average
+    # launch duration from CUDA events on the launch stream
+    dom_flop = FLOP_PER_CELL if fused else FLOP_PER_CELL_SWEEP
+    achieved = (dom_flop * cells / 1e12) / (sweep_ms / 1e3)
+    step_achieved = FLOP_PER_CELL * cells / 1e12 / (ms_per_step / 1e3)
+    if fused:
+        dom_kernel = "k_fused_strips"
+    else:
+        dom_kernel = "k_sweep_tiles" if sched[0] == P.SCHED_TILES else "k_sweep_strips"
     alg_bytes = sum(bytes_per_patch(n) for n in ps.n)
     hbm_peak = None
     try:
@@ -616,8 +632,11 @@ def main():
     step_ms_phase = float(ph.sum())
     # DRAM traffic of the dominant kernel (sweep): bytes per cell update from
     # the ncu capture of the small case, scaled to this launch's cells
-    tpc = profile_figure("k_sweep_strips_uneven_patches_4k.md", "traffic_bytes_per_cell_update")
-    traffic = tpc * cells if (tpc is not None and sched[0] == P.SCHED_STRIPS) else None
+    prof = {"k_fused_strips": "k_fused_strips_uneven_patches_4k.md",
+            "k_sweep_strips": "k_sweep_strips_uneven_patches_4k.md"}.get(dom_kernel)
+    tpc = profile_figure(prof, "traffic_bytes_per_cell_update") if prof else None
+    traffic = tpc * cells if tpc is not None else None
+    fp64_ipc = (profile_figure(prof, "fp64_inst_per_cell_update") if prof else None) or FP64_INST_PER_CELL
 
     # plain per-patch form (one launch per patch per phase), same workload
     plain = None
@@ -684,29 +703,36 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "batched persistent form, 50k uneven patches "
+            "config": {"workload": "batched step (%s form, CUDA graph), 50k uneven patches "
                                    "(%d patches, {8,16,32,64}^2 cells, %d cells, %.1f%% dry), "
                                    "radial-free random Gaussian bathymetry, 200-step config "
-                                   "timed over %d steps" % (len(ps), cells, 100 * ps.meta["dry_fraction"], args.steps),
+                                   "timed over %d steps" % ("fused" if fused else "unfused", len(ps), cells,
+                                                            100 * ps.meta["dry_fraction"], args.steps),
                        "patches": len(ps), "cells": cells, "grid_slots": args.grid,
                        "l2": "inputs (%.1f GB) larger than L2, no flush" % (ps.packed.nbytes / 1e9),
                        "parallelism": "replicas x%d" % ws if ws > 1 else "1 GPU"},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp64_peak, "traffic": traffic,
-                         "traffic_note": "sweep DRAM bytes per launch: ncu bytes/cell of the 4k-patch "
-                                         "capture x cells (profiles/k_sweep_strips_uneven_patches_4k.md)",
-                         "fp64_pipe_frac_sweep": (FP64_INST_PER_CELL * cells /
-                                                  (sweep_ms / 1e3) /
-                                                  (FP64_LANES_PER_SM_CLK * sm_count * (clk.get("sm_mhz") or 2070.0) * 1e6)),
+                         "kernel": dom_kernel,
+                         "achieved_note": "%d algorithmic flops per cell x %d cells / the kernel's mean "
+                                          "CUDA-event time (%.3f ms)" % (dom_flop, cells, sweep_ms),
+                         "step_frac": step_achieved / fp64_peak,
+                         "step_note": "%d flops per cell update x cells / ms_per_step, the whole step"
+                                      % FLOP_PER_CELL,
+                         "traffic_note": ("constant from a profile: DRAM bytes per cell of the ncu capture "
+                                          "on the 4k-patch case (profiles/%s) x cells" % prof) if prof else None,
+                         "fp64_pipe_frac": (fp64_ipc * cells / (sweep_ms / 1e3) /
+                                            (FP64_LANES_PER_SM_CLK * sm_count * (clk.get("sm_mhz") or 2070.0) * 1e6)),
+                         "fp64_pipe_note": "FP64 instructions per cell from the same profile (a constant) x cells "
+                                           "/ kernel time / (2 FP64 lanes x SMs x median SM clock)",
                          "peak_source": "measured live (DFMA chain probe, FMA = 2 flops)",
                          "flop_per_cell": FLOP_PER_CELL,
-                         "kernels": ("k_sweep_tiles + k_update_tiles" if sched[0] == P.SCHED_TILES
-                                     else "k_sweep_strips + k_update_strips"),
                          "hbm": {"achieved_gbs": alg_bytes / (step_ms_phase / 1e3) / 1e9,
                                  "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json",
                                  "alg_bytes_per_step": alg_bytes}},
-            "phase_ms": {"reset": ph[0], "ghost_items": ph[1], "walls": ph[2], "sweep": ph[3],
-                         "update": ph[4]},
+            "phase_ms": ({"reset": ph[0], "fused_sweep": ph[3], "advance": ph[4]} if fused else
+                         {"reset": ph[0], "ghost_items": ph[1], "walls": ph[2], "sweep": ph[3],
+                          "update": ph[4]}),
             "schedule": {"kind": "tiles" if sched[0] == P.SCHED_TILES else "strips",
                          "variant": sched[1], "chunk": sched[2],
                          "form": "unfused" if sched[3] or not fused else "fused",
@@ -721,7 +747,9 @@ def main():
             "cpu_configs": cpu_cfg,
             "configs": configs,
             "clocks": clk,
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": step_launches * args.steps,
+            "gpu_launches_note": "kernel nodes of the captured step graph (pcg_get_step_launches, "
+                                 "%d) x timed steps" % step_launches,
             "wall_s": wall,
         }
         print(json.dumps(line))

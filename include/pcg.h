@@ -324,6 +324,10 @@ int pcg_run(pcg_context *ctx, int32_t steps, int32_t mode, double *dt_hist);
 int pcg_set_step_form(pcg_context *ctx, int32_t form);
 /* *fused = 1 if a step of `mode` takes the fused form with the current lists. */
 int pcg_get_step_form(pcg_context *ctx, int32_t mode, int32_t *fused);
+/* No counterpart in the reference.  *launches = the kernel launches one
+ * batched step issues: the kernel nodes of the CUDA graph that pcg_run last
+ * captured (0 before the first batched pcg_run or after the lists changed). */
+int pcg_get_step_launches(pcg_context *ctx, int32_t *launches);
 /* Cumulative interior cell updates and device time of pcg_step / pcg_run;
  * under local time stepping the cells of the leaves that advanced. */
 int pcg_stats(pcg_context *ctx, int64_t *cell_updates, double *device_ms);

@@ -264,6 +264,7 @@ struct pcg_context {
   bool fused_pending = false;
   bool fused_ready = false;
   bool graph_fused = false;
+  int graph_kernels = 0;  // kernel nodes of the captured step graph
   // second state set of every leaf (6 nx ny doubles at PatchDev::sh_off)
   double *d_shadow = nullptr;
   size_t shadow_cap = 0;
@@ -1983,6 +1984,20 @@ int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
   return PCG_OK;
 }
 
+// Kernel nodes of a captured graph (the launches one replay issues).
+static int count_kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+  int k = 0;
+  for (size_t i = 0; i < n; i++) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+  }
+  return k;
+}
+
 int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   if (!c || steps < 0 || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED))
     return fail(PCG_E_INVALID, "bad arguments");
@@ -2015,6 +2030,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
         if (erc != PCG_OK) return erc;
         if (ce != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        c->graph_kernels = count_kernel_nodes(g);
         cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
@@ -2048,6 +2064,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
       if (erc != PCG_OK) return erc;
       if (le != cudaSuccess) return fail(PCG_E_CUDA, cudaGetErrorString(le));
       if (ce != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      c->graph_kernels = count_kernel_nodes(g);
       cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
       cudaGraphDestroy(g);
       if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
@@ -2075,6 +2092,13 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->device_ms += ms;
   if (!c->ts_local || mode != PCG_MODE_BATCHED) c->cell_updates += c->cells_per_step * steps;
+  return PCG_OK;
+}
+
+int pcg_get_step_launches(pcg_context *c, int32_t *launches) {
+  if (!c || !launches) return fail(PCG_E_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  *launches = c->graph_valid ? c->graph_kernels : 0;
   return PCG_OK;
 }
 

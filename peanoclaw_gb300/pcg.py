@@ -134,6 +134,7 @@ SIGNATURES = {
     "pcg_step": (C.c_int, [_CTX, C.c_int32, _D]),
     "pcg_set_step_form": (C.c_int, [_CTX, C.c_int32]),
     "pcg_get_step_form": (C.c_int, [_CTX, C.c_int32, C.POINTER(C.c_int32)]),
+    "pcg_get_step_launches": (C.c_int, [_CTX, C.POINTER(C.c_int32)]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "pcg_synchronize": (C.c_int, [_CTX]),
@@ -423,6 +424,12 @@ class Context:
         v = C.c_int32()
         check(lib().pcg_get_step_form(self.h, int(mode), C.byref(v)))
         return bool(v.value)
+
+    def step_launches(self):
+        """Kernel launches of one captured batched step (pcg_get_step_launches)."""
+        v = C.c_int32()
+        check(lib().pcg_get_step_launches(self.h, C.byref(v)))
+        return int(v.value)
 
     def run(self, steps, mode=PCG_MODE_BATCHED):
         hist = np.zeros(steps * self.max_groups)

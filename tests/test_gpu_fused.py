@@ -85,6 +85,10 @@ def test_fused_equals_unfused_with_downloads_between_runs():
             rec = []
             for k in (1, 2, 3):
                 rec.append(list(ctx.run(k, P.PCG_MODE_BATCHED)[:, 0]))
+                # fused: sweep with ghost fill and deferred update, time
+                # advance, reset; unfused: reset, ghost fill, walls, sweep,
+                # update, dt history
+                assert ctx.step_launches() == (3 if form == P.FORM_AUTO else 6)
                 rec.append(_bits(ctx.download_many(ids, int(ps.packed.size))))
             for _ in range(2):
                 rec.append(list(ctx.step(P.PCG_MODE_BATCHED)))
