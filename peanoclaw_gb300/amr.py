@@ -438,6 +438,66 @@ def virtual_time_items(order, index, leaf):
     return np.array([(s, v) for v, s in rows], dtype=np.int32).reshape(-1, 2)
 
 
+_POOL = None
+
+
+def _pool():
+    global _POOL
+    if _POOL is None:
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+        _POOL = ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+    return _POOL
+
+
+def ghost_centers_many(pos, size, n):
+    """Cell centres with ghost ring of many patches at once, (K, n+2, n+2)
+    each: the values of scenarios._centers(pos[k], size[k], n, ghost=True),
+    element for element."""
+    pos = np.asarray(pos, dtype=np.float64).reshape(-1, 2)
+    size = np.asarray(size, dtype=np.float64).reshape(-1, 2)
+    r = np.arange(-1, n + 1)
+    h0 = (size[:, 0] / n)[:, None]
+    h1 = (size[:, 1] / n)[:, None]
+    xs = (pos[:, 0:1] + h0 * r) + h0 * 0.5
+    ys = (pos[:, 1:2] + h1 * r) + h1 * 0.5
+    K = len(pos)
+    X = np.ascontiguousarray(np.broadcast_to(xs[:, :, None], (K, n + 2, n + 2)))
+    Y = np.ascontiguousarray(np.broadcast_to(ys[:, None, :], (K, n + 2, n + 2)))
+    return X, Y
+
+
+def bathymetry_many(b_of, pos, size, n, chunk=None):
+    """b_of over the ghost-ring cell centres of many new patches: one
+    vectorised call per chunk of patches, the chunks spread over the host's
+    cores (numpy releases the interpreter lock inside its array loops).
+    b_of must be elementwise, as every scenario's is."""
+    X, Y = ghost_centers_many(pos, size, n)
+    return eval_many(b_of, X, Y, chunk)
+
+
+def eval_many(f, X, Y, chunk=None):
+    """f(X, Y) for an elementwise f over (K, ...) arrays, in chunks of patches
+    spread over the host's cores."""
+    K = len(X)
+    if K == 0:
+        return np.zeros_like(X)
+    if chunk is None:
+        workers = _pool()._max_workers
+        chunk = max(32, -(-K // workers))
+    parts = [(a, min(K, a + chunk)) for a in range(0, K, chunk)]
+    if len(parts) == 1:
+        return np.asarray(f(X, Y), dtype=np.float64)
+    out = np.empty(X.shape, dtype=np.float64)
+
+    def one(ab):
+        a, b = ab
+        out[a:b] = f(X[a:b], Y[a:b])
+
+    list(_pool().map(one, parts))
+    return out
+
+
 def remesh(grid, backend, g, b_of):
     """Apply grid.decide(g) through `backend` and update `grid`.
 
@@ -448,7 +508,6 @@ def remesh(grid, backend, g, b_of):
     interpolate_child(parent, child), coarsen(parent, children),
     switch_to_leaf(handle), install(layout, handles), restrict_all().
     Returns (#refined, #coarsened)."""
-    from .scenarios import _centers
     E1, R1 = grid.decide(g)
     E0, R0 = grid.arrays()
     if all(np.array_equal(a, b) for a, b in zip(E1 + R1, E0 + R0)):
@@ -468,9 +527,13 @@ def remesh(grid, backend, g, b_of):
                     if E0[l + 1][ch[1], ch[2]]:
                         continue
                     pos, size = grid.geometry(*ch)
-                    X, Y = _centers(pos, size, n, ghost=True)
-                    kids.append((parent, ch, pos, size, l + 1, t, b_of(X, Y)))
+                    kids.append([parent, ch, pos, size, l + 1, t, None])
             n_ref += 1
+        # bathymetry of the new children (with ghost ring) in one batch
+        bs = bathymetry_many(b_of, [k[2] for k in kids], [k[3] for k in kids], n)
+        for k, b in zip(kids, bs):
+            k[6] = b
+        kids = [tuple(k) for k in kids]
         if hasattr(backend, "create_children"):
             backend.create_children(kids)
         else:

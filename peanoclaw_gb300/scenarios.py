@@ -320,12 +320,21 @@ def amr_patchset(grid, h_of, b_of):
         ps.level.append(lay["level"][k])
         ps.wall.append(lay["wall"][k])
     ps.finalize_layout()
+    # every patch's cell centres at once; b and h evaluated in batches over
+    # the host's cores (the values of a per-patch evaluation, element for
+    # element)
+    from .amr import eval_many, ghost_centers_many
+    X, Y = ghost_centers_many(ps.pos, ps.size, n)
+    B = eval_many(b_of, X, Y)
+    leaves = [p for p in range(len(ps)) if ps.leaf[p]]
+    H = eval_many(h_of, np.ascontiguousarray(X[leaves, 1:-1, 1:-1]),
+                  np.ascontiguousarray(Y[leaves, 1:-1, 1:-1])) if leaves else None
+    hk = {p: k for k, p in enumerate(leaves)}
     for p in range(len(ps)):
         unew, uold, b = ps.views(p)
-        X, Y = _centers(ps.pos[p], ps.size[p], n, ghost=True)
-        b[:] = b_of(X, Y)
+        b[:] = B[p]
         if ps.leaf[p]:
-            unew[0] = h_of(X[1:-1, 1:-1], Y[1:-1, 1:-1])
+            unew[0] = H[hk[p]]
     ps.items = lay["items"]
     ps.flux_items = lay["flux_items"]
     ps.restrict_items = lay["restrict_items"]
