@@ -232,12 +232,14 @@ struct pcg_context {
   std::vector<int> restr_begin, flux_begin, restr_dsts;
   int4 *d_restr = nullptr, *d_flux = nullptr;
   int *d_restr_begin = nullptr, *d_flux_begin = nullptr, *d_restr_dsts = nullptr, *d_leaf_ids = nullptr;
-  int *d_restr_dirty = nullptr;
-  size_t d_rdirty_cap = 0;
-  pcg::RestrItemTab *d_restr_tab = nullptr;  // per restriction item, rewritten every step
-  size_t d_rtab_cap = 0;
-  int *d_restr_bad = nullptr;                // per destination: item-by-item form
-  size_t d_rbad_cap = 0;
+  pcg::RestrItemTab *d_restr_geo = nullptr;  // region geometry per restriction item
+  int *d_restr_geo_bad = nullptr;            // per destination: item-by-item form
+  int2 *d_restr_chunks = nullptr;            // (destination, chunk) work items of the restriction
+  std::vector<int2> h_restr_chunks;
+  size_t d_rgeo_cap = 0, d_rgeob_cap = 0, d_rch_cap = 0;
+  bool restr_geo_dirty = true;               // lists, geometry or restriction bounds changed
+  pcg::TransferCtl *d_xfer = nullptr;  // work counters and error word of k_level_transfer
+  bool xfer_pending = false;           // a level transfer ran since its error word was read
   size_t d_restr_cap = 0, d_flux_cap = 0, d_rb_cap = 0, d_fb_cap = 0, d_rd_cap = 0, d_leaf_cap = 0;
   double g_flux = 1.0;
 
@@ -666,9 +668,16 @@ int rebuild_topology(pcg_context *c) {
   if ((rc = ensure_device(c, &c->d_restr_begin, &c->d_rb_cap, c->restr_begin.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_flux_begin, &c->d_fb_cap, c->flux_begin.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_restr_dsts, &c->d_rd_cap, c->restr_dsts.size())) != PCG_OK) return rc;
-  if ((rc = ensure_device(c, &c->d_restr_dirty, &c->d_rdirty_cap, c->restr_dsts.size())) != PCG_OK) return rc;
-  if ((rc = ensure_device(c, &c->d_restr_tab, &c->d_rtab_cap, c->h_restr.size())) != PCG_OK) return rc;
-  if ((rc = ensure_device(c, &c->d_restr_bad, &c->d_rbad_cap, c->restr_dsts.size())) != PCG_OK) return rc;
+  c->h_restr_chunks.clear();
+  for (size_t b = 0; b < c->restr_dsts.size(); b++) {
+    const pcg::PatchDev &D = c->h_patches[c->restr_dsts[b]];
+    const int n = D.nx * D.ny;
+    for (int k = 0; k * pcg::kRestrChunkCells < n; k++) c->h_restr_chunks.push_back(make_int2((int)b, k));
+  }
+  if ((rc = ensure_device(c, &c->d_restr_chunks, &c->d_rch_cap, c->h_restr_chunks.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_restr_geo, &c->d_rgeo_cap, c->h_restr.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_restr_geo_bad, &c->d_rgeob_cap, c->restr_dsts.size())) != PCG_OK) return rc;
+  c->restr_geo_dirty = true;
   if ((rc = ensure_device(c, &c->d_leaf_ids, &c->d_leaf_cap, c->leaf_ids.size())) != PCG_OK) return rc;
   auto up = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) : cudaSuccess;
@@ -678,6 +687,7 @@ int rebuild_topology(pcg_context *c) {
   PCG_CUDA(up(c->d_restr_begin, c->restr_begin.data(), sizeof(int) * c->restr_begin.size()));
   PCG_CUDA(up(c->d_flux_begin, c->flux_begin.data(), sizeof(int) * c->flux_begin.size()));
   PCG_CUDA(up(c->d_restr_dsts, c->restr_dsts.data(), sizeof(int) * c->restr_dsts.size()));
+  PCG_CUDA(up(c->d_restr_chunks, c->h_restr_chunks.data(), sizeof(int2) * c->h_restr_chunks.size()));
   PCG_CUDA(up(c->d_leaf_ids, c->leaf_ids.data(), sizeof(int) * c->leaf_ids.size()));
   PCG_CUDA(up(c->d_vt, c->h_vt.data(), sizeof(int2) * c->h_vt.size()));
   PCG_CUDA(up(c->d_vt_virtuals, c->vt_virtuals.data(), sizeof(int) * c->vt_virtuals.size()));
@@ -731,33 +741,57 @@ int upload_group_max_dt(pcg_context *c) {
   return PCG_OK;
 }
 
+// The region geometry of the restriction list, when the lists, the patches'
+// geometry or the restriction bounds changed since it was built (called
+// before a step graph is captured, so that a graph holds no rebuild).
+int refresh_restr_geometry(pcg_context *c) {
+  if (!c->restr_geo_dirty || c->h_restr.empty()) return PCG_OK;
+  PCG_CUDA(pcg::launch_restr_geometry(c->stream, c->d_patches, c->d_times, c->d_restr, c->d_restr_begin,
+                                      (int)c->restr_dsts.size(), c->d_restr_geo, c->d_restr_geo_bad));
+  c->restr_geo_dirty = false;
+  return PCG_OK;
+}
+
 // Flux correction (computeFluxes of every leaf, then the correction list) and
 // restriction into the virtual patches (clear, restrict list, post-process),
-// the order in which SolveTimestep::enterCell and Remesh::leaveCell run them.
-int enqueue_post_update(pcg_context *c) {
+// the order in which SolveTimestep::enterCell and Remesh::leaveCell run them,
+// in one launch (k_level_transfer).
+int enqueue_level_transfer(pcg_context *c, bool flux, bool restr, const int *group_active, const int *pact) {
   using namespace pcg;
-  const int *ga = c->d_group_active;
-  if (!c->h_flux.empty()) {
-    PCG_CUDA(launch_compute_fluxes(c->stream, c->slab, c->d_patches, c->d_leaf_ids, (int)c->leaf_ids.size(),
-                                   c->g_flux, ga));
-    PCG_CUDA(launch_flux_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_flux, c->d_flux_begin,
-                               (int)c->flux_begin.size() - 1, ga));
+  flux = flux && !c->h_flux.empty();
+  restr = restr && !c->h_restr.empty();
+  const int n_leaf = flux ? (int)c->leaf_ids.size() : 0;
+  const int n_flux = flux ? (int)c->flux_begin.size() - 1 : 0;
+  const int n_restr = restr ? (int)c->h_restr_chunks.size() : 0;
+  const int grid = level_transfer_grid(c->num_sms, n_leaf, n_flux, n_restr);
+  if (grid <= 0) return PCG_OK;
+  if (restr) {
+    int rc = refresh_restr_geometry(c);
+    if (rc != PCG_OK) return rc;
   }
-  if (!c->h_restr.empty()) {
-    int nd = (int)c->restr_dsts.size();
-    // under local time stepping only destinations with an advancing source
-    const int *dirty = nullptr;
-    if (c->ts_local) {
-      PCG_CUDA(launch_restr_dirty(c->stream, c->d_restr, c->d_restr_begin, nd, c->d_pact, c->d_restr_dirty));
-      dirty = c->d_restr_dirty;
-    }
-    PCG_CUDA(launch_restr_prepare(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr, c->d_restr_begin,
-                                  c->d_restr_dsts, nd, c->d_restr_tab, c->d_restr_bad, ga, dirty));
-    PCG_CUDA(launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
-                                   c->d_restr_begin, nd, restr_split(nd, c->num_sms), c->d_restr_tab,
-                                   c->d_restr_bad, ga, dirty));
-    PCG_CUDA(launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd, ga,
-                                             dirty));
+  PCG_CUDA(launch_level_transfer(c->stream, grid, c->slab, c->d_patches, c->d_times, c->d_leaf_ids, n_leaf,
+                                 c->g_flux, c->d_flux, c->d_flux_begin, n_flux, c->d_restr, c->d_restr_begin,
+                                 c->d_restr_geo, c->d_restr_geo_bad, c->d_restr_chunks, n_restr, group_active,
+                                 pact, c->d_xfer));
+  c->xfer_pending = true;
+  return PCG_OK;
+}
+
+int enqueue_post_update(pcg_context *c) {
+  return enqueue_level_transfer(c, true, true, c->d_group_active, c->ts_local ? c->d_pact : nullptr);
+}
+
+// After the stream has been synchronised: the error word of the level
+// transfers since the last check (a phase wait that ran out).
+int check_level_transfer(pcg_context *c) {
+  if (!c->xfer_pending) return PCG_OK;
+  c->xfer_pending = false;
+  int err = 0;
+  PCG_CUDA(cudaMemcpy(&err, &c->d_xfer->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    PCG_CUDA(cudaMemset(c->d_xfer, 0, sizeof(pcg::TransferCtl)));
+    return fail(PCG_E_CUDA, "level transfer: a wait between its phases ran out; the step's flux correction "
+                            "and restriction are incomplete");
   }
   return PCG_OK;
 }
@@ -1131,6 +1165,8 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->d_dt_out, sizeof(double) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_solve_out, sizeof(double) * 2));
   CREATE_CK(cudaMalloc(&c->d_counter, sizeof(int)));
+  CREATE_CK(cudaMalloc(&c->d_xfer, sizeof(pcg::TransferCtl)));
+  CREATE_CK(cudaMemset(c->d_xfer, 0, sizeof(pcg::TransferCtl)));
   CREATE_CK(cudaMallocHost(&c->h_pinned, sizeof(double) * std::max(64, c->max_groups)));
 #undef CREATE_CK
   *out = c;
@@ -1170,9 +1206,10 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_restr_begin);
   cudaFree(c->d_flux_begin);
   cudaFree(c->d_restr_dsts);
-  cudaFree(c->d_restr_dirty);
-  cudaFree(c->d_restr_tab);
-  cudaFree(c->d_restr_bad);
+  cudaFree(c->d_xfer);
+  cudaFree(c->d_restr_geo);
+  cudaFree(c->d_restr_geo_bad);
+  cudaFree(c->d_restr_chunks);
   cudaFree(c->d_leaf_ids);
   cudaFree(c->d_plan);
   cudaFree(c->d_copy_plan);
@@ -1337,6 +1374,7 @@ int pcg_patch_set_time(pcg_context *c, int32_t id, const pcg_patch_time *t) {
   d.ru[0] = t->restr_upper[0]; d.ru[1] = t->restr_upper[1];
   PCG_CUDA(cudaMemcpyAsync(c->d_times + id, &d, sizeof(d), cudaMemcpyHostToDevice, c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
+  c->restr_geo_dirty = true;
   return PCG_OK;
 }
 
@@ -1544,6 +1582,7 @@ int pcg_patches_set_time(pcg_context *c, int32_t n, const int32_t *ids, const pc
   PCG_CUDA(pcg::launch_scatter_times(c->stream, c->d_copy_meta,
                                      reinterpret_cast<const pcg::PatchTimeDev *>(c->d_staging), n, c->d_times));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
+  c->restr_geo_dirty = true;
   return PCG_OK;
 }
 
@@ -1685,6 +1724,7 @@ int pcg_patches_set_restriction_bounds(pcg_context *c, int32_t n, const int32_t 
                                                                              c->d_times);
   PCG_CUDA(cudaGetLastError());
   PCG_CUDA(cudaStreamSynchronize(c->stream));
+  c->restr_geo_dirty = true;
   return PCG_OK;
 }
 
@@ -1843,18 +1883,10 @@ int pcg_restrict_all(pcg_context *c) {
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
-  if (!c->h_restr.empty()) {
-    int nd = (int)c->restr_dsts.size();
-    PCG_CUDA(pcg::launch_restr_prepare(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
-                                       c->d_restr_begin, c->d_restr_dsts, nd, c->d_restr_tab,
-                                       c->d_restr_bad));
-    PCG_CUDA(pcg::launch_restrict_items(c->stream, c->slab, c->d_patches, c->d_times, c->d_restr,
-                                        c->d_restr_begin, nd, pcg::restr_split(nd, c->num_sms),
-                                        c->d_restr_tab, c->d_restr_bad));
-    PCG_CUDA(pcg::launch_post_process_restriction(c->stream, c->slab, c->d_patches, c->d_restr_dsts, nd));
-  }
+  // every destination, whatever the groups' and leaves' state
+  if ((rc = enqueue_level_transfer(c, false, true, nullptr, nullptr)) != PCG_OK) return rc;
   PCG_CUDA(cudaStreamSynchronize(c->stream));
-  return PCG_OK;
+  return check_level_transfer(c);
 }
 
 int pcg_set_group_end_time(pcg_context *c, int32_t group, double time, double t_end) {
@@ -1976,6 +2008,10 @@ int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
                              c->stream));
   }
   PCG_CUDA(cudaStreamSynchronize(c->stream));
+  {
+    const int xrc = check_level_transfer(c);
+    if (xrc != PCG_OK) return xrc;
+  }
   float ms = 0.f;
   PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->device_ms += ms;
@@ -2013,6 +2049,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   if (!fused) {
     PCG_SETTLE(c);
     if ((rc = refresh_fin(c)) != PCG_OK) return rc;
+    if ((rc = refresh_restr_geometry(c)) != PCG_OK) return rc;
   }
   if ((rc = ensure_hist(c, steps)) != PCG_OK) return rc;
   PCG_CUDA(cudaMemsetAsync(c->d_counter, 0, sizeof(int), c->stream));
@@ -2088,6 +2125,10 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
     PCG_CUDA(cudaMemcpyAsync(dt_hist, c->d_hist, sizeof(double) * (size_t)steps * c->max_groups,
                              cudaMemcpyDeviceToHost, c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
+  {
+    const int xrc = check_level_transfer(c);
+    if (xrc != PCG_OK) return xrc;
+  }
   float ms = 0.f;
   PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->device_ms += ms;

@@ -181,8 +181,10 @@ __device__ __forceinline__ bool tl_equals(double a, double b) {
   return fabs(__dsub_rn(a, b)) <= kTarchEps;
 }
 
+// (the divides on the integer pipes: the IEEE quotients, without FP64-pipe
+// Newton steps)
 __device__ __forceinline__ double subcell(const PatchDev &p, int d) {
-  return __ddiv_rn(p.size[d], (double)(d == 0 ? p.nx : p.ny));
+  return ieee::div_rn(p.size[d], (double)(d == 0 ? p.nx : p.ny));
 }
 // Patch::getSubcellCenter: (pos + h*i) + h*0.5
 __device__ __forceinline__ double subcell_center(const PatchDev &p, int d, int i) {
@@ -191,7 +193,7 @@ __device__ __forceinline__ double subcell_center(const PatchDev &p, int d, int i
 }
 // SubgridIterator::getCellPosition: pos + i * (size * (1/n))
 __device__ __forceinline__ double iter_sub(const PatchDev &p, int d) {
-  return __dmul_rn(p.size[d], __ddiv_rn(1.0, (double)(d == 0 ? p.nx : p.ny)));
+  return __dmul_rn(p.size[d], ieee::rcp_rn((double)(d == 0 ? p.nx : p.ny)));
 }
 __device__ __forceinline__ double iter_pos(const PatchDev &p, int d, int i) {
   return __dadd_rn(p.pos[d], __dmul_rn((double)i, iter_sub(p, d)));

@@ -935,8 +935,9 @@ __device__ int regions_overlapped(const double lower[2], const double upper[2], 
   const double eps = 1e-12;
   int lo[2], up[2];
   for (int d = 0; d < 2; d++) {
-    double dl = __dadd_rn(__dmul_rn(__dsub_rn(lower[d], sp[d]), __ddiv_rn(1.0, sub[d])), eps);
-    double du = __dsub_rn(__dmul_rn(__dsub_rn(upper[d], sp[d]), __ddiv_rn(1.0, sub[d])), eps);
+    const double isub = ieee::rcp_rn(sub[d]);
+    double dl = __dadd_rn(__dmul_rn(__dsub_rn(lower[d], sp[d]), isub), eps);
+    double du = __dsub_rn(__dmul_rn(__dsub_rn(upper[d], sp[d]), isub), eps);
     dl = fmin(2147483647.0, dl);
     du = fmax(-2147483648.0, du);
     int a = (int)floor(dl), b = (int)floor(du);
@@ -968,11 +969,11 @@ __device__ void map_to_patch(const int roff[2], const int rsz[2], const PatchDev
     double ss = subcell(S, d), ds = subcell(D, d);
     double position = __dmul_rn(ss, (double)roff[d]);
     position = __dadd_rn(position, __dsub_rn(S.pos[d], D.pos[d]));
-    double ot = __ddiv_rn(__dadd_rn(position, eps), ds);
+    double ot = ieee::div_rn(__dadd_rn(position, eps), ds);
     ooff[d] = (int)ot;
     double size = __dmul_rn(ss, (double)(roff[d] + rsz[d]));
     size = __dadd_rn(size, __dsub_rn(S.pos[d], D.pos[d]));
-    double st = __ddiv_rn(__dsub_rn(size, eps), ds);
+    double st = ieee::div_rn(__dsub_rn(size, eps), ds);
     st = __dsub_rn(st, (double)ooff[d]);
     st = __dadd_rn(st, 1.0);
     osz[d] = (int)st;
@@ -1067,7 +1068,6 @@ __global__ void k_restrict(double *slab, const PatchDev *patches, const PatchTim
 // One warp per destination cell of a region: the lanes evaluate the
 // contributions of up to 32 source cells at a time, lane 0 adds them to the
 // cell's uOld / uNew values in source-cell order.
-constexpr int kRestrWarps = 6;   // warps per CTA of the batched restriction (one sum per thread)
 __device__ void restrict_items_in_order(double *slab, const PatchDev *patches, const PatchTimeDev *times,
                                         const int4 *items, int b0, int b1, double (*W)[32][6]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1192,210 +1192,141 @@ __device__ void restrict_items_in_order(double *slab, const PatchDev *patches, c
 }
 
 
-// Batched restriction, in two kernels per step.
+// Batched restriction of one destination (the restriction phase of
+// k_level_transfer): the table of its items, then each interior cell once.
 //
-// k_restr_prepare (one CTA per destination): clears the destination's
-// interior (uOld and uNew, as k_clear_interior) and writes the table of its
-// items [begin[b], begin[b+1]): per item the source, the time factors of its
-// uOld / uNew values at the virtual times 0 and 1, and its regions (item
-// order, then region order) mapped into the destination.  bad[b] is set when
-// the destination needs the item-by-item form instead (more than
-// kRestrMaxItems items, more than 3 unknowns, or a region leaving the
-// destination).
+// restr_table_entry: per item the source, the time factors of its uOld / uNew
+// values at the virtual times 0 and 1, and its regions (item order, then
+// region order) mapped into the destination; *bad is set when a region
+// leaves the destination (the item-by-item form is taken then).
 //
-// k_restrict_items (`split` CTAs per destination): each CTA copies the table
-// into shared memory; then one thread per (destination cell, unknown, time
-// level) walks the table in order and adds the terms of every source cell of
-// every matching region.  Each of a cell's six sums is therefore formed in
-// exactly the order of the item-by-item restriction (the six are independent
-// of each other), and the cells of one destination need no barrier between
-// items.  Only the cells of the regions' destination rectangles are visited
-// (with overlapped-only restriction these are the few cells under the
-// neighbours' ghost layers), rectangle by rectangle, each cell from the first
-// rectangle that holds it.  All rectangles of a destination form one task
-// space, dealt to its CTAs in blocks of one CTA's threads, so that a
-// destination with a few small rectangles (the rims of the adaptive
-// breaking dam: three of 54 tasks) runs them side by side in one CTA rather
-// than one after another; dealing tasks round-robin over the CTAs measured
-// 2x slower there.  Destinations flagged bad take
-// restrict_items_in_order in their first CTA.
-constexpr int kRestrPerCell = 6;                       // 3 unknowns x (uOld, uNew)
+// restr_cell_pair: the restricted uOld and uNew values of unknown q of the
+// destination cell (x, y) -- the sums that the reference's clear,
+// restrictSolution over the items in list order and postProcessRestriction
+// leave in the cell, each formed in exactly that order: from the cleared
+// 0.0, for every region of every item that holds the cell the terms of its
+// source cells in loop order, then h + (-1 b).  The two sums share the
+// regions, bounds and loads; the three unknowns of a cell are separate tasks.
+// Per item of a destination: its regions in the source (the first half of a
+// table entry, one thread per item).
+struct RestrItemPre {
+  double tfo, tfn;
+  int src, nr, swe, pad_;
+  int roff[8], rsz[8];
+};
 
-__global__ void __launch_bounds__(256)
-    k_restr_prepare(double *slab, const PatchDev *patches, const PatchTimeDev *times, const int4 *items,
-                    const int *begin, const int *ids, int count, RestrItemTab *tab, int *bad,
-                    const int *group_active, const int *dirty) {
-  __shared__ int s_bad;
-  if ((int)blockIdx.x >= count) return;
-  if (dirty && !dirty[blockIdx.x]) return;
-  const PatchDev D = patches[ids[blockIdx.x]];
-  if (group_active && !group_active[D.group]) return;
-  const int n = D.nx * D.ny;
-  for (int k = threadIdx.x; k < D.nq * n; k += blockDim.x) {
-    int q = k / n, c = k - q * n, x = c / D.ny, y = c - x * D.ny;
-    slab[idx_unew(D, q, x, y)] = 0.0;
-    slab[idx_uold(D, q, x, y)] = 0.0;
+// The time factors of a source's uOld / uNew values at the virtual times 0
+// and 1 (the interpolation weights of DefaultRestriction).
+__device__ __forceinline__ void restr_time_factors(const PatchDev &S, const PatchTimeDev &ST, double &tfo,
+                                                   double &tfn) {
+  tfo = 1.0;
+  tfn = 1.0;
+  if (tl_greater(ST.dt, 0.0)) {
+    double so = time_uold(S, ST), su = time_unew(S, ST);
+    tfo = ieee::div_rn(__dsub_rn(0.0, so), __dsub_rn(su, so));
+    tfn = ieee::div_rn(__dsub_rn(1.0, so), __dsub_rn(su, so));
   }
-  const int b0 = begin[blockIdx.x], ni = begin[blockIdx.x + 1] - b0;
-  if (threadIdx.x == 0) s_bad = (ni > kRestrMaxItems || D.nq > 3) ? 1 : 0;
-  __syncthreads();
-  const double eps = 1e-12;
-  for (int t = threadIdx.x; t < ni && !s_bad; t += blockDim.x) {
-    const int4 it = items[b0 + t];
-    const PatchDev S = patches[it.x];
-    const PatchTimeDev ST = times[it.x], DT = times[it.y];
-    RestrItemTab E;
-    int roff[8], rsz[8], nr;
-    int nn[2] = {S.nx, S.ny};
-    if (it.z != 0) {
-      double sp[2] = {S.pos[0], S.pos[1]}, ss[2] = {S.size[0], S.size[1]};
-      double sub[2] = {subcell(S, 0), subcell(S, 1)};
-      nr = regions_overlapped(DT.rl, DT.ru, sp, ss, sub, nn, roff, rsz);
-    } else {
-      nr = 1;
-      roff[0] = 0; roff[1] = 0; rsz[0] = nn[0]; rsz[1] = nn[1];
-    }
-    double tfo = 1.0, tfn = 1.0;
-    if (tl_greater(ST.dt, 0.0)) {
-      double so = time_uold(S, ST), su = time_unew(S, ST);
-      tfo = __ddiv_rn(__dsub_rn(0.0, so), __dsub_rn(su, so));
-      tfn = __ddiv_rn(__dsub_rn(1.0, so), __dsub_rn(su, so));
-    }
-    E.tfo = tfo; E.tfn = tfn; E.src = it.x; E.nr = nr; E.swe = it.w; E.pad_ = 0;
-    for (int r = 0; r < 4; r++) {
-      int doff[2] = {0, 0}, dsz[2] = {0, 0};
-      if (r < nr && !(it.z != 0 && !(rsz[2 * r] > 0 && rsz[2 * r + 1] > 0))) {
-        map_to_patch(&roff[2 * r], &rsz[2 * r], S, D, eps, doff, dsz);
-        if (dsz[0] > 0 && dsz[1] > 0 &&
-            (doff[0] < 0 || doff[1] < 0 || doff[0] + dsz[0] > D.nx || doff[1] + dsz[1] > D.ny))
-          atomicOr(&s_bad, 1);
-      }
-      for (int d = 0; d < 2; d++) {
-        E.doff[r][d] = doff[d];
-        E.dsz[r][d] = dsz[d] > 0 ? dsz[d] : 0;
-        E.ro[r][d] = r < nr ? roff[2 * r + d] : 0;
-        E.rs[r][d] = r < nr ? rsz[2 * r + d] : 0;
-      }
-    }
-    tab[b0 + t] = E;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) bad[blockIdx.x] = s_bad;
 }
 
-__global__ void __launch_bounds__(kRestrWarps * 32)
-    k_restrict_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                     const int4 *items, const int *begin, int split, const RestrItemTab *tab,
-                     const int *bad, const int *group_active, const int *dirty) {
-  __shared__ double W[kRestrWarps][32][6];
-  __shared__ RestrItemTab T[kRestrMaxItems];
-  __shared__ int P[4 * kRestrMaxItems + 1];
-  const int dst_block = blockIdx.x / split, part = blockIdx.x % split;
-  if (dirty && !dirty[dst_block]) return;
-  const int b0 = begin[dst_block], b1 = begin[dst_block + 1];
-  const PatchDev D = patches[items[b0].y];
-  if (group_active && !group_active[D.group]) return;
-  if (bad[dst_block]) {
-    if (part == 0) restrict_items_in_order(slab, patches, times, items, b0, b1, W);
-    return;
+__device__ void restr_item_pre(const PatchDev *patches, const PatchTimeDev *times, const int4 it,
+                               RestrItemPre &E) {
+  const PatchDev S = patches[it.x];
+  const PatchTimeDev DT = times[it.y];
+  int nn[2] = {S.nx, S.ny};
+  int nr;
+  if (it.z != 0) {
+    double sp[2] = {S.pos[0], S.pos[1]}, ss[2] = {S.size[0], S.size[1]};
+    double sub[2] = {subcell(S, 0), subcell(S, 1)};
+    nr = regions_overlapped(DT.rl, DT.ru, sp, ss, sub, nn, E.roff, E.rsz);
+  } else {
+    nr = 1;
+    for (int k = 0; k < 8; k++) { E.roff[k] = 0; E.rsz[k] = 0; }
+    E.rsz[0] = nn[0]; E.rsz[1] = nn[1];
   }
-  const int ni = b1 - b0;
-  for (int t = threadIdx.x; t < ni; t += blockDim.x) T[t] = tab[b0 + t];
-  __syncthreads();
-  // task prefix over the rectangles (item order, region order): all of a
-  // destination's rectangles form one task space, dealt to its CTAs in
-  // blocks of one CTA's threads
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int e = 0; e < 4 * ni; e++) {
-      const int te = e >> 2, re = e & 3;
-      P[e] = acc;
-      if (re < (T[te].nr < 4 ? T[te].nr : 4)) acc += T[te].dsz[re][0] * T[te].dsz[re][1] * kRestrPerCell;
-    }
-    P[4 * ni] = acc;
-  }
-  __syncthreads();
+  E.tfo = 1.0; E.tfn = 1.0; E.src = it.x; E.nr = nr; E.swe = it.w; E.pad_ = it.z;
+}
+
+// Region r of an item mapped into the destination (the second half, one
+// thread per (item, region)); *bad is set when it leaves the destination.
+__device__ void restr_item_region(const PatchDev *patches, const RestrItemPre &P, int r, const PatchDev &D,
+                                  RestrItemTab &E, int *bad) {
   const double eps = 1e-12;
-  const double dsub[2] = {iter_sub(D, 0), iter_sub(D, 1)};
-  const double dvol = __dmul_rn(dsub[0], dsub[1]);
-  // the cells of the regions' destination rectangles, rectangle by
-  // rectangle in table order; a cell inside an earlier rectangle as well is
-  // left to that one
-  const int stride = split * (int)blockDim.x;
-  const int ntask = P[4 * ni];
-  for (int k = part * (int)blockDim.x + (int)threadIdx.x; k < ntask; k += stride) {
-    // rectangle e holding task k: the last e with P[e] <= k and a
-    // non-empty task range (binary search over the prefix)
-    int lo = 0, hi = 4 * ni - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (P[mid] <= k) lo = mid;
-      else hi = mid - 1;
-    }
-    const int e = lo;
-    const int te = e >> 2, re = e & 3;
-    const int w1 = T[te].dsz[re][1];
-    const int kk = k - P[e];
-    const int cell = kk / kRestrPerCell, comp = kk - cell * kRestrPerCell;
-    const int q = comp % 3, level = comp / 3;  // level 0: uOld (time 0), 1: uNew (time 1)
-    if (q >= D.nq) continue;
-    const int x = T[te].doff[re][0] + cell / w1, y = T[te].doff[re][1] + cell % w1;
-    bool earlier = false;
-    for (int f = 0; f < e && !earlier; f++) {
-      const int tq = f >> 2, rq = f & 3;
-      if (rq >= (T[tq].nr < 4 ? T[tq].nr : 4)) continue;
-      earlier = x >= T[tq].doff[rq][0] && x < T[tq].doff[rq][0] + T[tq].dsz[rq][0] &&
-                y >= T[tq].doff[rq][1] && y < T[tq].doff[rq][1] + T[tq].dsz[rq][1];
-    }
-    if (earlier) continue;
-    // the cell's sum over every matching region of every item, in order
-    double dpos[2] = {0.0, 0.0};
-    double acc = 0.0;
-    bool any = false;
-    for (int t = 0; t < ni; t++) {
-      const int nr = T[t].nr < 4 ? T[t].nr : 4;
-      for (int r = 0; r < nr; r++) {
-        if (!(x >= T[t].doff[r][0] && x < T[t].doff[r][0] + T[t].dsz[r][0] && y >= T[t].doff[r][1] &&
-              y < T[t].doff[r][1] + T[t].dsz[r][1]))
-          continue;
-        if (!any) {
-          dpos[0] = iter_pos(D, 0, x);
-          dpos[1] = iter_pos(D, 1, y);
-        }
-        const PatchDev S = patches[T[t].src];
-        const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
-        int coff[2], csz[2];
-        for (int d = 0; d < 2; d++) {
-          double ot = ieee::div_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
-          int o = (int)ot;
-          double st = ieee::div_rn(__dsub_rn(__dsub_rn(__dadd_rn(dpos[d], dsub[d]), S.pos[d]), eps), ssub[d]);
-          st = __dsub_rn(st, ot);
-          st = __dadd_rn(st, 1.0);
-          int up = o + (int)st;
-          int rup = T[t].ro[r][d] + T[t].rs[r][d];
-          int oo = o > T[t].ro[r][d] ? o : T[t].ro[r][d];
-          int uu = up < rup ? up : rup;
-          coff[d] = oo;
-          csz[d] = uu - oo;
-        }
-        if (!(csz[0] > 0 && csz[1] > 0)) continue;
-        if (!any) {
-          any = true;
-          acc = level ? slab[idx_unew(D, q, x, y)] : slab[idx_uold(D, q, x, y)];
-        }
-        const double tf = level ? T[t].tfn : T[t].tfo;
-        const double itf = __dsub_rn(1.0, tf);
-        const bool addb = T[t].swe != 0 && q == 0;
-        for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++)
-          for (int sy = coff[1]; sy < coff[1] + csz[1]; sy++) {
-            const double spos[2] = {iter_pos(S, 0, sx), iter_pos(S, 1, sy)};
-            double region = 1.0;
-            for (int d = 0; d < 2; d++) {
-              double a = __dadd_rn(dpos[d], dsub[d]), b = __dadd_rn(spos[d], ssub[d]);
-              double lo = dpos[d] > spos[d] ? dpos[d] : spos[d];
-              region = __dmul_rn(region, __dsub_rn(a < b ? a : b, lo));
-              region = fmax(region, 0.0);
-            }
+  const int nr = P.nr;
+  int doff[2] = {0, 0}, dsz[2] = {0, 0};
+  if (r < nr && !(P.pad_ != 0 && !(P.rsz[2 * r] > 0 && P.rsz[2 * r + 1] > 0))) {
+    const PatchDev S = patches[P.src];
+    map_to_patch(&P.roff[2 * r], &P.rsz[2 * r], S, D, eps, doff, dsz);
+    if (dsz[0] > 0 && dsz[1] > 0 &&
+        (doff[0] < 0 || doff[1] < 0 || doff[0] + dsz[0] > D.nx || doff[1] + dsz[1] > D.ny))
+      atomicOr(bad, 1);
+  }
+  for (int d = 0; d < 2; d++) {
+    E.doff[r][d] = doff[d];
+    E.dsz[r][d] = dsz[d] > 0 ? dsz[d] : 0;
+    E.ro[r][d] = r < nr ? P.roff[2 * r + d] : 0;
+    E.rs[r][d] = r < nr ? P.rsz[2 * r + d] : 0;
+  }
+  if (r == 0) {
+    E.tfo = P.tfo; E.tfn = P.tfn; E.src = P.src; E.nr = nr; E.swe = P.swe; E.pad_ = 0;
+  }
+}
+
+__device__ __forceinline__ bool restr_covers(const RestrItemTab &E, int r, int x, int y) {
+  return x >= E.doff[r][0] && x < E.doff[r][0] + E.dsz[r][0] && y >= E.doff[r][1] &&
+         y < E.doff[r][1] + E.dsz[r][1];
+}
+
+constexpr int kRestrBatch = 3;
+__device__ void restr_cell_pair(double *slab, const PatchDev *patches, const PatchDev &D,
+                                const RestrItemTab *T, int ni, int x, int y, int q, const double dsub[2],
+                                double dvol) {
+  const double eps = 1e-12;
+  const double dpos[2] = {iter_pos(D, 0, x), iter_pos(D, 1, y)};
+  const double da[2] = {__dadd_rn(dpos[0], dsub[0]), __dadd_rn(dpos[1], dsub[1])};
+  double acc0 = 0.0, acc1 = 0.0;  // the cleared uOld / uNew values
+  for (int t = 0; t < ni; t++) {
+    const int nr = T[t].nr < 4 ? T[t].nr : 4;
+    for (int r = 0; r < nr; r++) {
+      if (!restr_covers(T[t], r, x, y)) continue;
+      const PatchDev S = patches[T[t].src];
+      const double ssub[2] = {iter_sub(S, 0), iter_sub(S, 1)};
+      int coff[2], csz[2];
+      for (int d = 0; d < 2; d++) {
+        double ot = ieee::div_rn(__dadd_rn(__dsub_rn(dpos[d], S.pos[d]), eps), ssub[d]);
+        int o = (int)ot;
+        double st = ieee::div_rn(__dsub_rn(__dsub_rn(da[d], S.pos[d]), eps), ssub[d]);
+        st = __dsub_rn(st, ot);
+        st = __dadd_rn(st, 1.0);
+        int up = o + (int)st;
+        int rup = T[t].ro[r][d] + T[t].rs[r][d];
+        int oo = o > T[t].ro[r][d] ? o : T[t].ro[r][d];
+        int uu = up < rup ? up : rup;
+        coff[d] = oo;
+        csz[d] = uu - oo;
+      }
+      if (!(csz[0] > 0 && csz[1] > 0)) continue;
+      const double tfo = T[t].tfo, tfn = T[t].tfn;
+      const double itfo = __dsub_rn(1.0, tfo), itfn = __dsub_rn(1.0, tfn);
+      const bool addb = T[t].swe != 0 && q == 0;
+      for (int sx = coff[0]; sx < coff[0] + csz[0]; sx++) {
+        // the x factor of the overlap area, once per source column
+        const double sp0 = __dadd_rn(S.pos[0], __dmul_rn((double)sx, ssub[0]));
+        const double b0 = __dadd_rn(sp0, ssub[0]);
+        const double lo0 = dpos[0] > sp0 ? dpos[0] : sp0;
+        const double r0 = fmax(__dmul_rn(1.0, __dsub_rn(da[0] < b0 ? da[0] : b0, lo0)), 0.0);
+        // the terms of up to kRestrBatch source cells of the column are
+        // formed side by side (independent divide chains), then added in
+        // source order
+        const int sy_end = coff[1] + csz[1];
+        for (int sy0 = coff[1]; sy0 < sy_end; sy0 += kRestrBatch) {
+          double t0[kRestrBatch], t1[kRestrBatch];
+#pragma unroll
+          for (int u = 0; u < kRestrBatch; u++) {
+            const int sy = sy0 + u < sy_end ? sy0 + u : sy_end - 1;
+            const double sp1 = __dadd_rn(S.pos[1], __dmul_rn((double)sy, ssub[1]));
+            const double b1 = __dadd_rn(sp1, ssub[1]);
+            const double lo1 = dpos[1] > sp1 ? dpos[1] : sp1;
+            const double region = fmax(__dmul_rn(r0, __dsub_rn(da[1] < b1 ? da[1] : b1, lo1)), 0.0);
             double vo = slab[idx_uold(S, q, sx, sy)];
             double vn = slab[idx_unew(S, q, sx, sy)];
             if (addb) {
@@ -1403,16 +1334,26 @@ __global__ void __launch_bounds__(kRestrWarps * 32)
               vo = __dadd_rn(vo, bb);
               vn = __dadd_rn(vn, bb);
             }
-            acc = __dadd_rn(acc, ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itf), __dmul_rn(vn, tf)), region),
-                                              dvol));
+            t0[u] = ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfo), __dmul_rn(vn, tfo)), region), dvol);
+            t1[u] = ieee::div_rn(__dmul_rn(__dadd_rn(__dmul_rn(vo, itfn), __dmul_rn(vn, tfn)), region), dvol);
           }
+#pragma unroll
+          for (int u = 0; u < kRestrBatch; u++)
+            if (sy0 + u < sy_end) {
+              acc0 = __dadd_rn(acc0, t0[u]);
+              acc1 = __dadd_rn(acc1, t1[u]);
+            }
+        }
       }
     }
-    if (any) {
-      if (level) slab[idx_unew(D, q, x, y)] = acc;
-      else slab[idx_uold(D, q, x, y)] = acc;
-    }
   }
+  if (q == 0) {
+    const double nb = __dmul_rn(-1.0, slab[idx_pw(D, 0, x, y)]);
+    acc0 = __dadd_rn(acc0, nb);
+    acc1 = __dadd_rn(acc1, nb);
+  }
+  slab[idx_uold(D, q, x, y)] = acc0;
+  slab[idx_unew(D, q, x, y)] = acc1;
 }
 
 __global__ void k_post_process_restriction(double *slab, const PatchDev *patches, const int *ids, int count,
@@ -1444,30 +1385,50 @@ __device__ __forceinline__ void compute_flux(int dim, const double u[3], double 
   f[1 + dim] = __dadd_rn(f[1 + dim], pr);
 }
 
+// The face flux of face cell c of side (dim, dir) of a patch: the mean of
+// the fluxes of its uOld ghost and boundary cells (Numerics::computeFluxes).
+__device__ __forceinline__ void face_flux(const double *slab, const PatchDev &P, int c, int dim, int dir,
+                                          double gf, double f[3]) {
+  const int n[2] = {P.nx, P.ny};
+  const int inner = (dir == -1) ? 0 : n[dim] - 1;
+  const int ghost = (dir == -1) ? -1 : n[dim];
+  double gu[3], iu[3], gfx[3], ifx[3];
+  for (int q = 0; q < 3; q++) {
+    int gx = dim == 0 ? ghost : c, gy = dim == 0 ? c : ghost;
+    int ix = dim == 0 ? inner : c, iy = dim == 0 ? c : inner;
+    gu[q] = slab[idx_uold(P, q, gx, gy)];
+    iu[q] = slab[idx_uold(P, q, ix, iy)];
+  }
+  compute_flux(dim, gu, gf, gfx);
+  compute_flux(dim, iu, gf, ifx);
+  for (int q = 0; q < 3; q++) f[q] = __dmul_rn(0.5, __dadd_rn(gfx[q], ifx[q]));
+}
+
+// Face cell k of a patch's four sides in storage order: (dim, dir, c).
+__device__ __forceinline__ void face_of(const PatchDev &P, int k, int &dim, int &dir, int &c) {
+  if (k < 2 * P.ny) { dim = 0; dir = (k < P.ny) ? -1 : 1; c = k % P.ny; }
+  else { int r = k - 2 * P.ny; dim = 1; dir = (r < P.nx) ? -1 : 1; c = r % P.nx; }
+}
+
+// Numerics::computeFluxes of one patch: the face fluxes stored in the
+// patch's flux area, by all threads of the CTA.
+__device__ void store_patch_fluxes(double *slab, const PatchDev &P, double gf) {
+  const int total = 2 * (P.ny + P.nx);
+  for (int k = threadIdx.x; k < total; k += blockDim.x) {
+    int dim, dir, c;
+    face_of(P, k, dim, dir, c);
+    double f[3];
+    face_flux(slab, P, c, dim, dir, gf, f);
+    for (int q = 0; q < 3; q++) slab[idx_flux(P, q, c, dim, dir)] = f[q];
+  }
+}
+
 __global__ void k_compute_fluxes(double *slab, const PatchDev *patches, const int *ids, int count, double gf,
                                  const int *group_active) {
   if ((int)blockIdx.x >= count) return;
   PatchDev P = patches[ids[blockIdx.x]];
   if (group_active && !group_active[P.group]) return;
-  int n[2] = {P.nx, P.ny};
-  int total = 2 * (n[1] + n[0]);
-  for (int k = threadIdx.x; k < total; k += blockDim.x) {
-    int dim, dir, c;
-    if (k < 2 * n[1]) { dim = 0; dir = (k < n[1]) ? -1 : 1; c = k % n[1]; }
-    else { int r = k - 2 * n[1]; dim = 1; dir = (r < n[0]) ? -1 : 1; c = r % n[0]; }
-    int inner = (dir == -1) ? 0 : n[dim] - 1;
-    int ghost = (dir == -1) ? -1 : n[dim];
-    double gu[3], iu[3], gfx[3], ifx[3];
-    for (int q = 0; q < 3; q++) {
-      int gx = dim == 0 ? ghost : c, gy = dim == 0 ? c : ghost;
-      int ix = dim == 0 ? inner : c, iy = dim == 0 ? c : inner;
-      gu[q] = slab[idx_uold(P, q, gx, gy)];
-      iu[q] = slab[idx_uold(P, q, ix, iy)];
-    }
-    compute_flux(dim, gu, gf, gfx);
-    compute_flux(dim, iu, gf, ifx);
-    for (int q = 0; q < 3; q++) slab[idx_flux(P, q, c, dim, dir)] = __dmul_rn(0.5, __dadd_rn(gfx[q], ifx[q]));
-  }
+  store_patch_fluxes(slab, P, gf);
 }
 
 // DefaultFluxCorrectionTemplate::applyCorrection; the corrections of several
@@ -1526,20 +1487,23 @@ __global__ void k_flux_correction(double *slab, const PatchDev *patches, const P
   flux_correction_one(slab, patches, times, src, dst, dim, dir);
 }
 
-// Batched flux correction: block b applies the items [begin[b], begin[b+1])
-// (all with the same destination) in list order.  Within an item one thread
-// owns each (destination face cell, unknown) and adds the corrections of the
-// source face cells that overlap it in source order (the order of
-// flux_correction_one; the three unknowns are separate sums); the source
-// cells' destination ranges are computed once per item into shared memory.
+// Flux correction of one destination, item after item (the form of
+// k_level_transfer's flux phase for destinations whose items exceed its
+// shared-memory tables): the items [b0, b1) (all with the same destination)
+// in list order, reading the stored face fluxes.  Within
+// an item one thread owns each (destination face cell, unknown) and adds the
+// corrections of the source face cells that overlap it in source order (the
+// order of flux_correction_one; the three unknowns are separate sums); the
+// source cells' destination ranges are computed once per item into shared
+// memory (s_lb, s_ub: kFluxMaxCells each).  Called by all threads of a CTA
+// of at least kFluxThreads threads.
 constexpr int kFluxLanes = 32;                 // face cells per round
 constexpr int kFluxThreads = 3 * kFluxLanes;   // x 3 unknowns
 constexpr int kFluxMaxCells = 1024;
-__global__ void __launch_bounds__(kFluxThreads)
-    k_flux_items(double *slab, const PatchDev *patches, const PatchTimeDev *times,
-                 const int4 *items, const int *begin, const int *group_active) {
-  __shared__ int s_lb[kFluxMaxCells], s_ub[kFluxMaxCells];
-  for (int k = begin[blockIdx.x]; k < begin[blockIdx.x + 1]; k++) {
+__device__ void flux_destination_seq(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                     const int4 *items, int b0, int b1, const int *group_active, int *s_lb,
+                                     int *s_ub) {
+  for (int k = b0; k < b1; k++) {
     const int4 it = items[k];  // src, dst, dim, dir
     if (group_active && !group_active[patches[it.y].group]) continue;
     const PatchDev S = patches[it.x], D = patches[it.y];
@@ -1567,7 +1531,7 @@ __global__ void __launch_bounds__(kFluxThreads)
     const double spp = po == 0 ? S.pos[0] : S.pos[1], dpp = po == 0 ? D.pos[0] : D.pos[1];
     const double sso = other == 0 ? ssub0 : ssub1, dso = other == 0 ? dsub0 : dsub1;
     const double spo = other == 0 ? S.pos[0] : S.pos[1], dpo = other == 0 ? D.pos[0] : D.pos[1];
-    for (int cs = threadIdx.x; cs < sno; cs += kFluxThreads) {
+    for (int cs = threadIdx.x; cs < sno; cs += blockDim.x) {
       double npos = __dadd_rn(spp, __dmul_rn(ssp, (double)cs));
       double lb = fmax(dpp, npos);
       double ub = fmin(__dadd_rn(dpp, dsp), __dadd_rn(npos, ssp));
@@ -1576,26 +1540,465 @@ __global__ void __launch_bounds__(kFluxThreads)
     }
     __syncthreads();
     const int dinner = (-dir == -1) ? 0 : dnd - 1;
-    const int q = (int)threadIdx.x / kFluxLanes;
-    for (int cd = (int)threadIdx.x - q * kFluxLanes; cd < dno; cd += kFluxLanes) {
-      const int ux = dim == 0 ? dinner : cd, uy = dim == 0 ? cd : dinner;
-      if (ux < 0 || uy < 0 || ux >= D.nx || uy >= D.ny) continue;
-      const double dF = slab[idx_flux(D, q, cd, dim, -dir)];
-      const double a2 = __dadd_rn(dpo, __dmul_rn(__dadd_rn((double)cd, 1.0), dso));
-      const double b2 = __dadd_rn(dpo, __dmul_rn((double)cd, dso));
-      for (int cs = 0; cs < sno; cs++) {
-        if (cd < s_lb[cs] || cd >= s_ub[cs]) continue;
-        double a1 = __dadd_rn(spo, __dmul_rn(__dadd_rn((double)cs, 1.0), sso));
-        double b1 = __dadd_rn(spo, __dmul_rn((double)cs, sso));
-        double area = __dmul_rn(1.0, __dsub_rn(a1 < a2 ? a1 : a2, b1 > b2 ? b1 : b2));
-        if (area < 0.0) area = 0.0;
-        double sF = slab[idx_flux(S, q, cs, dim, dir)];
-        double corr = ieee::div_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF, dF), tov), area), dvol);
-        long long id = idx_unew(D, q, ux, uy);
-        slab[id] = __dadd_rn(slab[id], corr);
+    if ((int)threadIdx.x < kFluxThreads) {
+      const int q = (int)threadIdx.x / kFluxLanes;
+      for (int cd = (int)threadIdx.x - q * kFluxLanes; cd < dno; cd += kFluxLanes) {
+        const int ux = dim == 0 ? dinner : cd, uy = dim == 0 ? cd : dinner;
+        if (ux < 0 || uy < 0 || ux >= D.nx || uy >= D.ny) continue;
+        const double dF = slab[idx_flux(D, q, cd, dim, -dir)];
+        const double a2 = __dadd_rn(dpo, __dmul_rn(__dadd_rn((double)cd, 1.0), dso));
+        const double b2 = __dadd_rn(dpo, __dmul_rn((double)cd, dso));
+        for (int cs = 0; cs < sno; cs++) {
+          if (cd < s_lb[cs] || cd >= s_ub[cs]) continue;
+          double a1 = __dadd_rn(spo, __dmul_rn(__dadd_rn((double)cs, 1.0), sso));
+          double b1 = __dadd_rn(spo, __dmul_rn((double)cs, sso));
+          double area = __dmul_rn(1.0, __dsub_rn(a1 < a2 ? a1 : a2, b1 > b2 ? b1 : b2));
+          if (area < 0.0) area = 0.0;
+          double sF = slab[idx_flux(S, q, cs, dim, dir)];
+          double corr = ieee::div_rn(__dmul_rn(__dmul_rn(__dsub_rn(sF, dF), tov), area), dvol);
+          long long id = idx_unew(D, q, ux, uy);
+          slab[id] = __dadd_rn(slab[id], corr);
+        }
       }
     }
     __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Level transfer of the batched step in one launch: the face fluxes of every
+// leaf (computeFluxes), the flux-correction list (applyCorrection) and the
+// restriction list into the virtual patches (clear, restrictSolution over
+// the items in list order, postProcessRestriction), the order in which
+// SolveTimestep::enterCell and GridLevelTransfer run them.
+//
+// A persistent grid claims work items from two queues:
+//   A: [0, F)     flux destinations, then
+//      [F, F+R)   restriction destinations (their sources include corrected
+//                 leaves: they wait until every flux destination is done)
+//   B: [0, S)     storage: the face fluxes of kTransferLeaves leaves into
+//                 their flux areas (the corrections compute the face fluxes
+//                 they need themselves, so nothing waits for these)
+// The first F CTAs (R when there is no flux list) start on queue A, the
+// others on queue B, so that the storage runs beside the corrections; a CTA
+// whose queue is empty takes from the other one.  The flux items were all
+// claimed before any restriction item, by CTAs that are running and wait on
+// nothing, so the wait ends; it is bounded all the same, and one that runs
+// out sets ctl->err (read by the host after the step) and skips its item.
+// The last CTA to leave resets the counters for the next launch.
+//
+// Flux destination: per item (one CTA thread each) its geometry; per source
+// face cell its destination range and face flux and per destination face cell
+// its face flux, all at once; then one thread per (destination face cell,
+// unknown) -- the first item whose side holds the cell owns it -- adds the
+// corrections of every item's overlapping source cells in list order, then
+// source order (flux_correction_one's order).  A destination with more items
+// or face cells than the tables hold stores the face fluxes of its patches
+// and takes flux_destination_seq.
+//
+// Restriction destination: the table of its items (one thread per item, then
+// per (item, region)); every interior cell that no mapped region holds gets
+// the cleared and post-processed values (h = 0 + (-1 b), hu = hv = 0); the
+// (cell, unknown) pairs that regions hold are listed and computed by
+// restr_cell_pair over the CTA's threads.  A destination with more items
+// than the table holds, more than 3 unknowns, a region leaving it or more
+// pairs than the list holds takes the item-by-item form (clear,
+// restrict_items_in_order, post-process).
+// ---------------------------------------------------------------------------
+constexpr int kTransferLeaves = 2;
+constexpr int kTransferMaxPairs = 3 * kRestrChunkCells;
+constexpr int kTransferSpin = 1 << 20;
+constexpr int kTransferWarps = kTransferThreads / 32;
+constexpr int kXferFluxItems = 32;
+constexpr int kXferFluxCells = 512;
+
+struct XferFluxItem {
+  int src, dim, dir, sno, dno, so, dof, dinner;
+  double tov, dvol, spo, sso, dpo, dso, spp, ssp, dpp, dsp;
+};
+struct XferFluxSmem {
+  XferFluxItem it[kXferFluxItems];
+  int lb[kXferFluxCells], ub[kXferFluxCells];
+  double sF[3][kXferFluxCells], dF[3][kXferFluxCells];
+  int ni, nsrc, ndst, bad;
+};
+struct XferRestrSmem {
+  RestrItemTab T[kRestrMaxItems];
+  union {
+    int pairs[kTransferMaxPairs];
+    double W[kTransferWarps][32][6];
+  } u;
+  int bad, npairs;
+};
+constexpr size_t kTransferSmem =
+    sizeof(XferFluxSmem) > sizeof(XferRestrSmem) ? sizeof(XferFluxSmem) : sizeof(XferRestrSmem);
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// All threads: every earlier write of the CTA is done; one release-ordered
+// increment of `counter`.
+__device__ __forceinline__ void transfer_done(unsigned *counter) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(counter, 1u);
+  }
+}
+
+// All threads: wait until *counter reaches target (bounded); false when the
+// wait ran out or another wait already did (ctl->err set).
+__device__ bool transfer_wait(const unsigned *counter, unsigned target, TransferCtl *ctl, int *s_flag) {
+  if (threadIdx.x == 0) {
+    int ok = 0;
+    for (int i = 0; i < kTransferSpin; i++) {
+      if (ld_acquire_gpu(counter) >= target) { ok = 1; break; }
+      if (*(volatile int *)&ctl->err) break;
+      __nanosleep(64);
+    }
+    if (!ok) atomicCAS(&ctl->err, 0, 1);
+    __threadfence();
+    *s_flag = ok;
+  }
+  __syncthreads();
+  const bool ok = *s_flag != 0;
+  __syncthreads();
+  return ok;
+}
+
+__device__ void flux_destination(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                 const int4 *items, int b0, int b1, const int *group_active, double gf,
+                                 XferFluxSmem &M) {
+  const int ni = b1 - b0;
+  const PatchDev D = patches[items[b0].y];
+  if (group_active && !group_active[D.group]) return;
+  if (threadIdx.x == 0) M.bad = ni > kXferFluxItems ? 1 : 0;
+  __syncthreads();
+  if (!M.bad) {
+    for (int t = threadIdx.x; t < ni; t += blockDim.x) {
+      const int4 it = items[b0 + t];  // src, dst, dim, dir
+      const PatchDev S = patches[it.x];
+      const PatchTimeDev ST = times[it.x], DT = times[it.y];
+      XferFluxItem &I = M.it[t];
+      const int dim = it.z, dir = it.w, other = 1 - dim;
+      I.src = it.x; I.dim = dim; I.dir = dir;
+      I.sno = other == 0 ? S.nx : S.ny;
+      I.dno = other == 0 ? D.nx : D.ny;
+      I.dinner = (-dir == -1) ? 0 : (dim == 0 ? D.nx : D.ny) - 1;
+      const double lo = fmax(ST.time, DT.time);
+      const double hi = fmin(__dadd_rn(ST.time, ST.dt), __dadd_rn(DT.time, DT.dt));
+      I.tov = __dsub_rn(hi, lo);
+      int rdim = 0;
+      for (int d = 0; d < 2; d++) {
+        if (tl_greater(D.pos[d], S.pos[d])) rdim = d;
+        else if (tl_greater(S.pos[d], D.pos[d])) rdim = d;
+      }
+      const double ssub0 = subcell(S, 0), ssub1 = subcell(S, 1), dsub0 = subcell(D, 0), dsub1 = subcell(D, 1);
+      I.dvol = __dmul_rn(dsub0, dsub1);
+      const int po = 1 - rdim;
+      I.ssp = po == 0 ? ssub0 : ssub1; I.dsp = po == 0 ? dsub0 : dsub1;
+      I.spp = po == 0 ? S.pos[0] : S.pos[1]; I.dpp = po == 0 ? D.pos[0] : D.pos[1];
+      I.sso = other == 0 ? ssub0 : ssub1; I.dso = other == 0 ? dsub0 : dsub1;
+      I.spo = other == 0 ? S.pos[0] : S.pos[1]; I.dpo = other == 0 ? D.pos[0] : D.pos[1];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int so = 0, dof = 0;
+      for (int t = 0; t < ni; t++) {
+        M.it[t].so = so; M.it[t].dof = dof;
+        so += M.it[t].sno; dof += M.it[t].dno;
+      }
+      M.nsrc = so; M.ndst = dof;
+      if (so > kXferFluxCells || dof > kXferFluxCells) M.bad = 1;
+    }
+    __syncthreads();
+  }
+  if (M.bad) {
+    // the item-by-item form reads the stored face fluxes: store those of
+    // the destination and of every source first
+    store_patch_fluxes(slab, D, gf);
+    for (int k = b0; k < b1; k++) store_patch_fluxes(slab, patches[items[k].x], gf);
+    __syncthreads();
+    flux_destination_seq(slab, patches, times, items, b0, b1, group_active, &M.lb[0], &M.ub[0]);
+    return;
+  }
+  // source cells: destination range and face flux; destination face cells:
+  // face flux
+  const double heps = 1e-10;
+  for (int e = threadIdx.x; e < M.nsrc + M.ndst; e += blockDim.x) {
+    const bool src = e < M.nsrc;
+    const int f = src ? e : e - M.nsrc;
+    int t = 0;
+    while (t + 1 < ni && (src ? M.it[t + 1].so : M.it[t + 1].dof) <= f) t++;
+    const XferFluxItem &I = M.it[t];
+    double F[3];
+    if (src) {
+      const int cs = f - I.so;
+      const PatchDev S = patches[I.src];
+      double npos = __dadd_rn(I.spp, __dmul_rn(I.ssp, (double)cs));
+      double lb = fmax(I.dpp, npos);
+      double ub = fmin(__dadd_rn(I.dpp, I.dsp), __dadd_rn(npos, I.ssp));
+      M.lb[f] = (int)ieee::div_rn(__dadd_rn(__dsub_rn(lb, I.dpp), heps), I.dsp);
+      M.ub[f] = (int)ceil(ieee::div_rn(__dsub_rn(__dsub_rn(ub, I.dpp), heps), I.dsp));
+      face_flux(slab, S, cs, I.dim, I.dir, gf, F);
+      for (int q = 0; q < 3; q++) M.sF[q][f] = F[q];
+    } else {
+      const int cd = f - I.dof;
+      face_flux(slab, D, cd, I.dim, -I.dir, gf, F);
+      for (int q = 0; q < 3; q++) M.dF[q][f] = F[q];
+    }
+  }
+  __syncthreads();
+  // one thread per (destination face cell, unknown), owned by the first item
+  // whose side holds the cell
+  for (int task = threadIdx.x; task < 3 * M.ndst; task += blockDim.x) {
+    const int j = task / 3, q = task - 3 * j;
+    int k = 0;
+    while (k + 1 < ni && M.it[k + 1].dof <= j) k++;
+    const int cd0 = j - M.it[k].dof;
+    const int ux = M.it[k].dim == 0 ? M.it[k].dinner : cd0, uy = M.it[k].dim == 0 ? cd0 : M.it[k].dinner;
+    bool owner = true;
+    for (int k2 = 0; k2 < k && owner; k2++) {
+      const XferFluxItem &I = M.it[k2];
+      if (I.dim == 0 ? (ux == I.dinner && uy < I.dno) : (uy == I.dinner && ux < I.dno)) owner = false;
+    }
+    if (!owner || ux < 0 || uy < 0 || ux >= D.nx || uy >= D.ny) continue;
+    const long long id = idx_unew(D, q, ux, uy);
+    double acc = 0.0;
+    bool any = false;
+    for (int k2 = k; k2 < ni; k2++) {
+      const XferFluxItem &I = M.it[k2];
+      if (!(I.dim == 0 ? (ux == I.dinner && uy < I.dno) : (uy == I.dinner && ux < I.dno))) continue;
+      const int cd = I.dim == 0 ? uy : ux;
+      const double dF = M.dF[q][I.dof + cd];
+      const double a2 = __dadd_rn(I.dpo, __dmul_rn(__dadd_rn((double)cd, 1.0), I.dso));
+      const double b2 = __dadd_rn(I.dpo, __dmul_rn((double)cd, I.dso));
+      for (int cs = 0; cs < I.sno; cs++) {
+        if (cd < M.lb[I.so + cs] || cd >= M.ub[I.so + cs]) continue;
+        double a1 = __dadd_rn(I.spo, __dmul_rn(__dadd_rn((double)cs, 1.0), I.sso));
+        double b1 = __dadd_rn(I.spo, __dmul_rn((double)cs, I.sso));
+        double area = __dmul_rn(1.0, __dsub_rn(a1 < a2 ? a1 : a2, b1 > b2 ? b1 : b2));
+        if (area < 0.0) area = 0.0;
+        double corr = ieee::div_rn(__dmul_rn(__dmul_rn(__dsub_rn(M.sF[q][I.so + cs], dF), I.tov), area), I.dvol);
+        if (!any) {
+          acc = slab[id];
+          any = true;
+        }
+        acc = __dadd_rn(acc, corr);
+      }
+    }
+    if (any) slab[id] = acc;
+  }
+}
+
+// The region geometry of every restriction item (regions in the source,
+// mapped into the destination), one CTA per destination, into geo (indexed
+// like the items) and geo_bad[b] (the destination takes the item-by-item
+// form).  It depends on the patches' geometry and the destinations'
+// restriction bounds only, so it is rebuilt when those change, not per step.
+__global__ void __launch_bounds__(128)
+    k_restr_geometry(const PatchDev *patches, const PatchTimeDev *times, const int4 *items, const int *begin,
+                     int n_dst, RestrItemTab *geo, int *geo_bad) {
+  __shared__ RestrItemPre pre[kRestrMaxItems];
+  __shared__ int s_bad;
+  const int b = blockIdx.x;
+  if (b >= n_dst) return;
+  const int b0 = begin[b], b1 = begin[b + 1], ni = b1 - b0;
+  const PatchDev D = patches[items[b0].y];
+  if (threadIdx.x == 0) s_bad = (ni > kRestrMaxItems || D.nq > 3) ? 1 : 0;
+  __syncthreads();
+  if (!s_bad) {
+    for (int t = threadIdx.x; t < ni; t += blockDim.x) restr_item_pre(patches, times, items[b0 + t], pre[t]);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 4 * ni; e += blockDim.x) {
+      RestrItemTab E;
+      restr_item_region(patches, pre[e >> 2], e & 3, D, E, &s_bad);
+      // each thread writes its own region's fields; region 0 also the header
+      RestrItemTab &G = geo[b0 + (e >> 2)];
+      const int r = e & 3;
+      for (int d = 0; d < 2; d++) {
+        G.doff[r][d] = E.doff[r][d];
+        G.dsz[r][d] = E.dsz[r][d];
+        G.ro[r][d] = E.ro[r][d];
+        G.rs[r][d] = E.rs[r][d];
+      }
+      if (r == 0) {
+        G.tfo = E.tfo; G.tfn = E.tfn; G.src = E.src; G.nr = E.nr; G.swe = E.swe; G.pad_ = 0;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) geo_bad[b] = s_bad;
+}
+
+// One chunk of a restriction destination: cells [c0, c1) of its interior.
+__device__ void restrict_destination(double *slab, const PatchDev *patches, const PatchTimeDev *times,
+                                     const int4 *items, int b0, int b1, const PatchDev &D,
+                                     const RestrItemTab *geo, int bad, int c0, int c1, XferRestrSmem &M) {
+  const int ni = b1 - b0;
+  const int n = D.nx * D.ny;
+  if (threadIdx.x == 0) {
+    M.bad = bad;
+    M.npairs = 0;
+  }
+  __syncthreads();
+  if (M.bad) {
+    // item-by-item form, by the destination's first chunk: clear, every item
+    // in order, post-process
+    if (c0 != 0) return;
+    for (int k = threadIdx.x; k < D.nq * n; k += blockDim.x) {
+      int q = k / n, c = k - q * n, x = c / D.ny, y = c - x * D.ny;
+      slab[idx_unew(D, q, x, y)] = 0.0;
+      slab[idx_uold(D, q, x, y)] = 0.0;
+    }
+    __syncthreads();
+    restrict_items_in_order(slab, patches, times, items, b0, b1, M.u.W);
+    __syncthreads();
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      int x = c / D.ny, y = c % D.ny;
+      double bb = slab[idx_pw(D, 0, x, y)];
+      long long io = idx_uold(D, 0, x, y), in = idx_unew(D, 0, x, y);
+      slab[io] = __dadd_rn(slab[io], __dmul_rn(-1.0, bb));
+      slab[in] = __dadd_rn(slab[in], __dmul_rn(-1.0, bb));
+    }
+    return;
+  }
+  // the items' table: geometry, and this step's time factors
+  for (int t = threadIdx.x; t < ni; t += blockDim.x) {
+    RestrItemTab E = geo[b0 + t];
+    restr_time_factors(patches[E.src], times[E.src], E.tfo, E.tfn);
+    M.T[t] = E;
+  }
+  __syncthreads();
+  int *pairs = M.u.pairs;
+  for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) {
+    const int x = c / D.ny, y = c - x * D.ny;
+    bool held = false;
+    for (int t = 0; t < ni && !held; t++) {
+      const int nr = M.T[t].nr < 4 ? M.T[t].nr : 4;
+      for (int r = 0; r < nr && !held; r++) held = restr_covers(M.T[t], r, x, y);
+    }
+    if (!held) {
+      const double nb = __dmul_rn(-1.0, slab[idx_pw(D, 0, x, y)]);
+      const double h = __dadd_rn(0.0, nb);
+      slab[idx_uold(D, 0, x, y)] = h;
+      slab[idx_unew(D, 0, x, y)] = h;
+      for (int q = 1; q < D.nq; q++) {
+        slab[idx_uold(D, q, x, y)] = 0.0;
+        slab[idx_unew(D, q, x, y)] = 0.0;
+      }
+    } else {
+      // at most 3 unknowns x kRestrChunkCells cells: the list always holds them
+      const int k = atomicAdd(&M.npairs, D.nq);
+      for (int q = 0; q < D.nq; q++) pairs[k + q] = c * 4 + q;
+    }
+  }
+  __syncthreads();
+  const double dsub[2] = {iter_sub(D, 0), iter_sub(D, 1)};
+  const double dvol = __dmul_rn(dsub[0], dsub[1]);
+  const int np = M.npairs;
+  for (int k = threadIdx.x; k < np; k += blockDim.x) {
+    const int c = pairs[k] >> 2, q = pairs[k] & 3;
+    const int x = c / D.ny, y = c - x * D.ny;
+    restr_cell_pair(slab, patches, D, M.T, ni, x, y, q, dsub, dvol);
+  }
+}
+
+__global__ void __launch_bounds__(kTransferThreads, 1)
+    k_level_transfer(double *slab, const PatchDev *patches, const PatchTimeDev *times, const int *leaf_ids,
+                     int n_leaf, double gf, const int4 *flux_items, const int *flux_begin, int n_flux,
+                     const int4 *restr_items, const int *restr_begin, const RestrItemTab *restr_geo,
+                     const int *restr_geo_bad, const int2 *restr_chunks, int n_restr, const int *group_active,
+                     const int *pact, TransferCtl *ctl) {
+  extern __shared__ __align__(16) unsigned char xfer_smem[];
+  __shared__ int s_item, s_flag;
+  const int n_store = (n_leaf + kTransferLeaves - 1) / kTransferLeaves;
+  const int n_a = n_flux + n_restr;
+  int g_a = n_flux > 0 ? n_flux : n_restr;
+  bool on_a = (int)blockIdx.x < g_a || n_store == 0;  // thread 0's queue
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int it = -1;
+      for (int tries = 0; tries < 2 && it < 0; tries++) {
+        if (on_a) {
+          const unsigned k = atomicAdd(&ctl->next, 1u);
+          if ((int)k < n_a) it = (int)k;
+          else on_a = false;
+        } else {
+          const unsigned k = atomicAdd(&ctl->next_store, 1u);
+          if ((int)k < n_store) it = n_a + (int)k;
+          else on_a = true;
+        }
+      }
+      s_item = it;
+    }
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();
+    if (item < 0) break;
+    if (item < n_flux) {
+      flux_destination(slab, patches, times, flux_items, flux_begin[item], flux_begin[item + 1], group_active, gf,
+                       *reinterpret_cast<XferFluxSmem *>(xfer_smem));
+      transfer_done(&ctl->done_flux);
+    } else if (item < n_flux + n_restr) {
+      if (!transfer_wait(&ctl->done_flux, (unsigned)n_flux, ctl, &s_flag)) continue;
+      const int2 ch = restr_chunks[item - n_flux];  // destination, chunk
+      const int b = ch.x;
+      const int b0 = restr_begin[b], b1 = restr_begin[b + 1];
+      const PatchDev D = patches[restr_items[b0].y];
+      if (group_active && !group_active[D.group]) continue;
+      if (pact) {
+        // local time stepping: only destinations with an advancing source
+        int any = 0;
+        for (int k = b0 + (int)threadIdx.x; k < b1; k += blockDim.x) any |= pact[restr_items[k].x] ? 1 : 0;
+        if (!__syncthreads_or(any)) continue;
+      }
+      const int c0 = ch.y * kRestrChunkCells, n = D.nx * D.ny;
+      restrict_destination(slab, patches, times, restr_items, b0, b1, D, restr_geo, restr_geo_bad[b], c0,
+                           c0 + kRestrChunkCells < n ? c0 + kRestrChunkCells : n,
+                           *reinterpret_cast<XferRestrSmem *>(xfer_smem));
+      __syncthreads();
+    } else {
+      // the face fluxes of up to kTransferLeaves leaves, all their face cells at once
+      const int l0 = (item - n_flux - n_restr) * kTransferLeaves;
+      const int l1 = l0 + kTransferLeaves < n_leaf ? l0 + kTransferLeaves : n_leaf;
+      int tot = 0;
+      for (int l = l0; l < l1; l++) {
+        const PatchDev &P = patches[leaf_ids[l]];
+        tot += 2 * (P.nx + P.ny);
+      }
+      for (int k = threadIdx.x; k < tot; k += blockDim.x) {
+        int l = l0, kk = k;
+        while (true) {
+          const PatchDev &P = patches[leaf_ids[l]];
+          const int m = 2 * (P.nx + P.ny);
+          if (kk < m || l + 1 >= l1) break;
+          kk -= m;
+          l++;
+        }
+        const PatchDev P = patches[leaf_ids[l]];
+        if (group_active && !group_active[P.group]) continue;
+        int dim, dir, c;
+        face_of(P, kk, dim, dir, c);
+        double f[3];
+        face_flux(slab, P, c, dim, dir, gf, f);
+        for (int q = 0; q < 3; q++) slab[idx_flux(P, q, c, dim, dir)] = f[q];
+      }
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl->exited, 1u) == gridDim.x - 1) {
+      ctl->next = 0;
+      ctl->next_store = 0;
+      ctl->done_flux = 0;
+      ctl->exited = 0;
+      __threadfence();
+    }
   }
 }
 
@@ -1993,55 +2396,6 @@ cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patch
   return cudaGetLastError();
 }
 
-// Destinations of the restriction list with at least one advancing source
-// (local time stepping): the others' restricted values would not change.
-__global__ void k_restr_dirty(const int4 *__restrict__ items, const int *__restrict__ begin,
-                              const int *__restrict__ pact, int *__restrict__ dirty) {
-  int any = 0;
-  for (int k = begin[blockIdx.x] + threadIdx.x; k < begin[blockIdx.x + 1]; k += blockDim.x)
-    any |= pact[items[k].x] ? 1 : 0;
-  any = __syncthreads_or(any);
-  if (threadIdx.x == 0) dirty[blockIdx.x] = any;
-}
-
-cudaError_t launch_restr_dirty(cudaStream_t st, const int4 *items, const int *begin, int n_dst, const int *pact,
-                               int *dirty) {
-  if (n_dst <= 0) return cudaSuccess;
-  k_restr_dirty<<<n_dst, 128, 0, st>>>(items, begin, pact, dirty);
-  return cudaGetLastError();
-}
-
-// CTAs per destination of the batched restriction: about four CTAs per SM
-// over all destinations, at most 16.  A destination's task space is dealt in
-// blocks of one CTA's threads, so CTAs beyond its task count only read the
-// table and return.
-int restr_split(int n_dst, int num_sms) {
-  if (n_dst <= 0) return 1;
-  const int target = 4 * (num_sms > 0 ? num_sms : 1);
-  return std::max(1, std::min(16, (target + n_dst - 1) / n_dst));
-}
-
-cudaError_t launch_restr_prepare(cudaStream_t st, double *slab, const PatchDev *patches,
-                                 const PatchTimeDev *times, const int4 *items, const int *begin,
-                                 const int *ids, int n_dst, RestrItemTab *tab, int *bad,
-                                 const int *group_active, const int *dirty) {
-  if (n_dst <= 0) return cudaSuccess;
-  k_restr_prepare<<<n_dst, 256, 0, st>>>(slab, patches, times, items, begin, ids, n_dst, tab, bad,
-                                         group_active, dirty);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst, int split, const RestrItemTab *tab, const int *bad,
-                                  const int *group_active, const int *dirty) {
-  if (n_dst <= 0) return cudaSuccess;
-  if (split < 1 || (int64_t)n_dst * split > 0x7fffffff) return cudaErrorInvalidValue;
-  k_restrict_items<<<n_dst * split, kRestrWarps * 32, 0, st>>>(slab, patches, times, items, begin, split, tab,
-                                                               bad, group_active, dirty);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
                                             const int *ids, int count, const int *group_active,
                                             const int *dirty) {
@@ -2057,11 +2411,50 @@ cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev 
   return cudaGetLastError();
 }
 
-cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *patches,
-                              const PatchTimeDev *times, const int4 *items, const int *begin,
-                              int n_dst, const int *group_active) {
+static cudaError_t level_transfer_setup() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_level_transfer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kTransferSmem);
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+cudaError_t launch_restr_geometry(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
+                                  const int4 *items, const int *begin, int n_dst, RestrItemTab *geo,
+                                  int *geo_bad) {
   if (n_dst <= 0) return cudaSuccess;
-  k_flux_items<<<n_dst, kFluxThreads, 0, st>>>(slab, patches, times, items, begin, group_active);
+  k_restr_geometry<<<n_dst, 128, 0, st>>>(patches, times, items, begin, n_dst, geo, geo_bad);
+  return cudaGetLastError();
+}
+
+int level_transfer_grid(int num_sms, int n_leaf, int n_flux, int n_restr) {
+  const int items = (n_leaf + kTransferLeaves - 1) / kTransferLeaves + n_flux + n_restr;
+  if (items <= 0) return 0;
+  if (level_transfer_setup() != cudaSuccess) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level_transfer, kTransferThreads, kTransferSmem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int cap = (num_sms > 0 ? num_sms : 1) * per_sm;
+  return items < cap ? items : cap;
+}
+
+cudaError_t launch_level_transfer(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                                  const PatchTimeDev *times, const int *leaf_ids, int n_leaf, double gf,
+                                  const int4 *flux_items, const int *flux_begin, int n_flux,
+                                  const int4 *restr_items, const int *restr_begin,
+                                  const RestrItemTab *restr_geo, const int *restr_geo_bad,
+                                  const int2 *restr_chunks, int n_restr, const int *group_active,
+                                  const int *pact, TransferCtl *ctl) {
+  if (grid <= 0) return cudaSuccess;
+  cudaError_t e = level_transfer_setup();
+  if (e != cudaSuccess) return e;
+  k_level_transfer<<<grid, kTransferThreads, kTransferSmem, st>>>(slab, patches, times, leaf_ids, n_leaf, gf, flux_items,
+                                                      flux_begin, n_flux, restr_items, restr_begin, restr_geo,
+                                                      restr_geo_bad, restr_chunks, n_restr, group_active, pact,
+                                                      ctl);
   return cudaGetLastError();
 }
 

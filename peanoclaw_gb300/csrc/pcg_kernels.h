@@ -105,35 +105,53 @@ cudaError_t launch_interpolate(cudaStream_t st, double *slab, const PatchDev *pa
 cudaError_t launch_restrict(cudaStream_t st, double *slab, const PatchDev *patches,
                             const PatchTimeDev *times, int src, int dst, int only_overlapped, int swe);
 // Per-item table of the batched restriction (regions mapped into the
-// destination, time factors), written by k_restr_prepare each step.
+// destination, time factors), built in shared memory by k_level_transfer.
 constexpr int kRestrMaxItems = 128;
 struct RestrItemTab {
   double tfo, tfn;
   int src, nr, swe, pad_;
   int doff[4][2], dsz[4][2], ro[4][2], rs[4][2];
 };
-int restr_split(int n_dst, int num_sms);
-// Clears the interior of every destination ids[b] and writes the tables of
-// its items into tab (indexed like items) and bad[b].
-cudaError_t launch_restr_prepare(cudaStream_t st, double *slab, const PatchDev *patches,
-                                 const PatchTimeDev *times, const int4 *items, const int *begin,
-                                 const int *ids, int n_dst, RestrItemTab *tab, int *bad,
-                                 const int *group_active = nullptr, const int *dirty = nullptr);
-cudaError_t launch_restrict_items(cudaStream_t st, double *slab, const PatchDev *patches,
-                                  const PatchTimeDev *times, const int4 *items, const int *begin,
-                                  int n_dst, int split, const RestrItemTab *tab, const int *bad,
-                                  const int *group_active = nullptr, const int *dirty = nullptr);
-cudaError_t launch_restr_dirty(cudaStream_t st, const int4 *items, const int *begin, int n_dst, const int *pact,
-                               int *dirty);
+// Work counters of k_level_transfer (its two queues, the finished flux
+// destinations, the CTAs that left; zero between launches: the kernel's last
+// CTA resets them) and its error word (1: a phase wait ran out).
+struct TransferCtl {
+  unsigned next, next_store, done_flux, exited;
+  int err, pad_[3];
+};
+constexpr int kTransferThreads = 256;
+// Interior cells of a restriction destination per work item of
+// k_level_transfer (one item per destination up to 64 x 64 cells: splitting
+// a destination's cells over several items measured slower, each item
+// reloading the table).
+constexpr int kRestrChunkCells = 4096;
+// Grid of k_level_transfer: one CTA per work item, at most the resident CTAs.
+int level_transfer_grid(int num_sms, int n_leaf, int n_flux, int n_restr);
+// Region geometry of the restriction items of n_dst destinations (begin)
+// into geo (indexed like the items) and geo_bad (per destination).
+cudaError_t launch_restr_geometry(cudaStream_t st, const PatchDev *patches, const PatchTimeDev *times,
+                                  const int4 *items, const int *begin, int n_dst, RestrItemTab *geo,
+                                  int *geo_bad);
+// Flux correction and restriction phases of a batched step in one launch:
+// the face fluxes of leaf_ids[0, n_leaf) (n_leaf = 0: none), the flux items
+// of n_flux destinations (flux_begin), then the restriction items of the
+// destinations (restr_begin, region geometry from launch_restr_geometry) in
+// n_restr chunks (restr_chunks: destination, chunk of kRestrChunkCells
+// cells); pact (local time stepping, may be null) limits the restriction to
+// destinations with an advancing source.
+cudaError_t launch_level_transfer(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                                  const PatchTimeDev *times, const int *leaf_ids, int n_leaf, double gf,
+                                  const int4 *flux_items, const int *flux_begin, int n_flux,
+                                  const int4 *restr_items, const int *restr_begin,
+                                  const RestrItemTab *restr_geo, const int *restr_geo_bad,
+                                  const int2 *restr_chunks, int n_restr, const int *group_active,
+                                  const int *pact, TransferCtl *ctl);
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
                                             const int *ids, int count,
                                             const int *group_active = nullptr, const int *dirty = nullptr);
 cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const int *ids, int count, double gf,
                                   const int *group_active = nullptr);
-cudaError_t launch_flux_items(cudaStream_t st, double *slab, const PatchDev *patches,
-                              const PatchTimeDev *times, const int4 *items, const int *begin,
-                              int n_dst, const int *group_active = nullptr);
 cudaError_t launch_gather_cells(cudaStream_t st, const double *slab, const PatchDev *patches,
                                 const int *ids, const long long *out_off, int count, double *out);
 cudaError_t launch_switch_to_leaf(cudaStream_t st, double *slab, const PatchDev *patches,
