@@ -88,9 +88,9 @@ def parse():
     ap.add_argument("--remesh-steps", type=int, default=300)
     ap.add_argument("--remesh-every", type=int, default=10)
     ap.add_argument("--lts-t-end", type=float, default=0.02)
-    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-requests", type=int, default=128)
     ap.add_argument("--serve-rate", type=float, default=8.0)
-    ap.add_argument("--serve-batch", type=int, default=8,
+    ap.add_argument("--serve-batch", type=int, default=32,
                     help="batched steps per replay of the step graph in the serving loop")
     return ap.parse_args()
 
@@ -507,27 +507,36 @@ def bench_remesh(prm, steps, every):
             "remesh_s_mean": float(np.mean(remesh_s)), "wall_s": wall}
 
 
-def bench_serving(args, prm):
+def bench_serving(args, prm, batched_value=None):
     """Scenario stream with Poisson arrivals (seed 42): radial dam breaks and
-    Gaussian-hump tsunamis, 1e4..4e6 cells, end time U[0.05, 0.5]."""
+    Gaussian-hump tsunamis, 1e4..4e6 cells (the finest level's effective
+    resolution), 1-3 levels of adaptive 3x refinement (adaptive requests keep
+    their hierarchy on the device and remesh every 32 of their steps), end
+    time U[0.05, 0.5]."""
     from peanoclaw_gb300 import serving as SV
-    reqs = SV.make_requests(args.serve_requests, rate=args.serve_rate, seed=42, n=32)
+    reqs = SV.make_requests(args.serve_requests, rate=args.serve_rate, seed=42, n=32, levels=(1, 3))
     need = sum(int(r.cells * 1.4) for r in reqs)
-    srv = SV.Server(slab_doubles=int(need * 8) + (1 << 24), max_groups=32, max_patches=80000, params=prm,
-                    steps_per_batch=args.serve_batch)
+    srv = SV.Server(slab_doubles=int(need * 8) + (1 << 24), max_groups=32, max_patches=400000, params=prm,
+                    steps_per_batch=args.serve_batch, remesh_every=max(32, args.serve_batch))
     try:
         _, ms0 = srv.ctx.stats()
-        done, wall = srv.serve(reqs, max_wall=240.0)
+        done, wall = srv.serve(reqs, max_wall=300.0)
         _, ms1 = srv.ctx.stats()
+        remesh_s, relist_s, remeshes = srv.remesh_s, srv.relist_s, srv.remeshes
     finally:
         srv.close()
     lat = np.array([r.finished - r.arrival for r in done])
     cu = sum(r.cell_updates for r in done)
+    value = cu / wall
     return {"requests": len(reqs), "completed": len(done), "rate_per_s": args.serve_rate,
+            "adaptive_requests": int(sum(r.levels > 1 for r in reqs)),
+            "levels": {str(k): int(sum(r.levels == k for r in reqs)) for k in (1, 2, 3)},
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
-            "cell_updates_per_s": cu / wall, "wall_s": wall,
-            "device_busy": (ms1 - ms0) / 1e3 / wall,
+            "cell_updates_per_s": value, "wall_s": wall,
+            "device_busy": (ms1 - ms0) / 1e3 / wall, "remesh_s": remesh_s, "remeshes": remeshes,
+            "remesh_relist_s": relist_s,
+            "vs_batched_50k": (value / batched_value) if batched_value else None,
             "max_concurrent_groups": 32, "steps_per_batch": args.serve_batch}
 
 
@@ -693,7 +702,7 @@ def main():
         legs = {"radial_dam_break_9x9x16": lambda: bench_radial(prm),
                 "adaptive_breaking_dam_3_levels": lambda: bench_amr(prm, args.amr_steps),
                 "adaptive_tsunami_remesh": lambda: bench_remesh(prm, args.remesh_steps, args.remesh_every),
-                "serving_stream": lambda: bench_serving(args, prm),
+                "serving_stream": lambda: bench_serving(args, prm, value / ws),
                 "local_time_stepping_breaking_dam": lambda: bench_lts(prm, args.lts_t_end)}
         only = set(args.config_legs.split(",")) if args.config_legs else set(legs)
         configs = {k: f() for k, f in legs.items() if k in only}

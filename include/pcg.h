@@ -276,7 +276,9 @@ int pcg_set_ghost_items(pcg_context *ctx, const pcg_ghost_item *items, int32_t n
 int pcg_set_restriction_items(pcg_context *ctx, int32_t n, const int32_t *src, const int32_t *dst,
                               int32_t only_overlapped);
 /* Flux correction after the update of every grid step: computeFluxes of every
- * leaf (g_flux as in Numerics::computeFlux), then
+ * leaf of the groups that the list's patches belong to (g_flux as in
+ * Numerics::computeFlux; a group without items is a simulation without flux
+ * correction and its flux areas are not written), then
  * applyFluxCorrection(src[k], dst[k], dim[k], dir[k]) in list order per
  * destination (SolveTimestep.cpp:674-679, FluxCorrectionFunctor). */
 int pcg_set_flux_correction_items(pcg_context *ctx, int32_t n, const int32_t *src, const int32_t *dst,

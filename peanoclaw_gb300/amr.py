@@ -699,6 +699,11 @@ class DeviceAmr:
         known[vid] = True
         plo[vid] = lo
         pup[vid] = up
+        self.install_lists(lay, ids)
+
+    def install_lists(self, lay, ids):
+        """The grid's ghost, restriction, virtual-time and flux-correction
+        lists with patch ids, into the context."""
         from .scenarios import remap_items
         self.ctx.set_ghost_items(remap_items(lay["items"], ids))
         r = lay["restrict_items"]

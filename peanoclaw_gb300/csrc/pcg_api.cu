@@ -146,6 +146,7 @@ struct pcg_context {
 
   int max_patches = 0, max_groups = 1;
   int slot_hint = 0;
+  int patch_hw = 0;  // ids in use are below this (the patch table uploads [0, patch_hw))
   std::vector<pcg::PatchDev> h_patches;
   std::vector<int64_t> h_len;
   std::vector<char> used;
@@ -191,7 +192,10 @@ struct pcg_context {
   pcg::GhostItemDev *d_items = nullptr;
   size_t d_items_cap = 0;
   // flat ghost-cell list of the batched fill (copies first) + interpolation plan
-  std::vector<pcg::GhostCellDev> h_gcells;
+  std::vector<int2> h_gexp;   // (item, first ghost-cell entry) per item with cells, then (-1, total)
+  int2 *d_gexp = nullptr;
+  size_t d_gexp_cap = 0;
+  int64_t n_gcells = 0;
   int n_copy_cells = 0, n_interp_cells = 0;
   pcg::GhostCellDev *d_gcells = nullptr;
   size_t d_gcells_cap = 0;
@@ -232,6 +236,9 @@ struct pcg_context {
   std::vector<int> restr_begin, flux_begin, restr_dsts;
   int4 *d_restr = nullptr, *d_flux = nullptr;
   int *d_restr_begin = nullptr, *d_flux_begin = nullptr, *d_restr_dsts = nullptr, *d_leaf_ids = nullptr;
+  std::vector<int> flux_leaf_ids;  // leaves of the groups with flux-correction items
+  int *d_flux_leaf_ids = nullptr;
+  size_t d_fleaf_cap = 0;
   pcg::RestrItemTab *d_restr_geo = nullptr;  // region geometry per restriction item
   int *d_restr_geo_bad = nullptr;            // per destination: item-by-item form
   int2 *d_restr_chunks = nullptr;            // (destination, chunk) work items of the restriction
@@ -347,8 +354,11 @@ int ensure_device(pcg_context *c, T **ptr, size_t *cap, size_t n) {
 
 int upload_patches(pcg_context *c) {
   if (!c->patches_dirty) return PCG_OK;
-  PCG_CUDA(cudaMemcpyAsync(c->d_patches, c->h_patches.data(),
-                           sizeof(pcg::PatchDev) * c->max_patches, cudaMemcpyHostToDevice, c->stream));
+  // entries from patch_hw on were never used: zero on the device since the
+  // context was created
+  if (c->patch_hw > 0)
+    PCG_CUDA(cudaMemcpyAsync(c->d_patches, c->h_patches.data(), sizeof(pcg::PatchDev) * (size_t)c->patch_hw,
+                             cudaMemcpyHostToDevice, c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   c->patches_dirty = false;
   return PCG_OK;
@@ -524,6 +534,14 @@ bool fused_lists_fit(pcg_context *c) {
 // and the per-patch strip lists (after the ghost-cell list and the
 // interpolation plan are on the device).
 int build_fused_tables(pcg_context *c) {
+  // the fused form applies to the synchronous step without restriction or
+  // flux-correction lists: otherwise its tables are not built (a change of
+  // the lists, the form or the time stepping rebuilds the topology)
+  if (c->form != PCG_FORM_AUTO || c->ts_local || !c->restr_user.empty() || !c->flux_user.empty()) {
+    c->fused_lists_ok = false;
+    c->shadow_need = 0;
+    return PCG_OK;
+  }
   c->fused_lists_ok = fused_lists_fit(c);
   c->h_face_begin.assign(c->max_patches, 0);
   int64_t nf = 0, sh = 0;
@@ -568,7 +586,7 @@ int rebuild_topology(pcg_context *c) {
   c->h_wall.clear();
   c->leaf_ids.clear();
   c->cells_per_step = 0;
-  for (int p = 0; p < c->max_patches; p++) {
+  for (int p = 0; p < c->patch_hw; p++) {
     pcg::PatchDev &P = c->h_patches[p];
     P.tile_begin = 0;
     P.tile_count = 0;
@@ -595,15 +613,26 @@ int rebuild_topology(pcg_context *c) {
   c->h_items.clear();
   c->item_first.assign(c->max_patches, 0);
   c->item_count.assign(c->max_patches, 0);
-  std::vector<std::vector<int>> by_dst(c->max_patches);
+  // counting sort of the items by destination (stable: user order within one)
+  std::vector<int> dst_start(c->patch_hw + 1, 0), by_dst;
   for (size_t k = 0; k < c->items_user.size(); k++) {
     const pcg_ghost_item &u = c->items_user[k];
-    if (!valid_id(c, u.src) || !valid_id(c, u.dst)) continue;
-    by_dst[u.dst].push_back((int)k);
+    if (valid_id(c, u.src) && valid_id(c, u.dst)) dst_start[u.dst + 1]++;
   }
-  for (int p = 0; p < c->max_patches; p++) {
+  for (int p = 0; p < c->patch_hw; p++) dst_start[p + 1] += dst_start[p];
+  by_dst.resize(dst_start[c->patch_hw]);
+  {
+    std::vector<int> fill(dst_start.begin(), dst_start.end() - 1);
+    for (size_t k = 0; k < c->items_user.size(); k++) {
+      const pcg_ghost_item &u = c->items_user[k];
+      if (valid_id(c, u.src) && valid_id(c, u.dst)) by_dst[fill[u.dst]++] = (int)k;
+    }
+  }
+  c->h_items.reserve(by_dst.size());
+  for (int p = 0; p < c->patch_hw; p++) {
     c->item_first[p] = (int)c->h_items.size();
-    for (int k : by_dst[p]) {
+    for (int i = dst_start[p]; i < dst_start[p + 1]; i++) {
+      const int k = by_dst[i];
       const pcg_ghost_item &u = c->items_user[k];
       pcg::GhostItemDev d;
       d.kind = u.kind; d.src = u.src; d.dst = u.dst;
@@ -615,17 +644,24 @@ int rebuild_topology(pcg_context *c) {
     c->item_count[p] = (int)c->h_items.size() - c->item_first[p];
   }
   // flat ghost-cell list: every cell of every COPY item, then of every INTERP item
-  c->h_gcells.clear();
+  // (expanded on the device from one (item, first entry) pair per item)
+  c->h_gexp.clear();
+  int64_t ncell = 0;
   for (int pass = 0; pass < 2; pass++) {
     for (size_t k = 0; k < c->h_items.size(); k++) {
       const pcg::GhostItemDev &it = c->h_items[k];
       if (it.kind != pass) continue;
-      int nc = it.size[0] * it.size[1];
-      for (int q = 0; q < nc; q++) c->h_gcells.push_back(pcg::GhostCellDev{(int)k, q});
+      const int nc = it.size[0] * it.size[1];
+      if (nc <= 0) continue;
+      c->h_gexp.push_back(make_int2((int)k, (int)ncell));
+      ncell += nc;
     }
-    if (pass == 0) c->n_copy_cells = (int)c->h_gcells.size();
+    if (pass == 0) c->n_copy_cells = (int)ncell;
   }
-  c->n_interp_cells = (int)c->h_gcells.size() - c->n_copy_cells;
+  if (ncell > INT32_MAX) return fail(PCG_E_INVALID, "too many ghost cells");
+  c->h_gexp.push_back(make_int2(-1, (int)ncell));
+  c->n_gcells = ncell;
+  c->n_interp_cells = (int)ncell - c->n_copy_cells;
   // restriction and flux-correction items grouped by destination, list order kept
   auto group_by_dst = [&](const std::vector<int4> &in, std::vector<int4> &out, std::vector<int> &begin,
                           std::vector<int> *dsts) {
@@ -647,6 +683,19 @@ int rebuild_topology(pcg_context *c) {
   };
   group_by_dst(c->restr_user, c->h_restr, c->restr_begin, &c->restr_dsts);
   group_by_dst(c->flux_user, c->h_flux, c->flux_begin, nullptr);
+  // computeFluxes runs for the leaves of the groups (simulations) that have
+  // flux correction, so that one group's flux areas do not depend on the
+  // lists of the others
+  {
+    std::vector<char> gflux(c->max_groups, 0);
+    for (const int4 &f : c->h_flux) {
+      gflux[c->h_patches[f.x].group] = 1;
+      gflux[c->h_patches[f.y].group] = 1;
+    }
+    c->flux_leaf_ids.clear();
+    for (int p : c->leaf_ids)
+      if (gflux[c->h_patches[p].group]) c->flux_leaf_ids.push_back(p);
+  }
   c->h_vt.clear();
   c->vt_virtuals.clear();
   {
@@ -679,6 +728,8 @@ int rebuild_topology(pcg_context *c) {
   if ((rc = ensure_device(c, &c->d_restr_geo_bad, &c->d_rgeob_cap, c->restr_dsts.size())) != PCG_OK) return rc;
   c->restr_geo_dirty = true;
   if ((rc = ensure_device(c, &c->d_leaf_ids, &c->d_leaf_cap, c->leaf_ids.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_flux_leaf_ids, &c->d_fleaf_cap, c->flux_leaf_ids.size())) != PCG_OK)
+    return rc;
   auto up = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) : cudaSuccess;
   };
@@ -689,9 +740,11 @@ int rebuild_topology(pcg_context *c) {
   PCG_CUDA(up(c->d_restr_dsts, c->restr_dsts.data(), sizeof(int) * c->restr_dsts.size()));
   PCG_CUDA(up(c->d_restr_chunks, c->h_restr_chunks.data(), sizeof(int2) * c->h_restr_chunks.size()));
   PCG_CUDA(up(c->d_leaf_ids, c->leaf_ids.data(), sizeof(int) * c->leaf_ids.size()));
+  PCG_CUDA(up(c->d_flux_leaf_ids, c->flux_leaf_ids.data(), sizeof(int) * c->flux_leaf_ids.size()));
   PCG_CUDA(up(c->d_vt, c->h_vt.data(), sizeof(int2) * c->h_vt.size()));
   PCG_CUDA(up(c->d_vt_virtuals, c->vt_virtuals.data(), sizeof(int) * c->vt_virtuals.size()));
-  if ((rc = ensure_device(c, &c->d_gcells, &c->d_gcells_cap, c->h_gcells.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_gcells, &c->d_gcells_cap, (size_t)c->n_gcells)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_gexp, &c->d_gexp_cap, c->h_gexp.size())) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_plan, &c->d_plan_cap, (size_t)c->n_interp_cells)) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_copy_plan, &c->d_copy_plan_cap, (size_t)c->n_copy_cells)) != PCG_OK) return rc;
   if ((rc = ensure_device(c, &c->d_item_step, &c->d_item_step_cap, c->h_items.size())) != PCG_OK) return rc;
@@ -707,9 +760,9 @@ int rebuild_topology(pcg_context *c) {
   if (!c->h_items.empty())
     PCG_CUDA(cudaMemcpyAsync(c->d_items, c->h_items.data(), sizeof(pcg::GhostItemDev) * c->h_items.size(),
                              cudaMemcpyHostToDevice, c->stream));
-  if (!c->h_gcells.empty())
-    PCG_CUDA(cudaMemcpyAsync(c->d_gcells, c->h_gcells.data(), sizeof(pcg::GhostCellDev) * c->h_gcells.size(),
-                             cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(cudaMemcpyAsync(c->d_gexp, c->h_gexp.data(), sizeof(int2) * c->h_gexp.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+  PCG_CUDA(pcg::launch_expand_gcells(c->stream, c->d_gexp, (int)c->h_gexp.size() - 1, c->d_gcells));
   c->patches_dirty = true;
   if ((rc = upload_patches(c)) != PCG_OK) return rc;
   PCG_CUDA(pcg::launch_build_interp_plan(c->stream, c->d_patches, c->d_items, c->d_gcells + c->n_copy_cells,
@@ -760,7 +813,7 @@ int enqueue_level_transfer(pcg_context *c, bool flux, bool restr, const int *gro
   using namespace pcg;
   flux = flux && !c->h_flux.empty();
   restr = restr && !c->h_restr.empty();
-  const int n_leaf = flux ? (int)c->leaf_ids.size() : 0;
+  const int n_leaf = flux ? (int)c->flux_leaf_ids.size() : 0;
   const int n_flux = flux ? (int)c->flux_begin.size() - 1 : 0;
   const int n_restr = restr ? (int)c->h_restr_chunks.size() : 0;
   const int grid = level_transfer_grid(c->num_sms, n_leaf, n_flux, n_restr);
@@ -769,7 +822,7 @@ int enqueue_level_transfer(pcg_context *c, bool flux, bool restr, const int *gro
     int rc = refresh_restr_geometry(c);
     if (rc != PCG_OK) return rc;
   }
-  PCG_CUDA(launch_level_transfer(c->stream, grid, c->slab, c->d_patches, c->d_times, c->d_leaf_ids, n_leaf,
+  PCG_CUDA(launch_level_transfer(c->stream, grid, c->slab, c->d_patches, c->d_times, c->d_flux_leaf_ids, n_leaf,
                                  c->g_flux, c->d_flux, c->d_flux_begin, n_flux, c->d_restr, c->d_restr_begin,
                                  c->d_restr_geo, c->d_restr_geo_bad, c->d_restr_chunks, n_restr, group_active,
                                  pact, c->d_xfer));
@@ -1128,6 +1181,7 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->slab, sizeof(double) * c->slab_doubles));
   c->free_list[0] = c->slab_doubles / kAlign * kAlign;
   CREATE_CK(cudaMalloc(&c->d_patches, sizeof(pcg::PatchDev) * c->max_patches));
+  CREATE_CK(cudaMemset(c->d_patches, 0, sizeof(pcg::PatchDev) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_times, sizeof(pcg::PatchTimeDev) * c->max_patches));
   CREATE_CK(cudaMemset(c->d_times, 0, sizeof(pcg::PatchTimeDev) * c->max_patches));
   CREATE_CK(cudaMalloc(&c->d_patch_smax, sizeof(unsigned long long) * c->max_patches));
@@ -1201,6 +1255,7 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_dt_out);
   cudaFree(c->d_items);
   cudaFree(c->d_gcells);
+  cudaFree(c->d_gexp);
   cudaFree(c->d_restr);
   cudaFree(c->d_flux);
   cudaFree(c->d_restr_begin);
@@ -1210,6 +1265,7 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_restr_geo);
   cudaFree(c->d_restr_geo_bad);
   cudaFree(c->d_restr_chunks);
+  cudaFree(c->d_flux_leaf_ids);
   cudaFree(c->d_leaf_ids);
   cudaFree(c->d_plan);
   cudaFree(c->d_copy_plan);
@@ -1297,6 +1353,7 @@ int pcg_patch_alloc(pcg_context *c, const pcg_patch_desc *d, int32_t *id) {
   PCG_CUDA(cudaMemcpyAsync(c->d_times + slot, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream));
   c->patches_dirty = c->topo_dirty = true;
   c->slot_hint = slot + 1;
+  if (slot + 1 > c->patch_hw) c->patch_hw = slot + 1;
   *id = slot;
   return PCG_OK;
 }
@@ -1680,8 +1737,9 @@ int pcg_patches_get_time(pcg_context *c, int32_t n, const int32_t *ids, pcg_patc
   if (n == 0) return PCG_OK;
   std::lock_guard<std::mutex> lk(c->mu);
   PCG_CUDA(cudaSetDevice(c->device));
-  std::vector<pcg::PatchTimeDev> all(c->max_patches);
-  PCG_CUDA(cudaMemcpyAsync(all.data(), c->d_times, sizeof(pcg::PatchTimeDev) * c->max_patches,
+  // every listed id is in use, so below the high-water mark
+  std::vector<pcg::PatchTimeDev> all(c->patch_hw);
+  PCG_CUDA(cudaMemcpyAsync(all.data(), c->d_times, sizeof(pcg::PatchTimeDev) * (size_t)c->patch_hw,
                            cudaMemcpyDeviceToHost, c->stream));
   PCG_CUDA(cudaStreamSynchronize(c->stream));
   for (int32_t k = 0; k < n; k++) {
@@ -1972,6 +2030,7 @@ int pcg_set_time_stepping(pcg_context *c, int32_t mode) {
   if (local != c->ts_local) {
     c->ts_local = local;
     c->graph_valid = false;
+    c->topo_dirty = true;  // the fused form's tables depend on it
   }
   return PCG_OK;
 }
@@ -2150,6 +2209,7 @@ int pcg_set_step_form(pcg_context *c, int32_t form) {
   if (c->form != form) {
     c->form = form;
     c->graph_valid = false;
+    c->topo_dirty = true;  // the fused form's tables are built for PCG_FORM_AUTO only
   }
   return PCG_OK;
 }

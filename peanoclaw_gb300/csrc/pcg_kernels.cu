@@ -2458,6 +2458,20 @@ cudaError_t launch_level_transfer(cudaStream_t st, int grid, double *slab, const
   return cudaGetLastError();
 }
 
+// The flat ghost-cell list: block b writes the cells of item exp[b].x, the
+// (item, cell) pairs [exp[b].y, exp[b + 1].y) of the list.
+__global__ void k_expand_gcells(const int2 *__restrict__ exp, GhostCellDev *__restrict__ out) {
+  const int2 e = exp[blockIdx.x];
+  const int count = exp[blockIdx.x + 1].y - e.y;
+  for (int q = threadIdx.x; q < count; q += blockDim.x) out[e.y + q] = GhostCellDev{e.x, q};
+}
+
+cudaError_t launch_expand_gcells(cudaStream_t st, const int2 *exp, int n_items, GhostCellDev *out) {
+  if (n_items <= 0) return cudaSuccess;
+  k_expand_gcells<<<n_items, 64, 0, st>>>(exp, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_scan_fin(cudaStream_t st, const double *slab, const PatchDev *patches, int count,
                             int *fin) {
   if (count <= 0) return cudaSuccess;

@@ -152,6 +152,9 @@ cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const
 cudaError_t launch_compute_fluxes(cudaStream_t st, double *slab, const PatchDev *patches,
                                   const int *ids, int count, double gf,
                                   const int *group_active = nullptr);
+// The flat ghost-cell list from exp[0, n_items] (item, first list entry;
+// exp[n_items].y = the list length).
+cudaError_t launch_expand_gcells(cudaStream_t st, const int2 *exp, int n_items, GhostCellDev *out);
 cudaError_t launch_gather_cells(cudaStream_t st, const double *slab, const PatchDev *patches,
                                 const int *ids, const long long *out_off, int count, double *out);
 cudaError_t launch_switch_to_leaf(cudaStream_t st, double *slab, const PatchDev *patches,

@@ -38,3 +38,32 @@ def test_admission_refuses_when_hbm_is_full():
         assert not srv.resident
     finally:
         srv.close()
+
+
+def test_adaptive_requests_identical_alone_and_in_the_mix():
+    """Requests with 2-3 levels of 3x refinement (interpolation, flux
+    correction and restriction every step, remeshed every 8 of their own
+    steps from the device criterion) next to uniform ones: each adaptive
+    result -- its hierarchy and every patch vector in grid order -- is the
+    same alone (one step per replay) and in the mix (8 steps per replay)."""
+    from peanoclaw_gb300 import serving as SV
+
+    reqs = SV.make_requests(6, rate=200.0, seed=12, cells=(2e4, 2e5), t_end=(0.01, 0.02), n=16,
+                            levels=(1, 3))
+    assert sorted(set(r.levels for r in reqs)) == [1, 2, 3]
+    srv = SV.Server(slab_doubles=16_000_000, max_groups=3, max_patches=8192, steps_per_batch=8,
+                    remesh_every=8)
+    try:
+        done, wall = srv.serve(reqs, max_wall=300.0)
+        assert srv.remesh_s > 0.0
+    finally:
+        srv.close()
+    assert len(done) == len(reqs)
+    for mixed in done:
+        if mixed.levels == 1 and mixed.rid % 2:
+            continue
+        alone = SV.run_alone(mixed, slab_doubles=8_000_000, remesh_every=8)
+        assert alone.steps == mixed.steps
+        assert alone.result.shape == mixed.result.shape
+        assert np.array_equal(alone.result.view(np.int64), mixed.result.view(np.int64)), mixed.rid
+        assert np.all(np.isfinite(mixed.result))
