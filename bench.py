@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default batched schedule instead of autotuning it")
+    ap.add_argument("--schedule", default="",
+                    help="fix the schedule instead of autotuning: tiles/VARIANT or strips/VARIANT/CHUNK")
     ap.add_argument("--form", default="auto", choices=["auto", "fused", "unfused"],
                     help="step form: the autotuner's pick, or the fused / unfused form on the default "
                          "strip schedule (no autotuning)")
@@ -587,9 +589,13 @@ def main():
     # one or two steps per candidate) and the graph instantiation
     if args.form != "auto":
         ctx.set_step_form(P.FORM_UNFUSED if args.form == "unfused" else P.FORM_AUTO)
+    if args.schedule:
+        f = args.schedule.split("/")
+        kind = P.SCHED_TILES if f[0] == "tiles" else P.SCHED_STRIPS
+        ctx.set_schedule(kind, int(f[1]) if len(f) > 1 else 0, int(f[2]) if len(f) > 2 else 32)
     ctx.run(max(1, args.warmup), P.PCG_MODE_BATCHED)
     tuned = None
-    if not args.no_autotune and args.form == "auto":
+    if not args.no_autotune and args.form == "auto" and not args.schedule:
         tuned = ctx.autotune(reps=2)
         ctx.run(2, P.PCG_MODE_BATCHED)
     sched = ctx.get_schedule()

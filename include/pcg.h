@@ -380,6 +380,12 @@ int pcg_set_virtual_time_items(pcg_context *ctx, int32_t n, const int32_t *leaf,
  * BATCHED sweep and update map patches onto the GPU; every schedule computes
  * bit-identical results.
  *   kind 0: one 16x16 tile of a patch per CTA iteration (256 threads);
+ *           variant 0 stages the tile + halo with per-thread loads,
+ *           variant 1 with tensor copies (TMA: cp.async.bulk.tensor of the
+ *           uNew, uOld and bathymetry boxes, per-patch tensor maps); variant 1
+ *           needs leaves of even size, ghost width 1, 3 unknowns and the
+ *           bathymetry as the only parameter field (PCG_E_INVALID at the
+ *           step otherwise);
  *   kind 1: warp strips: a warp marches strips of up to 32 rows and `chunk`
  *           columns (1..32) of one or more patches along x; `variant` picks
  *           the CTA size / register budget (0..4: 4 warps x 4 CTAs/SM,
@@ -395,7 +401,8 @@ typedef struct pcg_schedule {
 /* Fix the schedule of the context (overrides any tuned choice). */
 int pcg_set_schedule(pcg_context *ctx, const pcg_schedule *s);
 int pcg_get_schedule(pcg_context *ctx, pcg_schedule *s);
-/* Autotuner: runs `reps` BATCHED steps with each candidate schedule (tiles;
+/* Autotuner: runs `reps` BATCHED steps with each candidate schedule (tiles,
+ * also with TMA staging where the leaves allow it;
  * strips x 5 variants x chunk 32 / 16, in the fused step form where it
  * applies; then the fastest strip schedule in the unfused form), times each candidate's steps with
  * CUDA events, keeps the fastest for this context and caches it for the

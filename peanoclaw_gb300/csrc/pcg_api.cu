@@ -245,7 +245,11 @@ struct pcg_context {
   std::vector<int2> h_restr_chunks;
   size_t d_rgeo_cap = 0, d_rgeob_cap = 0, d_rch_cap = 0;
   bool restr_geo_dirty = true;               // lists, geometry or restriction bounds changed
-  pcg::TransferCtl *d_xfer = nullptr;  // work counters and error word of k_level_transfer
+  pcg::TileMaps *d_tile_maps = nullptr;  // tensor maps of the TMA tile sweep, per patch id
+  size_t d_tmaps_cap = 0;
+  bool tma_ok = false;                   // every leaf has a shape the TMA tile staging takes
+  bool tile_maps_valid = false;
+  pcg::TransferCtl *d_xfer = nullptr;  // work counters and error word of k_level_transfer (and the TMA sweep)
   bool xfer_pending = false;           // a level transfer ran since its error word was read
   size_t d_restr_cap = 0, d_flux_cap = 0, d_rb_cap = 0, d_fb_cap = 0, d_rd_cap = 0, d_leaf_cap = 0;
   double g_flux = 1.0;
@@ -585,6 +589,7 @@ int rebuild_topology(pcg_context *c) {
   c->h_tiles.clear();
   c->h_wall.clear();
   c->leaf_ids.clear();
+  c->tile_maps_valid = false;
   c->cells_per_step = 0;
   for (int p = 0; p < c->patch_hw; p++) {
     pcg::PatchDev &P = c->h_patches[p];
@@ -608,6 +613,8 @@ int rebuild_topology(pcg_context *c) {
     P.tile_count = (int)c->h_tiles.size() - P.tile_begin;
     if (P.wall) c->h_wall.push_back(p);
   }
+  c->tma_ok = !c->leaf_ids.empty();
+  for (int p : c->leaf_ids) c->tma_ok = c->tma_ok && pcg::tma_tile_shape(c->h_patches[p]);
   // items: keep the user's order within each destination (plain form needs
   // per-destination ranges; the batched kernel relies on disjoint writes)
   c->h_items.clear();
@@ -843,6 +850,9 @@ int check_level_transfer(pcg_context *c) {
   PCG_CUDA(cudaMemcpy(&err, &c->d_xfer->err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
     PCG_CUDA(cudaMemset(c->d_xfer, 0, sizeof(pcg::TransferCtl)));
+    if (err == 2)
+      return fail(PCG_E_CUDA, "TMA tile sweep: the staging copies of a tile did not complete in time; the step's "
+                              "sweep is incomplete");
     return fail(PCG_E_CUDA, "level transfer: a wait between its phases ran out; the step's flux correction "
                             "and restriction are incomplete");
   }
@@ -858,10 +868,38 @@ int refresh_fin(pcg_context *c) {
   return PCG_OK;
 }
 
+// Tensor maps of the TMA tile sweep for every leaf (built when the variant
+// first runs after a topology change; the patches' data do not move).
+int ensure_tile_maps(pcg_context *c) {
+  if (c->tile_maps_valid) return PCG_OK;
+  if (!c->tma_ok) return fail(PCG_E_INVALID, "the TMA tile staging needs leaves of even size with ghost width 1, "
+                                            "3 unknowns and the bathymetry field only");
+  std::vector<pcg::TileMaps> h((size_t)std::max(1, c->patch_hw));
+  for (int p : c->leaf_ids) {
+    cudaError_t e = pcg::encode_tile_maps(c->h_patches[p], c->slab, &h[p]);
+    if (e != cudaSuccess) return fail(PCG_E_CUDA, std::string("tensor map of patch ") + std::to_string(p) + ": " +
+                                                      cudaGetErrorString(e));
+  }
+  int rc;
+  if ((rc = ensure_device(c, &c->d_tile_maps, &c->d_tmaps_cap, h.size())) != PCG_OK) return rc;
+  PCG_CUDA(cudaMemcpyAsync(c->d_tile_maps, h.data(), sizeof(pcg::TileMaps) * h.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  c->tile_maps_valid = true;
+  return PCG_OK;
+}
+
 // Batched sweep and update with the context's schedule.
 int enqueue_sweep(pcg_context *c) {
   using namespace pcg;
-  if (c->sched.kind == PCG_SCHED_TILES)
+  if (c->sched.kind == PCG_SCHED_TILES && c->sched.variant == 1) {
+    int rc = ensure_tile_maps(c);
+    if (rc != PCG_OK) return rc;
+    PCG_CUDA(launch_sweep_tma(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tile_maps, c->d_tiles, 0,
+                              (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt, c->d_group_active,
+                              c->d_fin, c->ts_local ? c->d_pact : nullptr, &c->d_xfer->err));
+    c->xfer_pending = true;
+  } else if (c->sched.kind == PCG_SCHED_TILES)
     PCG_CUDA(launch_sweep(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_tiles, 0,
                           (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
                           c->d_group_active, c->d_fin, c->ts_local ? c->d_pact : nullptr));
@@ -1262,6 +1300,7 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_flux_begin);
   cudaFree(c->d_restr_dsts);
   cudaFree(c->d_xfer);
+  cudaFree(c->d_tile_maps);
   cudaFree(c->d_restr_geo);
   cudaFree(c->d_restr_geo_bad);
   cudaFree(c->d_restr_chunks);
@@ -2109,6 +2148,9 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
     PCG_SETTLE(c);
     if ((rc = refresh_fin(c)) != PCG_OK) return rc;
     if ((rc = refresh_restr_geometry(c)) != PCG_OK) return rc;
+    // (built outside the graph capture: they allocate)
+    if (c->sched.kind == PCG_SCHED_TILES && c->sched.variant == 1 && (rc = ensure_tile_maps(c)) != PCG_OK)
+      return rc;
   }
   if ((rc = ensure_hist(c, steps)) != PCG_OK) return rc;
   PCG_CUDA(cudaMemsetAsync(c->d_counter, 0, sizeof(int), c->stream));
@@ -2228,7 +2270,11 @@ namespace {
 
 int check_schedule(const pcg_schedule *s) {
   if (!s) return fail(PCG_E_INVALID, "null schedule");
-  if (s->kind == PCG_SCHED_TILES) return PCG_OK;
+  if (s->kind == PCG_SCHED_TILES) {
+    if (s->variant != 0 && s->variant != 1)
+      return fail(PCG_E_INVALID, "tile variant must be 0 (thread loads) or 1 (TMA staging)");
+    return PCG_OK;
+  }
   if (s->kind != PCG_SCHED_STRIPS) return fail(PCG_E_INVALID, "schedule kind must be 0 or 1");
   if (s->variant < 0 || s->variant >= pcg::kNumStripVariants)
     return fail(PCG_E_INVALID, "strip variant out of range");
@@ -2247,7 +2293,7 @@ int pcg_set_schedule(pcg_context *c, const pcg_schedule *s) {
   PCG_SETTLE(c);
   PCG_CUDA(cudaSetDevice(c->device));
   c->sched = *s;
-  if (c->sched.kind == PCG_SCHED_TILES) { c->sched.variant = 0; c->sched.chunk = 32; c->sched.unfused = 0; }
+  if (c->sched.kind == PCG_SCHED_TILES) { c->sched.chunk = 32; c->sched.unfused = 0; }
   c->sched_fixed = true;
   c->graph_valid = false;
   if (!c->topo_dirty) return apply_schedule(c);
@@ -2276,12 +2322,16 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
   std::vector<pcg_schedule> cand;
   cand.push_back(pcg_schedule{PCG_SCHED_TILES, 0, 32, 0});
+  if (c->tma_ok) cand.push_back(pcg_schedule{PCG_SCHED_TILES, 1, 32, 0});
   for (int chunk : {32, 16})
     for (int v = 0; v < pcg::kNumStripVariants; v++) cand.push_back(pcg_schedule{PCG_SCHED_STRIPS, v, chunk, 0});
   std::vector<double> t(cand.size(), 0.0);
   for (size_t k = 0; k < cand.size(); k++) {
     c->sched = cand[k];
     if ((rc = apply_schedule(c)) != PCG_OK) return rc;
+    // host-side set-up of a candidate stays out of its timed steps
+    if (c->sched.kind == PCG_SCHED_TILES && c->sched.variant == 1 && (rc = ensure_tile_maps(c)) != PCG_OK)
+      return rc;
     // strip candidates run the fused step where it applies, tiles the unfused one
     const bool fused = use_fused(c, PCG_MODE_BATCHED);
     if (fused) {

@@ -13,6 +13,8 @@
 #include "pcg_device.cuh"
 #include "pcg_kernels.h"
 
+#include <cuda.h>
+
 #include <algorithm>
 #include <cstdint>
 
@@ -57,6 +59,19 @@ __device__ __forceinline__ CellQ load_y(const SweepSmem &S, int i, int j) {
 // inside the patch and from uOld for the ghost ring.  Returns, in the calling
 // thread, the accumulated net updates of its cell (valid iff t < tw*th) and
 // the tile's max wave speed (valid in every thread).
+// One staged cell of a tile: its derived quantities into the tile's arrays.
+__device__ __forceinline__ void stage_cell(SweepSmem &S, int sx, int sy, double dry, double halfg, double h,
+                                           double hu, double hv, double b) {
+  CellQ qx, qy;
+  cell_derived(dry, halfg, h, hu, hv, b, qx, qy);
+  S.gh[sx][sy] = qx.gh; S.b[sx][sy] = b; S.eta[sx][sy] = qx.eta; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
+  S.s[sx][sy] = qx.s; S.p[sx][sy] = qx.p; S.q[sx][sy] = qy.p;
+  S.F[sx][sy] = qx.F; S.G[sx][sy] = qy.F; S.wet[sx][sy] = qx.wet ? 1 : 0;
+}
+
+__device__ __forceinline__ double sweep_tile_staged(SweepSmem &S, int tw, int th, double &nh, double &nhu,
+                                                    double &nhv);
+
 __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restrict__ slab,
                                              const PatchDev &P, const SweParamsDev &prm,
                                              int x0, int y0, int tw, int th, bool interior_is_unew,
@@ -86,14 +101,16 @@ __device__ __forceinline__ double sweep_tile(SweepSmem &S, const double *__restr
       hu = slab[idx_uold(P, 1, x, y)];
       hv = slab[idx_uold(P, 2, x, y)];
     }
-    double b = slab[idx_pw(P, 0, x, y)];
-    CellQ qx, qy;
-    cell_derived(dry, halfg, h, hu, hv, b, qx, qy);
-    S.gh[sx][sy] = qx.gh; S.b[sx][sy] = b; S.eta[sx][sy] = qx.eta; S.hu[sx][sy] = qx.hu; S.hv[sx][sy] = qy.hu;
-    S.s[sx][sy] = qx.s; S.p[sx][sy] = qx.p; S.q[sx][sy] = qy.p;
-    S.F[sx][sy] = qx.F; S.G[sx][sy] = qy.F; S.wet[sx][sy] = qx.wet ? 1 : 0;
+    stage_cell(S, sx, sy, dry, halfg, h, hu, hv, slab[idx_pw(P, 0, x, y)]);
   }
   __syncthreads();
+  return sweep_tile_staged(S, tw, th, nh, nhu, nhv);
+}
+
+// The edges, the accumulation and the max wave speed of a staged tile.
+__device__ __forceinline__ double sweep_tile_staged(SweepSmem &S, int tw, int th, double &nh, double &nhu,
+                                                    double &nhv) {
+  const int t = threadIdx.x;
   double smax = 0.0;
   double xr_h = 0.0, xr_hu = 0.0, yr_h = 0.0, yr_hv = 0.0;
   const bool active = t < tw * th;
@@ -186,6 +203,164 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
       if (fin) atomicOr(&fin[ti.pid], kFinUOld);
       atomicMax(&patch_smax[ti.pid], dbits(smax));
       double dtc = cfl_dt(prm, smax, subcell(P, 0), subcell(P, 1));
+      atomicMin(&group_dt[P.group], dbits(dtc));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged tile sweep (schedule: tiles, variant 1).  The same tiles and
+// arithmetic as k_sweep_tiles; the tile + halo is brought into shared memory
+// by three tensor copies (cp.async.bulk.tensor) per tile instead of per-thread
+// loads: the uNew box (interior cells), the uOld box (ghost ring) and the
+// bathymetry box, completing on one mbarrier.  Tensor maps per patch
+// (TileMaps, encoded on the host by encode_tile_maps): uNew as (ny, nx, 3),
+// uOld as (ny+2, nx+2, 3), b as (ny+2, nx+2), y innermost.  The innermost
+// start coordinate must be a multiple of 2 doubles (16 bytes): the uNew box
+// starts at y0 - 2 (tiles start at multiples of 16), the ghosted boxes at y0
+// (which is y0 - 1 in interior coordinates); boxes are min(16, n) + 4 resp.
+// + 2 doubles wide in y (even for even n), so only patches of even size take
+// this form.  Boxes reaching past the patch read zeros (out-of-bounds fill)
+// and those cells are taken from the uOld box.
+// ---------------------------------------------------------------------------
+struct __align__(128) TmaRaw {
+  __align__(128) double un[3 * (kTile + 2) * (kTile + 4)];
+  __align__(128) double uo[3 * (kTile + 2) * (kTile + 2)];
+  __align__(128) double bb[(kTile + 2) * (kTile + 2)];
+};
+constexpr int kTmaSpin = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *m, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *m, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *m, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *m, int c0, int c1,
+                                            int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(m))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *m, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(m))
+      : "memory");
+}
+
+// All threads: wait for the tile's copies (bounded); false if they did not
+// complete (the kernel then sets *err and stops).
+__device__ __forceinline__ bool tma_wait(uint64_t *m, unsigned parity) {
+  bool ok = false;
+  for (int i = 0; i < kTmaSpin && !ok; i++) ok = mbar_try_wait(m, parity);
+  return !__syncthreads_or(!ok);
+}
+
+// Issues the three copies of tile `ti` into R (by one thread).
+__device__ __forceinline__ void tma_issue_tile(TmaRaw &R, uint64_t *mbar, const TileMaps *maps, const TileItem &ti,
+                                               const PatchDev &P) {
+  const int bx = (P.nx < kTile ? P.nx : kTile) + 2;
+  const int byo = (P.ny < kTile ? P.ny : kTile) + 2, byn = byo + 2;
+  const TileMaps *M = &maps[ti.pid];
+  // earlier reads of R (generic proxy) are ordered before the copies (async
+  // proxy) by the barrier that ended them and this fence
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_expect_tx(mbar, (unsigned)(8 * (3 * bx * byn + 3 * bx * byo + bx * byo)));
+  tma_load_3d(R.un, &M->unew, mbar, ti.y0 - 2, ti.x0 - 1, 0);
+  tma_load_3d(R.uo, &M->uold, mbar, ti.y0, ti.x0, 0);
+  tma_load_2d(R.bb, &M->b, mbar, ti.y0, ti.x0);
+}
+
+// One raw buffer per CTA: a double-buffered form (the next tile's copies in
+// flight during the current sweep) measured slower, 17.8 against 14.7 ms per
+// step on the 50k mix, its 80 registers and 72 KB of shared memory leaving 3
+// CTAs per SM instead of 4 for this FP64-latency-bound sweep.
+__global__ void __launch_bounds__(kSweepThreads, 4)
+    k_sweep_tiles_tma(double *__restrict__ slab, const PatchDev *__restrict__ patches,
+                      const TileMaps *__restrict__ maps, const TileItem *__restrict__ tiles, int first, int count,
+                      SweParamsDev prm, unsigned long long *__restrict__ patch_smax,
+                      unsigned long long *__restrict__ group_dt, const int *__restrict__ group_active,
+                      int *__restrict__ fin, const int *__restrict__ pact, int *__restrict__ err) {
+  __shared__ SweepSmem S;
+  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  TmaRaw &R = *reinterpret_cast<TmaRaw *>(tma_smem);
+  if (threadIdx.x == 0) mbar_init(&mbar, 1);
+  __syncthreads();
+  unsigned parity = 0;
+  const double dry = prm.dry_tol;
+  const double halfg = __dmul_rn(0.5, prm.g);
+  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    const TileItem ti = tiles[first + it];
+    const PatchDev P = patches[ti.pid];
+    if (group_active && !group_active[P.group]) continue;
+    if (pact && !pact[ti.pid]) continue;
+    const int bx = (P.nx < kTile ? P.nx : kTile) + 2;
+    const int byo = (P.ny < kTile ? P.ny : kTile) + 2, byn = byo + 2;
+    if (threadIdx.x == 0) {
+      S.dxi = __ddiv_rn(1.0, subcell(P, 0));
+      S.dyi = __ddiv_rn(1.0, subcell(P, 1));
+      tma_issue_tile(R, &mbar, maps, ti, P);
+    }
+    if (!tma_wait(&mbar, parity)) {
+      // the copies did not complete: wait once more (bounded) so that none is
+      // left writing shared memory, report, and stop
+      tma_wait(&mbar, parity);
+      if (threadIdx.x == 0) atomicExch(err, 2);
+      return;
+    }
+    parity ^= 1u;
+    const int tw = ti.tw, th = ti.th, sw = tw + 2, sh = th + 2;
+    for (int k = threadIdx.x; k < sw * sh; k += blockDim.x) {
+      const int sx = k / sh, sy = k - sx * sh;
+      const bool cx = (sx == 0 || sx == sw - 1), cy = (sy == 0 || sy == sh - 1);
+      if (cx && cy) continue;
+      const int x = ti.x0 - 1 + sx, y = ti.y0 - 1 + sy;
+      const bool inside = (x >= 0 && x < P.nx && y >= 0 && y < P.ny);
+      double h, hu, hv;
+      if (inside) {
+        h = R.un[(0 * bx + sx) * byn + sy + 1];
+        hu = R.un[(1 * bx + sx) * byn + sy + 1];
+        hv = R.un[(2 * bx + sx) * byn + sy + 1];
+      } else {
+        h = R.uo[(0 * bx + sx) * byo + sy];
+        hu = R.uo[(1 * bx + sx) * byo + sy];
+        hv = R.uo[(2 * bx + sx) * byo + sy];
+      }
+      stage_cell(S, sx, sy, dry, halfg, h, hu, hv, R.bb[sx * byo + sy]);
+    }
+    __syncthreads();
+    double nh = 0, nhu = 0, nhv = 0;
+    const double smax = sweep_tile_staged(S, tw, th, nh, nhu, nhv);
+    const int t = threadIdx.x;
+    if (t < tw * th) {
+      const int x = ti.x0 + t / th, y = ti.y0 + t % th;
+      slab[idx_uold(P, 0, x, y)] = nh;
+      slab[idx_uold(P, 1, x, y)] = nhu;
+      slab[idx_uold(P, 2, x, y)] = nhv;
+    }
+    if (t == 0) {
+      if (fin) atomicOr(&fin[ti.pid], kFinUOld);
+      atomicMax(&patch_smax[ti.pid], dbits(smax));
+      const double dtc = cfl_dt(prm, smax, subcell(P, 0), subcell(P, 1));
       atomicMin(&group_dt[P.group], dbits(dtc));
     }
   }
@@ -2145,6 +2320,82 @@ cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev
   k_sweep_tiles<<<grid, kSweepThreads, 0, st>>>(slab, patches, tiles, first, count, prm, patch_smax,
                                                 group_dt, group_active, fin, pact);
   return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_tma(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                             const TileMaps *maps, const TileItem *tiles, int first, int count,
+                             const SweParamsDev &prm, unsigned long long *patch_smax, unsigned long long *group_dt,
+                             const int *group_active, int *fin, const int *pact, int *err) {
+  if (count <= 0) return cudaSuccess;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_sweep_tiles_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(TmaRaw));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_sweep_tiles_tma<<<grid, kSweepThreads, sizeof(TmaRaw), st>>>(slab, patches, maps, tiles, first, count, prm,
+                                                                 patch_smax, group_dt, group_active, fin, pact,
+                                                                 err);
+  return cudaGetLastError();
+}
+
+// Tensor maps of the TMA tile sweep for one patch of even size, ghost width 1,
+// 3 unknowns and the bathymetry as the only parameter field with ghost layer.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn g_encode_tiled = nullptr;
+
+cudaError_t encode_tile_maps(const PatchDev &P, double *slab, TileMaps *out) {
+  if (!g_encode_tiled) {
+    cudaDriverEntryPointQueryResult q;
+    void *f = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || !f) return cudaErrorSymbolNotFound;
+    g_encode_tiled = (EncodeTiledFn)f;
+  }
+  const cuuint32_t bx = (cuuint32_t)((P.nx < kTile ? P.nx : kTile) + 2);
+  const cuuint32_t byo = (cuuint32_t)((P.ny < kTile ? P.ny : kTile) + 2), byn = byo + 2;
+  const cuuint64_t nx = (cuuint64_t)P.nx, ny = (cuuint64_t)P.ny;
+  double *unew = slab + P.off;
+  double *uold = unew + 3 * nx * ny;
+  double *b = uold + 3 * (nx + 2) * (ny + 2);
+  const cuuint32_t es[3] = {1, 1, 1};
+  {
+    const cuuint64_t dims[3] = {ny, nx, 3};
+    const cuuint64_t strides[2] = {ny * 8, nx * ny * 8};
+    const cuuint32_t box[3] = {byn, bx, 3};
+    if (g_encode_tiled(&out->unew, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, unew, dims, strides, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  {
+    const cuuint64_t dims[3] = {ny + 2, nx + 2, 3};
+    const cuuint64_t strides[2] = {(ny + 2) * 8, (nx + 2) * (ny + 2) * 8};
+    const cuuint32_t box[3] = {byo, bx, 3};
+    if (g_encode_tiled(&out->uold, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, uold, dims, strides, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  {
+    const cuuint64_t dims[2] = {ny + 2, nx + 2};
+    const cuuint64_t strides[1] = {(ny + 2) * 8};
+    const cuuint32_t box[2] = {byo, bx};
+    if (g_encode_tiled(&out->b, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, b, dims, strides, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  return cudaSuccess;
+}
+
+bool tma_tile_shape(const PatchDev &P) {
+  return P.nx >= 2 && P.ny >= 2 && P.nx % 2 == 0 && P.ny % 2 == 0 && P.g == 1 && P.nq == 3 && P.np_wo == 0 &&
+         P.np_w == 1;
 }
 
 cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,

@@ -1,6 +1,8 @@
 // pcg_kernels.h -- host-side launchers of the kernels in pcg_kernels.cu.
 #pragma once
 
+#include <cuda.h>
+
 #include <cuda_runtime.h>
 
 #include <string>
@@ -17,6 +19,16 @@ cudaError_t launch_sweep(cudaStream_t st, int grid, double *slab, const PatchDev
                          const TileItem *tiles, int first, int count, const SweParamsDev &prm,
                          unsigned long long *patch_smax, unsigned long long *group_dt,
                          const int *group_active, int *fin = nullptr, const int *pact = nullptr);
+// TMA-staged tile sweep (tiles, variant 1): tensor maps per patch.
+struct TileMaps {
+  CUtensorMap unew, uold, b;
+};
+bool tma_tile_shape(const PatchDev &P);
+cudaError_t encode_tile_maps(const PatchDev &P, double *slab, TileMaps *out);
+cudaError_t launch_sweep_tma(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
+                             const TileMaps *maps, const TileItem *tiles, int first, int count,
+                             const SweParamsDev &prm, unsigned long long *patch_smax, unsigned long long *group_dt,
+                             const int *group_active, int *fin, const int *pact, int *err);
 cudaError_t launch_update(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                           PatchTimeDev *times, const TileItem *tiles, int first, int count,
                           const SweParamsDev &prm, const unsigned long long *patch_smax,

@@ -66,9 +66,10 @@ def test_schedule_bit_exact_on_ragged_sizes(sched):
 def test_autotuner_picks_a_candidate_and_keeps_results_exact():
     ps = S.uneven_patches(grid=4, sizes=(8, 16, 32, 64))
     out, dts, tuned, got = _gpu_run(ps, 3, autotune_reps=1)
-    # 11 candidates, and the best strip schedule in the unfused form when a
-    # strip schedule won
-    assert len(tuned) in (11, 12)
+    # 12 candidates (the sizes are even: tiles with TMA staging too), and the
+    # best strip schedule in the unfused form when a strip schedule won
+    assert len(tuned) in (12, 13)
+    assert any(k[:2] == (P.SCHED_TILES, 1) for k, _ in tuned)
     assert all(ms > 0.0 for _, ms in tuned)
     best = min(tuned, key=lambda t: t[1])[0]
     assert got == best
@@ -92,5 +93,31 @@ def test_schedule_arguments_are_checked():
         for bad in [(2, 0, 32), (1, 9, 32), (1, 5, 32), (1, 0, 0), (1, 0, 33)]:
             with pytest.raises(P.PcgError):
                 c.set_schedule(*bad)
+    finally:
+        c.close()
+
+
+def test_tma_tile_staging_bit_exact_on_even_sizes():
+    """Tiles staged by tensor copies (uNew, uOld and bathymetry boxes) on
+    even patch sizes whose tiles are partial (18 = 16 + 2, 34, 40) and on
+    8 x 8 patches (one tile smaller than the box), walls, copies and
+    interpolations between sizes: 12 steps bit for bit against the oracle."""
+    ps = S.uneven_patches(grid=5, sizes=(8, 18, 34, 40))
+    out, dts, _, got = _gpu_run(ps, 12, sched=(P.SCHED_TILES, 1, 32))
+    assert got[:2] == (P.SCHED_TILES, 1)
+    oout, odts = _oracle_run(ps, 12)
+    assert dts == odts
+    assert np.array_equal(out.view(np.int64), oout.view(np.int64))
+
+
+def test_tma_tile_staging_refuses_odd_sizes():
+    ps = S.uneven_patches(grid=3, sizes=(5, 12))
+    c = P.Context(slab_doubles=slab_for(ps), max_patches=len(ps) + 8, max_groups=1, params=PRM)
+    try:
+        gpu_patchset(c, ps)
+        c.set_group_max_dt(0, 1e9)
+        c.set_schedule(P.SCHED_TILES, 1, 32)
+        with pytest.raises(P.PcgError):
+            c.run(1, P.PCG_MODE_BATCHED)
     finally:
         c.close()
