@@ -427,6 +427,14 @@ int pcg_profile_step(pcg_context *ctx, double *ms);
  * context's device (dependent-chain loop on every SM); returns TFLOP/s with an
  * FMA counted as two flops. */
 int pcg_probe_fp64_peak(pcg_context *ctx, double *tflops);
+/* No counterpart in the reference.  Self-test of the level transfer's bounded
+ * waits (the wait of the restriction items for the flux corrections): runs
+ * the restriction items once with a wait that nothing can satisfy; every
+ * wait runs out after its spin limit (about 0.1 s), sets the error word and
+ * skips its item, so no patch data changes.  Returns PCG_OK when the host
+ * read the error back (and reset it), PCG_E_STATE otherwise; the context
+ * stays usable.  Needs a restriction list (PCG_E_STATE without one). */
+int pcg_selftest_transfer_wait(pcg_context *ctx);
 /* No counterpart in the reference.  Compares the library's integer-pipe FP64
  * divide, reciprocal and square root with the hardware IEEE operations on `samples`
  * pseudo-random operand pairs; *mismatches receives the number of results

@@ -2513,6 +2513,33 @@ int pcg_probe_fp64_peak(pcg_context *c, double *tflops) {
   return PCG_OK;
 }
 
+int pcg_selftest_transfer_wait(pcg_context *c) {
+  if (!c) return fail(PCG_E_INVALID, "null context");
+  std::lock_guard<std::mutex> lk(c->mu);
+  PCG_SETTLE(c);
+  PCG_CUDA(cudaSetDevice(c->device));
+  int rc = rebuild_topology(c);
+  if (rc != PCG_OK) return rc;
+  if (c->h_restr.empty()) return fail(PCG_E_STATE, "the self-test needs a restriction list");
+  if ((rc = refresh_restr_geometry(c)) != PCG_OK) return rc;
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  if ((rc = check_level_transfer(c)) != PCG_OK) return rc;
+  // restriction items only (no flux destinations, no face-flux storage), each
+  // waiting for one finished flux destination: nothing sets that counter
+  const int n_restr = (int)c->h_restr_chunks.size();
+  const int grid = pcg::level_transfer_grid(c->num_sms, 0, 0, n_restr);
+  PCG_CUDA(pcg::launch_level_transfer(c->stream, grid, c->slab, c->d_patches, c->d_times, c->d_flux_leaf_ids, 0,
+                                      c->g_flux, c->d_flux, c->d_flux_begin, 0, c->d_restr, c->d_restr_begin,
+                                      c->d_restr_geo, c->d_restr_geo_bad, c->d_restr_chunks, n_restr, nullptr,
+                                      nullptr, c->d_xfer, 1));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  int err = 0;
+  PCG_CUDA(cudaMemcpy(&err, &c->d_xfer->err, sizeof(int), cudaMemcpyDeviceToHost));
+  PCG_CUDA(cudaMemset(c->d_xfer, 0, sizeof(pcg::TransferCtl)));
+  if (err != 1) return fail(PCG_E_STATE, "the level transfer's bounded wait did not report running out");
+  return PCG_OK;
+}
+
 int pcg_check_ieee_emulation(pcg_context *c, int64_t samples, uint64_t seed, int64_t *mismatches) {
   if (!c || !mismatches || samples < 0) return fail(PCG_E_INVALID, "bad argument");
   std::lock_guard<std::mutex> lk(c->mu);

@@ -2087,7 +2087,7 @@ __global__ void __launch_bounds__(kTransferThreads, 1)
                      int n_leaf, double gf, const int4 *flux_items, const int *flux_begin, int n_flux,
                      const int4 *restr_items, const int *restr_begin, const RestrItemTab *restr_geo,
                      const int *restr_geo_bad, const int2 *restr_chunks, int n_restr, const int *group_active,
-                     const int *pact, TransferCtl *ctl) {
+                     const int *pact, int wait_bias, TransferCtl *ctl) {
   extern __shared__ __align__(16) unsigned char xfer_smem[];
   __shared__ int s_item, s_flag;
   const int n_store = (n_leaf + kTransferLeaves - 1) / kTransferLeaves;
@@ -2119,7 +2119,7 @@ __global__ void __launch_bounds__(kTransferThreads, 1)
                        *reinterpret_cast<XferFluxSmem *>(xfer_smem));
       transfer_done(&ctl->done_flux);
     } else if (item < n_flux + n_restr) {
-      if (!transfer_wait(&ctl->done_flux, (unsigned)n_flux, ctl, &s_flag)) continue;
+      if (!transfer_wait(&ctl->done_flux, (unsigned)(n_flux + wait_bias), ctl, &s_flag)) continue;
       const int2 ch = restr_chunks[item - n_flux];  // destination, chunk
       const int b = ch.x;
       const int b0 = restr_begin[b], b1 = restr_begin[b + 1];
@@ -2698,14 +2698,14 @@ cudaError_t launch_level_transfer(cudaStream_t st, int grid, double *slab, const
                                   const int4 *restr_items, const int *restr_begin,
                                   const RestrItemTab *restr_geo, const int *restr_geo_bad,
                                   const int2 *restr_chunks, int n_restr, const int *group_active,
-                                  const int *pact, TransferCtl *ctl) {
+                                  const int *pact, TransferCtl *ctl, int wait_bias) {
   if (grid <= 0) return cudaSuccess;
   cudaError_t e = level_transfer_setup();
   if (e != cudaSuccess) return e;
   k_level_transfer<<<grid, kTransferThreads, kTransferSmem, st>>>(slab, patches, times, leaf_ids, n_leaf, gf, flux_items,
                                                       flux_begin, n_flux, restr_items, restr_begin, restr_geo,
                                                       restr_geo_bad, restr_chunks, n_restr, group_active, pact,
-                                                      ctl);
+                                                      wait_bias, ctl);
   return cudaGetLastError();
 }
 

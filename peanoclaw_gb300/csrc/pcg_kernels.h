@@ -150,14 +150,16 @@ cudaError_t launch_restr_geometry(cudaStream_t st, const PatchDev *patches, cons
 // destinations (restr_begin, region geometry from launch_restr_geometry) in
 // n_restr chunks (restr_chunks: destination, chunk of kRestrChunkCells
 // cells); pact (local time stepping, may be null) limits the restriction to
-// destinations with an advancing source.
+// destinations with an advancing source.  wait_bias (0 in a step) is added
+// to the flux destinations the restriction items wait for: the self-test
+// sets it so that no wait can end.
 cudaError_t launch_level_transfer(cudaStream_t st, int grid, double *slab, const PatchDev *patches,
                                   const PatchTimeDev *times, const int *leaf_ids, int n_leaf, double gf,
                                   const int4 *flux_items, const int *flux_begin, int n_flux,
                                   const int4 *restr_items, const int *restr_begin,
                                   const RestrItemTab *restr_geo, const int *restr_geo_bad,
                                   const int2 *restr_chunks, int n_restr, const int *group_active,
-                                  const int *pact, TransferCtl *ctl);
+                                  const int *pact, TransferCtl *ctl, int wait_bias = 0);
 cudaError_t launch_post_process_restriction(cudaStream_t st, double *slab, const PatchDev *patches,
                                             const int *ids, int count,
                                             const int *group_active = nullptr, const int *dirty = nullptr);

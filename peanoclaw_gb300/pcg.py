@@ -135,6 +135,7 @@ SIGNATURES = {
     "pcg_set_step_form": (C.c_int, [_CTX, C.c_int32]),
     "pcg_get_step_form": (C.c_int, [_CTX, C.c_int32, C.POINTER(C.c_int32)]),
     "pcg_get_step_launches": (C.c_int, [_CTX, C.POINTER(C.c_int32)]),
+    "pcg_selftest_transfer_wait": (C.c_int, [_CTX]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "pcg_synchronize": (C.c_int, [_CTX]),
@@ -424,6 +425,11 @@ class Context:
         v = C.c_int32()
         check(lib().pcg_get_step_form(self.h, int(mode), C.byref(v)))
         return bool(v.value)
+
+    def selftest_transfer_wait(self):
+        """pcg_selftest_transfer_wait: the level transfer's bounded wait runs
+        out on purpose and is reported; raises PcgError otherwise."""
+        check(lib().pcg_selftest_transfer_wait(self.h))
 
     def step_launches(self):
         """Kernel launches of one captured batched step (pcg_get_step_launches)."""

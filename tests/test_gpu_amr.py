@@ -75,3 +75,30 @@ def test_breaking_dam_full_size_bit_exact(mode):
     ref = np.concatenate([p.u for p in pats])
     assert dts == odts
     assert np.array_equal(out.view(np.int64), ref.view(np.int64))
+
+
+@pytest.mark.gpu
+def test_bounded_transfer_wait_reports_and_context_stays_usable():
+    """The level transfer's wait between its flux and restriction phases is
+    bounded: made to wait for a counter nothing sets, every wait runs out,
+    the error word comes back to the host, and no patch data changed -- the
+    run continued afterwards equals the oracle bit for bit."""
+    ps = S.breaking_dam_amr(base=3, n=9, levels=3)
+    ctx = P.Context(slab_doubles=int(ps.packed.size * 1.3) + 4096, max_patches=len(ps) + 8, max_groups=1,
+                    params=PRM)
+    try:
+        ids = gpu_amr_patchset(ctx, ps)
+        ctx.restrict_all()
+        ctx.set_group_max_dt(0, 1e9)
+        dts = list(ctx.run(2, P.PCG_MODE_BATCHED)[:, 0])
+        ctx.selftest_transfer_wait()
+        dts += list(ctx.run(2, P.PCG_MODE_BATCHED)[:, 0])
+        out = ctx.download_many(ids, int(ps.packed.size))
+    finally:
+        ctx.close()
+    pats = oracle_amr_patchset(ps)
+    oracle_restrict_all(pats, ps)
+    odts = [oracle_amr_step(pats, ps, oracle_params(PRM), 1e9) for _ in range(4)]
+    assert dts == odts
+    ref = np.concatenate([p.u for p in pats])
+    assert np.array_equal(out.view(np.int64), ref.view(np.int64))
