@@ -78,8 +78,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default batched schedule instead of autotuning it")
     ap.add_argument("--schedule", default="",
-                    help="fix the schedule instead of autotuning: tiles/VARIANT or strips/VARIANT/CHUNK")
-    ap.add_argument("--form", default="auto", choices=["auto", "fused", "unfused"],
+                    help="fix the schedule instead of autotuning: tiles/VARIANT or "
+                         "strips/VARIANT/CHUNK[/fused|unfused|pipelined]")
+    ap.add_argument("--form", default="auto", choices=["auto", "fused", "unfused", "pipelined"],
                     help="step form: the autotuner's pick, or the fused / unfused form on the default "
                          "strip schedule (no autotuning)")
     ap.add_argument("--config-legs", default="",
@@ -587,12 +588,16 @@ def main():
 
     # warm-up, the schedule autotuner (untimed; it advances the simulation by
     # one or two steps per candidate) and the graph instantiation
-    if args.form != "auto":
+    if args.form in ("fused", "unfused"):
         ctx.set_step_form(P.FORM_UNFUSED if args.form == "unfused" else P.FORM_AUTO)
+    forms = {"fused": P.STRIPS_FUSED, "unfused": P.STRIPS_UNFUSED, "pipelined": P.STRIPS_PIPELINED}
     if args.schedule:
         f = args.schedule.split("/")
         kind = P.SCHED_TILES if f[0] == "tiles" else P.SCHED_STRIPS
-        ctx.set_schedule(kind, int(f[1]) if len(f) > 1 else 0, int(f[2]) if len(f) > 2 else 32)
+        ctx.set_schedule(kind, int(f[1]) if len(f) > 1 else 0, int(f[2]) if len(f) > 2 else 32,
+                         forms[f[3]] if len(f) > 3 else 0)
+    elif args.form == "pipelined":
+        ctx.set_schedule(P.SCHED_STRIPS, 2, 32, P.STRIPS_PIPELINED)
     ctx.run(max(1, args.warmup), P.PCG_MODE_BATCHED)
     tuned = None
     if not args.no_autotune and args.form == "auto" and not args.schedule:
@@ -600,6 +605,8 @@ def main():
         ctx.run(2, P.PCG_MODE_BATCHED)
     sched = ctx.get_schedule()
     fused = ctx.step_is_fused(P.PCG_MODE_BATCHED)
+    pipelined = sched[0] == P.SCHED_STRIPS and sched[3] == P.STRIPS_PIPELINED
+    form = "pipelined" if pipelined else "fused" if fused else "unfused"
     step_launches = ctx.step_launches()
     dist_barrier(dist)
     ctx.synchronize()
@@ -627,13 +634,17 @@ def main():
     import torch
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     # dominant kernel: the sweep (unfused form: k_sweep_strips / k_sweep_tiles,
-    # the sweep's flops) or the fused sweep (k_fused_strips: ghost fill,
-    # deferred update and sweep, all flops of a cell update); its average
-    # launch duration from CUDA events on the launch stream
-    dom_flop = FLOP_PER_CELL if fused else FLOP_PER_CELL_SWEEP
+    # the sweep's flops), the fused sweep (k_fused_strips: ghost fill,
+    # deferred update and sweep, all flops of a cell update) or the pipelined
+    # step (k_pipeline_step: update of one step with fill, walls and sweep of
+    # the next, all flops of a cell update); its average launch duration from
+    # CUDA events on the launch stream
+    dom_flop = FLOP_PER_CELL if (fused or pipelined) else FLOP_PER_CELL_SWEEP
     achieved = (dom_flop * cells / 1e12) / (sweep_ms / 1e3)
     step_achieved = FLOP_PER_CELL * cells / 1e12 / (ms_per_step / 1e3)
-    if fused:
+    if pipelined:
+        dom_kernel = "k_pipeline_step"
+    elif fused:
         dom_kernel = "k_fused_strips"
     else:
         dom_kernel = "k_sweep_tiles" if sched[0] == P.SCHED_TILES else "k_sweep_strips"
@@ -648,7 +659,8 @@ def main():
     # DRAM traffic of the dominant kernel (sweep): bytes per cell update from
     # the ncu capture of the small case, scaled to this launch's cells
     prof = {"k_fused_strips": "k_fused_strips_uneven_patches_4k.md",
-            "k_sweep_strips": "k_sweep_strips_uneven_patches_4k.md"}.get(dom_kernel)
+            "k_sweep_strips": "k_sweep_strips_uneven_patches_4k.md",
+            "k_pipeline_step": "k_pipeline_step_uneven_patches_4k.md"}.get(dom_kernel)
     tpc = profile_figure(prof, "traffic_bytes_per_cell_update") if prof else None
     traffic = tpc * cells if tpc is not None else None
     fp64_ipc = (profile_figure(prof, "fp64_inst_per_cell_update") if prof else None) or FP64_INST_PER_CELL
@@ -724,7 +736,7 @@ def main():
             "config": {"workload": "batched step (%s form, CUDA graph), 50k uneven patches "
                                    "(%d patches, {8,16,32,64}^2 cells, %d cells, %.1f%% dry), "
                                    "radial-free random Gaussian bathymetry, 200-step config "
-                                   "timed over %d steps" % ("fused" if fused else "unfused", len(ps), cells,
+                                   "timed over %d steps" % (form, len(ps), cells,
                                                             100 * ps.meta["dry_fraction"], args.steps),
                        "patches": len(ps), "cells": cells, "grid_slots": args.grid,
                        "l2": "inputs (%.1f GB) larger than L2, no flush" % (ps.packed.nbytes / 1e9),
@@ -748,14 +760,16 @@ def main():
                          "hbm": {"achieved_gbs": alg_bytes / (step_ms_phase / 1e3) / 1e9,
                                  "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json",
                                  "alg_bytes_per_step": alg_bytes}},
-            "phase_ms": ({"reset": ph[0], "fused_sweep": ph[3], "advance": ph[4]} if fused else
+            "phase_ms": ({"pre": ph[0], "pipelined_step": ph[3], "first_launch_fill_sweep": ph[1],
+                          "last_launch_update": ph[2]} if pipelined else
+                         {"reset": ph[0], "fused_sweep": ph[3], "advance": ph[4]} if fused else
                          {"reset": ph[0], "ghost_items": ph[1], "walls": ph[2], "sweep": ph[3],
                           "update": ph[4]}),
             "schedule": {"kind": "tiles" if sched[0] == P.SCHED_TILES else "strips",
                          "variant": sched[1], "chunk": sched[2],
-                         "form": "unfused" if sched[3] or not fused else "fused",
+                         "form": form,
                          "autotune_ms_per_step": ({"%s/%d/%d%s" % ("tiles" if k[0] == 0 else "strips", k[1], k[2],
-                                                                 "/unfused" if k[3] else ""): m
+                                                                 ("", "/unfused", "/pipelined")[k[3]]): m
                                                    for k, m in tuned} if tuned else None)},
             "parity": parity,
             "plain_per_patch_value": plain,
@@ -765,9 +779,10 @@ def main():
             "cpu_configs": cpu_cfg,
             "configs": configs,
             "clocks": clk,
-            "gpu_launches": step_launches * args.steps,
-            "gpu_launches_note": "kernel nodes of the captured step graph (pcg_get_step_launches, "
-                                 "%d) x timed steps" % step_launches,
+            "gpu_launches": step_launches * (args.steps + (1 if pipelined else 0)),
+            "gpu_launches_note": ("kernel nodes of the captured step graph (pcg_get_step_launches, "
+                                  "%d) x %s" % (step_launches, "(timed steps + 1): a pipelined run of K steps "
+                                                "replays it K + 1 times" if pipelined else "timed steps")),
             "wall_s": wall,
         }
         print(json.dumps(line))

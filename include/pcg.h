@@ -394,7 +394,15 @@ typedef struct pcg_schedule {
   int32_t kind;
   int32_t variant;
   int32_t chunk;
-  int32_t unfused;   /* strips: 1 = the unfused step form even where the fused one applies */
+  int32_t unfused;   /* strips: 1 = the unfused step form even where the fused one applies;
+                        2 = pcg_run in the pipelined form where it applies (the synchronous
+                        step without restriction or flux-correction lists, PCG_FORM_AUTO):
+                        per step a bookkeeping launch, a launch of the ghost items' time
+                        factors and one persistent kernel that updates step k - 1 and
+                        fills, walls and sweeps step k, its work items ordered by
+                        per-patch counters (waits limited to 0.2 s: PCG_E_CUDA and an
+                        incomplete run if one runs out); a run of K steps is K + 1 such
+                        launch triples; pcg_step takes the unfused form */
 } pcg_schedule;
 #define PCG_SCHED_TILES 0
 #define PCG_SCHED_STRIPS 1
@@ -404,7 +412,8 @@ int pcg_get_schedule(pcg_context *ctx, pcg_schedule *s);
 /* Autotuner: runs `reps` BATCHED steps with each candidate schedule (tiles,
  * also with TMA staging where the leaves allow it;
  * strips x 5 variants x chunk 32 / 16, in the fused step form where it
- * applies; then the fastest strip schedule in the unfused form), times each candidate's steps with
+ * applies; then the fastest strip schedule in the unfused form, and in the
+ * pipelined form as one run of `reps` steps), times each candidate's steps with
  * CUDA events, keeps the fastest for this context and caches it for the
  * process under the key (SM count, histogram of leaf patch shapes), so later
  * contexts with the same patch mix start with it.  The simulation advances by
@@ -421,7 +430,12 @@ int pcg_autotune(pcg_context *ctx, int32_t reps, pcg_schedule *tried, double *ms
  * reset, ghost items, walls, sweep and update.  In the fused form the ghost
  * fill, walls and update are inside the sweep launch: ms[1] = ms[2] = 0,
  * ms[3] is the fused kernel, ms[4] the time advance, ms[0] the reset and
- * item factors of the next step. */
+ * item factors of the next step.  In the pipelined form (schedule field
+ * unfused = 2) a run of two steps is timed: ms[3] its middle step kernel
+ * (update of the first step, fill, walls and sweep of the second), ms[0]
+ * the two launches before it, ms[1] the first step kernel (fill, walls and
+ * sweep only), ms[2] the last (update only), ms[4] = 0; the simulation
+ * advances by two steps. */
 int pcg_profile_step(pcg_context *ctx, double *ms);
 /* No counterpart in the reference.  Measures the FP64 FMA throughput of the
  * context's device (dependent-chain loop on every SM); returns TFLOP/s with an

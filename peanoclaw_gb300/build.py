@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libpcg.so")
 PYCLAW_LIB = os.path.join(OUT, "libpcg_pyclaw.so")
 PYCLAW_SOURCE = "pcg_pyclaw.cpp"
-SOURCES = ["pcg_kernels.cu", "pcg_strips.cu", "pcg_fused.cu", "pcg_api.cu", "pcg_amr.cpp"]
+SOURCES = ["pcg_kernels.cu", "pcg_strips.cu", "pcg_fused.cu", "pcg_pipeline.cu", "pcg_api.cu", "pcg_amr.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
          "-Xptxas", "-warn-spills"]

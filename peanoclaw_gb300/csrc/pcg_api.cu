@@ -5,6 +5,7 @@
 // work list; host calls only enqueue work on the context's stream.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -302,6 +303,25 @@ struct pcg_context {
   pcg::StripGroup *d_pgroups = nullptr;
   size_t d_pitems_cap = 0, d_pgroups_cap = 0;
 
+  // pipelined batched step (pcg_pipeline.cu): its work queue and per-patch
+  // counter targets for the current lists and strip items (built when the
+  // form first runs after a change), the counters, the control word, and
+  // the swept step's dt, activity and max speeds (the updated step's are
+  // d_group_dt, d_group_active, d_patch_smax); the form of the captured graph
+  bool pipe_valid = false;
+  bool graph_pipe = false;
+  int n_pipe_queue = 0;
+  int pipe_grid = 0;
+  unsigned *d_pipe_queue = nullptr;
+  size_t d_pipe_queue_cap = 0;
+  int *d_pipe_need = nullptr, *d_pipe_cnt = nullptr;
+  size_t d_pipe_need_cap = 0, d_pipe_cnt_cap = 0;
+  pcg::PipeCtl *d_pipe_ctl = nullptr;
+  unsigned long long *d_pipe_dt = nullptr, *d_pipe_smax = nullptr;
+  int *d_pipe_active = nullptr;
+  size_t d_pipe_dt_cap = 0, d_pipe_smax_cap = 0, d_pipe_active_cap = 0;
+  size_t d_pipe_ctl_cap = 0;
+
   int64_t cell_updates = 0;
   double device_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -476,6 +496,11 @@ int apply_schedule(pcg_context *c) {
   PCG_CUDA(pcg::fused_occupancy(v, &fused_sm));
   if (fused_sm < 1) fused_sm = 1;
   c->fused_grid = (int)std::min<int64_t>((int64_t)c->num_sms * fused_sm, need);
+  int pipe_sm = 0;
+  PCG_CUDA(pcg::pipeline_occupancy(v, &pipe_sm));
+  if (pipe_sm < 1) pipe_sm = 1;
+  c->pipe_grid = c->num_sms * pipe_sm;
+  c->pipe_valid = false;
   c->graph_valid = false;
   return PCG_OK;
 }
@@ -1026,6 +1051,276 @@ bool use_fused(pcg_context *c, int mode) {
          (mode == PCG_MODE_PLAIN || c->sched.kind == PCG_SCHED_STRIPS);
 }
 
+// Whether a batched run takes the pipelined form: the strip schedule asks
+// for it (unfused = 2) and the step is the synchronous one without
+// restriction or flux-correction lists.
+bool use_pipeline(pcg_context *c, int mode) {
+  return mode == PCG_MODE_BATCHED && c->form == PCG_FORM_AUTO && c->sched.kind == PCG_SCHED_STRIPS &&
+         c->sched.unfused == 2 && !c->ts_local && c->h_restr.empty() && c->h_flux.empty() && !c->leaf_ids.empty();
+}
+
+// Work queue and counter targets of the pipelined step (pcg_pipeline.cu) for
+// the current lists and strip items.  The strip updates are ranked in patch
+// order; every item gets a key: the rank of the last strip update among its
+// prerequisites (updates: their own rank); the queue holds, for key u in
+// increasing order, update u, then the ghost chunks, the wall patches and the
+// sweeps with key u.  An item's prerequisites then
+// all come before it (their keys are at most its own, with an earlier kind).
+int build_pipeline(pcg_context *c) {
+  const int np = c->max_patches;
+  const int n_upd = (int)c->h_sitems.size();
+  const int64_t n_ghost = c->n_gcells;
+  const int64_t n_chunks = (n_ghost + pcg::kPipeGhostChunk - 1) / pcg::kPipeGhostChunk;
+  if (n_ghost > INT32_MAX || n_upd > (int)pcg::kPipeIndexMask || n_chunks > (int64_t)pcg::kPipeIndexMask)
+    return fail(PCG_E_INVALID, "pipelined step: the strip or ghost-cell list is too long");
+  std::vector<int> need(4 * (size_t)np, 0);
+  std::vector<int> ukey(np, -1), ginkey(np, -1), goutkey(np, -1);
+  // updates in patch order (the strip list is sorted by strip shape): a
+  // patch's neighbours are then updated shortly before or after it, and its
+  // sweep can follow soon after its own update
+  std::vector<int> uorder(n_upd), urank(n_upd);
+  {
+    std::vector<int> first_pid(n_upd);
+    for (int i = 0; i < n_upd; i++) {
+      const pcg::StripItem &I = c->h_sitems[i];
+      int m = INT32_MAX;
+      for (int g = 0; g < I.ngroups; g++) m = std::min(m, c->h_sgroups[I.g0 + g].pid);
+      first_pid[i] = m;
+      uorder[i] = i;
+    }
+    std::stable_sort(uorder.begin(), uorder.end(), [&](int a, int b) { return first_pid[a] < first_pid[b]; });
+    for (int r = 0; r < n_upd; r++) urank[uorder[r]] = r;
+  }
+  for (int i = 0; i < n_upd; i++) {
+    const pcg::StripItem &I = c->h_sitems[i];
+    for (int g = 0; g < I.ngroups; g++) {
+      const int p = c->h_sgroups[I.g0 + g].pid;
+      need[p]++;
+      ukey[p] = std::max(ukey[p], urank[i]);
+    }
+  }
+  // every level waits `lag` ranks more than its prerequisites need: about
+  // half the resident warps' worth of queue entries, so that what an item
+  // waits for has usually finished when a warp takes it
+  const int lag = std::max(64, c->pipe_grid * pcg::kStripVariants[c->sched.variant].warps / 2);
+  std::vector<int> gkey((size_t)n_chunks, -1);
+  for (size_t r = 0; r + 1 < c->h_gexp.size(); r++) {
+    const int64_t b = c->h_gexp[r].y, e = c->h_gexp[r + 1].y;
+    if (e <= b) continue;
+    const pcg::GhostItemDev &it = c->h_items[c->h_gexp[r].x];
+    need[(size_t)np + it.dst] += (int)(e - b);
+    need[2 * (size_t)np + it.src] += (int)(e - b);
+    const int key = std::max(ukey[it.src], ukey[it.dst]) + lag;
+    for (int64_t ch = b / pcg::kPipeGhostChunk; ch <= (e - 1) / pcg::kPipeGhostChunk; ch++)
+      gkey[ch] = std::max(gkey[ch], key);
+  }
+  for (size_t r = 0; r + 1 < c->h_gexp.size(); r++) {
+    const int64_t b = c->h_gexp[r].y, e = c->h_gexp[r + 1].y;
+    if (e <= b) continue;
+    const pcg::GhostItemDev &it = c->h_items[c->h_gexp[r].x];
+    for (int64_t ch = b / pcg::kPipeGhostChunk; ch <= (e - 1) / pcg::kPipeGhostChunk; ch++) {
+      ginkey[it.dst] = std::max(ginkey[it.dst], gkey[ch]);
+      goutkey[it.src] = std::max(goutkey[it.src], gkey[ch]);
+    }
+  }
+  std::vector<int> wkey(np, -1);
+  for (int p : c->h_wall) {
+    need[3 * (size_t)np + p] = 1;
+    wkey[p] = std::max(ukey[p], ginkey[p]) + lag;
+  }
+  std::vector<int> skey(n_upd, -1);
+  for (int i = 0; i < n_upd; i++) {
+    const pcg::StripItem &I = c->h_sitems[i];
+    int k = -1;
+    for (int g = 0; g < I.ngroups; g++) {
+      const int p = c->h_sgroups[I.g0 + g].pid;
+      k = std::max({k, ukey[p], ginkey[p], goutkey[p], wkey[p]});
+    }
+    skey[i] = k + lag;
+  }
+  // bucket b = key + 1: counts per bucket and kind, then fill
+  int max_key = n_upd - 1;
+  for (int k : gkey) max_key = std::max(max_key, k);
+  for (int p : c->h_wall) max_key = std::max(max_key, wkey[p]);
+  for (int k : skey) max_key = std::max(max_key, k);
+  const size_t nb = (size_t)max_key + 2;
+  std::vector<int64_t> start(4 * nb + 1, 0);  // (bucket, kind) -> first queue position
+  auto slot = [](int key, unsigned kind) { return (size_t)(key + 1) * 4 + kind; };
+  for (int i = 0; i < n_upd; i++) start[slot(urank[i], pcg::kPipeUpdate) + 1]++;
+  for (int64_t ch = 0; ch < n_chunks; ch++) start[slot(gkey[ch], pcg::kPipeGhost) + 1]++;
+  for (int p : c->h_wall) start[slot(wkey[p], pcg::kPipeWall) + 1]++;
+  for (int i = 0; i < n_upd; i++) start[slot(skey[i], pcg::kPipeSweep) + 1]++;
+  for (size_t k = 1; k < start.size(); k++) start[k] += start[k - 1];
+  const int64_t n_queue = start.back();
+  std::vector<unsigned> queue((size_t)n_queue);
+  auto put = [&](int key, unsigned kind, int64_t index) {
+    queue[(size_t)start[slot(key, kind)]++] = (kind << pcg::kPipeKindShift) | (unsigned)index;
+  };
+  for (int i = 0; i < n_upd; i++) put(urank[i], pcg::kPipeUpdate, i);
+  for (int64_t ch = 0; ch < n_chunks; ch++) put(gkey[ch], pcg::kPipeGhost, ch);
+  for (size_t w = 0; w < c->h_wall.size(); w++) put(wkey[c->h_wall[w]], pcg::kPipeWall, (int64_t)w);
+  for (int i = 0; i < n_upd; i++) put(skey[i], pcg::kPipeSweep, i);
+  // the order the kernel relies on (every wait is for an earlier entry):
+  // checked here rather than found out as a wait that runs out
+  {
+    std::vector<int64_t> last_u(np, -1), last_gin(np, -1), last_gout(np, -1), wall_pos(np, -1);
+    std::vector<int64_t> chunk_pos((size_t)n_chunks, -1), sweep_pos(n_upd, -1);
+    for (int64_t q = 0; q < n_queue; q++) {
+      const unsigned kind = queue[(size_t)q] >> pcg::kPipeKindShift;
+      const int64_t i = queue[(size_t)q] & pcg::kPipeIndexMask;
+      if (kind == pcg::kPipeUpdate) {
+        const pcg::StripItem &I = c->h_sitems[(size_t)i];
+        for (int g = 0; g < I.ngroups; g++) last_u[c->h_sgroups[I.g0 + g].pid] = q;
+      } else if (kind == pcg::kPipeGhost) {
+        chunk_pos[(size_t)i] = q;
+      } else if (kind == pcg::kPipeWall) {
+        wall_pos[c->h_wall[(size_t)i]] = q;
+      } else {
+        sweep_pos[(size_t)i] = q;
+      }
+    }
+    bool ok = true;
+    for (size_t r = 0; r + 1 < c->h_gexp.size() && ok; r++) {
+      const int64_t b = c->h_gexp[r].y, e = c->h_gexp[r + 1].y;
+      if (e <= b) continue;
+      const pcg::GhostItemDev &it = c->h_items[c->h_gexp[r].x];
+      for (int64_t ch = b / pcg::kPipeGhostChunk; ch <= (e - 1) / pcg::kPipeGhostChunk; ch++) {
+        const int64_t q = chunk_pos[(size_t)ch];
+        ok = ok && q > last_u[it.src] && q > last_u[it.dst];
+        last_gin[it.dst] = std::max(last_gin[it.dst], q);
+        last_gout[it.src] = std::max(last_gout[it.src], q);
+      }
+    }
+    for (int p : c->h_wall) ok = ok && wall_pos[p] > last_u[p] && wall_pos[p] > last_gin[p];
+    for (int i = 0; i < n_upd && ok; i++) {
+      const pcg::StripItem &I = c->h_sitems[i];
+      for (int g = 0; g < I.ngroups; g++) {
+        const int p = c->h_sgroups[I.g0 + g].pid;
+        const int64_t q = sweep_pos[i];
+        ok = ok && q > last_u[p] && q > last_gin[p] && q > last_gout[p] && q > wall_pos[p];
+      }
+    }
+    if (!ok) return fail(PCG_E_STATE, "pipelined step: work queue out of order");
+  }
+  int rc;
+  if ((rc = ensure_device(c, &c->d_pipe_queue, &c->d_pipe_queue_cap, queue.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_pipe_need, &c->d_pipe_need_cap, need.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_pipe_cnt, &c->d_pipe_cnt_cap, need.size())) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_pipe_ctl, &c->d_pipe_ctl_cap, 1)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_pipe_dt, &c->d_pipe_dt_cap, (size_t)c->max_groups)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_pipe_active, &c->d_pipe_active_cap, (size_t)c->max_groups)) != PCG_OK) return rc;
+  if ((rc = ensure_device(c, &c->d_pipe_smax, &c->d_pipe_smax_cap, (size_t)np)) != PCG_OK) return rc;
+  if (!queue.empty())
+    PCG_CUDA(cudaMemcpyAsync(c->d_pipe_queue, queue.data(), sizeof(unsigned) * queue.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+  PCG_CUDA(cudaMemcpyAsync(c->d_pipe_need, need.data(), sizeof(int) * need.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+  PCG_CUDA(cudaMemsetAsync(c->d_pipe_ctl, 0, sizeof(pcg::PipeCtl), c->stream));
+  PCG_CUDA(cudaStreamSynchronize(c->stream));
+  c->n_pipe_queue = (int)n_queue;
+  c->pipe_valid = true;
+  c->graph_valid = false;
+  return PCG_OK;
+}
+
+pcg::PipeDev pipe_dev(pcg_context *c) {
+  pcg::PipeDev A;
+  A.slab = c->slab;
+  A.patches = c->d_patches;
+  A.times = c->d_times;
+  A.items = c->d_sitems;
+  A.groups = c->d_sgroups;
+  A.gitems = c->d_items;
+  A.cells = c->d_gcells;
+  A.copy_plan = c->d_copy_plan;
+  A.plan = c->d_plan;
+  A.ncopy = c->n_copy_cells;
+  A.n_ghost = (int)c->n_gcells;
+  A.item_step = c->d_item_step;
+  A.wall_patches = c->d_wall;
+  A.queue = c->d_pipe_queue;
+  A.n_queue = c->n_pipe_queue;
+  A.n_patches = c->max_patches;
+  A.cnt = c->d_pipe_cnt;
+  A.need = c->d_pipe_need;
+  A.cur_dt = c->d_group_dt;
+  A.nxt_dt = c->d_pipe_dt;
+  A.cur_smax = c->d_patch_smax;
+  A.nxt_smax = c->d_pipe_smax;
+  A.cur_active = c->d_group_active;
+  A.nxt_active = c->d_pipe_active;
+  A.fin = c->d_fin;
+  A.prm = c->prm;
+  A.ctl = c->d_pipe_ctl;
+  return A;
+}
+
+pcg::PipePreDev pipe_pre_dev(pcg_context *c) {
+  pcg::PipePreDev A;
+  A.n_groups = c->max_groups;
+  A.n_patches = c->max_patches;
+  A.group_max_dt = c->d_group_max_dt;
+  A.group_t_end = c->d_group_t_end;
+  A.group_time = c->d_group_time;
+  A.cur_dt = c->d_group_dt;
+  A.nxt_dt = c->d_pipe_dt;
+  A.cur_smax = c->d_patch_smax;
+  A.nxt_smax = c->d_pipe_smax;
+  A.cur_active = c->d_group_active;
+  A.nxt_active = c->d_pipe_active;
+  A.hist = c->d_hist;
+  A.hist_cap = c->hist_cap;
+  A.cnt = c->d_pipe_cnt;
+  A.ctl = c->d_pipe_ctl;
+  return A;
+}
+
+pcg::PipeItemsDev pipe_items_dev(pcg_context *c) {
+  pcg::PipeItemsDev A;
+  A.patches = c->d_patches;
+  A.times = c->d_times;
+  A.items = c->d_items;
+  A.n_items = (int)c->h_items.size();
+  A.cur_dt = c->d_group_dt;
+  A.cur_active = c->d_group_active;
+  A.item_step = c->d_item_step;
+  A.ctl = c->d_pipe_ctl;
+  return A;
+}
+
+// The bookkeeping and item launches before each pipelined step launch.
+int enqueue_pipeline_prep(pcg_context *c) {
+  PCG_CUDA(pcg::launch_pipeline_pre(c->stream, pipe_pre_dev(c)));
+  PCG_CUDA(pcg::launch_pipeline_items(c->stream, pipe_items_dev(c)));
+  return PCG_OK;
+}
+
+// One launch triple of a pipelined run (capturable).
+int enqueue_pipeline_launch(pcg_context *c) {
+  int rc = enqueue_pipeline_prep(c);
+  if (rc != PCG_OK) return rc;
+  PCG_CUDA(pcg::launch_pipeline_step(c->stream, c->sched.variant, c->pipe_grid, pipe_dev(c)));
+  return PCG_OK;
+}
+
+// Start of a pipelined run of `steps` steps (steps + 1 launch pairs follow).
+int start_pipeline_run(pcg_context *c, int steps) {
+  pcg::PipeCtl h{};
+  h.steps = steps;
+  PCG_CUDA(cudaMemcpyAsync(c->d_pipe_ctl, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  return PCG_OK;
+}
+
+// After the stream has been synchronised: the error word of the last
+// pipelined run (a wait that ran out).
+int check_pipeline(pcg_context *c) {
+  int err = 0;
+  PCG_CUDA(cudaMemcpy(&err, &c->d_pipe_ctl->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!err) return PCG_OK;
+  PCG_CUDA(cudaMemset(c->d_pipe_ctl, 0, sizeof(pcg::PipeCtl)));
+  return fail(PCG_E_CUDA, "pipelined step: a wait for another work item ran out; the run is incomplete");
+}
+
 // Back to the reference layout: every group with a pending update gets it
 // applied (uNew, uOld interior) and its walls filled from the previous state;
 // called by every entry point that reads or changes patch data, lists or
@@ -1329,6 +1624,13 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_finterps);
   cudaFree(c->d_pitems);
   cudaFree(c->d_pgroups);
+  cudaFree(c->d_pipe_queue);
+  cudaFree(c->d_pipe_need);
+  cudaFree(c->d_pipe_cnt);
+  cudaFree(c->d_pipe_ctl);
+  cudaFree(c->d_pipe_dt);
+  cudaFree(c->d_pipe_smax);
+  cudaFree(c->d_pipe_active);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -2144,6 +2446,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   if ((rc = check_mode(c, mode)) != PCG_OK) return rc;
   if ((rc = upload_group_max_dt(c)) != PCG_OK) return rc;
   const bool fused = use_fused(c, mode);
+  const bool pipe = !fused && use_pipeline(c, mode);
   if (!fused) {
     PCG_SETTLE(c);
     if ((rc = refresh_fin(c)) != PCG_OK) return rc;
@@ -2151,6 +2454,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
     // (built outside the graph capture: they allocate)
     if (c->sched.kind == PCG_SCHED_TILES && c->sched.variant == 1 && (rc = ensure_tile_maps(c)) != PCG_OK)
       return rc;
+    if (pipe && !c->pipe_valid && (rc = build_pipeline(c)) != PCG_OK) return rc;
   }
   if ((rc = ensure_hist(c, steps)) != PCG_OK) return rc;
   PCG_CUDA(cudaMemsetAsync(c->d_counter, 0, sizeof(int), c->stream));
@@ -2174,6 +2478,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
         if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
         c->graph_valid = true;
         c->graph_fused = true;
+        c->graph_pipe = false;
       }
       for (int s = 0; s < steps; s++) PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
     } else {
@@ -2185,8 +2490,30 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
     }
     c->fused_pending = true;
     PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+  } else if (pipe) {
+    if (!c->graph_valid || c->graph_fused || !c->graph_pipe) {
+      if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+      c->graph_valid = false;
+      cudaGraph_t g;
+      PCG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      int erc = enqueue_pipeline_launch(c);
+      cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+      if (erc != PCG_OK) return erc;
+      if (ce != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      c->graph_kernels = count_kernel_nodes(g);
+      cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+      c->graph_valid = true;
+      c->graph_fused = false;
+      c->graph_pipe = true;
+    }
+    if ((rc = start_pipeline_run(c, steps)) != PCG_OK) return rc;
+    PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+    for (int s = 0; s <= steps; s++) PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
   } else if (mode == PCG_MODE_BATCHED) {
-    if (!c->graph_valid || c->graph_fused) {
+    if (!c->graph_valid || c->graph_fused || c->graph_pipe) {
       if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
       c->graph_valid = false;
       cudaGraph_t g;
@@ -2208,6 +2535,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
       if (ie != cudaSuccess) return fail(PCG_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
       c->graph_valid = true;
       c->graph_fused = false;
+      c->graph_pipe = false;
     }
     PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < steps; s++) PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
@@ -2230,6 +2558,7 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
     const int xrc = check_level_transfer(c);
     if (xrc != PCG_OK) return xrc;
   }
+  if (pipe && (rc = check_pipeline(c)) != PCG_OK) return rc;
   float ms = 0.f;
   PCG_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->device_ms += ms;
@@ -2279,7 +2608,7 @@ int check_schedule(const pcg_schedule *s) {
   if (s->variant < 0 || s->variant >= pcg::kNumStripVariants)
     return fail(PCG_E_INVALID, "strip variant out of range");
   if (s->chunk < 1 || s->chunk > 32) return fail(PCG_E_INVALID, "strip chunk must be in 1..32");
-  if (s->unfused != 0 && s->unfused != 1) return fail(PCG_E_INVALID, "schedule field unfused must be 0 or 1");
+  if (s->unfused < 0 || s->unfused > 2) return fail(PCG_E_INVALID, "schedule field unfused must be 0, 1 or 2");
   return PCG_OK;
 }
 
@@ -2386,6 +2715,35 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
     t.back() /= reps;
     if (t.back() < t[best]) best = cand.size() - 1;
   }
+  // the fastest strip schedule in the pipelined form, where it applies: a run
+  // of reps steps (reps + 1 launch pairs), timed as a whole
+  if (cand[best].kind == PCG_SCHED_STRIPS) {
+    pcg_schedule u = cand[best];
+    u.unfused = 2;
+    c->sched = u;
+    if ((rc = apply_schedule(c)) != PCG_OK) return rc;
+    if (use_pipeline(c, PCG_MODE_BATCHED)) {
+      cand.push_back(u);
+      t.push_back(0.0);
+      PCG_SETTLE(c);
+      if ((rc = refresh_fin(c)) != PCG_OK) return rc;
+      if ((rc = build_pipeline(c)) != PCG_OK) return rc;
+      if ((rc = ensure_hist(c, reps)) != PCG_OK) return rc;
+      if ((rc = start_pipeline_run(c, reps)) != PCG_OK) return rc;
+      PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
+      for (int r = 0; r <= reps; r++)
+        if ((rc = enqueue_pipeline_launch(c)) != PCG_OK) return rc;
+      PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
+      PCG_CUDA(cudaStreamSynchronize(c->stream));
+      if ((rc = check_pipeline(c)) != PCG_OK) return rc;
+      float e = 0.f;
+      PCG_CUDA(cudaEventElapsedTime(&e, c->ev0, c->ev1));
+      t.back() = e / reps;
+      c->device_ms += e;
+      c->cell_updates += c->cells_per_step * reps;
+      if (t.back() < t[best]) best = cand.size() - 1;
+    }
+  }
   c->sched = cand[best];
   c->sched_fixed = true;
   if ((rc = apply_schedule(c)) != PCG_OK) return rc;
@@ -2453,6 +2811,40 @@ int pcg_profile_step(pcg_context *c, double *ms) {
     ms[4] = t[1];
     for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
     c->cell_updates += c->cells_per_step;
+    return PCG_OK;
+  }
+  if (use_pipeline(c, PCG_MODE_BATCHED)) {
+    // a pipelined run of two steps; its middle launch pair (update of the
+    // first step, fill, walls and sweep of the second) is the steady state
+    PCG_SETTLE(c);
+    if ((rc = refresh_fin(c)) != PCG_OK) return rc;
+    if (!c->pipe_valid && (rc = build_pipeline(c)) != PCG_OK) return rc;
+    if ((rc = ensure_hist(c, 2)) != PCG_OK) return rc;
+    if ((rc = start_pipeline_run(c, 2)) != PCG_OK) return rc;
+    cudaEvent_t ev[7];
+    for (int i = 0; i < 7; i++) PCG_CUDA(cudaEventCreate(&ev[i]));
+    const pcg::PipeDev pd = pipe_dev(c);
+    PCG_CUDA(cudaEventRecord(ev[0], c->stream));
+    for (int l = 0; l < 3; l++) {
+      if ((rc = enqueue_pipeline_prep(c)) != PCG_OK) return rc;
+      PCG_CUDA(cudaEventRecord(ev[2 * l + 1], c->stream));
+      PCG_CUDA(pcg::launch_pipeline_step(c->stream, c->sched.variant, c->pipe_grid, pd));
+      PCG_CUDA(cudaEventRecord(ev[2 * l + 2], c->stream));
+    }
+    PCG_CUDA(cudaStreamSynchronize(c->stream));
+    float t_pre = 0.f, t_first = 0.f, t_step = 0.f, t_last = 0.f;
+    PCG_CUDA(cudaEventElapsedTime(&t_first, ev[1], ev[2]));
+    PCG_CUDA(cudaEventElapsedTime(&t_pre, ev[2], ev[3]));
+    PCG_CUDA(cudaEventElapsedTime(&t_step, ev[3], ev[4]));
+    PCG_CUDA(cudaEventElapsedTime(&t_last, ev[5], ev[6]));
+    for (int i = 0; i < 7; i++) cudaEventDestroy(ev[i]);
+    if ((rc = check_pipeline(c)) != PCG_OK) return rc;
+    ms[0] = t_pre;
+    ms[1] = t_first;
+    ms[2] = t_last;
+    ms[3] = t_step;
+    ms[4] = 0.0;
+    c->cell_updates += 2 * c->cells_per_step;
     return PCG_OK;
   }
   PCG_SETTLE(c);

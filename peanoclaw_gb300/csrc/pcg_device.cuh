@@ -134,6 +134,20 @@ __device__ __forceinline__ bool small_mag(double x) {
 constexpr int kFinUOld = 1;  // patch finiteness flags (see k_scan_fin)
 constexpr int kFinB = 2;
 
+// Loads of patch data; kL2: through L2 only (ld.global.cg), for kernels in
+// which other SMs write the data while the kernel runs (an SM's L1 is not
+// coherent with those writes).
+template <bool kL2>
+__device__ __forceinline__ double ldd(const double *p) {
+  if constexpr (kL2) return __ldcg(p);
+  else return *p;
+}
+template <bool kL2>
+__device__ __forceinline__ int ldi(const int *p) {
+  if constexpr (kL2) return __ldcg(p);
+  else return *p;
+}
+
 constexpr int kTile = 16;           // tile edge of the sweep
 constexpr int kSweepThreads = 256;  // kTile * kTile
 constexpr int kFlagLeaf = 1;

@@ -11,6 +11,7 @@
 //   k_restrict                       DefaultRestriction (+ SWE h+b wrapping)
 //   k_compute_fluxes / k_flux_corr   DefaultFluxCorrection
 #include "pcg_device.cuh"
+#include "pcg_ghost_ops.cuh"
 #include "pcg_kernels.h"
 
 #include <cuda.h>
@@ -635,14 +636,6 @@ __global__ void __launch_bounds__(kSweepThreads)
 // ===========================================================================
 // Ghost layers
 // ===========================================================================
-__device__ __forceinline__ double transfer_tf(const PatchDev &S, const PatchTimeDev &ST,
-                                              const PatchDev &D, const PatchTimeDev &DT) {
-  double dtu = time_unew(D, DT);
-  if (is_virtual(S)) return ieee::div_rn(__dsub_rn(dtu, 0.0), 1.0);
-  double su = time_unew(S, ST), so = time_uold(S, ST);
-  if (tl_greater(__dsub_rn(su, so), 0.0)) return ieee::div_rn(__dsub_rn(dtu, so), __dsub_rn(su, so));
-  return 1.0;
-}
 
 // DefaultTransferTemplate::transferGhostlayer body for cell k of the region.
 __device__ __forceinline__ void transfer_cell(double *slab, const PatchDev &S, const PatchDev &D,
@@ -654,25 +647,6 @@ __device__ __forceinline__ void transfer_cell(double *slab, const PatchDev &S, c
     double vo = slab[idx_uold(S, q, so[0] + x, so[1] + y)];
     slab[idx_uold(D, q, dof[0] + x, dof[1] + y)] = __dadd_rn(__dmul_rn(vn, tf), __dmul_rn(vo, itf));
   }
-}
-
-__device__ __forceinline__ double interp_tf(const PatchDev &S, const PatchTimeDev &ST,
-                                            const PatchDev &D, const PatchTimeDev &DT,
-                                            bool to_current, bool use_unew_uold) {
-  double tf;
-  if (tl_equals(ST.dt, 0.0)) {
-    tf = 1.0;
-  } else if (use_unew_uold) {
-    double so = time_uold(S, ST), su = time_unew(S, ST);
-    double num = to_current ? __dsub_rn(time_uold(D, DT), so) : __dsub_rn(time_unew(D, DT), so);
-    tf = ieee::div_rn(num, __dsub_rn(su, so));
-  } else {
-    double den = __dsub_rn(__dadd_rn(ST.time, ST.dt), ST.time);
-    double num = to_current ? __dsub_rn(DT.time, ST.time)
-                            : __dsub_rn(__dadd_rn(DT.time, DT.dt), ST.time);
-    tf = ieee::div_rn(num, den);
-  }
-  return fmax(0.0, fmin(1.0, tf));
 }
 
 // DefaultInterpolationTemplate::interpolateSolution body for destination cell
@@ -796,7 +770,9 @@ __global__ void k_build_copy_plan(const PatchDev *__restrict__ patches,
 __device__ __forceinline__ void item_step_one(const PatchDev *__restrict__ patches,
                                               const PatchTimeDev *__restrict__ times,
                                               const GhostItemDev *__restrict__ items, int i,
-                                              GhostItemStepDev *__restrict__ out);
+                                              GhostItemStepDev *__restrict__ out) {
+  out[i] = item_step_value<false>(patches, times, items, i);
+}
 
 __global__ void k_item_step(const PatchDev *__restrict__ patches,
                             const PatchTimeDev *__restrict__ times,
@@ -830,24 +806,6 @@ __global__ void k_reset_items(int n_groups, const double *__restrict__ group_max
   for (int k = i; k < count; k += stride) item_step_one(patches, times, items, k, out);
 }
 
-__device__ __forceinline__ void item_step_one(const PatchDev *__restrict__ patches,
-                                              const PatchTimeDev *__restrict__ times,
-                                              const GhostItemDev *__restrict__ items, int i,
-                                              GhostItemStepDev *__restrict__ out) {
-  {
-    const GhostItemDev it = items[i];
-    const PatchDev &S = patches[it.src], &D = patches[it.dst];
-    const PatchTimeDev &ST = times[it.src], &DT = times[it.dst];
-    GhostItemStepDev r;
-    r.tf = it.kind == 0 ? transfer_tf(S, ST, D, DT) : interp_tf(S, ST, D, DT, false, true);
-    r.itf = __dsub_rn(1.0, r.tf);
-    r.vn_src = (int)vol_new(S);
-    r.vo_src = (int)vol_old(S);
-    r.vo_dst = (int)vol_old(D);
-    r.nq = it.kind == 0 ? S.nq : (D.nq < 3 ? D.nq : 3);
-    out[i] = r;
-  }
-}
 
 // Batched ghost fill over the flat ghost-cell list: entries [0, ncopy) copy
 // (DefaultTransfer's time-interpolated copy, offsets from the copy plan),
@@ -863,77 +821,9 @@ __global__ void __launch_bounds__(256)
                   const int *__restrict__ group_active, const int *__restrict__ fin,
                   const int *__restrict__ pact) {
   const int total = ncopy + ninterp;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    if (e < ncopy) {
-      const CopyPlanDev pl = copy_plan[e];
-      if (group_active && !group_active[patches[pl.dst_pid].group]) continue;
-      if (pact && !pact[pl.dst_pid]) continue;
-      const GhostItemStepDev I = item_step[pl.item];
-      double vn[3], vo[3];
-      const int nq = I.nq < 3 ? I.nq : 3;
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        if (q < nq) {
-          vn[q] = slab[pl.src_new + (long long)q * I.vn_src];
-          vo[q] = slab[pl.src_old + (long long)q * I.vo_src];
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-        if (q < nq)
-          slab[pl.dst + (long long)q * I.vo_dst] = __dadd_rn(__dmul_rn(vn[q], I.tf), __dmul_rn(vo[q], I.itf));
-      for (int q = 3; q < I.nq; q++)  // more than three unknowns (not the SWE case)
-        slab[pl.dst + (long long)q * I.vo_dst] =
-            __dadd_rn(__dmul_rn(slab[pl.src_new + (long long)q * I.vn_src], I.tf),
-                      __dmul_rn(slab[pl.src_old + (long long)q * I.vo_src], I.itf));
-      continue;
-    }
-    const GhostCellDev gc = cells[e];
-    const GhostItemDev it = items[gc.item];
-    const PatchDev S = patches[it.src], D = patches[it.dst];
-    if (group_active && !group_active[D.group]) continue;
-    if (pact && !pact[it.dst]) continue;
-    const InterpPlanDev pl = plan[e - ncopy];
-    const GhostItemStepDev I = item_step[gc.item];
-    const double tf = I.tf, one_m_tf = I.itf;
-    int cx = it.dst_off[0] + gc.k / it.size[1], cy = it.dst_off[1] + gc.k % it.size[1];
-    double acc[3];
-    const int nq = I.nq;
-    for (int q = 0; q < nq; q++) acc[q] = 0.0;
-    // time factor 1 with a leaf source whose uOld and b interior are below
-    // 2^1022: (uOld [+ b]) * 0 + (uNew [+ b]) * 1 is exactly uNew [+ b] up to
-    // the sign of a zero, which the accumulator (started at +0, never -0)
-    // absorbs, so uOld is not needed
-    if (fin && dbits(tf) == 0x3FF0000000000000ull && is_leaf(S) &&
-        (fin[it.src] & (kFinUOld | kFinB)) == (kFinUOld | kFinB)) {
-      for (int kk = 0; kk < 4; kk++) {
-        const int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
-        const double sf = pl.sf[kk];
-        const double bb = slab[idx_pw(S, 0, nxi, nyi)];
-        acc[0] = __dadd_rn(acc[0], __dmul_rn(sf, __dadd_rn(slab[idx_unew(S, 0, nxi, nyi)], bb)));
-        for (int q = 1; q < nq; q++) acc[q] = __dadd_rn(acc[q], __dmul_rn(sf, slab[idx_unew(S, q, nxi, nyi)]));
-      }
-      acc[0] = __dadd_rn(acc[0], __dmul_rn(-1.0, slab[idx_pw(D, 0, cx, cy)]));
-      for (int q = 0; q < nq; q++) slab[idx_uold(D, q, cx, cy)] = acc[q];
-      continue;
-    }
-    for (int kk = 0; kk < 4; kk++) {
-      int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
-      double sf = pl.sf[kk];
-      for (int q = 0; q < nq; q++) {
-        double so = slab[idx_uold(S, q, nxi, nyi)];
-        double sn = slab[idx_unew(S, q, nxi, nyi)];
-        if (q == 0) {
-          double bb = slab[idx_pw(S, 0, nxi, nyi)];
-          so = __dadd_rn(so, bb);
-          sn = __dadd_rn(sn, bb);
-        }
-        acc[q] = __dadd_rn(acc[q], __dmul_rn(sf, __dadd_rn(__dmul_rn(so, one_m_tf), __dmul_rn(sn, tf))));
-      }
-    }
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(-1.0, slab[idx_pw(D, 0, cx, cy)]));
-    for (int q = 0; q < nq; q++) slab[idx_uold(D, q, cx, cy)] = acc[q];
-  }
+  const auto step = [item_step](int item) { return item_step[item]; };
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x)
+    ghost_entry<false>(slab, patches, items, cells, ncopy, copy_plan, plan, step, e, group_active, fin, pact);
 }
 
 // Batched ghost fill: one warp per item.  Items write disjoint ghost cells.
@@ -961,32 +851,6 @@ __global__ void k_ghost_items(double *__restrict__ slab, const PatchDev *__restr
   }
 }
 
-// SWEKernel::fillBoundaryLayer for one face; reads interior cells from uNew
-// when `interior_from_unew` (the copy uNew -> uOld of SolveTimestep is implicit
-// in the batched form), ghost cells from uOld.
-__device__ __forceinline__ void wall_face(double *slab, const PatchDev &P, int dim, int up,
-                                          bool interior_from_unew, int lane, int nl) {
-  if (dim == 0) {
-    int xi = up ? P.nx : -1;
-    int sx = xi + (up ? -1 : 1);
-    for (int k = lane; k < (P.ny + 2) * P.nq; k += nl) {
-      int yi = k / P.nq - 1, q = k % P.nq;
-      bool inside = yi >= 0 && yi < P.ny;
-      double v = (interior_from_unew && inside) ? slab[idx_unew(P, q, sx, yi)] : slab[idx_uold(P, q, sx, yi)];
-      slab[idx_uold(P, q, xi, yi)] = (q == dim + 1) ? -v : v;
-    }
-  } else {
-    int yi = up ? P.ny : -1;
-    int sy = yi + (up ? -1 : 1);
-    for (int k = lane; k < (P.nx + 2) * P.nq; k += nl) {
-      int xi = k / P.nq - 1, q = k % P.nq;
-      bool inside = xi >= 0 && xi < P.nx;
-      double v = (interior_from_unew && inside) ? slab[idx_unew(P, q, xi, sy)] : slab[idx_uold(P, q, xi, sy)];
-      slab[idx_uold(P, q, xi, yi)] = (q == dim + 1) ? -v : v;
-    }
-  }
-}
-
 // Walls of the listed patches in the order of SolveTimestep::fillBoundaryLayers:
 // (0,lower), (1,upper), (0,upper), (1,lower).  One warp per patch.
 __global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ patches,
@@ -1002,7 +866,7 @@ __global__ void k_walls(double *__restrict__ slab, const PatchDev *__restrict__ 
     if (pact && !pact[wall_patches[w]]) continue;
     for (int f = 0; f < 4; f++) {
       int d = order[f][0], up = order[f][1];
-      if (P.wall & (1 << (2 * d + up))) wall_face(slab, P, d, up, from_unew != 0, lane, 32);
+      if (P.wall & (1 << (2 * d + up))) wall_face<false>(slab, P, d, up, from_unew != 0, lane, 32);
       __syncwarp();
     }
   }
@@ -1034,7 +898,7 @@ __global__ void k_fill_patch(double *__restrict__ slab, const PatchDev *__restri
   const int order[4][2] = {{0, 0}, {1, 1}, {0, 1}, {1, 0}};
   for (int f = 0; f < 4; f++) {
     int d = order[f][0], up = order[f][1];
-    if (P.wall & (1 << (2 * d + up))) wall_face(slab, P, d, up, true, lane, blockDim.x);
+    if (P.wall & (1 << (2 * d + up))) wall_face<false>(slab, P, d, up, true, lane, blockDim.x);
     __syncthreads();
   }
 }
@@ -1067,7 +931,7 @@ __global__ void k_swap_unew_uold(double *slab, const PatchDev *patches, int pid)
 
 __global__ void k_fill_boundary_layer(double *slab, const PatchDev *patches, int pid, int dim, int up) {
   PatchDev P = patches[pid];
-  wall_face(slab, P, dim, up, false, threadIdx.x, blockDim.x);
+  wall_face<false>(slab, P, dim, up, false, threadIdx.x, blockDim.x);
 }
 
 __global__ void k_transfer(double *slab, const PatchDev *patches, const PatchTimeDev *times,

@@ -236,4 +236,89 @@ cudaError_t launch_build_fused_ghosts(cudaStream_t st, const PatchDev *patches, 
                                       const int *face_begin, int *face, int *corner, FusedCopyDev *copies,
                                       FusedInterpDev *interps);
 
+// ---- pipelined batched step (pcg_pipeline.cu)
+// A run of `steps` steps is steps + 1 launches of [k_pipeline_pre,
+// k_pipeline_step]: launch k updates with the dt of step k - 1 (k > 0) and
+// fills, walls and sweeps step k (k < steps), its work items taken in queue
+// order by every warp and held back by per-patch counters until what they
+// read is written.  The step index k lives in PipeCtl (set to 0 with `steps`
+// by the host before the first launch; the kernel's last CTA advances it).
+struct PipeCtl {
+  int head;    // next queue entry
+  int err;     // 1: a wait for a counter ran out
+  int k;       // launch index within the run
+  int steps;   // steps of the run
+  int exited;  // CTAs that left the kernel (reset by the last one)
+  int pad_[3];
+};
+// Queue entries: item kind in the top two bits, index below.
+constexpr unsigned kPipeUpdate = 0, kPipeGhost = 1, kPipeWall = 2, kPipeSweep = 3;
+constexpr int kPipeKindShift = 30;
+constexpr unsigned kPipeIndexMask = (1u << kPipeKindShift) - 1;
+// Ghost-cell entries per ghost work item (four per lane).
+constexpr int kPipeGhostChunk = 128;
+// Per-patch counters and their targets, four arrays of n_patches each:
+// strip groups updated (target: the patch's strip groups), ghost cells written
+// into the patch, ghost cells read from the patch (targets: the list's
+// counts), walls filled (target 1 for a patch on the wall list, else 0).
+struct PipeDev {
+  double *slab;
+  const PatchDev *patches;
+  PatchTimeDev *times;
+  const StripItem *items;
+  const StripGroup *groups;
+  const GhostItemDev *gitems;
+  const GhostCellDev *cells;
+  const CopyPlanDev *copy_plan;
+  const InterpPlanDev *plan;
+  int ncopy, n_ghost;
+  const GhostItemStepDev *item_step;  // per ghost item, from k_pipeline_items
+  const int *wall_patches;
+  const unsigned *queue;
+  int n_queue, n_patches;
+  int *cnt;
+  const int *need;
+  // dt, activity and max speed of the step being updated (cur) and of the
+  // step being swept (nxt)
+  unsigned long long *cur_dt, *nxt_dt, *cur_smax, *nxt_smax;
+  int *cur_active, *nxt_active;
+  int *fin;
+  SweParamsDev prm;
+  PipeCtl *ctl;
+};
+// Group and patch bookkeeping between two pipelined launches: the swept
+// step's dt, activity and max speeds become the updated step's, its dt is
+// recorded (hist[(k - 1) * n_groups + g] while k - 1 < hist_cap) and the
+// group times advance; the next step's dt caps, activity and max speeds are
+// reset; counters and the queue head are zeroed.
+struct PipePreDev {
+  int n_groups, n_patches;
+  const double *group_max_dt, *group_t_end;
+  double *group_time;
+  unsigned long long *cur_dt, *nxt_dt, *cur_smax, *nxt_smax;
+  int *cur_active, *nxt_active;
+  double *hist;
+  int hist_cap;
+  int *cnt;
+  PipeCtl *ctl;
+};
+cudaError_t launch_pipeline_pre(cudaStream_t st, const PipePreDev &A);
+// Per-item time factors and strides of the ghost fill of step k (k <
+// steps), from the time intervals the update of step k - 1 will leave (a
+// leaf of a group that advanced by dt > 0: time + previous dt, dt), the same
+// arithmetic as the update's; launched after k_pipeline_pre.
+struct PipeItemsDev {
+  const PatchDev *patches;
+  const PatchTimeDev *times;
+  const GhostItemDev *items;
+  int n_items;
+  const unsigned long long *cur_dt;
+  const int *cur_active;
+  GhostItemStepDev *item_step;
+  const PipeCtl *ctl;
+};
+cudaError_t launch_pipeline_items(cudaStream_t st, const PipeItemsDev &A);
+cudaError_t launch_pipeline_step(cudaStream_t st, int variant, int grid, const PipeDev &A);
+cudaError_t pipeline_occupancy(int variant, int *blocks_per_sm);
+
 }  // namespace pcg

@@ -73,6 +73,10 @@ class Schedule(C.Structure):
 
 SCHED_TILES = 0
 SCHED_STRIPS = 1
+# values of the schedule's `unfused` field for strips
+STRIPS_FUSED = 0       # the fused step where it applies
+STRIPS_UNFUSED = 1     # separate launches
+STRIPS_PIPELINED = 2   # one persistent kernel per step (pcg_pipeline.cu)
 TS_GLOBAL = 0
 TS_LOCAL = 1
 
@@ -452,7 +456,8 @@ class Context:
 
     def set_schedule(self, kind, variant=0, chunk=32, unfused=0):
         """Fix the batched sweep/update schedule (SCHED_TILES or SCHED_STRIPS;
-        unfused = 1 keeps strips in the unfused step form)."""
+        for strips, unfused = STRIPS_UNFUSED keeps the unfused step form and
+        STRIPS_PIPELINED runs pcg_run in the pipelined form)."""
         s = Schedule(kind, variant, chunk, unfused)
         check(lib().pcg_set_schedule(self.h, C.byref(s)))
 
@@ -473,7 +478,8 @@ class Context:
         return [(tried[k].as_tuple(), float(ms[k])) for k in range(min(n.value, cap))]
 
     def profile_step(self):
-        """Device ms of (reset, ghost items, walls, sweep, update) of one batched step."""
+        """Device ms of (reset, ghost items, walls, sweep, update) of one batched
+        step (fused and pipelined forms: see pcg_profile_step)."""
         ms = np.zeros(5)
         check(lib().pcg_profile_step(self.h, dptr(ms)))
         return ms

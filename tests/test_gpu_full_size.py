@@ -1,7 +1,8 @@
 """Full-size checks on the 50k-patch uneven mosaic (224 x 224 slots, 67.8 M
-cells): three batched steps bit for bit against the oracle on the whole
-mosaic, the warp-strip and the tile schedules (two independent work
-decompositions) give bit-identical states and dts over six steps, every value
+cells): three batched steps of the fused and of the pipelined form bit for
+bit against the oracle on the whole mosaic, the warp-strip, the tile and the
+pipelined schedules (independent work decompositions) give bit-identical
+states and dts over six steps, every value
 stays finite and the depth non-negative, and a device-side end time stops the
 run exactly."""
 import numpy as np
@@ -44,20 +45,27 @@ def _run(ps, sched, steps, t_end=1e-3):
         c.close()
 
 
-def test_full_mosaic_matches_the_oracle(mosaic):
-    """The headline workload itself, three steps, every patch vector (ghost
-    layers and signed zeros included) and every dt bit for bit."""
+@pytest.fixture(scope="module")
+def oracle_3_steps(mosaic):
     ps = mosaic
-    steps = 3
-    got, dts, _ = _run(ps, (P.SCHED_STRIPS, 2, 32), steps, t_end=np.inf)
     pats = oracle_patchset(ps)
     from oracle import oracle as O
-    odts = [O.grid_step(pats, ps.items, ps.wall, oracle_params(PRM), np.inf)[0] for _ in range(steps)]
+    odts = [O.grid_step(pats, ps.items, ps.wall, oracle_params(PRM), np.inf)[0] for _ in range(3)]
+    return np.concatenate([p.u for p in pats]), odts
+
+
+@pytest.mark.parametrize("form", [P.STRIPS_FUSED, P.STRIPS_PIPELINED])
+def test_full_mosaic_matches_the_oracle(mosaic, oracle_3_steps, form):
+    """The headline workload itself, three steps of the fused and of the
+    pipelined form, every patch vector (ghost layers and signed zeros
+    included) and every dt bit for bit."""
+    ps = mosaic
+    got, dts, _ = _run(ps, (P.SCHED_STRIPS, 2, 32, form), 3, t_end=np.inf)
+    ref, odts = oracle_3_steps
     assert list(dts) == odts
     for p in range(0, len(ps), 4096):
-        assert np.array_equal(got[ps.offsets[p]:ps.offsets[p] + ps.vec_len(p)].view(np.int64),
-                              pats[p].u.view(np.int64)), p
-    ref = np.concatenate([p.u for p in pats])
+        a, b = ps.offsets[p], ps.offsets[p] + ps.vec_len(p)
+        assert np.array_equal(got[a:b].view(np.int64), ref[a:b].view(np.int64)), p
     assert np.array_equal(got.view(np.int64), ref.view(np.int64))
 
 
@@ -65,8 +73,11 @@ def test_schedules_agree_at_full_size(mosaic):
     ps = mosaic
     a, da, ta = _run(ps, (P.SCHED_STRIPS, 2, 32), 6)
     b, db, tb = _run(ps, (P.SCHED_TILES, 0, 32), 6)
+    c, dc, tc = _run(ps, (P.SCHED_STRIPS, 2, 32, P.STRIPS_PIPELINED), 6)
     assert np.array_equal(da, db) and ta == tb
     assert np.array_equal(a.view(np.int64), b.view(np.int64))
+    assert np.array_equal(da, dc) and ta == tc
+    assert np.array_equal(a.view(np.int64), c.view(np.int64))
     assert np.all(np.isfinite(a))
     n_h = [ps.offsets[p] + np.arange(ps.n[p] ** 2) for p in range(0, len(ps), 97)]
     assert np.all(a[np.concatenate(n_h)] >= 0.0)

@@ -67,8 +67,9 @@ def test_autotuner_picks_a_candidate_and_keeps_results_exact():
     ps = S.uneven_patches(grid=4, sizes=(8, 16, 32, 64))
     out, dts, tuned, got = _gpu_run(ps, 3, autotune_reps=1)
     # 12 candidates (the sizes are even: tiles with TMA staging too), and the
-    # best strip schedule in the unfused form when a strip schedule won
-    assert len(tuned) in (12, 13)
+    # best strip schedule in the unfused form (where the fused one applied)
+    # and in the pipelined form when a strip schedule won
+    assert len(tuned) in (12, 13, 14)
     assert any(k[:2] == (P.SCHED_TILES, 1) for k, _ in tuned)
     assert all(ms > 0.0 for _, ms in tuned)
     best = min(tuned, key=lambda t: t[1])[0]
