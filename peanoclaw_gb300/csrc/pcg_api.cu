@@ -206,6 +206,11 @@ struct pcg_context {
   size_t d_copy_plan_cap = 0;
   pcg::GhostItemStepDev *d_item_step = nullptr;
   size_t d_item_step_cap = 0;
+  // per patch the uOld interior bands the ghost fill reads (int4: x lower,
+  // x upper, y lower, y upper) and the strip update's full-write flag: 0
+  // inside a batched run but for its last step, else nonzero
+  int4 *d_band = nullptr;
+  int *d_upd_full = nullptr;
 
   std::vector<pcg::TileItem> h_tiles;
   pcg::TileItem *d_tiles = nullptr;
@@ -801,6 +806,9 @@ int rebuild_topology(pcg_context *c) {
                                          c->n_interp_cells, c->d_plan));
   PCG_CUDA(pcg::launch_build_copy_plan(c->stream, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
                                        c->d_copy_plan));
+  PCG_CUDA(cudaMemsetAsync(c->d_band, 0, sizeof(int4) * c->max_patches, c->stream));
+  PCG_CUDA(pcg::launch_build_bands(c->stream, c->d_patches, c->d_items, c->d_gcells, c->n_copy_cells,
+                                   c->n_interp_cells, c->d_plan, (int *)c->d_band));
   if ((rc = build_fused_tables(c)) != PCG_OK) return rc;
   int per_sm = 0;
   PCG_CUDA(pcg::sweep_occupancy(&per_sm));
@@ -938,16 +946,22 @@ int enqueue_sweep(pcg_context *c) {
 
 int enqueue_update(pcg_context *c) {
   using namespace pcg;
-  if (c->sched.kind == PCG_SCHED_TILES)
+  if (c->sched.kind == PCG_SCHED_TILES) {
     PCG_CUDA(launch_update(c->stream, c->sweep_grid, c->slab, c->d_patches, c->d_times, c->d_tiles, 0,
                            (int)c->h_tiles.size(), c->prm, c->d_patch_smax, c->d_group_dt,
                            c->d_group_active, c->d_fin, c->ts_local ? c->d_pact : nullptr,
                            c->ts_local ? c->d_pdt : nullptr));
-  else
+  } else {
+    pcg::UpdateBands ub;
+    ub.band = c->d_band;
+    ub.full = c->d_upd_full;
+    ub.group_time = c->d_group_time;
+    ub.group_t_end = c->d_group_t_end;
     PCG_CUDA(launch_update_strips(c->stream, c->update_grid, c->slab, c->d_patches, c->d_times,
                                   c->d_sitems, c->d_sgroups, (int)c->h_sitems.size(), c->prm,
                                   c->d_patch_smax, c->d_group_dt, c->d_group_active, c->d_fin,
-                                  c->ts_local ? c->d_pact : nullptr, c->ts_local ? c->d_pdt : nullptr));
+                                  c->ts_local ? c->d_pact : nullptr, c->ts_local ? c->d_pdt : nullptr, ub));
+  }
   return PCG_OK;
 }
 
@@ -1552,6 +1566,10 @@ int pcg_create(const pcg_config *cfg, pcg_context **out) {
   CREATE_CK(cudaMalloc(&c->d_dt_out, sizeof(double) * c->max_groups));
   CREATE_CK(cudaMalloc(&c->d_solve_out, sizeof(double) * 2));
   CREATE_CK(cudaMalloc(&c->d_counter, sizeof(int)));
+  CREATE_CK(cudaMalloc(&c->d_band, sizeof(int4) * c->max_patches));
+  CREATE_CK(cudaMemset(c->d_band, 0, sizeof(int4) * c->max_patches));
+  CREATE_CK(cudaMalloc(&c->d_upd_full, sizeof(int)));
+  CREATE_CK(cudaMemset(c->d_upd_full, 1, sizeof(int)));
   CREATE_CK(cudaMalloc(&c->d_xfer, sizeof(pcg::TransferCtl)));
   CREATE_CK(cudaMemset(c->d_xfer, 0, sizeof(pcg::TransferCtl)));
   CREATE_CK(cudaMallocHost(&c->h_pinned, sizeof(double) * std::max(64, c->max_groups)));
@@ -1624,6 +1642,8 @@ int pcg_destroy(pcg_context *c) {
   cudaFree(c->d_finterps);
   cudaFree(c->d_pitems);
   cudaFree(c->d_pgroups);
+  cudaFree(c->d_band);
+  cudaFree(c->d_upd_full);
   cudaFree(c->d_pipe_queue);
   cudaFree(c->d_pipe_need);
   cudaFree(c->d_pipe_cnt);
@@ -2537,8 +2557,18 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
       c->graph_fused = false;
       c->graph_pipe = false;
     }
+    // strip updates write the old state only where the next ghost fill reads
+    // it, except in the run's last step (only ghost fills and sweeps read
+    // the uOld interior in between: no level transfers, no local time
+    // stepping); after the run the flag is back to full writes
+    const bool bands = c->sched.kind == PCG_SCHED_STRIPS && !c->ts_local && c->h_restr.empty() &&
+                       c->h_flux.empty() && steps > 1;
     PCG_CUDA(cudaEventRecord(c->ev0, c->stream));
-    for (int s = 0; s < steps; s++) PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    if (bands) PCG_CUDA(cudaMemsetAsync(c->d_upd_full, 0, sizeof(int), c->stream));
+    for (int s = 0; s < steps; s++) {
+      if (bands && s == steps - 1) PCG_CUDA(cudaMemsetAsync(c->d_upd_full, 1, sizeof(int), c->stream));
+      PCG_CUDA(cudaGraphLaunch(c->graph, c->stream));
+    }
     PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
   } else {
     PCG_CUDA(cudaEventRecord(c->ev0, c->stream));

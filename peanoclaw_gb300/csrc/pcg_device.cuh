@@ -148,6 +148,18 @@ __device__ __forceinline__ int ldi(const int *p) {
   else return *p;
 }
 
+// Old-state writes of the strip update.  band: per patch the depths of the
+// uOld interior bands the batched ghost fill reads (x lower, x upper, y
+// lower, y upper); null: the whole interior.  A step writes only the bands
+// unless *full is nonzero or the group reaches its end time with this step
+// (t_end - (time + dt) not > 0), so that the reference layout holds after
+// the last step of a run and of a group.
+struct UpdateBands {
+  const int4 *band = nullptr;
+  const int *full = nullptr;
+  const double *group_time = nullptr, *group_t_end = nullptr;
+};
+
 constexpr int kTile = 16;           // tile edge of the sweep
 constexpr int kSweepThreads = 256;  // kTile * kTile
 constexpr int kFlagLeaf = 1;

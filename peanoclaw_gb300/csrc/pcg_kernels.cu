@@ -744,6 +744,37 @@ __global__ void k_build_interp_plan(const PatchDev *__restrict__ patches,
   }
 }
 
+// uOld interior bands the batched ghost fill reads, per patch and face
+// (x lower, x upper, y lower, y upper): every source cell of a copy or an
+// interpolation entry is assigned to its nearest face, whose depth becomes
+// at least one more than the cell's distance from it.  Cells outside every
+// band are read by nothing but the next sweep, which overwrites them.
+__device__ __forceinline__ void band_mark(const PatchDev &S, int pid, int sx, int sy, int *band) {
+  if (sx < 0 || sx >= S.nx || sy < 0 || sy >= S.ny) return;
+  const int d[4] = {sx, S.nx - 1 - sx, sy, S.ny - 1 - sy};
+  int f = 0;
+  for (int k = 1; k < 4; k++)
+    if (d[k] < d[f]) f = k;
+  atomicMax(&band[4 * pid + f], d[f] + 1);
+}
+
+__global__ void k_build_bands(const PatchDev *__restrict__ patches, const GhostItemDev *__restrict__ items,
+                              const GhostCellDev *__restrict__ cells, int ncopy, int ninterp,
+                              const InterpPlanDev *__restrict__ plan, int *__restrict__ band) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ncopy + ninterp; e += gridDim.x * blockDim.x) {
+    const GhostCellDev gc = cells[e];
+    const GhostItemDev it = items[gc.item];
+    const PatchDev &S = patches[it.src];
+    if (e < ncopy) {
+      const int x = gc.k / it.size[1], y = gc.k - x * it.size[1];
+      band_mark(S, it.src, it.src_off[0] + x, it.src_off[1] + y, band);
+    } else {
+      const InterpPlanDev pl = plan[e - ncopy];
+      for (int kk = 0; kk < 4; kk++) band_mark(S, it.src, pl.bx + (kk & 1), pl.by + ((kk >> 1) & 1), band);
+    }
+  }
+}
+
 // Copy plan of the batched ghost fill: offsets of every COPY ghost cell,
 // computed once per grid change.
 __global__ void k_build_copy_plan(const PatchDev *__restrict__ patches,
@@ -2375,6 +2406,17 @@ cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, con
   int grid = (count + 255) / 256;
   if (grid > 152 * 32) grid = 152 * 32;
   k_build_copy_plan<<<grid, 256, 0, st>>>(patches, items, cells, count, plan);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_bands(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
+                               const GhostCellDev *cells, int ncopy, int ninterp, const InterpPlanDev *plan,
+                               int *band) {
+  const int total = ncopy + ninterp;
+  if (total <= 0) return cudaSuccess;
+  int grid = (total + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  k_build_bands<<<grid, 256, 0, st>>>(patches, items, cells, ncopy, ninterp, plan, band);
   return cudaGetLastError();
 }
 

@@ -78,6 +78,11 @@ cudaError_t launch_scan_fin(cudaStream_t st, const double *slab, const PatchDev 
                             int *fin);
 cudaError_t launch_build_copy_plan(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
                                    const GhostCellDev *cells, int count, CopyPlanDev *plan);
+// Per patch the depths (x lower, x upper, y lower, y upper; band[4 * pid ..],
+// zeroed before) of the uOld interior bands the batched ghost fill reads.
+cudaError_t launch_build_bands(cudaStream_t st, const PatchDev *patches, const GhostItemDev *items,
+                               const GhostCellDev *cells, int ncopy, int ninterp, const InterpPlanDev *plan,
+                               int *band);
 cudaError_t launch_reset_items(cudaStream_t st, int n_groups, const double *group_max_dt, const double *group_t_end,
                                const double *group_time, unsigned long long *group_dt, int *group_active,
                                int n_patches, unsigned long long *patch_smax, const PatchDev *patches,
@@ -201,7 +206,7 @@ cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const 
                                  const unsigned long long *patch_smax,
                                  const unsigned long long *group_dt, const int *group_active,
                                  int *fin, const int *pact = nullptr,
-                                 const unsigned long long *pdt = nullptr);
+                                 const unsigned long long *pdt = nullptr, const UpdateBands &ub = UpdateBands());
 
 // ---- fused batched step (pcg_fused.cu)
 // Everything the fused kernels read besides the work list: the slab and the

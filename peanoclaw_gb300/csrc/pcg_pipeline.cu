@@ -115,8 +115,9 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_pipeline_step(const
     if (kind == kPipeUpdate) {
       if (first) continue;
       const StripItem I = A.items[i];
-      strip::update_item<true, kPipeUpdateBatch>(A.slab, A.patches, A.times, I, A.groups, A.prm, A.cur_smax, A.cur_dt, A.cur_active,
-                               A.fin, nullptr, nullptr, lane);
+      strip::update_item<true, kPipeUpdateBatch>(A.slab, A.patches, A.times, I, A.groups, A.prm, A.cur_smax,
+                                                  A.cur_dt, A.cur_active, A.fin, nullptr, nullptr, UpdateBands(),
+                                                  lane);
       const int hs = I.hs, gi = lane / hs, j = lane - gi * hs;
       publish_fence();
       if (gi < I.ngroups && j == 0) atomicAdd(PIPE_CNT(0, A.groups[I.g0 + gi].pid), 1);

@@ -208,8 +208,9 @@ __device__ __forceinline__ void sweep_item(double *__restrict__ slab, const Patc
 
 // Update of one strip item with its group's dt (or the patch's own dt under
 // local time stepping): uNew <- uNew - dt * net update (dry clamps), uOld
-// interior <- previous uNew, time interval and next CFL estimate of the patch.
-// kBatch columns are loaded before any of them is stored.
+// interior <- previous uNew (only the bands of ub, see UpdateBands), time
+// interval and next CFL estimate of the patch.  kBatch columns are loaded
+// before any of them is stored.
 template <bool kL2, int kBatch = 4>
 __device__ __forceinline__ void update_item(double *__restrict__ slab, const PatchDev *__restrict__ patches,
                                             PatchTimeDev *__restrict__ times, const StripItem &I,
@@ -218,7 +219,7 @@ __device__ __forceinline__ void update_item(double *__restrict__ slab, const Pat
                                             const unsigned long long *__restrict__ group_dt,
                                             const int *__restrict__ group_active, int *__restrict__ fin,
                                             const int *__restrict__ pact, const unsigned long long *__restrict__ pdt,
-                                            int lane) {
+                                            const UpdateBands &ub, int lane) {
   const int hs = I.hs, w = I.w, G = I.ngroups;
   const int gi = lane / hs, j = lane - gi * hs;
   if (gi >= G) return;
@@ -231,6 +232,16 @@ __device__ __forceinline__ void update_item(double *__restrict__ slab, const Pat
   const long long vn = vol_new(P), vo = vol_old(P);
   long long in0 = idx_unew(P, 0, SG.x0, y), io0 = idx_uold(P, 0, SG.x0, y);
   const int sn = P.ny, so = P.ny + 2 * P.g;
+  // old-state writes: this lane's row and the columns of the x bands
+  int bx0 = P.nx, bx1 = 0;
+  bool row_old = true;
+  if (ub.band && !*ub.full &&
+      gt_nonneg(__dsub_rn(ub.group_t_end[P.group], __dadd_rn(ub.group_time[P.group], dt)), 0.0)) {
+    const int4 bd = ub.band[SG.pid];
+    bx0 = bd.x;
+    bx1 = P.nx - bd.y;
+    row_old = y < bd.z || y >= P.ny - bd.w;
+  }
   // loads of kBatch columns are issued before their stores (loads and
   // stores go through the same pointer, so the compiler cannot reorder them)
   bool big = false;  // an old value written to uOld is 2^1022 or more (or NaN)
@@ -253,7 +264,10 @@ __device__ __forceinline__ void update_item(double *__restrict__ slab, const Pat
         double nhv = __fma_rn(-dt, nt[k][2], st[k][2]);
         if (lt_ieee(nh, prm.dry_tol_update)) { nhu = 0.0; nhv = 0.0; }
         if (lt_zero(nh)) nh = 0.0;
-        slab[o] = st[k][0]; slab[o + vo] = st[k][1]; slab[o + 2 * vo] = st[k][2];
+        const int x = SG.x0 + c0 + k;
+        if (row_old || x < bx0 || x >= bx1) {
+          slab[o] = st[k][0]; slab[o + vo] = st[k][1]; slab[o + 2 * vo] = st[k][2];
+        }
         slab[a] = nh; slab[a + vn] = nhu; slab[a + 2 * vn] = nhv;
         big |= !(small_mag(st[k][0]) && small_mag(st[k][1]) && small_mag(st[k][2]));
       }

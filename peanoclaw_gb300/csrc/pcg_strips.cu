@@ -34,12 +34,13 @@ __global__ void __launch_bounds__(kWarps * 32)
                     const unsigned long long *__restrict__ patch_smax,
                     const unsigned long long *__restrict__ group_dt,
                     const int *__restrict__ group_active, int *__restrict__ fin,
-                    const int *__restrict__ pact, const unsigned long long *__restrict__ pdt) {
+                    const int *__restrict__ pact, const unsigned long long *__restrict__ pdt,
+                    const UpdateBands ub) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int it = blockIdx.x * kWarps + wid; it < count; it += gridDim.x * kWarps) {
     const StripItem I = items[it];
     strip::update_item<false>(slab, patches, times, I, groups, prm, patch_smax, group_dt, group_active, fin, pact,
-                              pdt, lane);
+                              pdt, ub, lane);
   }
 }
 
@@ -100,10 +101,11 @@ cudaError_t launch_update_strips(cudaStream_t st, int grid, double *slab, const 
                                  int count, const SweParamsDev &prm,
                                  const unsigned long long *patch_smax,
                                  const unsigned long long *group_dt, const int *group_active,
-                                 int *fin, const int *pact, const unsigned long long *pdt) {
+                                 int *fin, const int *pact, const unsigned long long *pdt,
+                                 const UpdateBands &ub) {
   if (count <= 0) return cudaSuccess;
   k_update_strips<8><<<grid, 256, 0, st>>>(slab, patches, times, items, groups, count, prm, patch_smax,
-                                           group_dt, group_active, fin, pact, pdt);
+                                           group_dt, group_active, fin, pact, pdt, ub);
   return cudaGetLastError();
 }
 

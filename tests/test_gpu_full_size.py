@@ -54,11 +54,12 @@ def oracle_3_steps(mosaic):
     return np.concatenate([p.u for p in pats]), odts
 
 
-@pytest.mark.parametrize("form", [P.STRIPS_FUSED, P.STRIPS_PIPELINED])
+@pytest.mark.parametrize("form", [P.STRIPS_FUSED, P.STRIPS_UNFUSED, P.STRIPS_PIPELINED])
 def test_full_mosaic_matches_the_oracle(mosaic, oracle_3_steps, form):
-    """The headline workload itself, three steps of the fused and of the
-    pipelined form, every patch vector (ghost layers and signed zeros
-    included) and every dt bit for bit."""
+    """The headline workload itself, three steps of the fused, the unfused
+    (old state written in bands inside the run) and the pipelined form, every
+    patch vector (ghost layers and signed zeros included) and every dt bit for
+    bit."""
     ps = mosaic
     got, dts, _ = _run(ps, (P.SCHED_STRIPS, 2, 32, form), 3, t_end=np.inf)
     ref, odts = oracle_3_steps
