@@ -306,6 +306,16 @@ int pcg_step(pcg_context *ctx, int32_t mode, double *dt_out);
 /* `steps` synchronous steps; BATCHED mode replays a captured CUDA graph.  The
  * dt of every step and group is written to dt_hist[steps * max_groups] (may be NULL). */
 int pcg_run(pcg_context *ctx, int32_t steps, int32_t mode, double *dt_hist);
+/* No counterpart in the reference.  pcg_run in two halves: pcg_run_async
+ * enqueues the run (steps >= 1) and returns; pcg_run_wait waits for it and
+ * does what pcg_run does after its launches (the dt record, the error words
+ * of bounded waits, the statistics).  In between the host may call the
+ * other entry points: their device work is ordered after the run on the
+ * context's stream (a call that reads device data waits for the run);
+ * pcg_run, pcg_run_async, pcg_step, pcg_autotune, pcg_profile_step and
+ * pcg_set_time_stepping return PCG_E_STATE until pcg_run_wait. */
+int pcg_run_async(pcg_context *ctx, int32_t steps, int32_t mode);
+int pcg_run_wait(pcg_context *ctx, double *dt_hist);
 /* No counterpart in the reference (its block applies the update right after
  * the sweep).  Step forms of pcg_step / pcg_run:
  *   PCG_FORM_AUTO (default): the fused form wherever it applies -- the

@@ -327,6 +327,11 @@ struct pcg_context {
   size_t d_pipe_dt_cap = 0, d_pipe_smax_cap = 0, d_pipe_active_cap = 0;
   size_t d_pipe_ctl_cap = 0;
 
+  // a run enqueued by pcg_run_async, completed by pcg_run_wait
+  bool run_pending = false;
+  int32_t run_steps = 0, run_mode = 0;
+  bool run_pipe = false;
+
   int64_t cell_updates = 0;
   double device_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -2386,6 +2391,7 @@ int pcg_set_virtual_time_items(pcg_context *c, int32_t n, const int32_t *leaf, c
 int pcg_set_time_stepping(pcg_context *c, int32_t mode) {
   if (!c || (mode != PCG_TS_GLOBAL && mode != PCG_TS_LOCAL)) return fail(PCG_E_INVALID, "bad time-stepping mode");
   std::lock_guard<std::mutex> lk(c->mu);
+  if (c->run_pending) return fail(PCG_E_STATE, "a run started by pcg_run_async is still pending");
   PCG_SETTLE(c);
   const bool local = mode == PCG_TS_LOCAL;
   if (local != c->ts_local) {
@@ -2399,6 +2405,7 @@ int pcg_set_time_stepping(pcg_context *c, int32_t mode) {
 int pcg_step(pcg_context *c, int32_t mode, double *dt_out) {
   if (!c || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED)) return fail(PCG_E_INVALID, "bad mode");
   std::lock_guard<std::mutex> lk(c->mu);
+  if (c->run_pending) return fail(PCG_E_STATE, "a run started by pcg_run_async is still pending");
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
@@ -2454,11 +2461,11 @@ static int count_kernel_nodes(cudaGraph_t g) {
   return k;
 }
 
-int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
-  if (!c || steps < 0 || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED))
-    return fail(PCG_E_INVALID, "bad arguments");
-  if (steps == 0) return PCG_OK;
-  std::lock_guard<std::mutex> lk(c->mu);
+namespace {
+
+// The launches of a run of `steps` steps (caller holds the context lock);
+// run_finish completes it.
+int run_enqueue(pcg_context *c, int32_t steps, int32_t mode) {
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
@@ -2580,6 +2587,19 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
     }
     PCG_CUDA(cudaEventRecord(c->ev1, c->stream));
   }
+  c->run_steps = steps;
+  c->run_mode = mode;
+  c->run_pipe = pipe;
+  return PCG_OK;
+}
+
+// After run_enqueue: the dt record, the wait for the stream, the error words
+// of the run's bounded waits, the statistics.
+int run_finish(pcg_context *c, double *dt_hist) {
+  const int32_t steps = c->run_steps, mode = c->run_mode;
+  const bool pipe = c->run_pipe;
+  int rc;
+
   if (dt_hist)
     PCG_CUDA(cudaMemcpyAsync(dt_hist, c->d_hist, sizeof(double) * (size_t)steps * c->max_groups,
                              cudaMemcpyDeviceToHost, c->stream));
@@ -2594,6 +2614,39 @@ int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
   c->device_ms += ms;
   if (!c->ts_local || mode != PCG_MODE_BATCHED) c->cell_updates += c->cells_per_step * steps;
   return PCG_OK;
+}
+
+}  // namespace
+
+int pcg_run(pcg_context *c, int32_t steps, int32_t mode, double *dt_hist) {
+  if (!c || steps < 0 || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED))
+    return fail(PCG_E_INVALID, "bad arguments");
+  if (steps == 0) return PCG_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (c->run_pending) return fail(PCG_E_STATE, "a run started by pcg_run_async is still pending");
+  int rc = run_enqueue(c, steps, mode);
+  if (rc != PCG_OK) return rc;
+  return run_finish(c, dt_hist);
+}
+
+int pcg_run_async(pcg_context *c, int32_t steps, int32_t mode) {
+  if (!c || steps < 1 || (mode != PCG_MODE_PLAIN && mode != PCG_MODE_BATCHED))
+    return fail(PCG_E_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (c->run_pending) return fail(PCG_E_STATE, "a run started by pcg_run_async is still pending");
+  int rc = run_enqueue(c, steps, mode);
+  if (rc != PCG_OK) return rc;
+  c->run_pending = true;
+  return PCG_OK;
+}
+
+int pcg_run_wait(pcg_context *c, double *dt_hist) {
+  if (!c) return fail(PCG_E_INVALID, "null context");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->run_pending) return fail(PCG_E_STATE, "no run started by pcg_run_async is pending");
+  c->run_pending = false;
+  PCG_CUDA(cudaSetDevice(c->device));
+  return run_finish(c, dt_hist);
 }
 
 int pcg_get_step_launches(pcg_context *c, int32_t *launches) {
@@ -2673,6 +2726,7 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
                  int32_t *n_tried) {
   if (!c || reps < 1 || cap < 0) return fail(PCG_E_INVALID, "bad arguments");
   std::lock_guard<std::mutex> lk(c->mu);
+  if (c->run_pending) return fail(PCG_E_STATE, "a run started by pcg_run_async is still pending");
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);
   if (rc != PCG_OK) return rc;
@@ -2807,6 +2861,7 @@ int pcg_stats(pcg_context *c, int64_t *cell_updates, double *device_ms) {
 int pcg_profile_step(pcg_context *c, double *ms) {
   if (!c || !ms) return fail(PCG_E_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(c->mu);
+  if (c->run_pending) return fail(PCG_E_STATE, "a run started by pcg_run_async is still pending");
   if (c->ts_local) return fail(PCG_E_STATE, "the phase profile times the global step only");
   PCG_CUDA(cudaSetDevice(c->device));
   int rc = rebuild_topology(c);

@@ -141,6 +141,8 @@ SIGNATURES = {
     "pcg_get_step_launches": (C.c_int, [_CTX, C.POINTER(C.c_int32)]),
     "pcg_selftest_transfer_wait": (C.c_int, [_CTX]),
     "pcg_run": (C.c_int, [_CTX, C.c_int32, C.c_int32, _D]),
+    "pcg_run_async": (C.c_int, [_CTX, C.c_int32, C.c_int32]),
+    "pcg_run_wait": (C.c_int, [_CTX, _D]),
     "pcg_stats": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "pcg_synchronize": (C.c_int, [_CTX]),
     "pcg_set_schedule": (C.c_int, [_CTX, C.POINTER(Schedule)]),
@@ -444,6 +446,18 @@ class Context:
     def run(self, steps, mode=PCG_MODE_BATCHED):
         hist = np.zeros(steps * self.max_groups)
         check(lib().pcg_run(self.h, steps, mode, dptr(hist)))
+        return hist.reshape(steps, self.max_groups)
+
+    def run_async(self, steps, mode=PCG_MODE_BATCHED):
+        """pcg_run_async: enqueue `steps` steps and return; run_wait() ends the run."""
+        check(lib().pcg_run_async(self.h, int(steps), mode))
+        self._async_steps = int(steps)
+
+    def run_wait(self):
+        """pcg_run_wait: the dt history of the run started by run_async."""
+        steps = self._async_steps
+        hist = np.zeros(steps * self.max_groups)
+        check(lib().pcg_run_wait(self.h, dptr(hist)))
         return hist.reshape(steps, self.max_groups)
 
     def stats(self):
