@@ -411,6 +411,12 @@ def bench_amr(prm, steps):
         S.install_amr(ctx, ps)
         ctx.restrict_all()
         ctx.set_group_max_dt(0, 1e9)
+        if mode == P.PCG_MODE_BATCHED:
+            # the schedule autotuner (untimed; it advances the simulation)
+            res["autotune"] = {"%s/%d/%d%s" % ("tiles" if k[0] == 0 else "strips", k[1], k[2],
+                                               ("", "/unfused", "/pipelined")[k[3]]): m
+                               for k, m in ctx.autotune(reps=2)}
+            res["schedule"] = "%d/%d/%d" % ctx.get_schedule()[:3]
         ctx.run(3, mode)
         c0, m0 = ctx.stats()
         ctx.run(k, mode)

@@ -421,7 +421,7 @@ int pcg_set_schedule(pcg_context *ctx, const pcg_schedule *s);
 int pcg_get_schedule(pcg_context *ctx, pcg_schedule *s);
 /* Autotuner: runs `reps` BATCHED steps with each candidate schedule (tiles,
  * also with TMA staging where the leaves allow it;
- * strips x 5 variants x chunk 32 / 16, in the fused step form where it
+ * strips x 5 variants x chunk 32 / 16 and variants 0, 2 x chunk 10 / 8, in the fused step form where it
  * applies; then the fastest strip schedule in the unfused form, and in the
  * pipelined form as one run of `reps` steps), times each candidate's steps with
  * CUDA events, keeps the fastest for this context and caches it for the

@@ -462,17 +462,20 @@ void build_strips(pcg_context *c, int chunk) {
 // Schedule of a patch mix the autotuner has not seen: small grids (fewer cells
 // than 4096 per SM) have more parallelism in 16x16 tiles (one thread per
 // cell) than in strips (one warp per strip); larger ones use strips of 8
-// warps per CTA with the widest chunk that still gives every SM two CTAs'
-// worth of strip items.
+// warps per CTA with the widest chunk that gives every SM at least one and a
+// half times the strip items its resident warps take at once (a last, nearly
+// empty wave of items costs a whole item time: on 27² patches one item per
+// patch fills 0.6 of the warps, two fill 1.1 waves, three 1.7).
 void default_schedule(pcg_context *c) {
   if (c->cells_per_step < (int64_t)c->num_sms * 4096) {
     c->sched = pcg_schedule{PCG_SCHED_TILES, 0, 32, 0};
     return;
   }
   int chunk = 32;
-  for (; chunk > 4; chunk /= 2) {
+  for (int ch : {32, 16, 10, 8, 4}) {
+    chunk = ch;
     build_strips(c, chunk);
-    if ((int64_t)c->h_sitems.size() >= (int64_t)c->num_sms * 16) break;
+    if ((int64_t)c->h_sitems.size() * 2 >= (int64_t)c->num_sms * 16 * 3) break;
   }
   c->sched = pcg_schedule{PCG_SCHED_STRIPS, 2, chunk, 0};
 }
@@ -2738,6 +2741,10 @@ int pcg_autotune(pcg_context *c, int32_t reps, pcg_schedule *tried, double *ms, 
   if (c->tma_ok) cand.push_back(pcg_schedule{PCG_SCHED_TILES, 1, 32, 0});
   for (int chunk : {32, 16})
     for (int v = 0; v < pcg::kNumStripVariants; v++) cand.push_back(pcg_schedule{PCG_SCHED_STRIPS, v, chunk, 0});
+  // narrower chunks for grids with few strips per SM (several items per
+  // patch: on 27² patches three 9-column chunks beat one of 27 or two of 14)
+  for (int chunk : {10, 8})
+    for (int v : {0, 2}) cand.push_back(pcg_schedule{PCG_SCHED_STRIPS, v, chunk, 0});
   std::vector<double> t(cand.size(), 0.0);
   for (size_t k = 0; k < cand.size(); k++) {
     c->sched = cand[k];
