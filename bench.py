@@ -388,6 +388,15 @@ def bench_radial(prm):
         ctx, ids = build_context(ps, prm)
         ctx.upload_many(ids, ps.packed)
         ctx.set_group_max_dt(0, 1e9)
+        if mode == P.PCG_MODE_BATCHED:
+            # the schedule autotuner, then the initial state again (it advanced it)
+            tuned = ctx.autotune(reps=3)
+            out["schedule"] = "%d/%d/%d/%d" % ctx.get_schedule()
+            out["autotune"] = {"%d/%d/%d/%d" % k: m for k, m in tuned}
+            ctx.upload_many(ids, ps.packed)
+            for p in ids:
+                ctx.set_time(p, time=0.0, dt=0.0, est_next=0.0)
+            ctx.set_group_end_time(0, 0.0, np.inf)
         c0, m0 = ctx.stats()
         ctx.run(100, mode)
         c1, m1 = ctx.stats()

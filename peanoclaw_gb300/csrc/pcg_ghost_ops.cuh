@@ -118,6 +118,33 @@ __device__ __forceinline__ void ghost_entry(double *__restrict__ slab, const Pat
   // absorbs, so uOld is not needed
   if (fin && dbits(tf) == 0x3FF0000000000000ull && is_leaf(S) &&
       (ldi<kL2>(fin + it.src) & (kFinUOld | kFinB)) == (kFinUOld | kFinB)) {
+    if (nq == 3) {
+      // the SWE case: all 16 source values and the destination's b loaded
+      // before the sums (in registers), then the same sums in the same order
+      double h[4], hu[4], hv[4], bb[4];
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++) {
+        const int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
+        bb[kk] = slab[idx_pw(S, 0, nxi, nyi)];
+        h[kk] = ldd<kL2>(slab + idx_unew(S, 0, nxi, nyi));
+        hu[kk] = ldd<kL2>(slab + idx_unew(S, 1, nxi, nyi));
+        hv[kk] = ldd<kL2>(slab + idx_unew(S, 2, nxi, nyi));
+      }
+      const double bd = slab[idx_pw(D, 0, cx, cy)];
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++) {
+        const double sf = pl.sf[kk];
+        a0 = __dadd_rn(a0, __dmul_rn(sf, __dadd_rn(h[kk], bb[kk])));
+        a1 = __dadd_rn(a1, __dmul_rn(sf, hu[kk]));
+        a2 = __dadd_rn(a2, __dmul_rn(sf, hv[kk]));
+      }
+      a0 = __dadd_rn(a0, __dmul_rn(-1.0, bd));
+      slab[idx_uold(D, 0, cx, cy)] = a0;
+      slab[idx_uold(D, 1, cx, cy)] = a1;
+      slab[idx_uold(D, 2, cx, cy)] = a2;
+      return;
+    }
     for (int kk = 0; kk < 4; kk++) {
       const int nxi = pl.bx + (kk & 1), nyi = pl.by + ((kk >> 1) & 1);
       const double sf = pl.sf[kk];
