@@ -38,22 +38,12 @@ __device__ __forceinline__ double interp_tf(const PatchDev &S, const PatchTimeDe
 
 // Per-step data of ghost item i: its time factor (and 1 - tf) from the two
 // patches' time intervals, and the unknown strides.
-template <bool kL2>
 __device__ __forceinline__ GhostItemStepDev item_step_value(const PatchDev *__restrict__ patches,
                                                             const PatchTimeDev *__restrict__ times,
                                                             const GhostItemDev *__restrict__ items, int i) {
   const GhostItemDev it = items[i];
   const PatchDev &S = patches[it.src], &D = patches[it.dst];
-  PatchTimeDev ST, DT;
-  if constexpr (kL2) {
-    const double *ps = reinterpret_cast<const double *>(times + it.src);
-    const double *pd = reinterpret_cast<const double *>(times + it.dst);
-    ST.time = __ldcg(ps); ST.dt = __ldcg(ps + 1); ST.min_nb_time = __ldcg(ps + 3); ST.max_nb_dt = __ldcg(ps + 4);
-    DT.time = __ldcg(pd); DT.dt = __ldcg(pd + 1); DT.min_nb_time = __ldcg(pd + 3); DT.max_nb_dt = __ldcg(pd + 4);
-  } else {
-    ST = times[it.src];
-    DT = times[it.dst];
-  }
+  const PatchTimeDev &ST = times[it.src], &DT = times[it.dst];
   GhostItemStepDev r;
   r.tf = it.kind == 0 ? transfer_tf(S, ST, D, DT) : interp_tf(S, ST, D, DT, false, true);
   r.itf = __dsub_rn(1.0, r.tf);

@@ -802,7 +802,7 @@ __device__ __forceinline__ void item_step_one(const PatchDev *__restrict__ patch
                                               const PatchTimeDev *__restrict__ times,
                                               const GhostItemDev *__restrict__ items, int i,
                                               GhostItemStepDev *__restrict__ out) {
-  out[i] = item_step_value<false>(patches, times, items, i);
+  out[i] = item_step_value(patches, times, items, i);
 }
 
 __global__ void k_item_step(const PatchDev *__restrict__ patches,
