@@ -1,8 +1,9 @@
 """The synthetic inputs follow the configurations' definitions (no GPU):
 sizes, seeds, value distributions and boundary conditions of the radial dam
-break (config 1), the uneven mosaic (config 3, at 64 x 64 slots; the bench's
-224 x 224 mosaic draws from the same generator), the coastal tsunami
-(config 5) and the request stream of the serving form (config 4)."""
+break (config 1), the 3-level breaking dam (config 2), the uneven mosaic
+(config 3, at 64 x 64 slots; the bench's 224 x 224 mosaic draws from the
+same generator), the coastal tsunami (config 5) and the request stream of
+the serving form (config 4)."""
 import numpy as np
 import pytest
 
@@ -23,6 +24,27 @@ def test_radial_dam_break_9x9_patches_of_16x16():
     w = np.array(ps.wall).reshape(9, 9)
     assert (w[0, :] & 1).all() and (w[-1, :] & 2).all() and (w[:, 0] & 4).all() and (w[:, -1] & 8).all()
     assert not w[1:-1, 1:-1].any()
+
+
+def test_breaking_dam_three_levels():
+    ps = S.breaking_dam_amr(base=9, n=27, levels=3)
+    leaves = [p for p in range(len(ps)) if ps.leaf[p]]
+    assert len(ps) == 1539 and len(leaves) == 1377 and set(ps.n) == {27}
+    # 3x refinement: patch edges 1/9, 1/27, 1/81 of the domain; the finest
+    # level sits on the dam (x = 0.5)
+    sizes = sorted({round(ps.size[p][0] * 81) for p in range(len(ps))})
+    assert sizes == [1, 3, 9]
+    fine = [p for p in leaves if round(ps.size[p][0] * 81) == 1]
+    assert fine and all(abs(ps.pos[p][0] + 0.5 / 81 - 0.5) < 0.1 for p in fine)
+    for p in leaves:
+        unew, _, b = ps.views(p)
+        X, Y = S._centers(ps.pos[p], ps.size[p], 27, ghost=True)
+        # h = 1 left of the dam, 0.5 right of it, at rest
+        assert np.array_equal(unew[0], np.where(X[1:-1, 1:-1] < 0.5, 1.0, 0.5))
+        assert not unew[1].any() and not unew[2].any()
+        # b = 0.2 exp(-|x - (0.7, 0.5)|^2 / (2 0.05^2)), ghost ring included
+        bb = 0.2 * np.exp(-((X - 0.7) ** 2 + (Y - 0.5) ** 2) / (2.0 * 0.05 * 0.05))
+        assert np.allclose(b, bb, rtol=0, atol=1e-15)
 
 
 def test_uneven_mosaic_sizes_and_values():
